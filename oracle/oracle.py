@@ -1,0 +1,345 @@
+"""CPU oracle for the hydrodynamic step -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU legs of ``bench.py``
+import this module; the product path never does.  It wraps the C
+restatement in ``rsd_oracle.c`` (assembly, lubrication, lattice) and states
+the solve chain with LAPACK DPOTRF/DPOTRI exactly as the reference calls
+them (through scipy's bundled LAPACK).
+
+Reference routines restated here (paths inside the reference project):
+  src/matrices.f90      MATREV 4-34, arrangResist 218-228, averageU 230-253,
+                        MobToResist_FTS 393-416, arrangement 432-445
+  src/stepper.f90       STEPPER_Stokesian 33-156, STEPPER_conf 160-227,
+                        STEPPER_NOGmres 348-410, Rheology 412-447
+  src/csd_post.f90      yetamu_solve 313-367, INIT_u_bg 442-479,
+                        calc_uo_bg 497-522
+  src/tensors.f90       EI_transY2 / EIN_transY2 890-919
+  src/mymodules.f90     dimensionless viscosity mu_f 816,846
+
+Parity status: the free-space pair tensors, the Y2 projection and MATREV are
+pinned against the reference's tablefar.txt (see tests/test_oracle_pins.py);
+the periodic Ewald sum, the lubrication assembly and the solve chain are
+restated from source with no reference outputs to pin them (parity unpinned
+for those parts).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "rsd_oracle.c")
+LIBDIR = os.path.join(HERE, "_build")
+LIB = os.path.join(LIBDIR, "librsd_oracle.so")
+
+PAI = 3.141592653589793238462643383279502884
+
+
+def build(force: bool = False) -> str:
+    """Compile the C restatement (plain gcc, FP contraction off so that x86
+    and Arm give the same bits, like gfortran at the reference's -O0)."""
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    os.makedirs(LIBDIR, exist_ok=True)
+    tmp = LIB + ".tmp%d" % os.getpid()
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
+                           "-o", tmp, SRC, "-lm"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.rsdo_per_grpery_inv_fri.restype = ctypes.c_int
+        L.rsdo_lubmxcalc.restype = ctypes.c_int
+        L.rsdo_lubtab_load.restype = ctypes.c_int
+        L.rsdo_lubtab_sizeof.restype = ctypes.c_int
+        L.rsdo_lattice_sizeof.restype = ctypes.c_int
+        _ = dp
+        _lib = L
+    return _lib
+
+
+class Lattice(ctypes.Structure):
+    """LATTICE_BASE module state (src/mymodules.f90:33-42)."""
+    _fields_ = [("LR", ctypes.c_double * 9), ("LI", ctypes.c_double * 9), ("LV", ctypes.c_double),
+                ("lammda", ctypes.c_double), ("sig", ctypes.c_double), ("logerr", ctypes.c_double),
+                ("phi", ctypes.c_double), ("NR", ctypes.c_int), ("NI", ctypes.c_int)]
+
+    @property
+    def lr(self):
+        return np.array(self.LR[:]).reshape(3, 3, order="F")
+
+    @property
+    def li(self):
+        return np.array(self.LI[:]).reshape(3, 3, order="F")
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def mu_f_dimensionless(mu_f_in: float = 1.0) -> float:
+    """mu_f after dimentionless_calc/translate (src/mymodules.f90:816,846)."""
+    lam_visc = 1.0 / PAI / mu_f_in
+    return mu_f_in * lam_visc
+
+
+def set_lattice_skew(T, LB, gamma, oscillation=False, gamma_alpha=0.0, frequency=0.0) -> Lattice:
+    lat = Lattice()
+    LB = np.ascontiguousarray(LB, dtype=np.float64)
+    LV = ctypes.c_double()
+    lib().rsdo_set_lattice_skew(ctypes.c_double(T), _p(LB), ctypes.c_double(gamma), ctypes.c_int(int(oscillation)),
+                                ctypes.c_double(gamma_alpha), ctypes.c_double(frequency),
+                                lat.LR, lat.LI, ctypes.byref(LV))
+    lat.LV = LV.value
+    return lat
+
+
+def calc_lattice_inverse(lat: Lattice, ews_err: float, radii) -> Lattice:
+    radii = np.ascontiguousarray(radii, dtype=np.float64)
+    lib().rsdo_calc_lattice_inverse(ctypes.byref(lat), ctypes.c_double(ews_err), ctypes.c_int(len(radii)), _p(radii))
+    return lat
+
+
+def per_skew_correction(lat: Lattice, R):
+    R = np.array(R, dtype=np.float64)
+    d = ctypes.c_double()
+    lib().rsdo_per_skew_correction(lat.LR, lat.LI, _p(R), ctypes.byref(d))
+    return R, d.value
+
+
+def period_correction(R, LB, T, gamma):
+    R = np.array(R, dtype=np.float64)
+    LB = np.ascontiguousarray(LB, dtype=np.float64)
+    lib().rsdo_period_correction(_p(R), _p(LB), ctypes.c_double(T), ctypes.c_double(gamma), ctypes.c_int(0),
+                                 ctypes.c_double(0.0), ctypes.c_double(0.0))
+    return R
+
+
+def per_rotne_prager_self(lat: Lattice, a: float):
+    TTS, RRS, QQS = np.zeros(9), np.zeros(9), np.zeros(25)
+    lib().rsdo_per_rotne_prager_self(ctypes.byref(lat), ctypes.c_double(a), _p(TTS), _p(RRS), _p(QQS))
+    return TTS.reshape(3, 3, order="F"), RRS.reshape(3, 3, order="F"), QQS.reshape(5, 5, order="F")
+
+
+def per_rotne_prager_ij(lat: Lattice, R, aI: float, aJ: float, include_k: bool = True):
+    R = np.ascontiguousarray(R, dtype=np.float64)
+    TT, RR, TR, QQ, G, H = (np.zeros(9), np.zeros(9), np.zeros(9), np.zeros(25), np.zeros(15), np.zeros(15))
+    lib().rsdo_per_rotne_prager_ij(ctypes.byref(lat), _p(R), ctypes.c_double(aI), ctypes.c_double(aJ),
+                                   ctypes.c_int(int(include_k)), _p(TT), _p(RR), _p(TR), _p(QQ), _p(G), _p(H))
+    f = lambda x, s: x.reshape(s, order="F")
+    return f(TT, (3, 3)), f(RR, (3, 3)), f(TR, (3, 3)), f(QQ, (5, 5)), f(G, (3, 5)), f(H, (3, 5))
+
+
+def per_grpery_inv_fri(pos, radii, lat: Lattice, ews_err: float, mu_f: float, correction_method: int = 0):
+    """PER_GRPERY_INV_FRI: returns (grmobmx (11N,11N) Fortran-ordered,
+    n_overlap).  APP/APQ/AQQ are grmobmx[:6N,:6N], [:6N,6N:], [6N:,6N:]."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    radii = np.ascontiguousarray(radii, dtype=np.float64)
+    N = len(radii)
+    G = np.zeros((11 * N, 11 * N), order="F")
+    nov = lib().rsdo_per_grpery_inv_fri(ctypes.c_int(N), _p(pos), _p(radii), ctypes.byref(lat),
+                                        ctypes.c_double(ews_err), ctypes.c_double(mu_f),
+                                        ctypes.c_int(correction_method), _p(G))
+    return G, nov
+
+
+def split_mobility(G, N):
+    return G[:6 * N, :6 * N], G[:6 * N, 6 * N:], G[6 * N:, 6 * N:]
+
+
+class LubTab:
+    """The three lubrication tables (src/hydro_lub.f90:400-596)."""
+
+    def __init__(self, directory: str):
+        self.buf = ctypes.create_string_buffer(lib().rsdo_lubtab_sizeof())
+        rc = lib().rsdo_lubtab_load(self.buf, directory.encode())
+        if rc != 0:
+            raise OSError("cannot read lubrication tables from %s" % directory)
+
+    def lubcalc(self, s: float):
+        o = np.zeros(19)
+        lib().rsdo_lubcalc(self.buf, ctypes.c_double(s), _p(o))
+        return o
+
+
+def lubmxcalc(pos, radii, lat: Lattice, mu_f: float, tab: LubTab, nb: int = 0, is_period: bool = True):
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    radii = np.ascontiguousarray(radii, dtype=np.float64)
+    N = len(radii)
+    rfu = np.zeros((6 * N, 6 * N), order="F")
+    rfe = np.zeros((6 * N, 5 * N), order="F")
+    rse = np.zeros((5 * N, 5 * N), order="F")
+    nc = lib().rsdo_lubmxcalc(ctypes.c_int(N), ctypes.c_int(nb), ctypes.c_int(int(is_period)), _p(pos), _p(radii),
+                              lat.LR, lat.LI, ctypes.c_double(mu_f), tab.buf, _p(rfu), _p(rfe), _p(rse))
+    return rfu, rfe, rse, nc
+
+
+# --------------------------------------------------------------- solve chain
+def matrev(A):
+    """MATREV (src/matrices.f90:4-34): DPOTRF('U'), DPOTRI('U'), mirror the
+    upper triangle into the lower.  Returns (inverse, info); like the
+    reference, a positive DPOTRF info is reported and the chain continues."""
+    from scipy.linalg import lapack
+    A = np.asfortranarray(A, dtype=np.float64).copy(order="F")
+    c, info = lapack.dpotrf(A, lower=0, clean=0, overwrite_a=1)
+    inv, info2 = lapack.dpotri(c, lower=0, overwrite_c=1)
+    iu = np.triu_indices(inv.shape[0], 1)
+    inv[(iu[1], iu[0])] = inv[iu]
+    return inv, int(info)
+
+
+def mob_to_resist_fts(G):
+    """MobToResist_FTS (src/matrices.f90:393-416) on the assembled 11N x 11N
+    mobility: the full grand resistance R_inf = M^-1."""
+    return matrev(G)
+
+
+def ein_trans_y2(Eij, N):
+    """EIN_transY2 (src/tensors.f90:905-919) with EI_transY2 890-903."""
+    Y2 = np.zeros(45)
+    lib().rsdo_tensor_Y2(_p(Y2))
+    Y2 = Y2.reshape(5, 3, 3, order="F")
+    EI = np.zeros(5)
+    for m in range(5):
+        a = 0.0
+        for i in range(3):
+            for j in range(3):
+                a = a + Eij[i, j] * Y2[m, i, j]
+        EI[m] = a
+    return np.tile(EI, N)
+
+
+def init_u_bg(gamma):
+    """INIT_u_bg (src/csd_post.f90:442-479) with EI_bg = 0 on input."""
+    EI_bg = np.zeros(6)
+    EI_bg[4] = gamma * 0.5
+    Eij = np.zeros((3, 3))
+    Eij[0, 0], Eij[1, 1], Eij[2, 2] = EI_bg[0], EI_bg[1], EI_bg[2]
+    Eij[0, 1] = Eij[1, 0] = EI_bg[3]
+    Eij[0, 2] = Eij[2, 0] = EI_bg[4]
+    Eij[1, 2] = Eij[2, 1] = EI_bg[5]
+    omega_bg = np.array([0.0, gamma * 0.5, 0.0])
+    eps = np.zeros((3, 3, 3))
+    eps[0, 1, 2] = eps[1, 2, 0] = eps[2, 0, 1] = 1.0
+    eps[0, 2, 1] = eps[2, 1, 0] = eps[1, 0, 2] = -1.0
+    omegaT = np.zeros((3, 3))
+    for I in range(3):
+        for J in range(3):
+            omegaT[I, J] = eps[J, I, 0] * omega_bg[0] + eps[J, I, 1] * omega_bg[1] + eps[J, I, 2] * omega_bg[2]
+    return Eij, omega_bg, omegaT
+
+
+def calc_uo_bg(pos, Eij, omega_bg, omegaT, u_bg=(0.0, 0.0, 0.0)):
+    """calc_uo_bg (src/csd_post.f90:497-522)."""
+    N = pos.shape[0]
+    UOE = omegaT + Eij
+    uo = np.zeros(6 * N)
+    for i in range(N):
+        uo[3 * i:3 * i + 3] = np.asarray(u_bg) + UOE @ pos[i]
+        uo[3 * N + 3 * i:3 * N + 3 * i + 3] = omega_bg
+    return uo
+
+
+def stepper_nogmres(G, rfu, rfe, rse, Fe, EIN, Fe_inter, conf, u_brown=None):
+    """STEPPER_NOGmres (src/stepper.f90:348-410) for the FTS periodic path,
+    with arrangement (src/matrices.f90:432-445) and Rheology
+    (src/stepper.f90:412-447).  Returns U_par, SijN_hyd, SijN_FP, SijN_B and
+    RPP as the caller sees it afterwards (overwritten by its inverse inside
+    Rheology), plus the MATREV infos."""
+    N = conf.shape[0]
+    R0, info_m = mob_to_resist_fts(G)
+    RPP = R0[:6 * N, :6 * N] + rfu
+    RPQ = R0[:6 * N, 6 * N:] + rfe
+    RQQ = R0[6 * N:, 6 * N:] + rse
+    UB = np.zeros(6 * N)
+    if u_brown is not None:
+        UB[:3 * N] = u_brown
+    APPR, info_r = matrev(RPP)
+    U_par = APPR @ (Fe + RPQ @ EIN)
+    RPPINV, _ = matrev(RPP)
+    mu = (RPQ.T @ RPPINV) @ RPQ - RQQ
+    SijN_hyd = mu @ EIN
+    RPP_inv, _ = matrev(RPP)
+    SijN_FP = (RPQ.T @ RPP_inv) @ Fe_inter
+    Y2 = np.zeros(45)
+    lib().rsdo_tensor_Y2(_p(Y2))
+    Y2 = Y2.reshape(5, 3, 3, order="F")
+    for kk in range(N):
+        Sij = np.zeros((3, 3))
+        for i in range(3):
+            for j in range(3):
+                Sij[i, j] = 0.5 * (conf[kk, i] * Fe_inter[3 * kk + j] + conf[kk, j] * Fe_inter[3 * kk + i])
+        part = np.array([sum(Sij[a, b] * Y2[m, a, b] for a in range(3) for b in range(3)) for m in range(5)])
+        SijN_FP[5 * kk:5 * kk + 5] += part
+    SijN_B = RPQ.T @ UB
+    return dict(U_par=U_par, SijN_hyd=SijN_hyd, SijN_FP=SijN_FP, SijN_B=SijN_B, RPP=RPP_inv,
+                info_m=info_m, info_r=info_r, RPQ=RPQ, RQQ=RQQ)
+
+
+def average_u(APP, N, mu_f, radii_test=1.0):
+    """averageU (src/matrices.f90:230-253)."""
+    F = np.zeros(6 * N)
+    F[0:3 * N:3] = 1.0 * (6.0 * PAI * mu_f * radii_test)
+    UU = APP @ F
+    return UU[0:3 * N:3].sum() / N
+
+
+def yetamu_solve(APP, SijN_hyd, SijN_FP, SijN_B, EIN, LV, mu_f, phi, N):
+    """yetamu_solve (src/csd_post.f90:313-367), non-GMRES build."""
+    y = np.zeros(5)
+    d = -2.0 * EIN[3::5]
+    y[0] = ((SijN_FP[3::5] + SijN_hyd[3::5] + SijN_B[3::5]) / d).sum() / LV / mu_f
+    y[1] = phi
+    y[2] = 1.0 / average_u(APP, N, mu_f)
+    y[3] = (SijN_B[3::5] / d).sum() / LV / mu_f
+    y[4] = (SijN_FP[3::5] / d).sum() / LV / mu_f
+    return y
+
+
+def stepper_stokesian(conf, radii, LB, T, dt, gamma, mu_f, ews_err, tab: LubTab, Fe=None, Fe_inter=None):
+    """One STEPPER_Stokesian step (src/stepper.f90:33-156) on the plain
+    LAPACK FTS periodic path with lubrication (no Brownian motion, no DEM
+    sub-stepping, no rigid bodies).  Returns the updated configuration and
+    everything the reference computes on the way."""
+    conf = np.array(conf, dtype=np.float64)
+    N = conf.shape[0]
+    Eij, omega_bg, omegaT = init_u_bg(gamma)
+    EIN = ein_trans_y2(Eij, N)
+    lat = set_lattice_skew(T, LB, gamma)
+    G, _ = per_grpery_inv_fri(conf, radii, lat, ews_err, mu_f, 0)
+    Fe = np.zeros(6 * N) if Fe is None else np.asarray(Fe, dtype=np.float64)
+    Fe_inter = np.zeros(6 * N) if Fe_inter is None else np.asarray(Fe_inter, dtype=np.float64)
+    rfu, rfe, rse, ncontact = lubmxcalc(conf, radii, lat, mu_f, tab)
+    out = stepper_nogmres(G, rfu, rfe, rse, Fe + Fe_inter, EIN, Fe_inter, conf)
+    U_rel = out["U_par"]
+    # STEPPER_conf (src/stepper.f90:160-227)
+    uo = calc_uo_bg(conf, Eij, omega_bg, omegaT)
+    U_pos = U_rel + uo
+    new = conf + dt * U_pos[:3 * N].reshape(N, 3)
+    for i in range(N):
+        new[i] = period_correction(new[i], LB, T, gamma)
+    uo = calc_uo_bg(new, Eij, omega_bg, omegaT)
+    U_pos = U_rel + uo
+    APP = G[:6 * N, :6 * N]
+    yeta = yetamu_solve(APP, out["SijN_hyd"], out["SijN_FP"], out["SijN_B"], EIN, lat.LV, mu_f, lat.phi, N)
+    out.update(conf=new, U_pos=U_pos, yeta_mu=yeta, EIN=EIN, lattice=lat, G=G, rfu=rfu, rfe=rfe, rse=rse,
+               ncontact=ncontact)
+    return out
+
+
+def box_length(N, phi, a=1.0):
+    """Cubic box edge for N spheres of radius a at volume fraction phi."""
+    return (N * 4.0 / 3.0 * math.pi * a ** 3 / phi) ** (1.0 / 3.0)
