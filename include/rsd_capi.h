@@ -1,0 +1,194 @@
+/*
+ * rsd_capi.h -- C-ABI of the GB300 (sm_103a) hydrodynamic step of
+ * regularized Stokesian dynamics.
+ *
+ * Every entry point replaces one subroutine of the Fortran reference
+ * (sherlockyzd/Regularized-Stokesian-Dynamics); the comment above each one
+ * names the routine and its file:line.  Conventions follow the Fortran side:
+ *   - all host arrays are column-major, leading dimension = row count, no
+ *     padding; p_pos is (3, nn), so particle a sits at p_pos[3a .. 3a+2];
+ *   - outputs are fully overwritten; inputs are not modified except where an
+ *     entry says "in place" (rsd_matrev, like MATREV);
+ *   - return 0 on success, a positive LAPACK-style INFO (leading minor k is
+ *     not positive definite) from the factorisations, or a negative RSD_E*
+ *     code; rsd_ctx_last_error() then holds a one-line message;
+ *   - one host thread per context; calls are synchronous with respect to the
+ *     host arrays they take (the caller may read outputs on return).
+ * Entry points ending in _dev take device pointers (cudaMalloc'ed, on the
+ * context's device) and run asynchronously on the context's stream; they
+ * return after enqueueing, except where an INFO must be read back.
+ */
+#ifndef RSD_CAPI_H
+#define RSD_CAPI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RSD_OK 0
+#define RSD_EARG (-1)     /* invalid argument (size, null pointer, lattice) */
+#define RSD_ECUDA (-2)    /* CUDA runtime error */
+#define RSD_ENAN (-3)     /* non-finite input or result */
+#define RSD_ETIMEOUT (-4) /* a bounded device wait ran out */
+#define RSD_ENOMEM (-5)   /* device allocation failed */
+#define RSD_EIO (-6)      /* lubrication table files unreadable */
+#define RSD_EUNSUP (-7)   /* option of the reference not built here */
+
+typedef struct rsd_ctx rsd_ctx;
+typedef struct rsd_lubtab rsd_lubtab;
+
+/* Module LATTICE_BASE (src/mymodules.f90:33-42): the Lees-Edwards lattice
+ * LR (3x3, column-major), its inverse LI, the cell volume LV, and the Ewald
+ * parameters that CALC_LATTICE_INVERSE derives from them. */
+typedef struct rsd_lattice {
+  double LR[9];
+  double LI[9];
+  double LV;
+  double lammda; /* Ewald splitting parameter, sqrt(pi)/LV^(1/3) */
+  double sig;
+  double logerr;
+  double phi; /* volume fraction sum(4/3 pi a^3)/LV */
+  int32_t NR; /* real-space images in [-NR,NR]^3 */
+  int32_t NI; /* reciprocal vectors in [-NI,NI]^3 \ {0} */
+} rsd_lattice;
+
+/* ---------------------------------------------------------------- context */
+/* Creates a context on CUDA device `device` (one stream, grow-only device
+ * buffers reused across calls). */
+int rsd_ctx_create(rsd_ctx** ctx, int device);
+int rsd_ctx_destroy(rsd_ctx* ctx);
+const char* rsd_ctx_last_error(const rsd_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that want to order
+ * their own work after _dev calls. */
+void* rsd_ctx_stream(rsd_ctx* ctx);
+/* Device-time of the last call's phases in milliseconds (assembly, lub,
+ * solve, update), measured with CUDA events on the context stream. */
+int rsd_ctx_phase_ms(const rsd_ctx* ctx, double ms[4]);
+
+/* ---------------------------------------------------------------- lattice */
+/* SET_LATTICE_SKEW (src/csd_post.f90:105-136) with MAT_INV3
+ * (src/tensors.f90:704-726): fills lat->LR, LI, LV for strain time T. */
+int rsd_set_lattice_skew(double T, const double LB[3], double gamma, int32_t oscillation, double gamma_alpha,
+                         double frequency, rsd_lattice* lat);
+/* CALC_LATTICE_INVERSE (src/csd_post.f90:158-183): lammda, sig, logerr, NR,
+ * NI and phi from LR, LV, EWS_ERR and the radii (module side effects that
+ * yetamu_solve later reads). */
+int rsd_calc_lattice_inverse(rsd_lattice* lat, double ews_err, int32_t nn, const double* radii);
+
+/* ------------------------------------------------- kernel 1: grand mobility */
+/* PER_GRPERY_INV_FRI (src/per_GRPY_YZD.f90:13-200): Ewald-summed periodic
+ * grand mobility, scaled by 1/(pi mu_f), split into APP (6nn x 6nn),
+ * APQ (6nn x 5nn), AQQ (5nn x 5nn).  Calls CALC_LATTICE_INVERSE first and
+ * leaves its results in *lat.  correction_method != 0 (overlap corrections
+ * of GRPY_YZD.f90:768-836) is not built: with an overlapping pair it returns
+ * RSD_EUNSUP, without one it is ignored, like the reference. */
+int rsd_per_grpery_inv_fri(rsd_ctx* ctx, int32_t nn, const double* p_pos, const double* radii, rsd_lattice* lat,
+                           double ews_err, double mu_f, int32_t correction_method, double* APP, double* APQ,
+                           double* AQQ);
+/* Same on device: writes the whole grmobmx (11nn x 11nn, leading dimension
+ * ldm >= 11nn) in the reference's row/column order. */
+int rsd_per_grpery_inv_fri_dev(rsd_ctx* ctx, int32_t nn, const double* d_pos, const double* d_radii,
+                               rsd_lattice* lat, double ews_err, double mu_f, int32_t correction_method,
+                               double* d_grmobmx, int64_t ldm);
+
+/* ------------------------------------------- kernel 2: lubrication R_lub-R_2B */
+/* The three tables lubtabcalc reads once (src/hydro_lub.f90:529-596):
+ * r2babc.dat (39 rows x 11), r2bgh.dat (47 x 7), r2bm.dat (47 x 4), each
+ * with one header line, from directory `dir` (the reference opens
+ * lubdat/ relative to its working directory). */
+int rsd_lubtab_load(rsd_lubtab** tab, const char* dir);
+/* Same tables from memory, rows in file order (row-major per row). */
+int rsd_lubtab_create(rsd_lubtab** tab, int32_t nabc, const double* abc, int32_t ngh, const double* gh, int32_t nm,
+                      const double* m);
+int rsd_lubtab_destroy(rsd_lubtab* tab);
+/* lubmxcalc (src/hydro_lub.f90:22-308): dense rfu (6nn x 6nn),
+ * rfe (6nn x 5nn), rse (5nn x 5nn).  Pairs with s = r/a_avg <= 2 are
+ * mirrored to 4.00001 - s like the reference; *n_contact (may be NULL)
+ * returns how many.  nb trailing boundary particles are skipped. */
+int rsd_lubmxcalc(rsd_ctx* ctx, const rsd_lubtab* tab, int32_t nn, int32_t nb, int32_t is_period,
+                  const double* p_pos, const double* radii, const rsd_lattice* lat, double mu_f, double* rfu,
+                  double* rfe, double* rse, int32_t* n_contact);
+/* Same on device, written into the grand layout L = [rfu rfe; rfe^T rse]
+ * (11nn x 11nn, leading dimension ldl).  accumulate != 0 adds L into d_L
+ * (arrangResist, src/matrices.f90:218-228) instead of overwriting it. */
+int rsd_lubmxcalc_dev(rsd_ctx* ctx, const rsd_lubtab* tab, int32_t nn, int32_t nb, int32_t is_period,
+                      const double* d_pos, const double* d_radii, const rsd_lattice* lat, double mu_f, double* d_L,
+                      int64_t ldl, int32_t accumulate, int32_t* n_contact);
+
+/* --------------------------------------------- kernel 3: grand resistance */
+/* MATREV (src/matrices.f90:4-34): SPD inverse in place (upper Cholesky,
+ * inverse, upper triangle mirrored).  *info > 0 as DPOTRF's INFO; the
+ * reference prints and continues, so A then holds an undefined result. */
+int rsd_matrev(rsd_ctx* ctx, int32_t n, double* A, int32_t* info);
+int rsd_matrev_dev(rsd_ctx* ctx, int32_t n, double* d_A, int64_t lda, int32_t* info);
+/* CHOLESKY (src/matrices.f90:126-157): lower factor, strict upper part
+ * zeroed.  Returns the positive INFO when not SPD (the reference stops). */
+int rsd_cholesky(rsd_ctx* ctx, int32_t n, double* B, int32_t* info);
+/* MobToResist_FTS (src/matrices.f90:393-416): RPP, RPQ, RQQ blocks of the
+ * inverse of [APP APQ; APQ^T AQQ]. */
+int rsd_mob_to_resist_fts(rsd_ctx* ctx, int32_t nn, const double* APP, const double* APQ, const double* AQQ,
+                          double* RPP, double* RPQ, double* RQQ, int32_t* info);
+/* arrangement (src/matrices.f90:432-445): mu = RPQ^T RPP^-1 RPQ - RQQ. */
+int rsd_arrangement(rsd_ctx* ctx, int32_t nn, const double* RPP, const double* RPQ, const double* RQQ, double* mu,
+                    int32_t* info);
+/* STEPPER_NOGmres (src/stepper.f90:348-410) for the FTS path, with
+ * MobToResist_FTS, arrangResist, arrangement and Rheology (412-447):
+ * U_par = RPP^-1 (Fe + RPQ EIN), SijN_hyd = mu EIN,
+ * SijN_FP = RPQ^T RPP^-1 Fe_inter + sym(x (x) F) in Y2,
+ * SijN_B = RPQ^T UB.  On return RPP holds the inverse of RPP0 + rfu, as the
+ * reference's Rheology leaves it.  u_brown (3nn) may be NULL (zero). */
+int rsd_stepper_nogmres(rsd_ctx* ctx, int32_t nn, const double* APP, const double* APQ, const double* AQQ,
+                        const double* rfu, const double* rfe, const double* rse, const double* Fe, const double* EIN,
+                        const double* Fe_inter, const double* conf, const double* u_brown, double* U_par,
+                        double* SijN_hyd, double* SijN_FP, double* SijN_B, double* RPP, int32_t* info);
+
+/* ------------------------------------------------------------ fused step */
+#define RSD_PREC_FP64 0  /* plain: every kernel in FP64 */
+#define RSD_PREC_MIXED 1 /* FP32 bulk + FP64 near terms and refinement */
+
+typedef struct rsd_step_params {
+  int32_t nn;        /* particles */
+  int32_t nb;        /* trailing boundary particles (skipped by lub) */
+  double LB[3];      /* box edges */
+  double T;          /* time at the start of the step (strain = gamma T) */
+  double dt;         /* time step */
+  double gamma;      /* shear rate */
+  double mu_f;       /* dimensionless viscosity (1/pi for the reference's units) */
+  double ews_err;    /* Ewald tolerance EWS_ERR = LINERR */
+  int32_t use_lub;   /* uselub */
+  int32_t precision; /* RSD_PREC_FP64 or RSD_PREC_MIXED */
+  double tol;        /* mixed: relative residual target of the refinement (0: 1e-12) */
+  int32_t max_iter;  /* mixed: refinement iteration cap (0: 50) */
+} rsd_step_params;
+
+typedef struct rsd_step_info {
+  int32_t info;       /* positive: leading minor not SPD (plain path) */
+  int32_t n_contact;  /* lub pairs with s <= 2 */
+  int32_t NR, NI;     /* Ewald images used */
+  int32_t iterations; /* mixed: refinement iterations */
+  double residual;    /* mixed: final relative residual */
+  double phi;         /* volume fraction */
+  double LV;          /* cell volume */
+} rsd_step_info;
+
+/* One STEPPER_Stokesian step (src/stepper.f90:33-156) on the periodic FTS
+ * path with lubrication: SET_LATTICE_SKEW, PER_GRPERY_INV_FRI, lubmxcalc,
+ * STEPPER_NOGmres, INIT_uo_bg/calc_uo_bg (src/csd_post.f90:442-522),
+ * STEPPER_conf with PERIOD_CORRECTION (src/stepper.f90:160-227,
+ * src/csd_post.f90:65-102) and yetamu_solve (src/csd_post.f90:313-367).
+ * conf (3 x nn) is advanced in place; U_pos (6nn), SijN (5nn, the hydrodynamic
+ * stresslet SijN_hyd) and yeta_mu[5] are written.  Fe (6nn) may be NULL. */
+int rsd_stepper_stokesian(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_step_params* p, double* conf,
+                          const double* radii, const double* Fe, double* U_pos, double* SijN, double yeta_mu[5],
+                          rsd_step_info* info);
+/* Same with device-resident arrays (no host copies). */
+int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_step_params* p, double* d_conf,
+                              const double* d_radii, const double* d_Fe, double* d_U_pos, double* d_SijN,
+                              double yeta_mu[5], rsd_step_info* info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RSD_CAPI_H */

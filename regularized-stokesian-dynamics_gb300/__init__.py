@@ -1,0 +1,360 @@
+"""GB300 (sm_103a) hydrodynamic step of regularized Stokesian dynamics.
+
+Host-side mirror of the Fortran reference's interface for the hot path
+(sherlockyzd/Regularized-Stokesian-Dynamics): the same subroutine names,
+argument meanings and error behaviour, over the C-ABI in include/rsd_capi.h.
+Arrays follow the Fortran layout: positions are (N, 3) C-ordered (= p_pos(3,N)
+column-major), matrices are returned Fortran-ordered.
+
+Everything computes on the GPU through librsd_gb300.so; importing this
+package without the built library raises ImportError (there is no CPU path).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "librsd_gb300.so")
+
+RSD_OK, RSD_EARG, RSD_ECUDA, RSD_ENAN, RSD_ETIMEOUT, RSD_ENOMEM, RSD_EIO, RSD_EUNSUP = 0, -1, -2, -3, -4, -5, -6, -7
+PREC_FP64, PREC_MIXED = 0, 1
+PAI = 3.141592653589793238462643383279502884
+
+if not os.path.exists(LIBPATH):
+    raise ImportError("librsd_gb300.so is not built (run regularized-stokesian-dynamics_gb300/build.py); "
+                      "this package has no CPU fallback")
+
+_lib = ctypes.CDLL(LIBPATH)
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+_vp = ctypes.c_void_p
+
+
+class Lattice(ctypes.Structure):
+    """rsd_lattice: module LATTICE_BASE (src/mymodules.f90:33-42)."""
+    _fields_ = [("LR", ctypes.c_double * 9), ("LI", ctypes.c_double * 9), ("LV", ctypes.c_double),
+                ("lammda", ctypes.c_double), ("sig", ctypes.c_double), ("logerr", ctypes.c_double),
+                ("phi", ctypes.c_double), ("NR", ctypes.c_int32), ("NI", ctypes.c_int32)]
+
+
+class StepParams(ctypes.Structure):
+    _fields_ = [("nn", ctypes.c_int32), ("nb", ctypes.c_int32), ("LB", ctypes.c_double * 3), ("T", ctypes.c_double),
+                ("dt", ctypes.c_double), ("gamma", ctypes.c_double), ("mu_f", ctypes.c_double),
+                ("ews_err", ctypes.c_double), ("use_lub", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("tol", ctypes.c_double), ("max_iter", ctypes.c_int32)]
+
+
+class StepInfo(ctypes.Structure):
+    _fields_ = [("info", ctypes.c_int32), ("n_contact", ctypes.c_int32), ("NR", ctypes.c_int32),
+                ("NI", ctypes.c_int32), ("iterations", ctypes.c_int32), ("residual", ctypes.c_double),
+                ("phi", ctypes.c_double), ("LV", ctypes.c_double)]
+
+
+def _sig(name, res, args):
+    f = getattr(_lib, name)
+    f.restype = res
+    f.argtypes = args
+    return f
+
+
+_i = ctypes.c_int
+_i32 = ctypes.c_int32
+_i64 = ctypes.c_int64
+_d = ctypes.c_double
+_LP = ctypes.POINTER(Lattice)
+_sig("rsd_ctx_create", _i, [ctypes.POINTER(_vp), _i])
+_sig("rsd_ctx_destroy", _i, [_vp])
+_sig("rsd_ctx_last_error", ctypes.c_char_p, [_vp])
+_sig("rsd_ctx_stream", _vp, [_vp])
+_sig("rsd_ctx_phase_ms", _i, [_vp, _dp])
+_sig("rsd_set_lattice_skew", _i, [_d, _dp, _d, _i32, _d, _d, _LP])
+_sig("rsd_calc_lattice_inverse", _i, [_LP, _d, _i32, _dp])
+_sig("rsd_per_grpery_inv_fri", _i, [_vp, _i32, _dp, _dp, _LP, _d, _d, _i32, _dp, _dp, _dp])
+_sig("rsd_per_grpery_inv_fri_dev", _i, [_vp, _i32, _vp, _vp, _LP, _d, _d, _i32, _vp, _i64])
+_sig("rsd_lubtab_load", _i, [ctypes.POINTER(_vp), ctypes.c_char_p])
+_sig("rsd_lubtab_create", _i, [ctypes.POINTER(_vp), _i32, _dp, _i32, _dp, _i32, _dp])
+_sig("rsd_lubtab_destroy", _i, [_vp])
+_sig("rsd_lubmxcalc", _i, [_vp, _vp, _i32, _i32, _i32, _dp, _dp, _LP, _d, _dp, _dp, _dp, _ip])
+_sig("rsd_lubmxcalc_dev", _i, [_vp, _vp, _i32, _i32, _i32, _vp, _vp, _LP, _d, _vp, _i64, _i32, _ip])
+_sig("rsd_matrev", _i, [_vp, _i32, _dp, _ip])
+_sig("rsd_matrev_dev", _i, [_vp, _i32, _vp, _i64, _ip])
+_sig("rsd_cholesky", _i, [_vp, _i32, _dp, _ip])
+_sig("rsd_mob_to_resist_fts", _i, [_vp, _i32, _dp, _dp, _dp, _dp, _dp, _dp, _ip])
+_sig("rsd_arrangement", _i, [_vp, _i32, _dp, _dp, _dp, _dp, _ip])
+_sig("rsd_stepper_nogmres", _i, [_vp, _i32] + [_dp] * 11 + [_dp] * 5 + [_ip])
+_sig("rsd_stepper_stokesian", _i, [_vp, _vp, ctypes.POINTER(StepParams), _dp, _dp, _dp, _dp, _dp, _dp,
+                                   ctypes.POINTER(StepInfo)])
+_sig("rsd_stepper_stokesian_dev", _i, [_vp, _vp, ctypes.POINTER(StepParams), _vp, _vp, _vp, _vp, _vp, _dp,
+                                       ctypes.POINTER(StepInfo)])
+
+EXPORTED = [n for n in dir(_lib) if n.startswith("rsd_")]
+
+
+def library():
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _f64(a, shape=None, order="C"):
+    a = np.require(np.asarray(a, dtype=np.float64), requirements=[order, "A", "W", "O"])
+    if shape is not None and a.shape != shape:
+        a = a.reshape(shape, order=order)
+    return a
+
+
+class RSDError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("rsd error %d: %s" % (code, msg))
+        self.code = code
+
+
+class Context:
+    """rsd_ctx on one CUDA device: one stream, grow-only device buffers."""
+
+    def __init__(self, device: int = 0):
+        self.h = _vp()
+        rc = _lib.rsd_ctx_create(ctypes.byref(self.h), device)
+        if rc != 0:
+            raise RSDError(rc, "cannot create a context on CUDA device %d" % device)
+        self.device = device
+
+    def check(self, rc):
+        if rc < 0:
+            raise RSDError(rc, (_lib.rsd_ctx_last_error(self.h) or b"").decode())
+        return rc
+
+    def phase_ms(self):
+        ms = np.zeros(4)
+        _lib.rsd_ctx_phase_ms(self.h, _p(ms))
+        return ms
+
+    @property
+    def stream(self):
+        return _lib.rsd_ctx_stream(self.h)
+
+    def close(self):
+        if self.h:
+            _lib.rsd_ctx_destroy(self.h)
+            self.h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LubTab:
+    """The three lubrication tables (hydro_lub.f90:529-596), read from a
+    directory holding r2babc.dat, r2bgh.dat and r2bm.dat."""
+
+    def __init__(self, directory: str):
+        self.h = _vp()
+        rc = _lib.rsd_lubtab_load(ctypes.byref(self.h), directory.encode())
+        if rc != 0:
+            raise RSDError(rc, "cannot read lubrication tables from %s" % directory)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _lib.rsd_lubtab_destroy(self.h)
+            self.h = _vp()
+
+
+# ------------------------------------------------------------------ lattice
+def SET_LATTICE_SKEW(T, LB, gamma, oscillation=False, gamma_alpha=0.0, frequency=0.0) -> Lattice:
+    """SET_LATTICE_SKEW (src/csd_post.f90:105-136)."""
+    lat = Lattice()
+    LB = _f64(LB)
+    rc = _lib.rsd_set_lattice_skew(T, _p(LB), gamma, int(oscillation), gamma_alpha, frequency, ctypes.byref(lat))
+    if rc:
+        raise RSDError(rc, "SET_LATTICE_SKEW")
+    return lat
+
+
+def CALC_LATTICE_INVERSE(lat: Lattice, ews_err, radii) -> Lattice:
+    """CALC_LATTICE_INVERSE (src/csd_post.f90:158-183)."""
+    r = _f64(radii)
+    rc = _lib.rsd_calc_lattice_inverse(ctypes.byref(lat), ews_err, len(r), _p(r))
+    if rc:
+        raise RSDError(rc, "CALC_LATTICE_INVERSE")
+    return lat
+
+
+# ------------------------------------------------------------------ kernel 1
+def PER_GRPERY_INV_FRI(ctx: Context, p_pos, radii, lattice: Lattice, ews_err, mu_f, correction_method=0):
+    """PER_GRPERY_INV_FRI (src/per_GRPY_YZD.f90:13-200): APP, APQ, AQQ."""
+    pos = _f64(p_pos)
+    r = _f64(radii)
+    N = len(r)
+    APP = np.empty((6 * N, 6 * N), order="F")
+    APQ = np.empty((6 * N, 5 * N), order="F")
+    AQQ = np.empty((5 * N, 5 * N), order="F")
+    ctx.check(_lib.rsd_per_grpery_inv_fri(ctx.h, N, _p(pos), _p(r), ctypes.byref(lattice), ews_err, mu_f,
+                                          correction_method, _p(APP), _p(APQ), _p(AQQ)))
+    return APP, APQ, AQQ
+
+
+def per_grpery_inv_fri_dev(ctx: Context, pos, radii, lattice: Lattice, ews_err, mu_f, out=None, correction_method=0):
+    """Device variant on torch CUDA tensors; returns the whole grmobmx as an
+    (11N, 11N) tensor whose memory is column-major (returned as a transpose
+    view, so indexing [i, j] is the Fortran element (i, j))."""
+    import torch
+    N = radii.shape[0]
+    n = 11 * N
+    buf = out if out is not None else torch.empty((n, n), dtype=torch.float64, device=pos.device)
+    torch.cuda.synchronize(pos.device)
+    ctx.check(_lib.rsd_per_grpery_inv_fri_dev(ctx.h, N, pos.data_ptr(), radii.data_ptr(), ctypes.byref(lattice),
+                                              ews_err, mu_f, correction_method, buf.data_ptr(), n))
+    _sync_ctx(ctx)
+    return buf.t()
+
+
+def _sync_ctx(ctx):
+    import torch
+    s = torch.cuda.ExternalStream(ctx.stream) if hasattr(torch.cuda, "ExternalStream") else None
+    if s is not None:
+        s.synchronize()
+    else:
+        torch.cuda.synchronize()
+
+
+# ------------------------------------------------------------------ kernel 2
+def lubmxcalc(ctx: Context, tab: LubTab, p_pos, radii, lattice: Lattice, mu_f, nb=0, is_period=True):
+    """lubmxcalc (src/hydro_lub.f90:22-308): rfu, rfe, rse and the number
+    of pairs found at s <= 2 (mirrored, like the reference)."""
+    pos = _f64(p_pos)
+    r = _f64(radii)
+    N = len(r)
+    rfu = np.empty((6 * N, 6 * N), order="F")
+    rfe = np.empty((6 * N, 5 * N), order="F")
+    rse = np.empty((5 * N, 5 * N), order="F")
+    nc = ctypes.c_int32(0)
+    ctx.check(_lib.rsd_lubmxcalc(ctx.h, tab.h, N, nb, int(is_period), _p(pos), _p(r),
+                                 ctypes.byref(lattice) if lattice is not None else None, mu_f, _p(rfu), _p(rfe),
+                                 _p(rse), ctypes.byref(nc)))
+    return rfu, rfe, rse, nc.value
+
+
+# ------------------------------------------------------------------ kernel 3
+def MATREV(ctx: Context, A):
+    """MATREV (src/matrices.f90:4-34): SPD inverse; returns (A^-1, info)."""
+    A = np.array(A, dtype=np.float64, order="F", copy=True)
+    info = ctypes.c_int32(0)
+    ctx.check(_lib.rsd_matrev(ctx.h, A.shape[0], _p(A), ctypes.byref(info)))
+    return A, info.value
+
+
+def CHOLESKY(ctx: Context, B):
+    """CHOLESKY (src/matrices.f90:126-157): lower factor, strict upper zero.
+    Raises when B is not positive definite (the reference STOPs)."""
+    B = np.array(B, dtype=np.float64, order="F", copy=True)
+    info = ctypes.c_int32(0)
+    rc = ctx.check(_lib.rsd_cholesky(ctx.h, B.shape[0], _p(B), ctypes.byref(info)))
+    if rc > 0:
+        raise RSDError(rc, "CHOLESKY: leading minor %d is not positive definite" % rc)
+    return B
+
+
+def MobToResist_FTS(ctx: Context, APP, APQ, AQQ):
+    """MobToResist_FTS (src/matrices.f90:393-416)."""
+    N = APP.shape[0] // 6
+    APP, APQ, AQQ = (np.asfortranarray(x, dtype=np.float64) for x in (APP, APQ, AQQ))
+    RPP = np.empty((6 * N, 6 * N), order="F")
+    RPQ = np.empty((6 * N, 5 * N), order="F")
+    RQQ = np.empty((5 * N, 5 * N), order="F")
+    info = ctypes.c_int32(0)
+    ctx.check(_lib.rsd_mob_to_resist_fts(ctx.h, N, _p(APP), _p(APQ), _p(AQQ), _p(RPP), _p(RPQ), _p(RQQ),
+                                         ctypes.byref(info)))
+    return RPP, RPQ, RQQ, info.value
+
+
+def arrangement(ctx: Context, RPP, RPQ, RQQ):
+    """arrangement (src/matrices.f90:432-445): mu = RPQ^T RPP^-1 RPQ - RQQ."""
+    N = RPP.shape[0] // 6
+    RPP, RPQ, RQQ = (np.asfortranarray(x, dtype=np.float64) for x in (RPP, RPQ, RQQ))
+    mu = np.empty((5 * N, 5 * N), order="F")
+    info = ctypes.c_int32(0)
+    ctx.check(_lib.rsd_arrangement(ctx.h, N, _p(RPP), _p(RPQ), _p(RQQ), _p(mu), ctypes.byref(info)))
+    return mu, info.value
+
+
+def STEPPER_NOGmres(ctx: Context, APP, APQ, AQQ, rfu, rfe, rse, Fe, EIN, Fe_inter, conf, u_brown=None):
+    """STEPPER_NOGmres (src/stepper.f90:348-410), FTS path."""
+    N = APP.shape[0] // 6
+    mats = [np.asfortranarray(x, dtype=np.float64) for x in (APP, APQ, AQQ, rfu, rfe, rse)]
+    Fe, EIN, Fe_inter = _f64(Fe), _f64(EIN), _f64(Fe_inter)
+    conf = _f64(conf)
+    ub = _f64(u_brown) if u_brown is not None else None
+    U_par = np.empty(6 * N)
+    Sh, Sfp, Sb = np.empty(5 * N), np.empty(5 * N), np.empty(5 * N)
+    RPP = np.empty((6 * N, 6 * N), order="F")
+    info = ctypes.c_int32(0)
+    ctx.check(_lib.rsd_stepper_nogmres(ctx.h, N, *[_p(m) for m in mats], _p(Fe), _p(EIN), _p(Fe_inter), _p(conf),
+                                       _p(ub) if ub is not None else None, _p(U_par), _p(Sh), _p(Sfp), _p(Sb),
+                                       _p(RPP), ctypes.byref(info)))
+    return dict(U_par=U_par, SijN_hyd=Sh, SijN_FP=Sfp, SijN_B=Sb, RPP=RPP, info=info.value)
+
+
+# ------------------------------------------------------------------ fused step
+def step_params(N, LB, T, dt, gamma, mu_f, ews_err, nb=0, use_lub=True, precision=PREC_FP64, tol=0.0, max_iter=0):
+    p = StepParams()
+    p.nn, p.nb = N, nb
+    for i in range(3):
+        p.LB[i] = LB[i]
+    p.T, p.dt, p.gamma, p.mu_f, p.ews_err = T, dt, gamma, mu_f, ews_err
+    p.use_lub, p.precision, p.tol, p.max_iter = int(use_lub), precision, tol, max_iter
+    return p
+
+
+def STEPPER_Stokesian(ctx: Context, tab: LubTab, conf, radii, T, dt, LB, gamma, mu_f, ews_err, Fe=None,
+                      precision=PREC_FP64, nb=0, use_lub=True, tol=0.0, max_iter=0):
+    """One STEPPER_Stokesian step (src/stepper.f90:33-156) on the periodic FTS
+    path with lubrication.  Returns the advanced configuration, U_pos, the
+    hydrodynamic stresslets SijN_hyd, yeta_mu and the step info."""
+    conf = np.array(conf, dtype=np.float64, order="C", copy=True)
+    r = _f64(radii)
+    N = len(r)
+    p = step_params(N, LB, T, dt, gamma, mu_f, ews_err, nb, use_lub, precision, tol, max_iter)
+    U_pos = np.empty(6 * N)
+    S = np.empty(5 * N)
+    y = np.zeros(5)
+    info = StepInfo()
+    fe = _f64(Fe) if Fe is not None else None
+    rc = _lib.rsd_stepper_stokesian(ctx.h, tab.h if tab is not None else None, ctypes.byref(p), _p(conf), _p(r),
+                                    _p(fe) if fe is not None else None, _p(U_pos), _p(S), _p(y), ctypes.byref(info))
+    ctx.check(rc)
+    return dict(conf=conf, U_pos=U_pos, SijN=S, yeta_mu=y, info=info, rc=rc)
+
+
+def stepper_stokesian_dev(ctx: Context, tab: LubTab, conf_t, radii_t, T, dt, LB, gamma, mu_f, ews_err, U_pos_t, S_t,
+                          Fe_t=None, precision=PREC_FP64, nb=0, use_lub=True, tol=0.0, max_iter=0):
+    """Device-resident step on torch CUDA tensors (conf_t advanced in place)."""
+    N = radii_t.shape[0]
+    p = step_params(N, LB, T, dt, gamma, mu_f, ews_err, nb, use_lub, precision, tol, max_iter)
+    y = np.zeros(5)
+    info = StepInfo()
+    rc = _lib.rsd_stepper_stokesian_dev(ctx.h, tab.h if tab is not None else None, ctypes.byref(p),
+                                        conf_t.data_ptr(), radii_t.data_ptr(),
+                                        Fe_t.data_ptr() if Fe_t is not None else None, U_pos_t.data_ptr(),
+                                        S_t.data_ptr(), _p(y), ctypes.byref(info))
+    ctx.check(rc)
+    return y, info
+
+
+def mu_f_dimensionless(mu_f_in=1.0):
+    """mu_f after dimentionless_calc/translate (src/mymodules.f90:816,846)."""
+    return mu_f_in * (1.0 / PAI / mu_f_in)
+
+
+def lubdat_dir():
+    """The committed copy of the reference's lubrication tables."""
+    return os.path.join(os.path.dirname(HERE), "tests", "golden", "lubdat")
+
+
+from . import configs  # noqa: E402,F401

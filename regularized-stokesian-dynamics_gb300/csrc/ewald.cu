@@ -1,0 +1,324 @@
+// Kernel 1: Ewald-summed periodic grand mobility (PER_GRPERY_INV_FRI,
+// src/per_GRPY_YZD.f90:13-200, with PER_ROTNE_PRAGER_SELF/IJ of
+// src/Ewald_summation.f90:19-423).
+//
+// Layout: the grand mobility M (11N x 11N, column-major, leading dimension
+// ldm) in the reference's order: rows/cols 3a..3a+2 translation of particle
+// a, 3N+3a.. rotation, 6N+5a.. stresslet (Y2 basis).
+//
+// Work split (thread per unordered pair a < b):
+//   ewald_ktable      per reciprocal vector k (half space k > 0): the
+//                     radius-independent weights S(k) k^alpha of the cos and
+//                     sin moments (pair independent, computed once per call)
+//   ewald_trig        per (k, particle): cos(k.x_a), sin(k.x_a), so that
+//                     cos(k.R_ab) = c_a c_b + s_a s_b needs no sincos per pair
+//   ewald_pair_k      per pair: reciprocal moments over the half space (x2),
+//                     epilogue, writes both 11x11 blocks of the pair
+//   ewald_pair_real   per pair: real-space moments over the image cube,
+//                     epilogue, adds into both blocks
+//   ewald_self        per particle: self block (images n != 0, k != 0, and
+//                     the analytic terms of PER_ROTNE_PRAGER_SELF 179-188)
+// The closed forms come from ewald_gen.cuh (generated by gen_ewald.py).
+#include <cuda_runtime.h>
+
+#include "ewald_gen.cuh"
+#include "rsd_internal.cuh"
+
+namespace {
+
+constexpr int KW = 3 + RSD_NMOM_KCOS + RSD_NMOM_KSIN;  // doubles per k entry
+
+__host__ __device__ inline void half_space_index(int h, int NI, int* nx, int* ny, int* nz) {
+  const int w = 2 * NI + 1;
+  const int q = (w * w * w - 1) / 2 + 1 + h;  // entries after the origin
+  *nx = q / (w * w) - NI;
+  *ny = (q / w) % w - NI;
+  *nz = q % w - NI;
+}
+
+// S(k) of F_Jk (Ewald_summation.f90:1067-1071): F_Jk = S (delta k^2 - k k)
+template <typename T>
+__device__ inline T kernel_S(T k2, T lam) {
+  const T l2 = lam * lam;
+  return T(8.0 * RSD_PI) * (T(1) + k2 / (T(4) * l2) + k2 * k2 / (T(8) * l2 * l2)) * exp(-k2 / (T(4) * l2)) / (k2 * k2);
+}
+
+__global__ void ewald_ktable(rsd_lat_dev L, int Kh, double* __restrict__ tab) {
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= Kh) return;
+  int nx, ny, nz;
+  half_space_index(h, L.NI, &nx, &ny, &nz);
+  double k[3];
+  for (int j = 0; j < 3; j++)
+    k[j] = 2.0 * RSD_PI * (nx * L.LI[0 + 3 * j] + ny * L.LI[1 + 3 * j] + nz * L.LI[2 + 3 * j]);
+  const double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+  const double S = kernel_S<double>(k2, L.lam);
+  double* e = tab + (size_t)h * KW;
+  e[0] = k[0];
+  e[1] = k[1];
+  e[2] = k[2];
+  rsd_kcos_weights<double>(k[0], k[1], k[2], S, L.lam, e + 3);
+  rsd_ksin_weights<double>(k[0], k[1], k[2], S, L.lam, e + 3 + RSD_NMOM_KCOS);
+}
+
+__global__ void ewald_trig(int nn, int Kh, const double* __restrict__ tab, const double* __restrict__ pos,
+                           double2* __restrict__ cs) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int h = blockIdx.y;
+  if (a >= nn) return;
+  const double* e = tab + (size_t)h * KW;
+  const double kr = e[0] * pos[3 * a] + e[1] * pos[3 * a + 1] + e[2] * pos[3 * a + 2];
+  double s, c;
+  sincos(kr, &s, &c);
+  cs[(size_t)h * nn + a] = make_double2(c, s);
+}
+
+// Scatter of the pair block (a,b), a < b, and its mirror (b,a) with
+// b -> -b, g -> -g (per_GRPY_YZD.f90:123-151,160-188).  v holds the 60
+// unique values (order of gen_ewald.py) already scaled; add != 0 adds.
+__device__ inline void store_pair(double* __restrict__ M, int64_t ld, int N, int a, int b, const double* v, int add) {
+  auto put = [&](int r, int c, double x) {
+    double* p = M + (int64_t)r + (int64_t)c * ld;
+    *p = add ? *p + x : x;
+  };
+  const int sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      const double tt = v[sym[i][j]], rr = v[6 + sym[i][j]];
+      double tr = 0.0;
+      if (i < j) tr = v[12 + (i == 0 ? j - 1 : 2)];
+      if (i > j) tr = -v[12 + (j == 0 ? i - 1 : 2)];
+      put(3 * a + i, 3 * b + j, tt);
+      put(3 * b + i, 3 * a + j, tt);
+      put(3 * N + 3 * a + i, 3 * N + 3 * b + j, rr);
+      put(3 * N + 3 * b + i, 3 * N + 3 * a + j, rr);
+      put(3 * a + i, 3 * N + 3 * b + j, tr);
+      put(3 * N + 3 * b + j, 3 * a + i, tr);
+      put(3 * b + i, 3 * N + 3 * a + j, -tr);
+      put(3 * N + 3 * a + j, 3 * b + i, -tr);
+    }
+  for (int i = 0; i < 3; i++)
+    for (int m = 0; m < 5; m++) {
+      const double g = v[30 + 5 * i + m], h = v[45 + 5 * i + m];
+      put(3 * a + i, 6 * N + 5 * b + m, g);
+      put(3 * N + 3 * a + i, 6 * N + 5 * b + m, h);
+      put(6 * N + 5 * b + m, 3 * a + i, g);
+      put(6 * N + 5 * b + m, 3 * N + 3 * a + i, h);
+      put(3 * b + i, 6 * N + 5 * a + m, -g);
+      put(3 * N + 3 * b + i, 6 * N + 5 * a + m, h);
+      put(6 * N + 5 * a + m, 3 * b + i, -g);
+      put(6 * N + 5 * a + m, 3 * N + 3 * b + i, h);
+    }
+  int q = 15;
+  double qq[5][5];
+  for (int x = 0; x < 5; x++)
+    for (int y = x; y < 5; y++) qq[x][y] = qq[y][x] = v[q++];
+  for (int x = 0; x < 5; x++)
+    for (int y = 0; y < 5; y++) {
+      put(6 * N + 5 * a + x, 6 * N + 5 * b + y, qq[x][y]);
+      put(6 * N + 5 * b + x, 6 * N + 5 * a + y, qq[x][y]);
+    }
+}
+
+// scale by nondim (1/(6 a_i) for TT, TR, G; 1/(6 a_i^3) for RR, QQ, H) and
+// by 1/(pi mu_f)
+__device__ inline void scale_block(double* v, double ai, double inv_pimu) {
+  const double na = inv_pimu / (6.0 * ai), na3 = inv_pimu / (6.0 * ai * ai * ai);
+  for (int q = 0; q < 60; q++) {
+    const bool a3 = (q >= 6 && q < 12) || (q >= 15 && q < 30) || q >= 45;
+    v[q] *= a3 ? na3 : na;
+  }
+}
+
+__device__ inline bool pair_of(int nn, int* a, int* b) {
+  *a = blockIdx.x * blockDim.x + threadIdx.x;
+  *b = blockIdx.y * blockDim.y + threadIdx.y;
+  return *a < nn && *b < nn && *a < *b;
+}
+
+__global__ void __launch_bounds__(128) ewald_pair_k(int nn, rsd_lat_dev L, int Kh, const double* __restrict__ tab,
+                                                    const double2* __restrict__ cs, const double* __restrict__ radii,
+                                                    double inv_pimu, double* __restrict__ M, int64_t ldm) {
+  int a, b;
+  if (!pair_of(nn, &a, &b)) return;
+  double ac[RSD_NMOM_KCOS], as[RSD_NMOM_KSIN];
+#pragma unroll
+  for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] = 0.0;
+#pragma unroll
+  for (int m = 0; m < RSD_NMOM_KSIN; m++) as[m] = 0.0;
+  for (int h = 0; h < Kh; h++) {
+    const double2 ua = cs[(size_t)h * nn + a], ub = cs[(size_t)h * nn + b];
+    const double c = ua.x * ub.x + ua.y * ub.y;  // cos(k.(x_a - x_b))
+    const double s = ua.y * ub.x - ua.x * ub.y;  // sin(k.(x_a - x_b))
+    const double* e = tab + (size_t)h * KW + 3;
+#pragma unroll
+    for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] = fma(__ldg(e + m), c, ac[m]);
+#pragma unroll
+    for (int m = 0; m < RSD_NMOM_KSIN; m++) as[m] = fma(__ldg(e + RSD_NMOM_KCOS + m), s, as[m]);
+  }
+  const double ai = radii[a], aj = radii[b], phix = L.phix;
+  double v[60], w[60];
+  rsd_kcos_epilogue<double>(ac, ai, aj, phix, v);
+  rsd_ksin_epilogue<double>(as, ai, aj, phix, w);
+  const double f = 2.0 / L.LV;  // half space counted twice
+#pragma unroll
+  for (int q = 0; q < 60; q++) v[q] = (v[q] + w[q]) * f;
+  scale_block(v, ai, inv_pimu);
+  store_pair(M, ldm, nn, a, b, v, 0);
+}
+
+__global__ void __launch_bounds__(128) ewald_pair_real(int nn, rsd_lat_dev L, const double* __restrict__ pos,
+                                                       const double* __restrict__ radii, double inv_pimu,
+                                                       double* __restrict__ M, int64_t ldm) {
+  int a, b;
+  if (!pair_of(nn, &a, &b)) return;
+  double R[3] = {pos[3 * a] - pos[3 * b], pos[3 * a + 1] - pos[3 * b + 1], pos[3 * a + 2] - pos[3 * b + 2]};
+  double dmin;
+  rsd_skew_correction(L.LR, L.LI, R, &dmin);
+  double acc[RSD_NMOM_REAL];
+#pragma unroll
+  for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = 0.0;
+  const double lam = L.lam, lam2 = lam * lam, cd = 2.0 * RSD_PIP5 * lam;
+  const int NR = L.NR;
+  for (int nx = -NR; nx <= NR; nx++)
+    for (int ny = -NR; ny <= NR; ny++) {
+      double x0 = R[0] + L.LR[0] * nx + L.LR[3] * ny - L.LR[6] * NR;
+      double x1 = R[1] + L.LR[1] * nx + L.LR[4] * ny - L.LR[7] * NR;
+      double x2 = R[2] + L.LR[2] * nx + L.LR[5] * ny - L.LR[8] * NR;
+      for (int nz = -NR; nz <= NR; nz++) {
+        const double r2 = x0 * x0 + x1 * x1 + x2 * x2;
+        const double r = sqrt(r2), ir = 1.0 / r;
+        const double E0 = erfc(lam * r), Ed = cd * exp(-r2 * lam2);
+        rsd_real_image<double>(x0, x1, x2, r, ir, E0, Ed, lam, acc);
+        x0 += L.LR[6];
+        x1 += L.LR[7];
+        x2 += L.LR[8];
+      }
+    }
+  double v[60];
+  rsd_real_epilogue<double>(acc, radii[a], radii[b], L.phix, v);
+  scale_block(v, radii[a], inv_pimu);
+  store_pair(M, ldm, nn, a, b, v, 1);
+}
+
+__global__ void __launch_bounds__(64) ewald_self(int nn, rsd_lat_dev L, int Kh, const double* __restrict__ tab,
+                                                 const double* __restrict__ radii, double inv_pimu,
+                                                 double* __restrict__ M, int64_t ldm) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nn) return;
+  const double ai = radii[a], lam = L.lam, lam2 = lam * lam, cd = 2.0 * RSD_PIP5 * lam;
+  double v[60], w[60];
+  {
+    double acc[RSD_NMOM_REAL];
+    for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = 0.0;
+    const int NR = L.NR;
+    for (int nx = -NR; nx <= NR; nx++)
+      for (int ny = -NR; ny <= NR; ny++)
+        for (int nz = -NR; nz <= NR; nz++) {
+          if (!nx && !ny && !nz) continue;  // PER_ROTNE_PRAGER_SELF 61
+          const double x0 = L.LR[0] * nx + L.LR[3] * ny + L.LR[6] * nz;
+          const double x1 = L.LR[1] * nx + L.LR[4] * ny + L.LR[7] * nz;
+          const double x2 = L.LR[2] * nx + L.LR[5] * ny + L.LR[8] * nz;
+          const double r2 = x0 * x0 + x1 * x1 + x2 * x2, r = sqrt(r2);
+          rsd_real_image<double>(x0, x1, x2, r, 1.0 / r, erfc(lam * r), cd * exp(-r2 * lam2), lam, acc);
+        }
+    rsd_real_epilogue<double>(acc, ai, ai, L.phix, v);
+  }
+  {
+    double ac[RSD_NMOM_KCOS];
+    for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] = 0.0;
+    for (int h = 0; h < Kh; h++) {
+      const double* e = tab + (size_t)h * KW + 3;
+      for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] += __ldg(e + m);
+    }
+    rsd_kcos_epilogue<double>(ac, ai, ai, L.phix, w);
+  }
+  // analytic self terms (Ewald_summation.f90:179-188)
+  const double sp = sqrt(RSD_PI), a3 = ai * ai * ai, l3 = lam * lam * lam;
+  const double ttsr = 1.0 - 6.0 * lam / sp * ai + 40.0 / 3.0 / sp * l3 * a3 * L.phix;
+  const double rrsr = 0.75 - 10.0 / sp * a3 * l3;
+  const double qqsr = 0.9 - l3 * a3 / 25.0 / sp * (50.0 - 126.0 * lam * lam * ai * ai) * 6.0;
+  for (int q = 0; q < 60; q++) v[q] += w[q] * (2.0 / L.LV);
+  v[0] += ttsr;
+  v[3] += ttsr;
+  v[5] += ttsr;
+  v[6] += rrsr;
+  v[9] += rrsr;
+  v[11] += rrsr;
+  const int dq[5] = {15, 20, 24, 27, 29};  // QQ diagonal in the upper-triangle order
+  for (int x = 0; x < 5; x++) v[dq[x]] += qqsr;
+  scale_block(v, ai, inv_pimu);
+  // diagonal block: TT, RR, QQ; TR, G, H are zero (per_GRPY_YZD.f90:63-66)
+  const int N = nn;
+  const int sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      M[(3 * a + i) + (int64_t)(3 * a + j) * ldm] = v[sym[i][j]];
+      M[(3 * N + 3 * a + i) + (int64_t)(3 * N + 3 * a + j) * ldm] = v[6 + sym[i][j]];
+      M[(3 * a + i) + (int64_t)(3 * N + 3 * a + j) * ldm] = 0.0;
+      M[(3 * N + 3 * a + j) + (int64_t)(3 * a + i) * ldm] = 0.0;
+    }
+  for (int i = 0; i < 3; i++)
+    for (int m = 0; m < 5; m++) {
+      M[(3 * a + i) + (int64_t)(6 * N + 5 * a + m) * ldm] = 0.0;
+      M[(3 * N + 3 * a + i) + (int64_t)(6 * N + 5 * a + m) * ldm] = 0.0;
+      M[(6 * N + 5 * a + m) + (int64_t)(3 * a + i) * ldm] = 0.0;
+      M[(6 * N + 5 * a + m) + (int64_t)(3 * N + 3 * a + i) * ldm] = 0.0;
+    }
+  int q = 15;
+  double qq[5][5];
+  for (int x = 0; x < 5; x++)
+    for (int y = x; y < 5; y++) qq[x][y] = qq[y][x] = v[q++];
+  for (int x = 0; x < 5; x++)
+    for (int y = 0; y < 5; y++) M[(6 * N + 5 * a + x) + (int64_t)(6 * N + 5 * a + y) * ldm] = qq[x][y];
+}
+
+__global__ void overlap_count(int nn, rsd_lat_dev L, const double* __restrict__ pos, const double* __restrict__ radii,
+                              int* __restrict__ count) {
+  int a, b;
+  if (!pair_of(nn, &a, &b)) return;
+  double R[3] = {pos[3 * a] - pos[3 * b], pos[3 * a + 1] - pos[3 * b + 1], pos[3 * a + 2] - pos[3 * b + 2]};
+  double d;
+  rsd_skew_correction(L.LR, L.LI, R, &d);
+  if (d <= radii[a] + radii[b]) atomicAdd(count, 1);
+}
+
+}  // namespace
+
+int rsd_count_overlaps(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
+                       int* count) {
+  rsd_lat_dev L = rsd_lat_pack(lat);
+  int* d = (int*)rsd_scratch(ctx, "overlap_count", sizeof(int));
+  if (!d) return RSD_ENOMEM;
+  RSD_CUDA(ctx, cudaMemsetAsync(d, 0, sizeof(int), ctx->stream));
+  dim3 blk(32, 4), grd((nn + 31) / 32, (nn + 3) / 4);
+  overlap_count<<<grd, blk, 0, ctx->stream>>>(nn, L, d_pos, d_radii, d);
+  RSD_CUDA(ctx, cudaGetLastError());
+  RSD_CUDA(ctx, cudaMemcpyAsync(count, d, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  RSD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return RSD_OK;
+}
+
+int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
+                       double mu_f, int precision, double* d_M, int64_t ldm) {
+  (void)precision;
+  if (nn < 1 || ldm < 11LL * nn) return rsd_fail(ctx, RSD_EARG, "bad size nn=%d ldm=%lld", nn, (long long)ldm);
+  rsd_lat_dev L = rsd_lat_pack(lat);
+  const int w = 2 * L.NI + 1;
+  const int Kh = (w * w * w - 1) / 2;
+  double* tab = (double*)rsd_scratch(ctx, "ewald_ktab", sizeof(double) * (size_t)Kh * KW);
+  double2* cs = (double2*)rsd_scratch(ctx, "ewald_trig", sizeof(double2) * (size_t)Kh * nn);
+  if (!tab || !cs) return RSD_ENOMEM;
+  const double inv_pimu = 1.0 / (RSD_PI * mu_f);
+  cudaStream_t s = ctx->stream;
+  ewald_ktable<<<(Kh + 127) / 128, 128, 0, s>>>(L, Kh, tab);
+  ewald_trig<<<dim3((nn + 127) / 128, Kh), 128, 0, s>>>(nn, Kh, tab, d_pos, cs);
+  ewald_self<<<(nn + 63) / 64, 64, 0, s>>>(nn, L, Kh, tab, d_radii, inv_pimu, d_M, ldm);
+  if (nn > 1) {
+    dim3 blk(32, 4), grd((nn + 31) / 32, (nn + 3) / 4);
+    ewald_pair_k<<<grd, blk, 0, s>>>(nn, L, Kh, tab, cs, d_radii, inv_pimu, d_M, ldm);
+    ewald_pair_real<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, d_M, ldm);
+  }
+  RSD_CUDA(ctx, cudaGetLastError());
+  return RSD_OK;
+}

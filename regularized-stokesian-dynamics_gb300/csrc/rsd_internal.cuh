@@ -1,0 +1,119 @@
+// Internal declarations shared by the CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <map>
+#include <string>
+
+#include "../../include/rsd_capi.h"
+
+#define RSD_PI 3.141592653589793238462643383279502884
+#define RSD_PIP5 0.564189583547756286948079451560772585844
+
+struct rsd_buf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct rsd_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::map<std::string, rsd_buf> bufs;  // grow-only device buffers by name
+  cudaEvent_t ev[8] = {};
+  double phase_ms[4] = {0, 0, 0, 0};
+  int* d_info = nullptr;  // device-side status words
+  int* h_info = nullptr;  // pinned mirror
+};
+
+struct rsd_lubtab {
+  int nabc = 0, ngh = 0, nm = 0;
+  double abc[64 * 11];
+  double gh[64 * 7];
+  double m[64 * 4];
+  // device copy, per device ordinal (small; uploaded on first use)
+  std::map<int, double*> dev;
+};
+
+// Error helpers: record a message in the context and return a status.
+int rsd_fail(rsd_ctx* ctx, int code, const char* fmt, ...);
+int rsd_cuda_check(rsd_ctx* ctx, cudaError_t e, const char* what);
+#define RSD_CUDA(ctx, call)                                   \
+  do {                                                        \
+    cudaError_t _e = (call);                                  \
+    if (_e != cudaSuccess) return rsd_cuda_check(ctx, _e, #call); \
+  } while (0)
+#define RSD_TRY(call)        \
+  do {                       \
+    int _rc = (call);        \
+    if (_rc != 0) return _rc; \
+  } while (0)
+
+// Grow-only named device buffer; returns nullptr (and sets ctx->err) on
+// allocation failure.
+void* rsd_scratch(rsd_ctx* ctx, const char* name, size_t bytes);
+int rsd_set_device(rsd_ctx* ctx);
+
+// ------------------------------------------------------------ lattice
+struct rsd_lat_dev {
+  double LR[9], LI[9], LV, lam, phix;
+  int NR, NI;
+};
+rsd_lat_dev rsd_lat_pack(const rsd_lattice* lat);
+
+// PER_SKEW_CORRECTION (src/csd_post.f90:24-63): minimum image in the
+// skewed lattice, testing the 8 corner shifts like the reference.
+__host__ __device__ inline void rsd_skew_correction(const double* LR, const double* LI, double R[3], double* dmin) {
+  double X[3], RC[3], RMIN[3];
+  for (int i = 0; i < 3; i++) X[i] = LI[i] * R[0] + LI[i + 3] * R[1] + LI[i + 6] * R[2];
+  for (int i = 0; i < 3; i++) {
+    X[i] = fmod(X[i], 1.0);
+    if (X[i] < 0.0) X[i] = X[i] + 1.0;
+  }
+  for (int i = 0; i < 3; i++) RC[i] = LR[i] * X[0] + LR[i + 3] * X[1] + LR[i + 6] * X[2];
+  double D0 = RC[0] * RC[0] + RC[1] * RC[1] + RC[2] * RC[2];
+  for (int i = 0; i < 3; i++) RMIN[i] = RC[i];
+  for (int m = 1; m < 8; m++) {
+    const double M0 = (m >> 2) & 1, M1 = (m >> 1) & 1, M2 = m & 1;
+    double d = 0.0, RL[3];
+    for (int i = 0; i < 3; i++) RL[i] = LR[i] * M0 + LR[i + 3] * M1 + LR[i + 6] * M2;
+    for (int i = 0; i < 3; i++) d += (RC[i] - RL[i]) * (RC[i] - RL[i]);
+    if (d < D0) {
+      D0 = d;
+      for (int i = 0; i < 3; i++) RMIN[i] = RC[i] - RL[i];
+    }
+  }
+  for (int i = 0; i < 3; i++) R[i] = RMIN[i];
+  *dmin = sqrt(D0);
+}
+
+// ------------------------------------------------------------ kernels
+// Ewald (ewald.cu)
+int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
+                       double mu_f, int precision, double* d_M, int64_t ldm);
+int rsd_count_overlaps(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
+                       int* count);
+// Lubrication (lub.cu)
+int rsd_lub_assemble(rsd_ctx* ctx, const rsd_lubtab* tab, int nn, int nb, int is_period, const double* d_pos,
+                     const double* d_radii, const rsd_lattice* lat, double mu_f, double* d_L, int64_t ldl,
+                     int accumulate, int* n_contact);
+// Dense linear algebra (dense.cu)
+int rsd_potrf_upper(rsd_ctx* ctx, int n, double* d_A, int64_t lda, int* info);
+int rsd_potri_upper(rsd_ctx* ctx, int n, double* d_A, int64_t lda);  // after potrf; result upper
+int rsd_mirror_upper(rsd_ctx* ctx, int n, double* d_A, int64_t lda);
+int rsd_trsv_upper(rsd_ctx* ctx, int n, const double* d_U, int64_t ldu, double* d_X, int64_t ldx, int nrhs,
+                   int transpose);
+// Tagged variants: the diagonal-block inverses of a factorisation are kept
+// in a scratch buffer named by `tag`, so two factorisations can coexist.
+int rsd_potrf_upper_tag(rsd_ctx* ctx, int n, double* d_A, int64_t lda, int* info, const char* tag);
+int rsd_potri_upper_tag(rsd_ctx* ctx, int n, double* d_A, int64_t lda, const char* tag);
+int rsd_potrs_upper_tag(rsd_ctx* ctx, int n, const double* d_U, int64_t ldu, double* d_X, int64_t ldx, int nrhs,
+                        const char* tag);
+void rsd_gemm_f64(cudaStream_t s, int m, int n, int k, double alpha, const double* A, int64_t lda, int ta,
+                  const double* B, int64_t ldb, int tb, double beta, double* C, int64_t ldc);
+int rsd_zero_lower(rsd_ctx* ctx, int n, double* d_A, int64_t lda);
+// A(rows x cols) += B, both column-major sub-blocks (step.cu)
+int rsd_axpy_block(rsd_ctx* ctx, int64_t rows, int64_t cols, const double* B, int64_t ldb, double* A, int64_t lda);
