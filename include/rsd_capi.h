@@ -66,6 +66,9 @@ void* rsd_ctx_stream(rsd_ctx* ctx);
 /* Device-time of the last call's phases in milliseconds (assembly, lub,
  * solve, update), measured with CUDA events on the context stream. */
 int rsd_ctx_phase_ms(const rsd_ctx* ctx, double ms[4]);
+/* Diagnostic (no counterpart in the reference): kernel launches issued by
+ * this library since it was loaded, over all contexts. */
+long long rsd_launch_count(void);
 
 /* ---------------------------------------------------------------- lattice */
 /* SET_LATTICE_SKEW (src/csd_post.f90:105-136) with MAT_INV3

@@ -70,6 +70,7 @@ _sig("rsd_ctx_destroy", _i, [_vp])
 _sig("rsd_ctx_last_error", ctypes.c_char_p, [_vp])
 _sig("rsd_ctx_stream", _vp, [_vp])
 _sig("rsd_ctx_phase_ms", _i, [_vp, _dp])
+_sig("rsd_launch_count", ctypes.c_longlong, [])
 _sig("rsd_set_lattice_skew", _i, [_d, _dp, _d, _i32, _d, _d, _LP])
 _sig("rsd_calc_lattice_inverse", _i, [_LP, _d, _i32, _dp])
 _sig("rsd_per_grpery_inv_fri", _i, [_vp, _i32, _dp, _dp, _LP, _d, _d, _i32, _dp, _dp, _dp])

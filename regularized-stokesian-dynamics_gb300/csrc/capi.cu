@@ -11,6 +11,9 @@
 
 #include "rsd_internal.cuh"
 
+std::atomic<long long> rsd_launches{0};
+extern "C" long long rsd_launch_count(void) { return rsd_launches.load(); }
+
 // ------------------------------------------------------------ errors
 int rsd_fail(rsd_ctx* ctx, int code, const char* fmt, ...) {
   if (ctx) {

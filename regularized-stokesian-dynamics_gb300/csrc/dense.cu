@@ -1,20 +1,25 @@
-// Kernel 3: dense SPD factorisation and inverse for the grand resistance
-// (MATREV, src/matrices.f90:4-34, which calls LAPACK DPOTRF('U') and
-// DPOTRI('U') and mirrors the upper triangle).  Column-major throughout.
+// Kernel 3: dense SPD factorisation, inverse and solves for the grand
+// resistance (MATREV, src/matrices.f90:4-34, which calls LAPACK DPOTRF('U')
+// and DPOTRI('U') and mirrors the upper triangle).  Column-major throughout,
+// templated on the element type: FP64 for the plain form, FP32 for the
+// factorisations of the mixed form.
 //
-//   rsd_potrf_upper   blocked right-looking Cholesky A = U^T U: per block
-//                     column one CTA factors the nb x nb diagonal block in
-//                     shared memory and inverts it (W = U_jj^-1); the panel
-//                     solve is W^T * panel and the trailing update a
-//                     symmetric rank-nb GEMM on the upper tiles only.
-//   rsd_potri_upper   A^-1 = U^-1 U^-T: blocked triangular inverse (each
-//                     step two GEMMs, the first skipping the zero triangle)
-//                     then the in-place product U^-1 U^-T by column blocks.
-//   rsd_trsv_upper    U^T y = b and U x = y for a few right-hand sides,
-//                     using the stored diagonal-block inverses.
-// The GEMM is one templated SIMT kernel (FP64 here; the FP32 instance
-// serves the mixed-precision path).
+//   potrf_upper   blocked right-looking Cholesky A = U^T U: per block column
+//                 one CTA factors the nb x nb diagonal block in shared memory
+//                 and inverts it (W = U_jj^-1); the panel solve is W^T * panel
+//                 and the trailing update a symmetric rank-nb GEMM on the
+//                 upper tiles only.
+//   potri_upper   A^-1 = U^-1 U^-T: blocked triangular inverse (two GEMMs per
+//                 step, the first skipping the zero triangle), then the
+//                 in-place product U^-1 U^-T by column blocks.
+//   potrs_upper   U^T y = b, U x = y for a few right-hand sides: right-looking
+//                 block substitution (diagonal blocks by their inverses, the
+//                 updates as wide GEMVs).
+//   gemv          y = alpha op(A) X + beta y for 1..4 columns, split over k
+//                 with a fixed-order second pass (deterministic).
 #include <cuda_runtime.h>
+
+#include <string>
 
 #include "rsd_internal.cuh"
 
@@ -58,7 +63,6 @@ __global__ void __launch_bounds__(256) gemm_kernel(GemmP g) {
 #pragma unroll
     for (int j = 0; j < TN; j++) acc[i][j] = T(0);
   for (int k0 = kbeg; k0 < kend; k0 += BK) {
-    // A tile: op(A)(row0+i, k0+p)
     if (!g.ta) {
       for (int e = t; e < BM * BK; e += 256) {
         const int i = e % BM, p = e / BM, gr = row0 + i, gk = k0 + p;
@@ -70,7 +74,6 @@ __global__ void __launch_bounds__(256) gemm_kernel(GemmP g) {
         As[p][i] = (gr < g.m && gk < kend) ? A[gk + (int64_t)gr * g.lda] : T(0);
       }
     }
-    // B tile: op(B)(k0+p, col0+c)
     if (!g.tb) {
       for (int e = t; e < BN * BK; e += 256) {
         const int p = e % BK, c = e / BK, gc = col0 + c, gk = k0 + p;
@@ -111,11 +114,23 @@ __global__ void __launch_bounds__(256) gemm_kernel(GemmP g) {
     }
 }
 
-template <typename T, int BM, int BN, int BK>
+template <typename T>
+struct Tile;
+template <>
+struct Tile<double> {
+  static constexpr int BM = 64, BN = 64, BK = 16;
+};
+template <>
+struct Tile<float> {
+  static constexpr int BM = 128, BN = 128, BK = 16;
+};
+
+template <typename T>
 void launch_gemm(cudaStream_t s, const GemmP& g) {
   if (g.m <= 0 || g.n <= 0) return;
+  constexpr int BM = Tile<T>::BM, BN = Tile<T>::BN, BK = Tile<T>::BK;
   dim3 grd((g.m + BM - 1) / BM, (g.n + BN - 1) / BN);
-  gemm_kernel<T, BM, BN, BK><<<grd, 256, 0, s>>>(g);
+  gemm_kernel<T, BM, BN, BK><<<grd, 256, 0, s>>>(g); RSD_LAUNCH_NOTE();
 }
 
 GemmP gp(int m, int n, int k, double alpha, const void* A, int64_t lda, int ta, const void* B, int64_t ldb, int tb,
@@ -137,40 +152,41 @@ GemmP gp(int m, int n, int k, double alpha, const void* A, int64_t lda, int ta, 
   return g;
 }
 
+constexpr int NB = 128;  // block size of the blocked factorisations
+
 // One CTA: Cholesky (upper) of the jb x jb diagonal block in shared memory,
 // then W = U^-1 (upper, zero below).  info: first failing global index + 1.
-__global__ void __launch_bounds__(256) potf2_upper_inv(double* __restrict__ A, int64_t lda, int jb,
-                                                       double* __restrict__ W, int ldw, int* __restrict__ info,
-                                                       int j0) {
-  extern __shared__ double sm[];
-  double* S = sm;             // jb x jb, column-major, ld = jb
-  double* col = sm + jb * jb;  // scratch column
+template <typename T>
+__global__ void __launch_bounds__(256) potf2_upper_inv(T* __restrict__ A, int64_t lda, int jb, T* __restrict__ W,
+                                                       int ldw, int* __restrict__ info, int j0) {
+  extern __shared__ unsigned char smraw[];
+  T* S = (T*)smraw;      // jb x jb, column-major, ld = jb
+  T* col = S + jb * jb;  // scratch column
   __shared__ int failed;
   const int t = threadIdx.x;
   for (int e = t; e < jb * jb; e += blockDim.x) {
     const int i = e % jb, j = e / jb;
-    S[e] = (i <= j) ? A[i + (int64_t)j * lda] : 0.0;
+    S[e] = (i <= j) ? A[i + (int64_t)j * lda] : T(0);
   }
   if (t == 0) failed = 0;
   __syncthreads();
   for (int k = 0; k < jb; k++) {
     if (t == 0) {
-      const double d = S[k + k * jb];
-      if (!(d > 0.0) || !isfinite(d)) {
+      const T d = S[k + k * jb];
+      if (!(d > T(0)) || !isfinite(d)) {
         failed = 1;
-        if (atomicCAS(info, 0, j0 + k + 1) == 0) {
-        }
+        atomicCAS(info, 0, j0 + k + 1);
       } else {
         S[k + k * jb] = sqrt(d);
       }
     }
     __syncthreads();
     if (failed) break;
-    const double dk = S[k + k * jb];
+    const T dk = S[k + k * jb];
     for (int j = k + 1 + t; j < jb; j += blockDim.x) S[k + j * jb] /= dk;
     __syncthreads();
     for (int j = k + 1 + t; j < jb; j += blockDim.x) {
-      const double skj = S[k + j * jb];
+      const T skj = S[k + j * jb];
       for (int i = k + 1; i <= j; i++) S[i + j * jb] -= S[k + i * jb] * skj;
     }
     __syncthreads();
@@ -181,14 +197,13 @@ __global__ void __launch_bounds__(256) potf2_upper_inv(double* __restrict__ A, i
   }
   __syncthreads();
   if (failed) {
-    for (int e = t; e < jb * jb; e += blockDim.x) W[(e % jb) + (int64_t)(e / jb) * ldw] = 0.0;
+    for (int e = t; e < jb * jb; e += blockDim.x) W[(e % jb) + (int64_t)(e / jb) * ldw] = T(0);
     return;
   }
-  // in-place upper triangular inverse, column by column
   for (int j = 0; j < jb; j++) {
-    const double wjj = 1.0 / S[j + j * jb];
+    const T wjj = T(1) / S[j + j * jb];
     for (int i = t; i < j; i += blockDim.x) {
-      double s = 0.0;
+      T s = T(0);
       for (int p = i; p < j; p++) s += S[i + p * jb] * S[p + j * jb];
       col[i] = -s * wjj;
     }
@@ -199,96 +214,274 @@ __global__ void __launch_bounds__(256) potf2_upper_inv(double* __restrict__ A, i
   }
   for (int e = t; e < jb * jb; e += blockDim.x) {
     const int i = e % jb, j = e / jb;
-    W[i + (int64_t)j * ldw] = (i <= j) ? S[e] : 0.0;
+    W[i + (int64_t)j * ldw] = (i <= j) ? S[e] : T(0);
   }
 }
 
-__global__ void zero_lower_k(int n, double* __restrict__ A, int64_t lda) {
+// Inverses of all diagonal blocks of an upper triangular U (one CTA each).
+template <typename T>
+__global__ void __launch_bounds__(256) trtri_diag(int n, const T* __restrict__ U, int64_t ldu, T* __restrict__ W) {
+  extern __shared__ unsigned char smraw[];
+  T* S = (T*)smraw;
+  T* col = S + NB * NB;
+  const int b = blockIdx.x, j0 = b * NB, jb = min(NB, n - j0), t = threadIdx.x;
+  const T* Ub = U + j0 + (int64_t)j0 * ldu;
+  for (int e = t; e < jb * jb; e += blockDim.x) {
+    const int i = e % jb, j = e / jb;
+    S[e] = (i <= j) ? Ub[i + (int64_t)j * ldu] : T(0);
+  }
+  __syncthreads();
+  for (int j = 0; j < jb; j++) {
+    const T wjj = T(1) / S[j + j * jb];
+    for (int i = t; i < j; i += blockDim.x) {
+      T s = T(0);
+      for (int p = i; p < j; p++) s += S[i + p * jb] * S[p + j * jb];
+      col[i] = -s * wjj;
+    }
+    __syncthreads();
+    for (int i = t; i < j; i += blockDim.x) S[i + j * jb] = col[i];
+    if (t == 0) S[j + j * jb] = wjj;
+    __syncthreads();
+  }
+  T* Wb = W + (size_t)b * NB * NB;
+  for (int e = t; e < NB * NB; e += blockDim.x) {
+    const int i = e % NB, j = e / NB;
+    Wb[e] = (i < jb && j < jb && i <= j) ? S[i + j * jb] : T(0);
+  }
+}
+
+template <typename T>
+__global__ void zero_lower_k(int n, T* __restrict__ A, int64_t lda) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)n * n) return;
   const int i = (int)(t % n), j = (int)(t / n);
-  if (i > j) A[i + (int64_t)j * lda] = 0.0;
+  if (i > j) A[i + (int64_t)j * lda] = T(0);
 }
 
-// A(i,j) = A(j,i) for i > j, in 32x32 tiles through shared memory
-__global__ void mirror_upper_k(int n, double* __restrict__ A, int64_t lda) {
-  __shared__ double tile[32][33];
-  const int bi = blockIdx.x, bj = blockIdx.y;  // target tile rows bi, cols bj, bi >= bj
+template <typename T>
+__global__ void mirror_upper_k(int n, T* __restrict__ A, int64_t lda) {
+  __shared__ T tile[32][33];
+  const int bi = blockIdx.x, bj = blockIdx.y;
   if (bi < bj) return;
   const int tx = threadIdx.x, ty = threadIdx.y;
-  // load source tile (rows bj, cols bi) = upper part
   for (int r = ty; r < 32; r += 8) {
     const int i = bj * 32 + tx, j = bi * 32 + r;
-    tile[r][tx] = (i < n && j < n) ? A[i + (int64_t)j * lda] : 0.0;
+    tile[r][tx] = (i < n && j < n) ? A[i + (int64_t)j * lda] : T(0);
   }
   __syncthreads();
   for (int r = ty; r < 32; r += 8) {
-    const int i = bi * 32 + tx, j = bj * 32 + r;  // target (i, j) = source (j, i)
+    const int i = bi * 32 + tx, j = bj * 32 + r;
     if (i < n && j < n && i > j) A[i + (int64_t)j * lda] = tile[tx][r];
   }
 }
 
-constexpr int NB64 = 128;
+// y(m x r) = alpha A(m x k) X(k x r) + beta y, A column-major, split over k
+// into gridDim.y chunks; partials[chunk][col][row]
+template <typename T, int R>
+__global__ void gemv_n_part(int m, int k, const T* __restrict__ A, int64_t lda, const T* __restrict__ X, int64_t ldx,
+                            int kchunk, T* __restrict__ part) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  const int p0 = c * kchunk, p1 = min(k, p0 + kchunk);
+  if (i >= m) return;
+  T acc[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) acc[r] = T(0);
+  for (int p = p0; p < p1; p++) {
+    const T a = A[i + (int64_t)p * lda];
+#pragma unroll
+    for (int r = 0; r < R; r++) acc[r] = fma(a, X[p + (int64_t)r * ldx], acc[r]);
+  }
+#pragma unroll
+  for (int r = 0; r < R; r++) part[((size_t)c * R + r) * m + i] = acc[r];
+}
 
-int potf2_smem(int jb) { return (jb * jb + jb) * (int)sizeof(double); }
+template <typename T, int R>
+__global__ void gemv_reduce(int m, int nchunk, const T* __restrict__ part, T alpha, T beta, T* __restrict__ y,
+                            int64_t ldy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    T s = T(0);
+    for (int c = 0; c < nchunk; c++) s += part[((size_t)c * R + r) * m + i];
+    T* py = y + i + (int64_t)r * ldy;
+    *py = (beta == T(0)) ? alpha * s : alpha * s + beta * *py;
+  }
+}
+
+// y(m x r) = alpha A^T X + beta y with A (k x m) column-major: one warp per
+// output row (a column of A), lanes stride over k, shuffle reduction
+template <typename T, int R>
+__global__ void gemv_t_k(int m, int k, const T* __restrict__ A, int64_t lda, const T* __restrict__ X, int64_t ldx,
+                         T alpha, T beta, T* __restrict__ y, int64_t ldy) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= m) return;
+  const T* a = A + (int64_t)w * lda;
+  T acc[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) acc[r] = T(0);
+  for (int p = lane; p < k; p += 32) {
+    const T av = a[p];
+#pragma unroll
+    for (int r = 0; r < R; r++) acc[r] = fma(av, X[p + (int64_t)r * ldx], acc[r]);
+  }
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    T v = acc[r];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) {
+      T* py = y + w + (int64_t)r * ldy;
+      *py = (beta == T(0)) ? alpha * v : alpha * v + beta * *py;
+    }
+  }
+}
+
+// x_j <- W_jj x_j (trans = 0) or W_jj^T x_j (trans = 1) in place, one CTA
+template <typename T>
+__global__ void trsv_diag(int jb, const T* __restrict__ W, int ldw, int trans, T* __restrict__ X, int64_t ldx,
+                          int nrhs) {
+  __shared__ T b[NB * 4];
+  const int t = threadIdx.x;
+  for (int e = t; e < jb * nrhs; e += blockDim.x) b[e] = X[(e % jb) + (int64_t)(e / jb) * ldx];
+  __syncthreads();
+  for (int e = t; e < jb * nrhs; e += blockDim.x) {
+    const int i = e % jb, r = e / jb;
+    T s = T(0);
+    if (!trans)
+      for (int p = i; p < jb; p++) s += W[i + (int64_t)p * ldw] * b[p + r * jb];
+    else
+      for (int p = 0; p <= i; p++) s += W[p + (int64_t)i * ldw] * b[p + r * jb];
+    X[i + (int64_t)r * ldx] = s;
+  }
+}
+
+template <typename T>
+int smem_potf2(int jb) {
+  return (jb * jb + jb) * (int)sizeof(T);
+}
+
+template <typename T>
+const char* tname();
+template <>
+const char* tname<double>() {
+  return "d";
+}
+template <>
+const char* tname<float>() {
+  return "s";
+}
+
+template <typename T>
+T* diag_inverses(rsd_ctx* ctx, int n, const char* tag) {
+  const int nblk = (n + NB - 1) / NB;
+  std::string name = std::string("potrf_W_") + tname<T>() + tag;
+  return (T*)rsd_scratch(ctx, name.c_str(), sizeof(T) * (size_t)nblk * NB * NB);
+}
+
+template <typename T>
+int ensure_attrs(rsd_ctx* ctx) {
+  static bool done = false;
+  if (done) return RSD_OK;
+  RSD_CUDA(ctx, cudaFuncSetAttribute(potf2_upper_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_potf2<T>(NB)));
+  RSD_CUDA(ctx, cudaFuncSetAttribute(trtri_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_potf2<T>(NB)));
+  done = true;
+  return RSD_OK;
+}
 
 }  // namespace
 
-void rsd_gemm_f64(cudaStream_t s, int m, int n, int k, double alpha, const double* A, int64_t lda, int ta,
-                  const double* B, int64_t ldb, int tb, double beta, double* C, int64_t ldc) {
-  launch_gemm<double, 64, 64, 16>(s, gp(m, n, k, alpha, A, lda, ta, B, ldb, tb, beta, C, ldc));
+// ------------------------------------------------------------ templates
+template <typename T>
+void rsd_gemm(cudaStream_t s, int m, int n, int k, double alpha, const T* A, int64_t lda, int ta, const T* B,
+              int64_t ldb, int tb, double beta, T* C, int64_t ldc) {
+  launch_gemm<T>(s, gp(m, n, k, alpha, A, lda, ta, B, ldb, tb, beta, C, ldc));
 }
 
-int rsd_zero_lower(rsd_ctx* ctx, int n, double* d_A, int64_t lda) {
-  const int64_t tot = (int64_t)n * n;
-  zero_lower_k<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(n, d_A, lda);
-  RSD_CUDA(ctx, cudaGetLastError());
-  return RSD_OK;
-}
-
-int rsd_mirror_upper(rsd_ctx* ctx, int n, double* d_A, int64_t lda) {
-  const int nt = (n + 31) / 32;
-  mirror_upper_k<<<dim3(nt, nt), dim3(32, 8), 0, ctx->stream>>>(n, d_A, lda);
-  RSD_CUDA(ctx, cudaGetLastError());
-  return RSD_OK;
-}
-
-static double* diag_inverses(rsd_ctx* ctx, int n, const char* tag) {
-  const int nblk = (n + NB64 - 1) / NB64;
-  std::string name = std::string("potrf_W_") + tag;
-  return (double*)rsd_scratch(ctx, name.c_str(), sizeof(double) * (size_t)nblk * NB64 * NB64);
-}
-
-// Blocked upper Cholesky in place; the diagonal-block inverses are kept in
-// the scratch buffer named by `tag` for rsd_potri_upper / rsd_trsv_upper.
-int rsd_potrf_upper_tag(rsd_ctx* ctx, int n, double* d_A, int64_t lda, int* info, const char* tag) {
-  if (n < 1 || lda < n) return rsd_fail(ctx, RSD_EARG, "potrf: n=%d lda=%lld", n, (long long)lda);
+template <typename T>
+int rsd_gemv(rsd_ctx* ctx, int trans, int m, int k, T alpha, const T* A, int64_t lda, const T* X, int64_t ldx,
+             int nrhs, T beta, T* y, int64_t ldy) {
+  if (m <= 0) return RSD_OK;
+  if (nrhs < 1 || nrhs > 4) return rsd_fail(ctx, RSD_EARG, "gemv: nrhs %d", nrhs);
   cudaStream_t s = ctx->stream;
-  double* W = diag_inverses(ctx, n, tag);
-  double* P = (double*)rsd_scratch(ctx, "potrf_panel", sizeof(double) * (size_t)NB64 * n);
-  if (!W || !P) return RSD_ENOMEM;
-  static bool attr = false;
-  if (!attr) {
-    RSD_CUDA(ctx, cudaFuncSetAttribute(potf2_upper_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, potf2_smem(NB64)));
-    attr = true;
+  if (trans) {
+    const int warps = 8;
+#define GT(R) gemv_t_k<T, R><<<(m + warps - 1) / warps, 32 * warps, 0, s>>>(m, k, A, lda, X, ldx, alpha, beta, y, ldy)
+    switch (nrhs) {
+      case 1: GT(1); break;
+      case 2: GT(2); break;
+      case 3: GT(3); break;
+      default: GT(4); break;
+    }
+#undef GT
+    RSD_LAUNCH_NOTE();
+  } else {
+    // enough chunks of k to fill the GPU when m is small
+    const int rowblocks = (m + 255) / 256;
+    int nchunk = (4 * ctx->sm_count + rowblocks - 1) / rowblocks;
+    nchunk = max(1, min(nchunk, (k + 63) / 64));
+    const int kchunk = (k + nchunk - 1) / nchunk;
+    nchunk = (k + kchunk - 1) / kchunk;
+    if (nchunk < 1) nchunk = 1;
+    T* part = (T*)rsd_scratch(ctx, trans ? "gemv_part_t" : (sizeof(T) == 8 ? "gemv_part_d" : "gemv_part_s"),
+                              sizeof(T) * (size_t)nchunk * nrhs * m);
+    if (!part) return RSD_ENOMEM;
+#define GN(R)                                                                                      \
+  gemv_n_part<T, R><<<dim3(rowblocks, nchunk), 256, 0, s>>>(m, k, A, lda, X, ldx, kchunk, part); \
+  gemv_reduce<T, R><<<rowblocks, 256, 0, s>>>(m, nchunk, part, alpha, beta, y, ldy)
+    switch (nrhs) {
+      case 1: GN(1); break;
+      case 2: GN(2); break;
+      case 3: GN(3); break;
+      default: GN(4); break;
+    }
+#undef GN
+    RSD_LAUNCH_NOTE();
+    RSD_LAUNCH_NOTE();
   }
+  RSD_CUDA(ctx, cudaGetLastError());
+  return RSD_OK;
+}
+
+template <typename T>
+int rsd_zero_lower_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda) {
+  const int64_t tot = (int64_t)n * n;
+  zero_lower_k<T><<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(n, d_A, lda); RSD_LAUNCH_NOTE();
+  RSD_CUDA(ctx, cudaGetLastError());
+  return RSD_OK;
+}
+
+template <typename T>
+int rsd_mirror_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda) {
+  const int nt = (n + 31) / 32;
+  mirror_upper_k<T><<<dim3(nt, nt), dim3(32, 8), 0, ctx->stream>>>(n, d_A, lda); RSD_LAUNCH_NOTE();
+  RSD_CUDA(ctx, cudaGetLastError());
+  return RSD_OK;
+}
+
+template <typename T>
+int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const char* tag) {
+  if (n < 1 || lda < n) return rsd_fail(ctx, RSD_EARG, "potrf: n=%d lda=%lld", n, (long long)lda);
+  RSD_TRY(ensure_attrs<T>(ctx));
+  cudaStream_t s = ctx->stream;
+  T* W = diag_inverses<T>(ctx, n, tag);
+  T* P = (T*)rsd_scratch(ctx, sizeof(T) == 8 ? "potrf_panel_d" : "potrf_panel_s", sizeof(T) * (size_t)NB * n);
+  if (!W || !P) return RSD_ENOMEM;
   RSD_CUDA(ctx, cudaMemsetAsync(ctx->d_info, 0, sizeof(int), s));
-  for (int j0 = 0, b = 0; j0 < n; j0 += NB64, b++) {
-    const int jb = n - j0 < NB64 ? n - j0 : NB64;
-    double* Ajj = d_A + j0 + (int64_t)j0 * lda;
-    double* Wb = W + (size_t)b * NB64 * NB64;
-    potf2_upper_inv<<<1, 256, potf2_smem(jb), s>>>(Ajj, lda, jb, Wb, NB64, ctx->d_info, j0);
+  for (int j0 = 0, b = 0; j0 < n; j0 += NB, b++) {
+    const int jb = n - j0 < NB ? n - j0 : NB;
+    T* Ajj = d_A + j0 + (int64_t)j0 * lda;
+    T* Wb = W + (size_t)b * NB * NB;
+    potf2_upper_inv<T><<<1, 256, smem_potf2<T>(jb), s>>>(Ajj, lda, jb, Wb, NB, ctx->d_info, j0); RSD_LAUNCH_NOTE();
     const int rest = n - j0 - jb;
     if (rest > 0) {
-      double* Apan = d_A + j0 + (int64_t)(j0 + jb) * lda;
-      // panel: W^T * A(j0:j0+jb, j0+jb:n)
-      launch_gemm<double, 64, 64, 16>(s, gp(jb, rest, jb, 1.0, Wb, NB64, 1, Apan, lda, 0, 0.0, P, NB64));
-      RSD_CUDA(ctx, cudaMemcpy2DAsync(Apan, lda * sizeof(double), P, NB64 * sizeof(double), jb * sizeof(double),
-                                      rest, cudaMemcpyDeviceToDevice, s));
-      // trailing: A22 -= P^T P (upper tiles)
-      GemmP g = gp(rest, rest, jb, -1.0, P, NB64, 1, P, NB64, 0, 1.0, d_A + (j0 + jb) + (int64_t)(j0 + jb) * lda, lda);
+      T* Apan = d_A + j0 + (int64_t)(j0 + jb) * lda;
+      launch_gemm<T>(s, gp(jb, rest, jb, 1.0, Wb, NB, 1, Apan, lda, 0, 0.0, P, NB));
+      RSD_CUDA(ctx, cudaMemcpy2DAsync(Apan, lda * sizeof(T), P, NB * sizeof(T), jb * sizeof(T), rest,
+                                      cudaMemcpyDeviceToDevice, s));
+      GemmP g = gp(rest, rest, jb, -1.0, P, NB, 1, P, NB, 0, 1.0, d_A + (j0 + jb) + (int64_t)(j0 + jb) * lda, lda);
       g.uplo = 1;
-      launch_gemm<double, 64, 64, 16>(s, g);
+      launch_gemm<T>(s, g);
     }
   }
   RSD_CUDA(ctx, cudaGetLastError());
@@ -298,86 +491,151 @@ int rsd_potrf_upper_tag(rsd_ctx* ctx, int n, double* d_A, int64_t lda, int* info
   return RSD_OK;
 }
 
-int rsd_potrf_upper(rsd_ctx* ctx, int n, double* d_A, int64_t lda, int* info) {
-  return rsd_potrf_upper_tag(ctx, n, d_A, lda, info, "A");
+// inverses of the diagonal blocks of an upper factor U (n x n, ld ldu)
+template <typename T>
+int rsd_diag_inverses_t(rsd_ctx* ctx, int n, const T* U, int64_t ldu, const char* tag, T** Wout) {
+  RSD_TRY(ensure_attrs<T>(ctx));
+  T* W = diag_inverses<T>(ctx, n, tag);
+  if (!W) return RSD_ENOMEM;
+  const int nblk = (n + NB - 1) / NB;
+  trtri_diag<T><<<nblk, 256, smem_potf2<T>(NB), ctx->stream>>>(n, U, ldu, W); RSD_LAUNCH_NOTE();
+  RSD_CUDA(ctx, cudaGetLastError());
+  *Wout = W;
+  return RSD_OK;
 }
 
-// After rsd_potrf_upper_tag(.., tag): A <- A^-1 in the upper triangle.
-int rsd_potri_upper_tag(rsd_ctx* ctx, int n, double* d_A, int64_t lda, const char* tag) {
+// A <- A^-1 (upper triangle) from its upper Cholesky factor in A
+template <typename T>
+int rsd_potri_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, const char* tag) {
   cudaStream_t s = ctx->stream;
-  double* W = diag_inverses(ctx, n, tag);
-  double* T1 = (double*)rsd_scratch(ctx, "potri_T1", sizeof(double) * (size_t)NB64 * n);
-  if (!W || !T1) return RSD_ENOMEM;
-  RSD_TRY(rsd_zero_lower(ctx, n, d_A, lda));
-  // triangular inverse X = U^-1, left to right
-  for (int j0 = 0, b = 0; j0 < n; j0 += NB64, b++) {
-    const int jb = n - j0 < NB64 ? n - j0 : NB64;
-    double* Wb = W + (size_t)b * NB64 * NB64;
+  T* W = nullptr;
+  RSD_TRY(rsd_diag_inverses_t<T>(ctx, n, d_A, lda, tag, &W));
+  T* T1 = (T*)rsd_scratch(ctx, sizeof(T) == 8 ? "potri_T1_d" : "potri_T1_s", sizeof(T) * (size_t)NB * n);
+  if (!T1) return RSD_ENOMEM;
+  RSD_TRY(rsd_zero_lower_t<T>(ctx, n, d_A, lda));
+  for (int j0 = 0, b = 0; j0 < n; j0 += NB, b++) {
+    const int jb = n - j0 < NB ? n - j0 : NB;
+    T* Wb = W + (size_t)b * NB * NB;
     if (j0 > 0) {
       GemmP g = gp(j0, jb, j0, 1.0, d_A, lda, 0, d_A + (int64_t)j0 * lda, lda, 0, 0.0, T1, n);
       g.kA_row = 1;
       g.offA = 0;
-      launch_gemm<double, 64, 64, 16>(s, g);
-      launch_gemm<double, 64, 64, 16>(s, gp(j0, jb, jb, -1.0, T1, n, 0, Wb, NB64, 0, 0.0, d_A + (int64_t)j0 * lda, lda));
+      launch_gemm<T>(s, g);
+      launch_gemm<T>(s, gp(j0, jb, jb, -1.0, T1, n, 0, Wb, NB, 0, 0.0, d_A + (int64_t)j0 * lda, lda));
     }
-    RSD_CUDA(ctx, cudaMemcpy2DAsync(d_A + j0 + (int64_t)j0 * lda, lda * sizeof(double), Wb, NB64 * sizeof(double),
-                                    jb * sizeof(double), jb, cudaMemcpyDeviceToDevice, s));
+    RSD_CUDA(ctx, cudaMemcpy2DAsync(d_A + j0 + (int64_t)j0 * lda, lda * sizeof(T), Wb, NB * sizeof(T),
+                                    jb * sizeof(T), jb, cudaMemcpyDeviceToDevice, s));
   }
-  // A^-1 = X X^T, column blocks left to right (in place)
-  for (int i0 = 0; i0 < n; i0 += NB64) {
-    const int ib = n - i0 < NB64 ? n - i0 : NB64;
+  for (int i0 = 0; i0 < n; i0 += NB) {
+    const int ib = n - i0 < NB ? n - i0 : NB;
     const int m = i0 + ib, k = n - i0;
     GemmP g = gp(m, ib, k, 1.0, d_A + (int64_t)i0 * lda, lda, 0, d_A + i0 + (int64_t)i0 * lda, lda, 1, 0.0, T1, n);
     g.kA_row = 1;
     g.offA = -i0;
     g.kB_col = 1;
     g.offB = 0;
-    launch_gemm<double, 64, 64, 16>(s, g);
-    RSD_CUDA(ctx, cudaMemcpy2DAsync(d_A + (int64_t)i0 * lda, lda * sizeof(double), T1, n * sizeof(double),
-                                    m * sizeof(double), ib, cudaMemcpyDeviceToDevice, s));
+    launch_gemm<T>(s, g);
+    RSD_CUDA(ctx, cudaMemcpy2DAsync(d_A + (int64_t)i0 * lda, lda * sizeof(T), T1, n * sizeof(T), m * sizeof(T), ib,
+                                    cudaMemcpyDeviceToDevice, s));
   }
   RSD_CUDA(ctx, cudaGetLastError());
   return RSD_OK;
 }
 
-int rsd_potri_upper(rsd_ctx* ctx, int n, double* d_A, int64_t lda) { return rsd_potri_upper_tag(ctx, n, d_A, lda, "A"); }
-
-// Solve A X = B with A = U^T U factored by rsd_potrf_upper_tag(.., tag);
-// X (n x nrhs, leading dimension ldx) holds B on entry.
-int rsd_potrs_upper_tag(rsd_ctx* ctx, int n, const double* d_U, int64_t ldu, double* d_X, int64_t ldx, int nrhs,
-                        const char* tag) {
+// Solve (U^T U) X = B in place (X holds B), nrhs <= 4; W from the factor's
+// diagonal blocks (computed here when W == nullptr)
+template <typename T>
+int rsd_potrs_upper_t(rsd_ctx* ctx, int n, const T* d_U, int64_t ldu, T* d_X, int64_t ldx, int nrhs, const char* tag,
+                      const T* W) {
   cudaStream_t s = ctx->stream;
-  double* W = diag_inverses(ctx, n, tag);
-  double* T = (double*)rsd_scratch(ctx, "potrs_tmp", sizeof(double) * (size_t)NB64 * nrhs);
-  if (!W || !T) return RSD_ENOMEM;
-  const int nblk = (n + NB64 - 1) / NB64;
+  if (!W) {
+    T* Wn = nullptr;
+    RSD_TRY(rsd_diag_inverses_t<T>(ctx, n, d_U, ldu, tag, &Wn));
+    W = Wn;
+  }
+  const int nblk = (n + NB - 1) / NB;
+  if (nrhs > 4) {
+    // many right-hand sides: left-looking block substitution with GEMMs
+    T* Tb = (T*)rsd_scratch(ctx, sizeof(T) == 8 ? "potrs_tmp_d" : "potrs_tmp_s", sizeof(T) * (size_t)NB * nrhs);
+    if (!Tb) return RSD_ENOMEM;
+    for (int b = 0; b < nblk; b++) {
+      const int j0 = b * NB, jb = n - j0 < NB ? n - j0 : NB;
+      if (j0 > 0) launch_gemm<T>(s, gp(jb, nrhs, j0, -1.0, d_U + (int64_t)j0 * ldu, ldu, 1, d_X, ldx, 0, 1.0, d_X + j0, ldx));
+      launch_gemm<T>(s, gp(jb, nrhs, jb, 1.0, W + (size_t)b * NB * NB, NB, 1, d_X + j0, ldx, 0, 0.0, Tb, NB));
+      RSD_CUDA(ctx, cudaMemcpy2DAsync(d_X + j0, ldx * sizeof(T), Tb, NB * sizeof(T), jb * sizeof(T), nrhs,
+                                      cudaMemcpyDeviceToDevice, s));
+    }
+    for (int b = nblk - 1; b >= 0; b--) {
+      const int j0 = b * NB, jb = n - j0 < NB ? n - j0 : NB, rest = n - j0 - jb;
+      if (rest > 0)
+        launch_gemm<T>(s, gp(jb, nrhs, rest, -1.0, d_U + j0 + (int64_t)(j0 + jb) * ldu, ldu, 0, d_X + j0 + jb, ldx, 0,
+                             1.0, d_X + j0, ldx));
+      launch_gemm<T>(s, gp(jb, nrhs, jb, 1.0, W + (size_t)b * NB * NB, NB, 0, d_X + j0, ldx, 0, 0.0, Tb, NB));
+      RSD_CUDA(ctx, cudaMemcpy2DAsync(d_X + j0, ldx * sizeof(T), Tb, NB * sizeof(T), jb * sizeof(T), nrhs,
+                                      cudaMemcpyDeviceToDevice, s));
+    }
+    RSD_CUDA(ctx, cudaGetLastError());
+    return RSD_OK;
+  }
   // forward: U^T y = b
   for (int b = 0; b < nblk; b++) {
-    const int j0 = b * NB64, jb = n - j0 < NB64 ? n - j0 : NB64;
-    if (j0 > 0)
-      launch_gemm<double, 64, 64, 16>(s, gp(jb, nrhs, j0, -1.0, d_U + (int64_t)j0 * ldu, ldu, 1, d_X, ldx, 0, 1.0,
-                                            d_X + j0, ldx));
-    launch_gemm<double, 64, 64, 16>(s, gp(jb, nrhs, jb, 1.0, W + (size_t)b * NB64 * NB64, NB64, 1, d_X + j0, ldx, 0,
-                                          0.0, T, NB64));
-    RSD_CUDA(ctx, cudaMemcpy2DAsync(d_X + j0, ldx * sizeof(double), T, NB64 * sizeof(double), jb * sizeof(double),
-                                    nrhs, cudaMemcpyDeviceToDevice, s));
+    const int j0 = b * NB, jb = n - j0 < NB ? n - j0 : NB, rest = n - j0 - jb;
+    trsv_diag<T><<<1, 256, 0, s>>>(jb, W + (size_t)b * NB * NB, NB, 1, d_X + j0, ldx, nrhs); RSD_LAUNCH_NOTE();
+    if (rest > 0)
+      RSD_TRY(rsd_gemv<T>(ctx, 1, rest, jb, T(-1), d_U + j0 + (int64_t)(j0 + jb) * ldu, ldu, d_X + j0, ldx, nrhs,
+                          T(1), d_X + j0 + jb, ldx));
   }
   // backward: U x = y
   for (int b = nblk - 1; b >= 0; b--) {
-    const int j0 = b * NB64, jb = n - j0 < NB64 ? n - j0 : NB64;
-    const int rest = n - j0 - jb;
-    if (rest > 0)
-      launch_gemm<double, 64, 64, 16>(s, gp(jb, nrhs, rest, -1.0, d_U + j0 + (int64_t)(j0 + jb) * ldu, ldu, 0,
-                                            d_X + j0 + jb, ldx, 0, 1.0, d_X + j0, ldx));
-    launch_gemm<double, 64, 64, 16>(s, gp(jb, nrhs, jb, 1.0, W + (size_t)b * NB64 * NB64, NB64, 0, d_X + j0, ldx, 0,
-                                          0.0, T, NB64));
-    RSD_CUDA(ctx, cudaMemcpy2DAsync(d_X + j0, ldx * sizeof(double), T, NB64 * sizeof(double), jb * sizeof(double),
-                                    nrhs, cudaMemcpyDeviceToDevice, s));
+    const int j0 = b * NB, jb = n - j0 < NB ? n - j0 : NB;
+    trsv_diag<T><<<1, 256, 0, s>>>(jb, W + (size_t)b * NB * NB, NB, 0, d_X + j0, ldx, nrhs); RSD_LAUNCH_NOTE();
+    if (j0 > 0)
+      RSD_TRY(rsd_gemv<T>(ctx, 0, j0, jb, T(-1), d_U + (int64_t)j0 * ldu, ldu, d_X + j0, ldx, nrhs, T(1), d_X, ldx));
   }
   RSD_CUDA(ctx, cudaGetLastError());
   return RSD_OK;
 }
 
+template void rsd_gemm<float>(cudaStream_t, int, int, int, double, const float*, int64_t, int, const float*, int64_t,
+                              int, double, float*, int64_t);
+template int rsd_gemv<float>(rsd_ctx*, int, int, int, float, const float*, int64_t, const float*, int64_t, int, float,
+                             float*, int64_t);
+template int rsd_gemv<double>(rsd_ctx*, int, int, int, double, const double*, int64_t, const double*, int64_t, int,
+                              double, double*, int64_t);
+template int rsd_potrf_upper_t<float>(rsd_ctx*, int, float*, int64_t, int*, const char*);
+template int rsd_potri_upper_t<float>(rsd_ctx*, int, float*, int64_t, const char*);
+template int rsd_potrs_upper_t<float>(rsd_ctx*, int, const float*, int64_t, float*, int64_t, int, const char*,
+                                      const float*);
+template int rsd_mirror_upper_t<float>(rsd_ctx*, int, float*, int64_t);
+template int rsd_diag_inverses_t<float>(rsd_ctx*, int, const float*, int64_t, const char*, float**);
+
+// ------------------------------------------------------------ FP64 names
+void rsd_gemm_f64(cudaStream_t s, int m, int n, int k, double alpha, const double* A, int64_t lda, int ta,
+                  const double* B, int64_t ldb, int tb, double beta, double* C, int64_t ldc) {
+  launch_gemm<double>(s, gp(m, n, k, alpha, A, lda, ta, B, ldb, tb, beta, C, ldc));
+}
+int rsd_zero_lower(rsd_ctx* ctx, int n, double* d_A, int64_t lda) { return rsd_zero_lower_t<double>(ctx, n, d_A, lda); }
+int rsd_mirror_upper(rsd_ctx* ctx, int n, double* d_A, int64_t lda) {
+  return rsd_mirror_upper_t<double>(ctx, n, d_A, lda);
+}
+int rsd_potrf_upper_tag(rsd_ctx* ctx, int n, double* d_A, int64_t lda, int* info, const char* tag) {
+  return rsd_potrf_upper_t<double>(ctx, n, d_A, lda, info, tag);
+}
+int rsd_potrf_upper(rsd_ctx* ctx, int n, double* d_A, int64_t lda, int* info) {
+  return rsd_potrf_upper_t<double>(ctx, n, d_A, lda, info, "A");
+}
+int rsd_potri_upper_tag(rsd_ctx* ctx, int n, double* d_A, int64_t lda, const char* tag) {
+  return rsd_potri_upper_t<double>(ctx, n, d_A, lda, tag);
+}
+int rsd_potri_upper(rsd_ctx* ctx, int n, double* d_A, int64_t lda) {
+  return rsd_potri_upper_t<double>(ctx, n, d_A, lda, "A");
+}
+int rsd_potrs_upper_tag(rsd_ctx* ctx, int n, const double* d_U, int64_t ldu, double* d_X, int64_t ldx, int nrhs,
+                        const char* tag) {
+  // the factor's diagonal-block inverses are still in the tag's buffer
+  const double* W = diag_inverses<double>(ctx, n, tag);
+  return rsd_potrs_upper_t<double>(ctx, n, d_U, ldu, d_X, ldx, nrhs, tag, W);
+}
 int rsd_trsv_upper(rsd_ctx* ctx, int n, const double* d_U, int64_t ldu, double* d_X, int64_t ldx, int nrhs,
                    int transpose) {
   (void)transpose;

@@ -292,7 +292,7 @@ int rsd_count_overlaps(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
   if (!d) return RSD_ENOMEM;
   RSD_CUDA(ctx, cudaMemsetAsync(d, 0, sizeof(int), ctx->stream));
   dim3 blk(32, 4), grd((nn + 31) / 32, (nn + 3) / 4);
-  overlap_count<<<grd, blk, 0, ctx->stream>>>(nn, L, d_pos, d_radii, d);
+  overlap_count<<<grd, blk, 0, ctx->stream>>>(nn, L, d_pos, d_radii, d); RSD_LAUNCH_NOTE();
   RSD_CUDA(ctx, cudaGetLastError());
   RSD_CUDA(ctx, cudaMemcpyAsync(count, d, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   RSD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -311,13 +311,13 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
   if (!tab || !cs) return RSD_ENOMEM;
   const double inv_pimu = 1.0 / (RSD_PI * mu_f);
   cudaStream_t s = ctx->stream;
-  ewald_ktable<<<(Kh + 127) / 128, 128, 0, s>>>(L, Kh, tab);
-  ewald_trig<<<dim3((nn + 127) / 128, Kh), 128, 0, s>>>(nn, Kh, tab, d_pos, cs);
-  ewald_self<<<(nn + 63) / 64, 64, 0, s>>>(nn, L, Kh, tab, d_radii, inv_pimu, d_M, ldm);
+  ewald_ktable<<<(Kh + 127) / 128, 128, 0, s>>>(L, Kh, tab); RSD_LAUNCH_NOTE();
+  ewald_trig<<<dim3((nn + 127) / 128, Kh), 128, 0, s>>>(nn, Kh, tab, d_pos, cs); RSD_LAUNCH_NOTE();
+  ewald_self<<<(nn + 63) / 64, 64, 0, s>>>(nn, L, Kh, tab, d_radii, inv_pimu, d_M, ldm); RSD_LAUNCH_NOTE();
   if (nn > 1) {
     dim3 blk(32, 4), grd((nn + 31) / 32, (nn + 3) / 4);
-    ewald_pair_k<<<grd, blk, 0, s>>>(nn, L, Kh, tab, cs, d_radii, inv_pimu, d_M, ldm);
-    ewald_pair_real<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, d_M, ldm);
+    ewald_pair_k<<<grd, blk, 0, s>>>(nn, L, Kh, tab, cs, d_radii, inv_pimu, d_M, ldm); RSD_LAUNCH_NOTE();
+    ewald_pair_real<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, d_M, ldm); RSD_LAUNCH_NOTE();
   }
   RSD_CUDA(ctx, cudaGetLastError());
   return RSD_OK;

@@ -392,8 +392,8 @@ int rsd_lub_assemble(rsd_ctx* ctx, const rsd_lubtab* tab, int nn, int nb, int is
   int* dcon = (int*)rsd_scratch(ctx, "lub_contacts", sizeof(int) * 2);
   if (!cnt || !off || !dcon) return RSD_ENOMEM;
   const int wpb = 8;
-  lub_count<<<(nn + wpb - 1) / wpb, 32 * wpb, 0, s>>>(nn, nb, is_period, Ld, d_pos, d_radii, cnt);
-  lub_scan<<<1, 1024, 0, s>>>(nn, cnt, off);
+  lub_count<<<(nn + wpb - 1) / wpb, 32 * wpb, 0, s>>>(nn, nb, is_period, Ld, d_pos, d_radii, cnt); RSD_LAUNCH_NOTE();
+  lub_scan<<<1, 1024, 0, s>>>(nn, cnt, off); RSD_LAUNCH_NOTE();
   int npair = 0;
   RSD_CUDA(ctx, cudaMemcpyAsync(&npair, off + nn, sizeof(int), cudaMemcpyDeviceToHost, s));
   RSD_CUDA(ctx, cudaStreamSynchronize(s));
@@ -403,14 +403,14 @@ int rsd_lub_assemble(rsd_ctx* ctx, const rsd_lubtab* tab, int nn, int nb, int is
   RSD_CUDA(ctx, cudaMemsetAsync(dcon, 0, sizeof(int), s));
   if (!accumulate) {
     const int64_t tot = 121LL * nn * nn;
-    zero_matrix<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(11LL * nn, 11LL * nn, d_L, ldl);
+    zero_matrix<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(11LL * nn, 11LL * nn, d_L, ldl); RSD_LAUNCH_NOTE();
   }
   const double scale = 6.0 * (RSD_PI * mu_f);
   if (npair > 0) {
-    lub_list<<<(nn + wpb - 1) / wpb, 32 * wpb, 0, s>>>(nn, nb, is_period, Ld, d_pos, d_radii, off, pairs);
-    lub_pairs<<<(npair + 127) / 128, 128, 0, s>>>(npair, T, is_period, Ld, d_pos, d_radii, pairs, blk, dcon);
+    lub_list<<<(nn + wpb - 1) / wpb, 32 * wpb, 0, s>>>(nn, nb, is_period, Ld, d_pos, d_radii, off, pairs); RSD_LAUNCH_NOTE();
+    lub_pairs<<<(npair + 127) / 128, 128, 0, s>>>(npair, T, is_period, Ld, d_pos, d_radii, pairs, blk, dcon); RSD_LAUNCH_NOTE();
     const int64_t tc = 121LL * npair;
-    lub_cross<<<(unsigned)((tc + 255) / 256), 256, 0, s>>>(npair, nn, pairs, blk, scale, d_L, ldl, 1);
+    lub_cross<<<(unsigned)((tc + 255) / 256), 256, 0, s>>>(npair, nn, pairs, blk, scale, d_L, ldl, 1); RSD_LAUNCH_NOTE();
   }
   {
     int* cnt2 = (int*)rsd_scratch(ctx, "lub_count2", sizeof(int) * (nn + 1));
@@ -421,12 +421,12 @@ int rsd_lub_assemble(rsd_ctx* ctx, const rsd_lubtab* tab, int nn, int nb, int is
     RSD_CUDA(ctx, cudaMemsetAsync(cnt2, 0, sizeof(int) * (nn + 1), s));
     RSD_CUDA(ctx, cudaMemsetAsync(cur, 0, sizeof(int) * (nn + 1), s));
     if (npair > 0) {
-      lub_second_count<<<(npair + 255) / 256, 256, 0, s>>>(npair, pairs, cnt2);
-      lub_scan<<<1, 1024, 0, s>>>(nn, cnt2, off2);
-      lub_second_fill<<<(npair + 255) / 256, 256, 0, s>>>(npair, pairs, off2, cur, list2);
-      lub_second_sort<<<(nn + 127) / 128, 128, 0, s>>>(nn, off2, list2);
+      lub_second_count<<<(npair + 255) / 256, 256, 0, s>>>(npair, pairs, cnt2); RSD_LAUNCH_NOTE();
+      lub_scan<<<1, 1024, 0, s>>>(nn, cnt2, off2); RSD_LAUNCH_NOTE();
+      lub_second_fill<<<(npair + 255) / 256, 256, 0, s>>>(npair, pairs, off2, cur, list2); RSD_LAUNCH_NOTE();
+      lub_second_sort<<<(nn + 127) / 128, 128, 0, s>>>(nn, off2, list2); RSD_LAUNCH_NOTE();
       const int64_t ts = 121LL * nn;
-      lub_self<<<(unsigned)((ts + 255) / 256), 256, 0, s>>>(nn, off, off2, list2, blk, scale, d_L, ldl, 1);
+      lub_self<<<(unsigned)((ts + 255) / 256), 256, 0, s>>>(nn, off, off2, list2, blk, scale, d_L, ldl, 1); RSD_LAUNCH_NOTE();
     }
   }
   RSD_CUDA(ctx, cudaGetLastError());

@@ -1,3 +1,275 @@
-// Mixed-precision grand-resistance solve (FP32 factorisations with FP64
-// refinement).  Built in a later step; the fused step refuses the mode.
+// Mixed-precision grand-resistance solve: FP32 factorisations, FP64
+// refinement.  Same outputs as STEPPER_NOGmres (src/stepper.f90:348-410):
+// U_par = RPP^-1 (Fe + RPQ EIN) and SijN_hyd = (RPQ^T RPP^-1 RPQ - RQQ) EIN
+// with R = M^-1 + L, but without forming M^-1.
+//
+// Augmented system in (f, U), with w = [U; -EIN]:
+//     M f = w                    (f = R_inf w, the far-field forces)
+//     f_P + (L w)_P = Fe          (force balance with lubrication)
+// and then SijN_hyd = f_Q + (L w)_Q.  Its FP64 residual needs only the dense
+// FP64 products M f and L w (HBM-bound GEMVs).  The correction is solved
+// with FP32 factors:
+//   M' = [M_QQ M_QP; M_PQ M_PP] = U'^T U'  (stresslets ordered first), so the
+//   trailing block U'_PP is the Cholesky factor of the Schur complement
+//   A = M_PP - M_PQ M_QQ^-1 M_QP and (M^-1)_PP = A^-1 = U'_PP^-1 U'_PP^-T;
+//   RPP32 = A^-1 + rfu = V^T V.
+//   correction: y = M^-1 r1; dU = RPP^-1 (r2 - y_P); df = y + M^-1 [dU; 0].
+// Iterates until ||r|| <= tol ||b|| per right-hand side.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
 #include "rsd_internal.cuh"
+
+template <typename T>
+int rsd_gemv(rsd_ctx* ctx, int trans, int m, int k, T alpha, const T* A, int64_t lda, const T* X, int64_t ldx,
+             int nrhs, T beta, T* y, int64_t ldy);
+template <typename T>
+int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const char* tag);
+template <typename T>
+int rsd_potri_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, const char* tag);
+template <typename T>
+int rsd_potrs_upper_t(rsd_ctx* ctx, int n, const T* d_U, int64_t ldu, T* d_X, int64_t ldx, int nrhs, const char* tag,
+                      const T* W);
+template <typename T>
+int rsd_mirror_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda);
+template <typename T>
+int rsd_diag_inverses_t(rsd_ctx* ctx, int n, const T* U, int64_t ldu, const char* tag, T** Wout);
+
+namespace {
+
+// M32 = M in [Q, P] order, FP32
+__global__ void convert_perm(int N, int64_t n, const double* __restrict__ M, int64_t ld, float* __restrict__ M32) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * n) return;
+  const int64_t i = t % n, j = t / n;
+  const int64_t Q = 5LL * N;
+  const int64_t si = i < Q ? 6LL * N + i : i - Q, sj = j < Q ? 6LL * N + j : j - Q;
+  M32[i + j * n] = (float)M[si + sj * ld];
+}
+
+__global__ void copy_block_f(int64_t rows, int64_t cols, const float* __restrict__ S, int64_t lds,
+                             float* __restrict__ D, int64_t ldd) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= rows * cols) return;
+  const int64_t i = t % rows, j = t / rows;
+  D[i + j * ldd] = S[i + j * lds];
+}
+
+__global__ void add_lub_pp(int64_t P, float* __restrict__ A, const double* __restrict__ L, int64_t ldl) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= P * P) return;
+  const int64_t i = t % P, j = t / P;
+  A[i + j * P] += (float)L[i + j * ldl];
+}
+
+// w = [U; -EIN] per column
+__global__ void build_w(int64_t P, int64_t Q, int nr, const double* __restrict__ U, const double* __restrict__ ein,
+                        double* __restrict__ w) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t n = P + Q;
+  if (t >= n * nr) return;
+  const int64_t i = t % n, c = t / n;
+  w[t] = i < P ? U[i + c * P] : -ein[i - P];
+}
+
+// r2 = Fe_c - f_P - (Lw)_P  (Fe only in column 0 when have_fe)
+__global__ void build_r2(int64_t P, int64_t n, int nr, const double* __restrict__ Fe, int have_fe,
+                         const double* __restrict__ f, const double* __restrict__ Lw, double* __restrict__ r2) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= P * nr) return;
+  const int64_t i = t % P, c = t / P;
+  const double fe = (have_fe && c == 0) ? Fe[i] : 0.0;
+  r2[t] = fe - f[i + c * n] - Lw[i + c * n];
+}
+
+// per-column sums of squares of r1 (n), r2 (P) and of b = ([0; -EIN], Fe)
+__global__ void norms(int64_t P, int64_t n, int nr, const double* __restrict__ r1, const double* __restrict__ r2,
+                      const double* __restrict__ ein, const double* __restrict__ Fe, int have_fe,
+                      double* __restrict__ out) {
+  __shared__ double sr[256], sb[256];
+  const int c = blockIdx.x;
+  double a = 0, b = 0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const double v = r1[i + c * n];
+    a += v * v;
+    if (i >= P) {
+      const double e = ein[i - P];
+      b += e * e;
+    }
+  }
+  for (int64_t i = threadIdx.x; i < P; i += blockDim.x) {
+    const double v = r2[i + c * P];
+    a += v * v;
+    if (have_fe && c == 0) b += Fe[i] * Fe[i];
+  }
+  sr[threadIdx.x] = a;
+  sb[threadIdx.x] = b;
+  __syncthreads();
+  for (int d = 128; d > 0; d >>= 1) {
+    if (threadIdx.x < d) {
+      sr[threadIdx.x] += sr[threadIdx.x + d];
+      sb[threadIdx.x] += sb[threadIdx.x + d];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[2 * c] = sr[0];
+    out[2 * c + 1] = sb[0];
+  }
+}
+
+// x32' = perm(x) (FP32, [Q, P] order); x may have a zero Q part (zq)
+__global__ void to32_perm(int64_t P, int64_t Q, int nr, const double* __restrict__ x, int64_t ldx, int zq,
+                          float* __restrict__ y) {
+  const int64_t n = P + Q;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * nr) return;
+  const int64_t i = t % n, c = t / n;
+  double v;
+  if (i < Q)
+    v = zq ? 0.0 : x[P + i + c * ldx];
+  else
+    v = x[i - Q + c * ldx];
+  y[t] = (float)v;
+}
+
+// y (FP64, [P, Q] order) (+)= unperm(x32')
+__global__ void from32_perm(int64_t P, int64_t Q, int nr, const float* __restrict__ x, double* __restrict__ y,
+                            int add) {
+  const int64_t n = P + Q;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * nr) return;
+  const int64_t i = t % n, c = t / n;
+  const double v = (double)(i < P ? x[Q + i + c * n] : x[i - P + c * n]);
+  y[i + c * n] = add ? y[i + c * n] + v : v;
+}
+
+// u32 = r2 - y_P
+__global__ void rhs_u(int64_t P, int64_t n, int nr, const double* __restrict__ r2, const double* __restrict__ y,
+                      float* __restrict__ u) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= P * nr) return;
+  const int64_t i = t % P, c = t / P;
+  u[t] = (float)(r2[t] - y[i + c * n]);
+}
+
+__global__ void update_fu(int64_t P, int64_t n, int nr, const double* __restrict__ df, const float* __restrict__ du,
+                          double* __restrict__ f, double* __restrict__ U) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n * nr) f[t] += df[t];
+  if (t < P * nr) U[t] += (double)du[t];
+}
+
+// dU as an FP64 [dU; 0] vector block for the second M^-1 application
+__global__ void du_vec(int64_t P, int64_t n, int nr, const float* __restrict__ du, double* __restrict__ v) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * nr) return;
+  const int64_t i = t % n, c = t / n;
+  v[t] = i < P ? (double)du[i + c * P] : 0.0;
+}
+
+// S = f_Q + (Lw)_Q of column c; U_par = U column 0
+__global__ void outputs(int64_t P, int64_t Q, int c, const double* __restrict__ f, const double* __restrict__ Lw,
+                        const double* __restrict__ U, double* __restrict__ Upar, double* __restrict__ S) {
+  const int64_t n = P + Q;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < Q) S[t] = f[P + t + c * n] + Lw[P + t + c * n];
+  if (t < P) Upar[t] = U[t];
+}
+
+inline unsigned nblk(int64_t n) { return (unsigned)((n + 255) / 256); }
+
+}  // namespace
+
+int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d_pos, const double* d_radii,
+                    const rsd_lattice* lat, const rsd_lubtab* tab, const rsd_step_params* p, const double* ein,
+                    const double* Fe, double* U_par, double* S_hyd, rsd_step_info* info) {
+  cudaStream_t s = ctx->stream;
+  const int64_t N = nn, n = 11 * N, P = 6 * N, Q = 5 * N;
+  const int have_fe = Fe != nullptr;
+  const int nr = have_fe ? 2 : 1;
+  const double tol = p->tol > 0 ? p->tol : 1e-12;
+  const int maxit = p->max_iter > 0 ? p->max_iter : 50;
+  double* L = (double*)rsd_scratch(ctx, "mixed_L", sizeof(double) * n * n);
+  float* M32 = (float*)rsd_scratch(ctx, "mixed_M32", sizeof(float) * n * n);
+  float* A32 = (float*)rsd_scratch(ctx, "mixed_A32", sizeof(float) * P * P);
+  double* V = (double*)rsd_scratch(ctx, "mixed_vec", sizeof(double) * (size_t)nr * (7 * n + 2 * P) + 64 * 8);
+  float* V32 = (float*)rsd_scratch(ctx, "mixed_vec32", sizeof(float) * (size_t)nr * (n + P));
+  if (!L || !M32 || !A32 || !V || !V32) return RSD_ENOMEM;
+  double *f = V, *U = f + nr * n, *w = U + nr * P, *r1 = w + nr * n, *Lw = r1 + nr * n, *r2 = Lw + nr * n,
+         *y = r2 + nr * P, *y2 = y + nr * n, *dv = y2 + nr * n, *nrm = dv + nr * n;
+  float *t32 = V32, *u32 = V32 + nr * n;
+  // dense FP64 lubrication matrix (R_lub - R_2B in the grand layout)
+  int nc = 0;
+  if (p->use_lub) {
+    RSD_TRY(rsd_lub_assemble(ctx, tab, nn, p->nb, 1, d_pos, d_radii, lat, p->mu_f, L, n, 0, &nc));
+  } else {
+    RSD_CUDA(ctx, cudaMemsetAsync(L, 0, sizeof(double) * n * n, s));
+  }
+  info->n_contact = nc;
+  // FP32 factor of M' (stresslets first)
+  convert_perm<<<(unsigned)((n * n + 255) / 256), 256, 0, s>>>(nn, n, M, ld, M32); RSD_LAUNCH_NOTE();
+  int inf = 0;
+  RSD_TRY(rsd_potrf_upper_t<float>(ctx, (int)n, M32, n, &inf, "m32"));
+  if (inf) {
+    info->info = inf;
+    return rsd_fail(ctx, inf, "FP32 factor of the grand mobility: leading minor %d not positive", inf);
+  }
+  float* W_m = nullptr;
+  RSD_TRY(rsd_diag_inverses_t<float>(ctx, (int)n, M32, n, "m32", &W_m));
+  // A^-1 from the trailing factor block, then RPP32 = A^-1 + rfu and its factor
+  copy_block_f<<<nblk(P * P), 256, 0, s>>>(P, P, M32 + Q + Q * n, n, A32, P); RSD_LAUNCH_NOTE();
+  RSD_TRY(rsd_potri_upper_t<float>(ctx, (int)P, A32, P, "a32"));
+  RSD_TRY(rsd_mirror_upper_t<float>(ctx, (int)P, A32, P));
+  add_lub_pp<<<nblk(P * P), 256, 0, s>>>(P, A32, L, n); RSD_LAUNCH_NOTE();
+  RSD_TRY(rsd_potrf_upper_t<float>(ctx, (int)P, A32, P, &inf, "rpp32"));
+  if (inf) {
+    info->info = inf;
+    return rsd_fail(ctx, inf, "FP32 factor of RPP: leading minor %d not positive", inf);
+  }
+  float* W_r = nullptr;
+  RSD_TRY(rsd_diag_inverses_t<float>(ctx, (int)P, A32, P, "rpp32", &W_r));
+  // refinement
+  RSD_CUDA(ctx, cudaMemsetAsync(f, 0, sizeof(double) * nr * n, s));
+  RSD_CUDA(ctx, cudaMemsetAsync(U, 0, sizeof(double) * nr * P, s));
+  double worst = 0.0;
+  int it = 0;
+  std::vector<double> hn(2 * nr);
+  for (;; it++) {
+    build_w<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, U, ein, w); RSD_LAUNCH_NOTE();
+    RSD_CUDA(ctx, cudaMemcpyAsync(r1, w, sizeof(double) * nr * n, cudaMemcpyDeviceToDevice, s));
+    RSD_TRY(rsd_gemv<double>(ctx, 0, (int)n, (int)n, -1.0, M, ld, f, n, nr, 1.0, r1, n));
+    RSD_TRY(rsd_gemv<double>(ctx, 0, (int)n, (int)n, 1.0, L, n, w, n, nr, 0.0, Lw, n));
+    build_r2<<<nblk(P * nr), 256, 0, s>>>(P, n, nr, Fe, have_fe, f, Lw, r2); RSD_LAUNCH_NOTE();
+    norms<<<nr, 256, 0, s>>>(P, n, nr, r1, r2, ein, Fe, have_fe, nrm); RSD_LAUNCH_NOTE();
+    RSD_CUDA(ctx, cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 2 * nr, cudaMemcpyDeviceToHost, s));
+    RSD_CUDA(ctx, cudaStreamSynchronize(s));
+    worst = 0.0;
+    for (int c = 0; c < nr; c++) {
+      const double rr = sqrt(hn[2 * c]) / (sqrt(hn[2 * c + 1]) > 0 ? sqrt(hn[2 * c + 1]) : 1.0);
+      if (!std::isfinite(rr)) return rsd_fail(ctx, RSD_ENAN, "refinement residual is not finite");
+      worst = fmax(worst, rr);
+    }
+    if (worst <= tol || it >= maxit) break;
+    // y = M^-1 r1
+    to32_perm<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, r1, n, 0, t32); RSD_LAUNCH_NOTE();
+    RSD_TRY(rsd_potrs_upper_t<float>(ctx, (int)n, M32, n, t32, n, nr, "m32", W_m));
+    from32_perm<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, t32, y, 0); RSD_LAUNCH_NOTE();
+    // dU = RPP^-1 (r2 - y_P)
+    rhs_u<<<nblk(P * nr), 256, 0, s>>>(P, n, nr, r2, y, u32); RSD_LAUNCH_NOTE();
+    RSD_TRY(rsd_potrs_upper_t<float>(ctx, (int)P, A32, P, u32, P, nr, "rpp32", W_r));
+    // df = y + M^-1 [dU; 0]
+    du_vec<<<nblk(n * nr), 256, 0, s>>>(P, n, nr, u32, dv); RSD_LAUNCH_NOTE();
+    to32_perm<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, dv, n, 1, t32); RSD_LAUNCH_NOTE();
+    RSD_TRY(rsd_potrs_upper_t<float>(ctx, (int)n, M32, n, t32, n, nr, "m32", W_m));
+    from32_perm<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, t32, y, 1); RSD_LAUNCH_NOTE();
+    update_fu<<<nblk(n * nr), 256, 0, s>>>(P, n, nr, y, u32, f, U); RSD_LAUNCH_NOTE();
+  }
+  outputs<<<nblk(P), 256, 0, s>>>(P, Q, nr - 1, f, Lw, U, U_par, S_hyd); RSD_LAUNCH_NOTE();
+  RSD_CUDA(ctx, cudaGetLastError());
+  info->iterations = it;
+  info->residual = worst;
+  return RSD_OK;
+}

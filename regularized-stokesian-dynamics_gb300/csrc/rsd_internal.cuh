@@ -4,6 +4,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <atomic>
 #include <map>
 #include <string>
 
@@ -11,6 +12,11 @@
 
 #define RSD_PI 3.141592653589793238462643383279502884
 #define RSD_PIP5 0.564189583547756286948079451560772585844
+
+// Count of kernel launches issued by this library (a diagnostic the
+// benchmark reports for its timed region).
+extern std::atomic<long long> rsd_launches;
+#define RSD_LAUNCH_NOTE() rsd_launches.fetch_add(1, std::memory_order_relaxed)
 
 struct rsd_buf {
   void* p = nullptr;

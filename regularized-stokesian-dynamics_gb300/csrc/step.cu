@@ -136,7 +136,7 @@ __global__ void nan_check(int64_t n, const double* __restrict__ v, int* __restri
 int rsd_axpy_block(rsd_ctx* ctx, int64_t rows, int64_t cols, const double* B, int64_t ldb, double* A, int64_t lda) {
   const int64_t tot = rows * cols;
   if (tot <= 0) return RSD_OK;
-  axpy_block_k<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(rows, cols, B, ldb, A, lda);
+  axpy_block_k<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(rows, cols, B, ldb, A, lda); RSD_LAUNCH_NOTE();
   RSD_CUDA(ctx, cudaGetLastError());
   return RSD_OK;
 }
@@ -217,7 +217,7 @@ extern "C" int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, co
   ei5_of(Eij, ei5);
   double* d_ei5 = red + 512;
   RSD_CUDA(ctx, cudaMemcpyAsync(d_ei5, ei5, sizeof ei5, cudaMemcpyHostToDevice, s));
-  fill_ein<<<(unsigned)((Q + 255) / 256), 256, 0, s>>>(nn, d_ei5, ein);
+  fill_ein<<<(unsigned)((Q + 255) / 256), 256, 0, s>>>(nn, d_ei5, ein); RSD_LAUNCH_NOTE();
   if (d_Fe)
     RSD_CUDA(ctx, cudaMemcpyAsync(Fe, d_Fe, sizeof(double) * P, cudaMemcpyDeviceToDevice, s));
   else
@@ -227,7 +227,7 @@ extern "C" int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, co
   RSD_TRY(rsd_ewald_assemble(ctx, nn, d_conf, d_radii, &lat, p->mu_f, p->precision, M, n));
   cudaEventRecord(ctx->ev[1], s);
   // averageU on APP before it is overwritten
-  sum_app_xx<<<256, 256, 0, s>>>(nn, M, n, red);
+  sum_app_xx<<<256, 256, 0, s>>>(nn, M, n, red); RSD_LAUNCH_NOTE();
   std::vector<double> hred(256);
   RSD_CUDA(ctx, cudaMemcpyAsync(hred.data(), red, 256 * sizeof(double), cudaMemcpyDeviceToHost, s));
   int info_m = 0;
@@ -266,7 +266,7 @@ extern "C" int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, co
     RSD_CUDA(ctx, cudaGetLastError());
   } else {
     cudaEventRecord(ctx->ev[2], s);
-    RSD_TRY(rsd_mixed_solve(ctx, nn, M, n, d_conf, d_radii, &lat, tab, p, ein, Fe, Upar, S, &loc));
+    RSD_TRY(rsd_mixed_solve(ctx, nn, M, n, d_conf, d_radii, &lat, tab, p, ein, d_Fe ? Fe : nullptr, Upar, S, &loc));
     cudaEventRecord(ctx->ev[3], s);
   }
   cudaEventRecord(ctx->ev[4], s);
@@ -278,12 +278,12 @@ extern "C" int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, co
   f.T = p->T;
   f.dt = p->dt;
   f.gamma = p->gamma;
-  euler_update<<<(nn + 127) / 128, 128, 0, s>>>(nn, p->nb, f, Upar, d_conf, d_U_pos);
+  euler_update<<<(nn + 127) / 128, 128, 0, s>>>(nn, p->nb, f, Upar, d_conf, d_U_pos); RSD_LAUNCH_NOTE();
   RSD_CUDA(ctx, cudaMemcpyAsync(d_SijN, S, sizeof(double) * Q, cudaMemcpyDeviceToDevice, s));
-  yeta_sums<<<1, 256, 0, s>>>(nn, S, nullptr, nullptr, ein, red + 256);
+  yeta_sums<<<1, 256, 0, s>>>(nn, S, nullptr, nullptr, ein, red + 256); RSD_LAUNCH_NOTE();
   int* flag = ctx->d_info + 8;
   RSD_CUDA(ctx, cudaMemsetAsync(flag, 0, sizeof(int), s));
-  nan_check<<<(unsigned)((6 * nn + 255) / 256), 256, 0, s>>>(6LL * nn, d_U_pos, flag);
+  nan_check<<<(unsigned)((6 * nn + 255) / 256), 256, 0, s>>>(6LL * nn, d_U_pos, flag); RSD_LAUNCH_NOTE();
   cudaEventRecord(ctx->ev[5], s);
   double ys[3];
   RSD_CUDA(ctx, cudaMemcpyAsync(ys, red + 256, sizeof ys, cudaMemcpyDeviceToHost, s));
@@ -342,11 +342,3 @@ extern "C" int rsd_stepper_stokesian(rsd_ctx* ctx, const rsd_lubtab* tab, const 
   return RSD_OK;
 }
 
-// Placeholder for the mixed-precision solve until it is built: refuse.
-int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d_pos, const double* d_radii,
-                    const rsd_lattice* lat, const rsd_lubtab* tab, const rsd_step_params* p, const double* ein,
-                    const double* Fe, double* U_par, double* S_hyd, rsd_step_info* info) {
-  (void)nn, (void)M, (void)ld, (void)d_pos, (void)d_radii, (void)lat, (void)tab, (void)p, (void)ein, (void)Fe;
-  (void)U_par, (void)S_hyd, (void)info;
-  return rsd_fail(ctx, RSD_EUNSUP, "mixed precision not built yet");
-}

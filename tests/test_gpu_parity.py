@@ -244,3 +244,18 @@ def test_errors_are_reported_not_faulted(rsd, ctx):
     with pytest.raises(rsd.RSDError) as e:
         rsd.PER_GRPERY_INV_FRI(ctx, pos, radii, lat, 1e-10, -1.0)
     assert e.value.code == rsd.RSD_EARG
+
+
+@pytest.mark.parametrize("N,phi,gmin,have_fe", [(27, 0.2, 0.01, False), (64, 0.30, 0.01, True), (64, 0.45, 1e-3, False)])
+def test_mixed_step_meets_velocity_tolerance(rsd, ctx, tabs, N, phi, gmin, have_fe):
+    """Mixed form (FP32 factors + FP64 refinement): velocities and stresslets
+    within 1e-8 relative of the FP64 oracle."""
+    pos, radii, L = rsd.configs.packing(N, phi, gmin, seed=20260700 + N, sweeps=20)
+    Fe = np.random.default_rng(1).normal(size=6 * N) if have_fe else None
+    g = rsd.STEPPER_Stokesian(ctx, tabs[0], pos, radii, 0.0, 1e-3, [L, L, L], 1.0, MU, 1e-10, Fe=Fe,
+                              precision=rsd.PREC_MIXED)
+    r = o.stepper_stokesian(pos, radii, [L, L, L], 0.0, 1e-3, 1.0, MU, 1e-10, tabs[1], Fe=Fe)
+    assert g["info"].iterations >= 1 and g["info"].residual <= 1e-12
+    assert rel(g["U_pos"], r["U_pos"]) <= 1e-8
+    assert rel(g["SijN"], r["SijN_hyd"]) <= 1e-8
+    assert np.allclose(g["yeta_mu"], r["yeta_mu"], rtol=1e-8, atol=0)
