@@ -43,62 +43,102 @@ struct GemmP {
   int offB;
 };
 
+// C = alpha op(A) op(B) + beta C, one BM x BN tile per CTA of 256 threads
+// (each TM x TN outputs), k in steps of BK through double-buffered shared
+// memory with the next tile prefetched into registers during the FMAs.
 template <typename T, int BM, int BN, int BK>
 __global__ void __launch_bounds__(256) gemm_kernel(GemmP g) {
   constexpr int TM = BM / 16, TN = BN / 16;
+  constexpr int LA = BM * BK / 256, LB = BN * BK / 256;
   const int row0 = blockIdx.x * BM, col0 = blockIdx.y * BN;
   if (g.uplo && row0 >= col0 + BN) return;
   int kbeg = 0;
   if (g.kA_row) kbeg = max(kbeg, row0 + g.offA);
   if (g.kB_col) kbeg = max(kbeg, col0 + g.offB);
   const int kend = g.k;
-  __shared__ T As[BK][BM + 1];
-  __shared__ T Bs[BK][BN + 1];
+  __shared__ T As[2][BK][BM + 1];
+  __shared__ T Bs[2][BK][BN + 1];
   const int t = threadIdx.x, tx = t % 16, ty = t / 16;
   const T* A = (const T*)g.A;
   const T* B = (const T*)g.B;
+  T ra[LA], rb[LB];
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < LA; q++) {
+      const int e = t + 256 * q;
+      int i, p;
+      if (!g.ta) {
+        i = e % BM;
+        p = e / BM;
+      } else {
+        p = e % BK;
+        i = e / BK;
+      }
+      const int gr = row0 + i, gk = k0 + p;
+      ra[q] = (gr < g.m && gk < kend) ? (g.ta ? A[gk + (int64_t)gr * g.lda] : A[gr + (int64_t)gk * g.lda]) : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < LB; q++) {
+      const int e = t + 256 * q;
+      int c, p;
+      if (!g.tb) {
+        p = e % BK;
+        c = e / BK;
+      } else {
+        c = e % BN;
+        p = e / BN;
+      }
+      const int gc = col0 + c, gk = k0 + p;
+      rb[q] = (gc < g.n && gk < kend) ? (g.tb ? B[gc + (int64_t)gk * g.ldb] : B[gk + (int64_t)gc * g.ldb]) : T(0);
+    }
+  };
+  auto store = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < LA; q++) {
+      const int e = t + 256 * q;
+      if (!g.ta)
+        As[buf][e / BM][e % BM] = ra[q];
+      else
+        As[buf][e % BK][e / BK] = ra[q];
+    }
+#pragma unroll
+    for (int q = 0; q < LB; q++) {
+      const int e = t + 256 * q;
+      if (!g.tb)
+        Bs[buf][e % BK][e / BK] = rb[q];
+      else
+        Bs[buf][e / BN][e % BN] = rb[q];
+    }
+  };
   T acc[TM][TN];
 #pragma unroll
   for (int i = 0; i < TM; i++)
 #pragma unroll
     for (int j = 0; j < TN; j++) acc[i][j] = T(0);
+  int buf = 0;
+  if (kbeg < kend) {
+    load(kbeg);
+    store(0);
+  }
+  __syncthreads();
   for (int k0 = kbeg; k0 < kend; k0 += BK) {
-    if (!g.ta) {
-      for (int e = t; e < BM * BK; e += 256) {
-        const int i = e % BM, p = e / BM, gr = row0 + i, gk = k0 + p;
-        As[p][i] = (gr < g.m && gk < kend) ? A[gr + (int64_t)gk * g.lda] : T(0);
-      }
-    } else {
-      for (int e = t; e < BM * BK; e += 256) {
-        const int p = e % BK, i = e / BK, gr = row0 + i, gk = k0 + p;
-        As[p][i] = (gr < g.m && gk < kend) ? A[gk + (int64_t)gr * g.lda] : T(0);
-      }
-    }
-    if (!g.tb) {
-      for (int e = t; e < BN * BK; e += 256) {
-        const int p = e % BK, c = e / BK, gc = col0 + c, gk = k0 + p;
-        Bs[p][c] = (gc < g.n && gk < kend) ? B[gk + (int64_t)gc * g.ldb] : T(0);
-      }
-    } else {
-      for (int e = t; e < BN * BK; e += 256) {
-        const int c = e % BN, p = e / BN, gc = col0 + c, gk = k0 + p;
-        Bs[p][c] = (gc < g.n && gk < kend) ? B[gc + (int64_t)gk * g.ldb] : T(0);
-      }
-    }
-    __syncthreads();
+    const bool more = k0 + BK < kend;
+    if (more) load(k0 + BK);
 #pragma unroll
     for (int p = 0; p < BK; p++) {
       T a[TM], b[TN];
 #pragma unroll
-      for (int i = 0; i < TM; i++) a[i] = As[p][ty + 16 * i];
+      for (int i = 0; i < TM; i++) a[i] = As[buf][p][ty + 16 * i];
 #pragma unroll
-      for (int j = 0; j < TN; j++) b[j] = Bs[p][tx + 16 * j];
+      for (int j = 0; j < TN; j++) b[j] = Bs[buf][p][tx + 16 * j];
 #pragma unroll
       for (int i = 0; i < TM; i++)
 #pragma unroll
         for (int j = 0; j < TN; j++) acc[i][j] = fma(a[i], b[j], acc[i][j]);
     }
+    if (more) store(buf ^ 1);
     __syncthreads();
+    buf ^= 1;
   }
   T* C = (T*)g.C;
   const T alpha = (T)g.alpha, beta = (T)g.beta;
@@ -154,16 +194,16 @@ GemmP gp(int m, int n, int k, double alpha, const void* A, int64_t lda, int ta, 
 
 constexpr int NB = 128;  // block size of the blocked factorisations
 
-// One CTA: Cholesky (upper) of the jb x jb diagonal block in shared memory,
-// then W = U^-1 (upper, zero below).  info: first failing global index + 1.
+// One CTA: Cholesky (upper) of the jb x jb diagonal block in shared memory.
+// The trailing update of each column step is spread over a 16 x 16 thread
+// grid.  info: first failing global index + 1 (DPOTRF's INFO).
 template <typename T>
-__global__ void __launch_bounds__(256) potf2_upper_inv(T* __restrict__ A, int64_t lda, int jb, T* __restrict__ W,
-                                                       int ldw, int* __restrict__ info, int j0) {
+__global__ void __launch_bounds__(256) potf2_upper(T* __restrict__ A, int64_t lda, int jb, int* __restrict__ info,
+                                                   int j0) {
   extern __shared__ unsigned char smraw[];
-  T* S = (T*)smraw;      // jb x jb, column-major, ld = jb
-  T* col = S + jb * jb;  // scratch column
+  T* S = (T*)smraw;  // jb x jb, column-major, ld = jb
   __shared__ int failed;
-  const int t = threadIdx.x;
+  const int t = threadIdx.x, tx = t % 16, ty = t / 16;
   for (int e = t; e < jb * jb; e += blockDim.x) {
     const int i = e % jb, j = e / jb;
     S[e] = (i <= j) ? A[i + (int64_t)j * lda] : T(0);
@@ -182,12 +222,12 @@ __global__ void __launch_bounds__(256) potf2_upper_inv(T* __restrict__ A, int64_
     }
     __syncthreads();
     if (failed) break;
-    const T dk = S[k + k * jb];
-    for (int j = k + 1 + t; j < jb; j += blockDim.x) S[k + j * jb] /= dk;
+    const T rk = T(1) / S[k + k * jb];
+    for (int j = k + 1 + t; j < jb; j += blockDim.x) S[k + j * jb] *= rk;
     __syncthreads();
-    for (int j = k + 1 + t; j < jb; j += blockDim.x) {
+    for (int j = k + 1 + ty; j < jb; j += 16) {
       const T skj = S[k + j * jb];
-      for (int i = k + 1; i <= j; i++) S[i + j * jb] -= S[k + i * jb] * skj;
+      for (int i = k + 1 + tx; i <= j; i += 16) S[i + j * jb] -= S[k + i * jb] * skj;
     }
     __syncthreads();
   }
@@ -195,26 +235,37 @@ __global__ void __launch_bounds__(256) potf2_upper_inv(T* __restrict__ A, int64_
     const int i = e % jb, j = e / jb;
     if (i <= j) A[i + (int64_t)j * lda] = S[e];
   }
-  __syncthreads();
-  if (failed) {
-    for (int e = t; e < jb * jb; e += blockDim.x) W[(e % jb) + (int64_t)(e / jb) * ldw] = T(0);
-    return;
-  }
-  for (int j = 0; j < jb; j++) {
-    const T wjj = T(1) / S[j + j * jb];
-    for (int i = t; i < j; i += blockDim.x) {
-      T s = T(0);
-      for (int p = i; p < j; p++) s += S[i + p * jb] * S[p + j * jb];
-      col[i] = -s * wjj;
-    }
-    __syncthreads();
-    for (int i = t; i < j; i += blockDim.x) S[i + j * jb] = col[i];
-    if (t == 0) S[j + j * jb] = wjj;
-    __syncthreads();
-  }
-  for (int e = t; e < jb * jb; e += blockDim.x) {
+}
+
+// Panel solve U_jj^T X = B in place (B = A(j0:j0+jb, j0+jb:n)): the factor
+// block and 64 columns of B in shared memory, one thread per column
+// (forward substitution), coalesced loads and stores of the columns.
+constexpr int TRSM_COLS = 64;
+template <typename T>
+__global__ void __launch_bounds__(TRSM_COLS) trsm_panel(const T* __restrict__ Ujj, int64_t lda, int jb, int rest,
+                                                        T* __restrict__ B) {
+  extern __shared__ unsigned char smraw[];
+  T* S = (T*)smraw;        // jb x jb
+  T* Xs = S + jb * jb;     // row i, column c at Xs[i * TRSM_COLS + c]
+  const int t = threadIdx.x, c0 = blockIdx.x * TRSM_COLS;
+  for (int e = t; e < jb * jb; e += TRSM_COLS) {
     const int i = e % jb, j = e / jb;
-    W[i + (int64_t)j * ldw] = (i <= j) ? S[e] : T(0);
+    S[e] = (i <= j) ? Ujj[i + (int64_t)j * lda] : T(0);
+  }
+  for (int e = t; e < jb * TRSM_COLS; e += TRSM_COLS) {
+    const int i = e % jb, c = e / jb;
+    Xs[i * TRSM_COLS + c] = (c0 + c < rest) ? B[i + (int64_t)(c0 + c) * lda] : T(0);
+  }
+  __syncthreads();
+  for (int i = 0; i < jb; i++) {
+    T s = Xs[i * TRSM_COLS + t];
+    for (int p = 0; p < i; p++) s -= S[p + i * jb] * Xs[p * TRSM_COLS + t];
+    Xs[i * TRSM_COLS + t] = s / S[i + i * jb];
+  }
+  __syncthreads();
+  for (int e = t; e < jb * TRSM_COLS; e += TRSM_COLS) {
+    const int i = e % jb, c = e / jb;
+    if (c0 + c < rest) B[i + (int64_t)(c0 + c) * lda] = Xs[i * TRSM_COLS + c];
   }
 }
 
@@ -337,21 +388,25 @@ __global__ void gemv_t_k(int m, int k, const T* __restrict__ A, int64_t lda, con
   }
 }
 
-// x_j <- W_jj x_j (trans = 0) or W_jj^T x_j (trans = 1) in place, one CTA
+// x_j <- W_jj x_j (trans = 0) or W_jj^T x_j (trans = 1) in place, one CTA;
+// the block W_jj is staged in shared memory first
 template <typename T>
-__global__ void trsv_diag(int jb, const T* __restrict__ W, int ldw, int trans, T* __restrict__ X, int64_t ldx,
-                          int nrhs) {
-  __shared__ T b[NB * 4];
+__global__ void __launch_bounds__(256) trsv_diag(int jb, const T* __restrict__ W, int ldw, int trans,
+                                                 T* __restrict__ X, int64_t ldx, int nrhs) {
+  extern __shared__ unsigned char smraw[];
+  T* Ws = (T*)smraw;           // jb x jb
+  T* b = Ws + NB * NB;         // jb x nrhs
   const int t = threadIdx.x;
+  for (int e = t; e < jb * jb; e += blockDim.x) Ws[e] = W[(e % jb) + (int64_t)(e / jb) * ldw];
   for (int e = t; e < jb * nrhs; e += blockDim.x) b[e] = X[(e % jb) + (int64_t)(e / jb) * ldx];
   __syncthreads();
   for (int e = t; e < jb * nrhs; e += blockDim.x) {
     const int i = e % jb, r = e / jb;
     T s = T(0);
     if (!trans)
-      for (int p = i; p < jb; p++) s += W[i + (int64_t)p * ldw] * b[p + r * jb];
+      for (int p = i; p < jb; p++) s += Ws[i + p * jb] * b[p + r * jb];
     else
-      for (int p = 0; p <= i; p++) s += W[p + (int64_t)i * ldw] * b[p + r * jb];
+      for (int p = 0; p <= i; p++) s += Ws[p + i * jb] * b[p + r * jb];
     X[i + (int64_t)r * ldx] = s;
   }
 }
@@ -359,6 +414,14 @@ __global__ void trsv_diag(int jb, const T* __restrict__ W, int ldw, int trans, T
 template <typename T>
 int smem_potf2(int jb) {
   return (jb * jb + jb) * (int)sizeof(T);
+}
+template <typename T>
+int smem_trsm() {
+  return (NB * NB + NB * TRSM_COLS) * (int)sizeof(T);
+}
+template <typename T>
+int smem_trsv() {
+  return (NB * NB + NB * 4) * (int)sizeof(T);
 }
 
 template <typename T>
@@ -383,7 +446,9 @@ template <typename T>
 int ensure_attrs(rsd_ctx* ctx) {
   static bool done = false;
   if (done) return RSD_OK;
-  RSD_CUDA(ctx, cudaFuncSetAttribute(potf2_upper_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_potf2<T>(NB)));
+  RSD_CUDA(ctx, cudaFuncSetAttribute(potf2_upper<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_potf2<T>(NB)));
+  RSD_CUDA(ctx, cudaFuncSetAttribute(trsm_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_trsm<T>()));
+  RSD_CUDA(ctx, cudaFuncSetAttribute(trsv_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_trsv<T>()));
   RSD_CUDA(ctx, cudaFuncSetAttribute(trtri_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_potf2<T>(NB)));
   done = true;
   return RSD_OK;
@@ -465,24 +530,26 @@ int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const
   RSD_TRY(ensure_attrs<T>(ctx));
   cudaStream_t s = ctx->stream;
   T* W = diag_inverses<T>(ctx, n, tag);
-  T* P = (T*)rsd_scratch(ctx, sizeof(T) == 8 ? "potrf_panel_d" : "potrf_panel_s", sizeof(T) * (size_t)NB * n);
-  if (!W || !P) return RSD_ENOMEM;
+  if (!W) return RSD_ENOMEM;
   RSD_CUDA(ctx, cudaMemsetAsync(ctx->d_info, 0, sizeof(int), s));
-  for (int j0 = 0, b = 0; j0 < n; j0 += NB, b++) {
+  for (int j0 = 0; j0 < n; j0 += NB) {
     const int jb = n - j0 < NB ? n - j0 : NB;
     T* Ajj = d_A + j0 + (int64_t)j0 * lda;
-    T* Wb = W + (size_t)b * NB * NB;
-    potf2_upper_inv<T><<<1, 256, smem_potf2<T>(jb), s>>>(Ajj, lda, jb, Wb, NB, ctx->d_info, j0); RSD_LAUNCH_NOTE();
+    potf2_upper<T><<<1, 256, smem_potf2<T>(jb), s>>>(Ajj, lda, jb, ctx->d_info, j0); RSD_LAUNCH_NOTE();
     const int rest = n - j0 - jb;
     if (rest > 0) {
       T* Apan = d_A + j0 + (int64_t)(j0 + jb) * lda;
-      launch_gemm<T>(s, gp(jb, rest, jb, 1.0, Wb, NB, 1, Apan, lda, 0, 0.0, P, NB));
-      RSD_CUDA(ctx, cudaMemcpy2DAsync(Apan, lda * sizeof(T), P, NB * sizeof(T), jb * sizeof(T), rest,
-                                      cudaMemcpyDeviceToDevice, s));
-      GemmP g = gp(rest, rest, jb, -1.0, P, NB, 1, P, NB, 0, 1.0, d_A + (j0 + jb) + (int64_t)(j0 + jb) * lda, lda);
+      trsm_panel<T><<<(rest + TRSM_COLS - 1) / TRSM_COLS, TRSM_COLS, smem_trsm<T>(), s>>>(Ajj, lda, jb, rest, Apan); RSD_LAUNCH_NOTE();
+      // trailing: A22 -= Apan^T Apan (upper tiles)
+      GemmP g = gp(rest, rest, jb, -1.0, Apan, lda, 1, Apan, lda, 0, 1.0, d_A + (j0 + jb) + (int64_t)(j0 + jb) * lda, lda);
       g.uplo = 1;
       launch_gemm<T>(s, g);
     }
+  }
+  // diagonal-block inverses for the solves
+  {
+    const int nblk = (n + NB - 1) / NB;
+    trtri_diag<T><<<nblk, 256, smem_potf2<T>(NB), s>>>(n, d_A, lda, W); RSD_LAUNCH_NOTE();
   }
   RSD_CUDA(ctx, cudaGetLastError());
   RSD_CUDA(ctx, cudaMemcpyAsync(ctx->h_info, ctx->d_info, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -580,7 +647,7 @@ int rsd_potrs_upper_t(rsd_ctx* ctx, int n, const T* d_U, int64_t ldu, T* d_X, in
   // forward: U^T y = b
   for (int b = 0; b < nblk; b++) {
     const int j0 = b * NB, jb = n - j0 < NB ? n - j0 : NB, rest = n - j0 - jb;
-    trsv_diag<T><<<1, 256, 0, s>>>(jb, W + (size_t)b * NB * NB, NB, 1, d_X + j0, ldx, nrhs); RSD_LAUNCH_NOTE();
+    trsv_diag<T><<<1, 256, smem_trsv<T>(), s>>>(jb, W + (size_t)b * NB * NB, NB, 1, d_X + j0, ldx, nrhs); RSD_LAUNCH_NOTE();
     if (rest > 0)
       RSD_TRY(rsd_gemv<T>(ctx, 1, rest, jb, T(-1), d_U + j0 + (int64_t)(j0 + jb) * ldu, ldu, d_X + j0, ldx, nrhs,
                           T(1), d_X + j0 + jb, ldx));
@@ -588,7 +655,7 @@ int rsd_potrs_upper_t(rsd_ctx* ctx, int n, const T* d_U, int64_t ldu, T* d_X, in
   // backward: U x = y
   for (int b = nblk - 1; b >= 0; b--) {
     const int j0 = b * NB, jb = n - j0 < NB ? n - j0 : NB;
-    trsv_diag<T><<<1, 256, 0, s>>>(jb, W + (size_t)b * NB * NB, NB, 0, d_X + j0, ldx, nrhs); RSD_LAUNCH_NOTE();
+    trsv_diag<T><<<1, 256, smem_trsv<T>(), s>>>(jb, W + (size_t)b * NB * NB, NB, 0, d_X + j0, ldx, nrhs); RSD_LAUNCH_NOTE();
     if (j0 > 0)
       RSD_TRY(rsd_gemv<T>(ctx, 0, j0, jb, T(-1), d_U + (int64_t)j0 * ldu, ldu, d_X + j0, ldx, nrhs, T(1), d_X, ldx));
   }

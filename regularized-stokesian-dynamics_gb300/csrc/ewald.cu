@@ -21,12 +21,18 @@
 // The closed forms come from ewald_gen.cuh (generated by gen_ewald.py).
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "ewald_gen.cuh"
 #include "rsd_internal.cuh"
 
 namespace {
 
 constexpr int KW = 3 + RSD_NMOM_KCOS + RSD_NMOM_KSIN;  // doubles per k entry
+// Mixed form: FP64 for real images with lambda r below this, and for
+// reciprocal vectors with max|n_i| up to this shell.
+#define RSD_MIXED_RCUT 4.5
+#define RSD_MIXED_KSHELL 2
 
 __host__ __device__ inline void half_space_index(int h, int NI, int* nx, int* ny, int* nz) {
   const int w = 2 * NI + 1;
@@ -71,6 +77,50 @@ __global__ void ewald_trig(int nn, int Kh, const double* __restrict__ tab, const
   double s, c;
   sincos(kr, &s, &c);
   cs[(size_t)h * nn + a] = make_double2(c, s);
+}
+
+// Weights and trig tables restricted to a list of half-space indices, in
+// precision T (the mixed form splits the reciprocal sum by shell).
+template <typename T>
+__global__ void ewald_ktable_list(rsd_lat_dev L, int count, const int* __restrict__ hlist, T* __restrict__ tab) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= count) return;
+  int nx, ny, nz;
+  half_space_index(hlist[q], L.NI, &nx, &ny, &nz);
+  double k[3];
+  for (int j = 0; j < 3; j++)
+    k[j] = 2.0 * RSD_PI * (nx * L.LI[0 + 3 * j] + ny * L.LI[1 + 3 * j] + nz * L.LI[2 + 3 * j]);
+  const double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+  const double S = kernel_S<double>(k2, L.lam);
+  double wc[RSD_NMOM_KCOS], ws[RSD_NMOM_KSIN];
+  rsd_kcos_weights<double>(k[0], k[1], k[2], S, L.lam, wc);
+  rsd_ksin_weights<double>(k[0], k[1], k[2], S, L.lam, ws);
+  T* e = tab + (size_t)q * KW;
+  e[0] = (T)k[0];
+  e[1] = (T)k[1];
+  e[2] = (T)k[2];
+  for (int m = 0; m < RSD_NMOM_KCOS; m++) e[3 + m] = (T)wc[m];
+  for (int m = 0; m < RSD_NMOM_KSIN; m++) e[3 + RSD_NMOM_KCOS + m] = (T)ws[m];
+}
+
+template <typename T2>
+__global__ void ewald_trig_list(int nn, rsd_lat_dev L, const int* __restrict__ hlist, const double* __restrict__ pos,
+                                T2* __restrict__ cs) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = blockIdx.y;
+  if (a >= nn) return;
+  int nx, ny, nz;
+  half_space_index(hlist[q], L.NI, &nx, &ny, &nz);
+  double k[3];
+  for (int j = 0; j < 3; j++)
+    k[j] = 2.0 * RSD_PI * (nx * L.LI[0 + 3 * j] + ny * L.LI[1 + 3 * j] + nz * L.LI[2 + 3 * j]);
+  const double kr = k[0] * pos[3 * a] + k[1] * pos[3 * a + 1] + k[2] * pos[3 * a + 2];
+  double sn, c;
+  sincos(kr, &sn, &c);
+  T2 v;
+  v.x = c;
+  v.y = sn;
+  cs[(size_t)q * nn + a] = v;
 }
 
 // Scatter of the pair block (a,b), a < b, and its mirror (b,a) with
@@ -136,35 +186,79 @@ __device__ inline bool pair_of(int nn, int* a, int* b) {
   return *a < nn && *b < nn && *a < *b;
 }
 
-__global__ void __launch_bounds__(128) ewald_pair_k(int nn, rsd_lat_dev L, int Kh, const double* __restrict__ tab,
-                                                    const double2* __restrict__ cs, const double* __restrict__ radii,
-                                                    double inv_pimu, double* __restrict__ M, int64_t ldm) {
+template <typename T, typename T2>
+__global__ void __launch_bounds__(128) ewald_pair_k(int nn, rsd_lat_dev L, int Kh, const T* __restrict__ tab,
+                                                    const T2* __restrict__ cs, const double* __restrict__ radii,
+                                                    double inv_pimu, double* __restrict__ M, int64_t ldm, int add) {
+  constexpr int KWT = 3 + RSD_NMOM_KCOS + RSD_NMOM_KSIN;
   int a, b;
   if (!pair_of(nn, &a, &b)) return;
-  double ac[RSD_NMOM_KCOS], as[RSD_NMOM_KSIN];
+  T ac[RSD_NMOM_KCOS], as[RSD_NMOM_KSIN];
 #pragma unroll
-  for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] = 0.0;
+  for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] = T(0);
 #pragma unroll
-  for (int m = 0; m < RSD_NMOM_KSIN; m++) as[m] = 0.0;
+  for (int m = 0; m < RSD_NMOM_KSIN; m++) as[m] = T(0);
   for (int h = 0; h < Kh; h++) {
-    const double2 ua = cs[(size_t)h * nn + a], ub = cs[(size_t)h * nn + b];
-    const double c = ua.x * ub.x + ua.y * ub.y;  // cos(k.(x_a - x_b))
-    const double s = ua.y * ub.x - ua.x * ub.y;  // sin(k.(x_a - x_b))
-    const double* e = tab + (size_t)h * KW + 3;
+    const T2 ua = cs[(size_t)h * nn + a], ub = cs[(size_t)h * nn + b];
+    const T c = ua.x * ub.x + ua.y * ub.y;  // cos(k.(x_a - x_b))
+    const T s = ua.y * ub.x - ua.x * ub.y;  // sin(k.(x_a - x_b))
+    const T* e = tab + (size_t)h * KWT + 3;
 #pragma unroll
     for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] = fma(__ldg(e + m), c, ac[m]);
 #pragma unroll
     for (int m = 0; m < RSD_NMOM_KSIN; m++) as[m] = fma(__ldg(e + RSD_NMOM_KCOS + m), s, as[m]);
   }
-  const double ai = radii[a], aj = radii[b], phix = L.phix;
-  double v[60], w[60];
-  rsd_kcos_epilogue<double>(ac, ai, aj, phix, v);
-  rsd_ksin_epilogue<double>(as, ai, aj, phix, w);
+  const T ai = (T)radii[a], aj = (T)radii[b], phix = (T)L.phix;
+  T v[60], w[60];
+  rsd_kcos_epilogue<T>(ac, ai, aj, phix, v);
+  rsd_ksin_epilogue<T>(as, ai, aj, phix, w);
+  double o[60];
   const double f = 2.0 / L.LV;  // half space counted twice
 #pragma unroll
-  for (int q = 0; q < 60; q++) v[q] = (v[q] + w[q]) * f;
-  scale_block(v, ai, inv_pimu);
-  store_pair(M, ldm, nn, a, b, v, 0);
+  for (int q = 0; q < 60; q++) o[q] = ((double)v[q] + (double)w[q]) * f;
+  scale_block(o, radii[a], inv_pimu);
+  store_pair(M, ldm, nn, a, b, o, add);
+}
+
+// Real-space images over the cube [-NR,NR]^3: MODE 0 all of them, MODE 1
+// those with |x| < rc (lambda r < RSD_MIXED_RCUT), MODE 2 the others.  The
+// radial functions of erfc(lambda r) cancel badly in FP32 at large lambda r,
+// so FP32 is kept for images where every term is below ~1e-9 of a block.
+template <typename T, int MODE>
+__global__ void __launch_bounds__(128) ewald_pair_real_t(int nn, rsd_lat_dev L, const double* __restrict__ pos,
+                                                         const double* __restrict__ radii, double inv_pimu,
+                                                         double rc2, double* __restrict__ M, int64_t ldm) {
+  int a, b;
+  if (!pair_of(nn, &a, &b)) return;
+  double R[3] = {pos[3 * a] - pos[3 * b], pos[3 * a + 1] - pos[3 * b + 1], pos[3 * a + 2] - pos[3 * b + 2]};
+  double dmin;
+  rsd_skew_correction(L.LR, L.LI, R, &dmin);
+  T acc[RSD_NMOM_REAL];
+#pragma unroll
+  for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = T(0);
+  const T lam = (T)L.lam, lam2 = lam * lam, cd = T(2.0 * RSD_PIP5) * lam;
+  const int NR = L.NR;
+  for (int nx = -NR; nx <= NR; nx++)
+    for (int ny = -NR; ny <= NR; ny++)
+      for (int nz = -NR; nz <= NR; nz++) {
+        const double d0 = R[0] + L.LR[0] * nx + L.LR[3] * ny + L.LR[6] * nz;
+        const double d1 = R[1] + L.LR[1] * nx + L.LR[4] * ny + L.LR[7] * nz;
+        const double d2 = R[2] + L.LR[2] * nx + L.LR[5] * ny + L.LR[8] * nz;
+        const bool near = d0 * d0 + d1 * d1 + d2 * d2 < rc2;
+        if ((MODE == 1 && !near) || (MODE == 2 && near)) continue;
+        const T x0 = (T)d0, x1 = (T)d1, x2 = (T)d2;
+        const T r2 = x0 * x0 + x1 * x1 + x2 * x2;
+        const T r = sqrt(r2), ir = T(1) / r;
+        const T E0 = erfc(lam * r), Ed = cd * exp(-r2 * lam2);
+        rsd_real_image<T>(x0, x1, x2, r, ir, E0, Ed, lam, acc);
+      }
+  T v[60];
+  rsd_real_epilogue<T>(acc, (T)radii[a], (T)radii[b], (T)L.phix, v);
+  double o[60];
+#pragma unroll
+  for (int q = 0; q < 60; q++) o[q] = (double)v[q];
+  scale_block(o, radii[a], inv_pimu);
+  store_pair(M, ldm, nn, a, b, o, 1);
 }
 
 __global__ void __launch_bounds__(128) ewald_pair_real(int nn, rsd_lat_dev L, const double* __restrict__ pos,
@@ -301,7 +395,6 @@ int rsd_count_overlaps(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
 
 int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
                        double mu_f, int precision, double* d_M, int64_t ldm) {
-  (void)precision;
   if (nn < 1 || ldm < 11LL * nn) return rsd_fail(ctx, RSD_EARG, "bad size nn=%d ldm=%lld", nn, (long long)ldm);
   rsd_lat_dev L = rsd_lat_pack(lat);
   const int w = 2 * L.NI + 1;
@@ -316,8 +409,44 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
   ewald_self<<<(nn + 63) / 64, 64, 0, s>>>(nn, L, Kh, tab, d_radii, inv_pimu, d_M, ldm); RSD_LAUNCH_NOTE();
   if (nn > 1) {
     dim3 blk(32, 4), grd((nn + 31) / 32, (nn + 3) / 4);
-    ewald_pair_k<<<grd, blk, 0, s>>>(nn, L, Kh, tab, cs, d_radii, inv_pimu, d_M, ldm); RSD_LAUNCH_NOTE();
-    ewald_pair_real<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, d_M, ldm); RSD_LAUNCH_NOTE();
+    if (precision == RSD_PREC_MIXED) {
+      // FP64: real images with lambda r < RSD_MIXED_RCUT and reciprocal
+      // vectors with max|n_i| <= RSD_MIXED_KSHELL; FP32 for the rest (each
+      // block then within ~1e-11 of the all-FP64 sum).
+      const double rc = RSD_MIXED_RCUT / L.lam, rc2 = rc * rc;
+      std::vector<int> h64, h32;
+      for (int h = 0; h < Kh; h++) {
+        int nx, ny, nz;
+        half_space_index(h, L.NI, &nx, &ny, &nz);
+        (abs(nx) <= RSD_MIXED_KSHELL && abs(ny) <= RSD_MIXED_KSHELL && abs(nz) <= RSD_MIXED_KSHELL ? h64 : h32).push_back(h);
+      }
+      const int K64 = (int)h64.size(), K32 = (int)h32.size();
+      int* dh = (int*)rsd_scratch(ctx, "ewald_hlist", sizeof(int) * (size_t)Kh);
+      double* t64 = (double*)rsd_scratch(ctx, "ewald_ktab64", sizeof(double) * (size_t)(K64 > 0 ? K64 : 1) * KW);
+      float* t32 = (float*)rsd_scratch(ctx, "ewald_ktab32", sizeof(float) * (size_t)(K32 > 0 ? K32 : 1) * KW);
+      double2* c64 = (double2*)rsd_scratch(ctx, "ewald_trig64", sizeof(double2) * (size_t)(K64 > 0 ? K64 : 1) * nn);
+      float2* c32 = (float2*)rsd_scratch(ctx, "ewald_trig32", sizeof(float2) * (size_t)(K32 > 0 ? K32 : 1) * nn);
+      if (!dh || !t64 || !t32 || !c64 || !c32) return RSD_ENOMEM;
+      std::vector<int> all(h64);
+      all.insert(all.end(), h32.begin(), h32.end());
+      RSD_CUDA(ctx, cudaMemcpyAsync(dh, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice, s));
+      RSD_CUDA(ctx, cudaStreamSynchronize(s));
+      if (K64) {
+        ewald_ktable_list<double><<<(K64 + 127) / 128, 128, 0, s>>>(L, K64, dh, t64); RSD_LAUNCH_NOTE();
+        ewald_trig_list<double2><<<dim3((nn + 127) / 128, K64), 128, 0, s>>>(nn, L, dh, d_pos, c64); RSD_LAUNCH_NOTE();
+      }
+      if (K32) {
+        ewald_ktable_list<float><<<(K32 + 127) / 128, 128, 0, s>>>(L, K32, dh + K64, t32); RSD_LAUNCH_NOTE();
+        ewald_trig_list<float2><<<dim3((nn + 127) / 128, K32), 128, 0, s>>>(nn, L, dh + K64, d_pos, c32); RSD_LAUNCH_NOTE();
+      }
+      ewald_pair_k<double, double2><<<grd, blk, 0, s>>>(nn, L, K64, t64, c64, d_radii, inv_pimu, d_M, ldm, 0); RSD_LAUNCH_NOTE();
+      ewald_pair_k<float, float2><<<grd, blk, 0, s>>>(nn, L, K32, t32, c32, d_radii, inv_pimu, d_M, ldm, 1); RSD_LAUNCH_NOTE();
+      ewald_pair_real_t<double, 1><<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, d_M, ldm); RSD_LAUNCH_NOTE();
+      ewald_pair_real_t<float, 2><<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, d_M, ldm); RSD_LAUNCH_NOTE();
+    } else {
+      ewald_pair_k<double, double2><<<grd, blk, 0, s>>>(nn, L, Kh, tab, cs, d_radii, inv_pimu, d_M, ldm, 0); RSD_LAUNCH_NOTE();
+      ewald_pair_real<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, d_M, ldm); RSD_LAUNCH_NOTE();
+    }
   }
   RSD_CUDA(ctx, cudaGetLastError());
   return RSD_OK;

@@ -209,6 +209,7 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
     RSD_CUDA(ctx, cudaMemsetAsync(L, 0, sizeof(double) * n * n, s));
   }
   info->n_contact = nc;
+  cudaEventRecord(ctx->ev[6], s);
   // FP32 factor of M' (stresslets first)
   convert_perm<<<(unsigned)((n * n + 255) / 256), 256, 0, s>>>(nn, n, M, ld, M32); RSD_LAUNCH_NOTE();
   int inf = 0;

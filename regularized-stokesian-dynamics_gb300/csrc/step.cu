@@ -295,8 +295,17 @@ extern "C" int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, co
   cudaEventElapsedTime(&t23, ctx->ev[2], ctx->ev[3]);
   cudaEventElapsedTime(&t45, ctx->ev[3], ctx->ev[5]);
   ctx->phase_ms[0] = t01;
-  ctx->phase_ms[1] = t23;
-  ctx->phase_ms[2] = t12 + t45;
+  if (p->precision == RSD_PREC_MIXED) {
+    // the lubrication assembly sits inside the mixed solve (event 6)
+    float t26, t63;
+    cudaEventElapsedTime(&t26, ctx->ev[2], ctx->ev[6]);
+    cudaEventElapsedTime(&t63, ctx->ev[6], ctx->ev[3]);
+    ctx->phase_ms[1] = t26;
+    ctx->phase_ms[2] = t12 + t63 + t45;
+  } else {
+    ctx->phase_ms[1] = t23;
+    ctx->phase_ms[2] = t12 + t45;
+  }
   ctx->phase_ms[3] = 0;
   double sxx = 0.0;
   for (int b = 0; b < 256; b++) sxx += hred[b];
