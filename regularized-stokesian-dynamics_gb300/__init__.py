@@ -20,6 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(HERE, "librsd_gb300.so")
 
 RSD_OK, RSD_EARG, RSD_ECUDA, RSD_ENAN, RSD_ETIMEOUT, RSD_ENOMEM, RSD_EIO, RSD_EUNSUP = 0, -1, -2, -3, -4, -5, -6, -7
+RSD_ELIMIT = -8
 PREC_FP64, PREC_MIXED = 0, 1
 PAI = 3.141592653589793238462643383279502884
 
@@ -75,6 +76,7 @@ _sig("rsd_set_lattice_skew", _i, [_d, _dp, _d, _i32, _d, _d, _LP])
 _sig("rsd_calc_lattice_inverse", _i, [_LP, _d, _i32, _dp])
 _sig("rsd_per_grpery_inv_fri", _i, [_vp, _i32, _dp, _dp, _LP, _d, _d, _i32, _dp, _dp, _dp])
 _sig("rsd_per_grpery_inv_fri_dev", _i, [_vp, _i32, _vp, _vp, _LP, _d, _d, _i32, _vp, _i64])
+_sig("rsd_per_grpery_inv_fri_static", _i, [_i32, _vp, _vp, _LP, _d, _d, _vp, _i64, _vp])
 _sig("rsd_lubtab_load", _i, [ctypes.POINTER(_vp), ctypes.c_char_p])
 _sig("rsd_lubtab_create", _i, [ctypes.POINTER(_vp), _i32, _dp, _i32, _dp, _i32, _dp])
 _sig("rsd_lubtab_destroy", _i, [_vp])
