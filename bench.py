@@ -39,7 +39,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["mixed", "fp64"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--N", type=int, default=2048)
     ap.add_argument("--phi", type=float, default=0.5)
     ap.add_argument("--gmin", type=float, default=1e-4)
@@ -136,6 +137,29 @@ def fp64_gemm_peak(torch, dev):
     return best
 
 
+def fp32_gemm_peak(torch, dev):
+    """cuBLAS SGEMM rate (TF32 off), TFLOP/s: the denominator for the FP32
+    factorisations of the mixed form."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float32, device=dev)
+    b = torch.randn(n, n, dtype=torch.float32, device=dev)
+    c = a @ b
+    torch.cuda.synchronize(dev)
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        c = a @ b
+        e1.record()
+        torch.cuda.synchronize(dev)
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del a, b, c
+    return best
+
+
 def ewald_flops(N, NR, NI):
     """Algorithmic FLOP of one grand-mobility assembly: 500 per real image and
     150 per reciprocal vector, over the unordered pairs (all images) and the
@@ -148,8 +172,11 @@ def ewald_flops(N, NR, NI):
 
 def solve_flops(N, precision):
     """Plain FP64: Cholesky + SPD inverse of M (n^3, n = 11N) and Cholesky of
-    RPP ((6N)^3/3): 1403 N^3."""
-    return 1403.0 * N ** 3
+    RPP ((6N)^3/3): 1403 N^3.  Mixed: FP32 Cholesky of M' (n^3/3), inverse of
+    its 6N Schur factor (2 (6N)^3/3) and Cholesky of RPP ((6N)^3/3): 660 N^3."""
+    if precision == "fp64":
+        return 1403.0 * N ** 3
+    return (1331.0 / 3.0 + 216.0) * N ** 3
 
 
 def cpu_step_sample(pos, radii, L, N, dt, threads):
@@ -327,19 +354,54 @@ def main():
             te = float(t.item())
         e2e = {"value": ws * args.steps / te, "unit": "steps/s", "h2d_bytes_per_step": 8 * (3 * N + N),
                "d2h_bytes_per_step": 8 * (3 * N + 6 * N + 5 * N)}
+    # the plain FP64 form on the same start configuration: its steps/s and the
+    # mixed form's velocity / stresslet error against it
+    plain = None
+    if not args.no_plain and args.precision == "mixed":
+        c0 = torch.tensor(pos, dtype=torch.float64, device=dev)
+        Um, Sm = torch.empty_like(U_t), torch.empty_like(S_t)
+        rsd.stepper_stokesian_dev(ctx, tab, c0.clone(), radii_t, 0.0, args.dt, [L, L, L], 1.0, mu, 1e-10, Um, Sm,
+                                  precision=rsd.PREC_MIXED)
+        Up, Sp = torch.empty_like(U_t), torch.empty_like(S_t)
+        rsd.stepper_stokesian_dev(ctx, tab, c0.clone(), radii_t, 0.0, args.dt, [L, L, L], 1.0, mu, 1e-10, Up, Sp,
+                                  precision=rsd.PREC_FP64)  # warm-up of the plain path's buffers
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        rsd.stepper_stokesian_dev(ctx, tab, c0.clone(), radii_t, 0.0, args.dt, [L, L, L], 1.0, mu, 1e-10, Up, Sp,
+                                  precision=rsd.PREC_FP64)
+        p1.record(stream)
+        torch.cuda.synchronize(dev)
+        pms = p0.elapsed_time(p1)
+        pph = ctx.phase_ms()
+        verr = float((Um - Up).abs().max() / Up.abs().max())
+        serr = float((Sm - Sp).abs().max() / Sp.abs().max())
+        plain = {"steps_per_s": 1000.0 / pms, "ms_per_step": pms,
+                 "phases_ms": {"assembly": pph[0], "lub": pph[1], "solve": pph[2]},
+                 "solve_tflops_fp64": solve_flops(N, "fp64") / (pph[2] * 1e-3) / 1e12,
+                 "mixed_over_plain": (1000.0 / pms and value / ws / (1000.0 / pms)),
+                 "vel_err_mixed_vs_fp64": verr, "stresslet_err_mixed_vs_fp64": serr}
     if rank != 0:
         if ws > 1:
             dist.barrier()
         return
     peaks = measured_peaks()
     fp64_peak = None if args.no_peaks else fp64_gemm_peak(torch, dev)
+    fp32_peak = None if args.no_peaks else fp32_gemm_peak(torch, dev)
     NR, NI = infos[0][0], infos[0][1]
     ph = phases / args.steps
     asm_flop = ewald_flops(N, NR, NI)
     asm_rate = asm_flop / (ph[0] * 1e-3) / 1e12
-    solve_rate = solve_flops(N, args.precision) / (ph[2] * 1e-3) / 1e12
+    factor_ms = ph[2] - ph[3]
+    solve_rate = solve_flops(N, args.precision) / (factor_ms * 1e-3) / 1e12
     dominant = "solve" if ph[2] >= ph[0] else "assembly"
-    rate = solve_rate if dominant == "solve" else asm_rate
+    if dominant == "solve":
+        rate, pk = solve_rate, (fp64_peak if args.precision == "fp64" else fp32_peak)
+        pipe = "FP64" if args.precision == "fp64" else "FP32"
+        src = ("cuBLAS %s 8192^3 measured in this run (the measured-peaks file has BF16 and HBM only)"
+               % ("DGEMM" if args.precision == "fp64" else "SGEMM, TF32 off"))
+    else:
+        rate, pk, pipe = asm_rate, fp64_peak, "FP64"
+        src = "cuBLAS DGEMM 8192^3 measured in this run (the measured-peaks file has BF16 and HBM only)"
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "traffic.txt")
     if os.path.exists(tfile):
@@ -347,10 +409,9 @@ def main():
             k, _, v = line.partition("=")
             if k.strip() == "%s_%s_bytes_per_launch" % (dominant, args.precision):
                 traffic = float(v)
-    roofline = {"bound": "tensor", "pipe": "FP64", "kernel": dominant, "achieved": rate,
-                "peak": fp64_peak, "unit": "TFLOP/s", "frac": (rate / fp64_peak) if fp64_peak else None,
-                "traffic": traffic,
-                "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (the measured-peaks file has no FP64 entry)"}
+    roofline = {"bound": "tensor", "pipe": pipe, "kernel": "%s (%s)" % (dominant, args.precision), "achieved": rate,
+                "peak": pk, "unit": "TFLOP/s", "frac": (rate / pk) if pk else None, "traffic": traffic,
+                "peak_source": src}
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -365,7 +426,9 @@ def main():
                        "precision": args.precision, "NR": NR, "NI": NI,
                        "l2": "inputs larger than L2 (grand mobility %.2f GB)" % (8 * (11 * N) ** 2 / 1e9),
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
-            "phases_ms": {"assembly": ph[0], "lub": ph[1], "solve": ph[2]},
+            "phases_ms": {"assembly": ph[0], "lub": ph[1], "solve": ph[2], "refinement": ph[3]},
+            "plain_fp64": plain,
+            "refinement": {"iterations": [i[2] for i in infos], "residual": [i[3] for i in infos]},
             "kernels": {"assembly_tflops": asm_rate, "solve_tflops": solve_rate,
                         "assembly_algorithmic_flop": asm_flop, "solve_algorithmic_flop": solve_flops(N, args.precision)},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}

@@ -64,8 +64,9 @@ const char* rsd_ctx_last_error(const rsd_ctx* ctx);
 /* The context's CUDA stream (a cudaStream_t), for callers that want to order
  * their own work after _dev calls. */
 void* rsd_ctx_stream(rsd_ctx* ctx);
-/* Device-time of the last call's phases in milliseconds (assembly, lub,
- * solve, update), measured with CUDA events on the context stream. */
+/* Device-time of the last step's phases in milliseconds: assembly, lub,
+ * solve (including the update), and the refinement part of the solve (mixed
+ * form; 0 otherwise), measured with CUDA events on the context stream. */
 int rsd_ctx_phase_ms(const rsd_ctx* ctx, double ms[4]);
 /* Diagnostic (no counterpart in the reference): kernel launches issued by
  * this library since it was loaded, over all contexts. */

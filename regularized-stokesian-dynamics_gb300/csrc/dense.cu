@@ -154,6 +154,170 @@ __global__ void __launch_bounds__(256) gemm_kernel(GemmP g) {
     }
 }
 
+// FP32 GEMM with 16-byte vector accesses (aligned operands only): 128 x 128
+// tile per CTA of 256 threads, each thread an 8 x 8 block made of two 4-row
+// and two 4-column strips, so the shared-memory fragments and the C
+// epilogue are float4 accesses; k in steps of 8, double-buffered with the
+// next tile prefetched into registers.
+__global__ void __launch_bounds__(256) sgemm_vec(GemmP g) {
+  constexpr int BM = 128, BN = 128, BK = 8;
+  const int row0 = blockIdx.x * BM, col0 = blockIdx.y * BN;
+  if (g.uplo && row0 >= col0 + BN) return;
+  int kbeg = 0;
+  if (g.kA_row) kbeg = max(kbeg, row0 + g.offA);
+  if (g.kB_col) kbeg = max(kbeg, col0 + g.offB);
+  kbeg &= ~3;  // stays 16-byte aligned; the extra k columns are zeros in op(A)/op(B)
+  const int kend = g.k;
+  __shared__ __align__(16) float As[2][BK][BM];
+  __shared__ __align__(16) float Bs[2][BK][BN];
+  const int t = threadIdx.x, tx = t % 16, ty = t / 16;
+  const float* A = (const float*)g.A;
+  const float* B = (const float*)g.B;
+  float4 ra, rb;
+  // op(A) tile element coordinates of this thread's float4
+  int ai, ap, bc, bp;
+  if (!g.ta) {
+    ai = (t % 32) * 4;  // 4 consecutive rows
+    ap = t / 32;
+  } else {
+    ai = t / 2;  // one row, 4 consecutive k
+    ap = (t % 2) * 4;
+  }
+  if (!g.tb) {
+    bc = t / 2;  // one column, 4 consecutive k
+    bp = (t % 2) * 4;
+  } else {
+    bc = (t % 32) * 4;  // 4 consecutive columns
+    bp = t / 32;
+  }
+  auto ldA = [&](int k0) {
+    float v[4];
+    if (!g.ta) {
+      const int gr = row0 + ai, gk = k0 + ap;
+      if (gk < kend && gr + 3 < g.m) {
+        ra = *reinterpret_cast<const float4*>(A + gr + (int64_t)gk * g.lda);
+        return;
+      }
+      for (int q = 0; q < 4; q++) v[q] = (gk < kend && gr + q < g.m) ? A[gr + q + (int64_t)gk * g.lda] : 0.f;
+    } else {
+      const int gr = row0 + ai, gk = k0 + ap;
+      if (gr < g.m && gk + 3 < kend) {
+        ra = *reinterpret_cast<const float4*>(A + gk + (int64_t)gr * g.lda);
+        return;
+      }
+      for (int q = 0; q < 4; q++) v[q] = (gr < g.m && gk + q < kend) ? A[gk + q + (int64_t)gr * g.lda] : 0.f;
+    }
+    ra = make_float4(v[0], v[1], v[2], v[3]);
+  };
+  auto ldB = [&](int k0) {
+    float v[4];
+    if (!g.tb) {
+      const int gc = col0 + bc, gk = k0 + bp;
+      if (gc < g.n && gk + 3 < kend) {
+        rb = *reinterpret_cast<const float4*>(B + gk + (int64_t)gc * g.ldb);
+        return;
+      }
+      for (int q = 0; q < 4; q++) v[q] = (gc < g.n && gk + q < kend) ? B[gk + q + (int64_t)gc * g.ldb] : 0.f;
+    } else {
+      const int gc = col0 + bc, gk = k0 + bp;
+      if (gk < kend && gc + 3 < g.n) {
+        rb = *reinterpret_cast<const float4*>(B + gc + (int64_t)gk * g.ldb);
+        return;
+      }
+      for (int q = 0; q < 4; q++) v[q] = (gk < kend && gc + q < g.n) ? B[gc + q + (int64_t)gk * g.ldb] : 0.f;
+    }
+    rb = make_float4(v[0], v[1], v[2], v[3]);
+  };
+  auto stA = [&](int buf) {
+    if (!g.ta) {
+      *reinterpret_cast<float4*>(&As[buf][ap][ai]) = ra;
+    } else {
+      As[buf][ap + 0][ai] = ra.x;
+      As[buf][ap + 1][ai] = ra.y;
+      As[buf][ap + 2][ai] = ra.z;
+      As[buf][ap + 3][ai] = ra.w;
+    }
+  };
+  auto stB = [&](int buf) {
+    if (!g.tb) {
+      Bs[buf][bp + 0][bc] = rb.x;
+      Bs[buf][bp + 1][bc] = rb.y;
+      Bs[buf][bp + 2][bc] = rb.z;
+      Bs[buf][bp + 3][bc] = rb.w;
+    } else {
+      *reinterpret_cast<float4*>(&Bs[buf][bp][bc]) = rb;
+    }
+  };
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; i++)
+#pragma unroll
+    for (int j = 0; j < 8; j++) acc[i][j] = 0.f;
+  int buf = 0;
+  if (kbeg < kend) {
+    ldA(kbeg);
+    ldB(kbeg);
+    stA(0);
+    stB(0);
+  }
+  __syncthreads();
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+    const bool more = k0 + BK < kend;
+    if (more) {
+      ldA(k0 + BK);
+      ldB(k0 + BK);
+    }
+#pragma unroll
+    for (int p = 0; p < BK; p++) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][p][tx * 4]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][p][64 + tx * 4]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[buf][p][ty * 4]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[buf][p][64 + ty * 4]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    if (more) {
+      stA(buf ^ 1);
+      stB(buf ^ 1);
+    }
+    __syncthreads();
+    buf ^= 1;
+  }
+  float* C = (float*)g.C;
+  const float alpha = (float)g.alpha, beta = (float)g.beta;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const int c = col0 + (j < 4 ? ty * 4 + j : 64 + ty * 4 + j - 4);
+    if (c >= g.n) continue;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int r = row0 + h * 64 + tx * 4;
+      float* pc = C + r + (int64_t)c * g.ldc;
+      const float* av = &acc[h * 4][j];
+      if (r + 3 < g.m) {
+        float4 o;
+        if (g.beta == 0.0) {
+          o = make_float4(alpha * av[0], alpha * av[8], alpha * av[16], alpha * av[24]);
+        } else {
+          const float4 old = *reinterpret_cast<const float4*>(pc);
+          o = make_float4(alpha * av[0] + beta * old.x, alpha * av[8] + beta * old.y, alpha * av[16] + beta * old.z,
+                          alpha * av[24] + beta * old.w);
+        }
+        *reinterpret_cast<float4*>(pc) = o;
+      } else {
+        for (int q = 0; q < 4; q++)
+          if (r + q < g.m) pc[q] = (g.beta == 0.0) ? alpha * av[8 * q] : alpha * av[8 * q] + beta * pc[q];
+      }
+    }
+  }
+}
+
+inline bool aligned16(const void* p, int64_t ld) { return ((uintptr_t)p % 16 == 0) && (ld % 4 == 0); }
+
 template <typename T>
 struct Tile;
 template <>
@@ -168,6 +332,11 @@ struct Tile<float> {
 template <typename T>
 void launch_gemm(cudaStream_t s, const GemmP& g) {
   if (g.m <= 0 || g.n <= 0) return;
+  if (sizeof(T) == 4 && aligned16(g.A, g.lda) && aligned16(g.B, g.ldb) && aligned16(g.C, g.ldc)) {
+    dim3 grd((g.m + 127) / 128, (g.n + 127) / 128);
+    sgemm_vec<<<grd, 256, 0, s>>>(g); RSD_LAUNCH_NOTE();
+    return;
+  }
   constexpr int BM = Tile<T>::BM, BN = Tile<T>::BN, BK = Tile<T>::BK;
   dim3 grd((g.m + BM - 1) / BM, (g.n + BN - 1) / BN);
   gemm_kernel<T, BM, BN, BK><<<grd, 256, 0, s>>>(g); RSD_LAUNCH_NOTE();

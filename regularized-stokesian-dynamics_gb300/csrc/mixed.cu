@@ -233,6 +233,7 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   float* W_r = nullptr;
   RSD_TRY(rsd_diag_inverses_t<float>(ctx, (int)P, A32, P, "rpp32", &W_r));
   // refinement
+  cudaEventRecord(ctx->ev[7], s);
   RSD_CUDA(ctx, cudaMemsetAsync(f, 0, sizeof(double) * nr * n, s));
   RSD_CUDA(ctx, cudaMemsetAsync(U, 0, sizeof(double) * nr * P, s));
   double worst = 0.0;

@@ -302,11 +302,14 @@ extern "C" int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, co
     cudaEventElapsedTime(&t63, ctx->ev[6], ctx->ev[3]);
     ctx->phase_ms[1] = t26;
     ctx->phase_ms[2] = t12 + t63 + t45;
+    float t73;  // refinement part of the solve (event 7 = factors done)
+    cudaEventElapsedTime(&t73, ctx->ev[7], ctx->ev[3]);
+    ctx->phase_ms[3] = t73;
   } else {
     ctx->phase_ms[1] = t23;
     ctx->phase_ms[2] = t12 + t45;
   }
-  ctx->phase_ms[3] = 0;
+  if (p->precision != RSD_PREC_MIXED) ctx->phase_ms[3] = 0;
   double sxx = 0.0;
   for (int b = 0; b < 256; b++) sxx += hred[b];
   const double f6 = 6.0 * RSD_PI * p->mu_f * 1.0;  // radii_test = 1 after non-dimensionalisation
