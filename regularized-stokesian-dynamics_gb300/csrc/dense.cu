@@ -740,6 +740,27 @@ int rsd_diag_inverses_t(rsd_ctx* ctx, int n, const T* U, int64_t ldu, const char
   return RSD_OK;
 }
 
+// In-place inverse of an upper triangular matrix A (n x n, lower part zero):
+// blocked, left to right; W holds the inverses of A's NB diagonal blocks.
+template <typename T>
+int trtri_inplace_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, const T* W, T* T1, int64_t ldt) {
+  cudaStream_t s = ctx->stream;
+  for (int j0 = 0, b = 0; j0 < n; j0 += NB, b++) {
+    const int jb = n - j0 < NB ? n - j0 : NB;
+    const T* Wb = W + (size_t)b * NB * NB;
+    if (j0 > 0) {
+      GemmP g = gp(j0, jb, j0, 1.0, d_A, lda, 0, d_A + (int64_t)j0 * lda, lda, 0, 0.0, T1, ldt);
+      g.kA_row = 1;
+      g.offA = 0;
+      launch_gemm<T>(s, g);
+      launch_gemm<T>(s, gp(j0, jb, jb, -1.0, T1, ldt, 0, Wb, NB, 0, 0.0, d_A + (int64_t)j0 * lda, lda));
+    }
+    RSD_CUDA(ctx, cudaMemcpy2DAsync(d_A + j0 + (int64_t)j0 * lda, lda * sizeof(T), Wb, NB * sizeof(T),
+                                    jb * sizeof(T), jb, cudaMemcpyDeviceToDevice, s));
+  }
+  return RSD_OK;
+}
+
 // A <- A^-1 (upper triangle) from its upper Cholesky factor in A
 template <typename T>
 int rsd_potri_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, const char* tag) {
@@ -749,19 +770,7 @@ int rsd_potri_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, const char* tag)
   T* T1 = (T*)rsd_scratch(ctx, sizeof(T) == 8 ? "potri_T1_d" : "potri_T1_s", sizeof(T) * (size_t)NB * n);
   if (!T1) return RSD_ENOMEM;
   RSD_TRY(rsd_zero_lower_t<T>(ctx, n, d_A, lda));
-  for (int j0 = 0, b = 0; j0 < n; j0 += NB, b++) {
-    const int jb = n - j0 < NB ? n - j0 : NB;
-    T* Wb = W + (size_t)b * NB * NB;
-    if (j0 > 0) {
-      GemmP g = gp(j0, jb, j0, 1.0, d_A, lda, 0, d_A + (int64_t)j0 * lda, lda, 0, 0.0, T1, n);
-      g.kA_row = 1;
-      g.offA = 0;
-      launch_gemm<T>(s, g);
-      launch_gemm<T>(s, gp(j0, jb, jb, -1.0, T1, n, 0, Wb, NB, 0, 0.0, d_A + (int64_t)j0 * lda, lda));
-    }
-    RSD_CUDA(ctx, cudaMemcpy2DAsync(d_A + j0 + (int64_t)j0 * lda, lda * sizeof(T), Wb, NB * sizeof(T),
-                                    jb * sizeof(T), jb, cudaMemcpyDeviceToDevice, s));
-  }
+  RSD_TRY(trtri_inplace_t<T>(ctx, n, d_A, lda, W, T1, n));
   for (int i0 = 0; i0 < n; i0 += NB) {
     const int ib = n - i0 < NB ? n - i0 : NB;
     const int m = i0 + ib, k = n - i0;
@@ -773,6 +782,64 @@ int rsd_potri_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, const char* tag)
     launch_gemm<T>(s, g);
     RSD_CUDA(ctx, cudaMemcpy2DAsync(d_A + (int64_t)i0 * lda, lda * sizeof(T), T1, n * sizeof(T), m * sizeof(T), ib,
                                     cudaMemcpyDeviceToDevice, s));
+  }
+  RSD_CUDA(ctx, cudaGetLastError());
+  return RSD_OK;
+}
+
+// Inverses of the NB2 x NB2 diagonal blocks of an upper factor U, for the
+// wide-block solves: each block copied out (lower part zero) and inverted in
+// place by the blocked triangular inverse.  W2: nblk2 blocks of NB2 x NB2.
+constexpr int NB2 = 512;
+__global__ void copy_upper_block(int jb, const float* __restrict__ U, int64_t ldu, float* __restrict__ D) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= NB2 * NB2) return;
+  const int i = t % NB2, j = t / NB2;
+  D[t] = (i < jb && j < jb && i <= j) ? U[i + (int64_t)j * ldu] : (i == j ? 1.0f : 0.0f);
+}
+
+int rsd_wide_inverses_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const char* tag, float** W2out) {
+  const int nblk2 = (n + NB2 - 1) / NB2;
+  std::string name = std::string("wide_W_") + tag;
+  float* W2 = (float*)rsd_scratch(ctx, name.c_str(), sizeof(float) * (size_t)nblk2 * NB2 * NB2);
+  float* Wt = (float*)rsd_scratch(ctx, "wide_Wsmall", sizeof(float) * (size_t)(NB2 / NB) * NB * NB);
+  float* T1 = (float*)rsd_scratch(ctx, "wide_T1", sizeof(float) * (size_t)NB * NB2);
+  if (!W2 || !Wt || !T1) return RSD_ENOMEM;
+  RSD_TRY(ensure_attrs<float>(ctx));
+  for (int b = 0; b < nblk2; b++) {
+    const int j0 = b * NB2, jb = n - j0 < NB2 ? n - j0 : NB2;
+    float* D = W2 + (size_t)b * NB2 * NB2;
+    copy_upper_block<<<(NB2 * NB2 + 255) / 256, 256, 0, ctx->stream>>>(jb, U + j0 + (int64_t)j0 * ldu, ldu, D); RSD_LAUNCH_NOTE();
+    trtri_diag<float><<<NB2 / NB, 256, smem_potf2<float>(NB), ctx->stream>>>(NB2, D, NB2, Wt); RSD_LAUNCH_NOTE();
+    RSD_TRY(trtri_inplace_t<float>(ctx, NB2, D, NB2, Wt, T1, NB2));
+  }
+  RSD_CUDA(ctx, cudaGetLastError());
+  *W2out = W2;
+  return RSD_OK;
+}
+
+// (U^T U) X = B with the NB2 block inverses: per block two wide GEMVs
+// (diagonal block by its inverse, then the update of the remaining rows).
+// X holds B on entry; Y is a work vector of the same shape.
+int rsd_potrs_wide_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const float* W2, float* X, int64_t ldx,
+                     int nrhs, float* Y) {
+  const int nblk2 = (n + NB2 - 1) / NB2;
+  // forward: U^T y = b, y_b = W_b^T (b_b - sum) ; X keeps the running rhs
+  for (int b = 0; b < nblk2; b++) {
+    const int j0 = b * NB2, jb = n - j0 < NB2 ? n - j0 : NB2, rest = n - j0 - jb;
+    RSD_TRY(rsd_gemv<float>(ctx, 1, jb, jb, 1.0f, W2 + (size_t)b * NB2 * NB2, NB2, X + j0, ldx, nrhs, 0.0f, Y + j0,
+                            ldx));
+    if (rest > 0)
+      RSD_TRY(rsd_gemv<float>(ctx, 1, rest, jb, -1.0f, U + j0 + (int64_t)(j0 + jb) * ldu, ldu, Y + j0, ldx, nrhs, 1.0f,
+                              X + j0 + jb, ldx));
+  }
+  // backward: U x = y ; Y keeps the running rhs, X receives x
+  for (int b = nblk2 - 1; b >= 0; b--) {
+    const int j0 = b * NB2, jb = n - j0 < NB2 ? n - j0 : NB2;
+    RSD_TRY(rsd_gemv<float>(ctx, 0, jb, jb, 1.0f, W2 + (size_t)b * NB2 * NB2, NB2, Y + j0, ldx, nrhs, 0.0f, X + j0,
+                            ldx));
+    if (j0 > 0)
+      RSD_TRY(rsd_gemv<float>(ctx, 0, j0, jb, -1.0f, U + (int64_t)j0 * ldu, ldu, X + j0, ldx, nrhs, 1.0f, Y, ldx));
   }
   RSD_CUDA(ctx, cudaGetLastError());
   return RSD_OK;

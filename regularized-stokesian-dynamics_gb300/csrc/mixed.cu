@@ -36,6 +36,9 @@ template <typename T>
 int rsd_mirror_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda);
 template <typename T>
 int rsd_diag_inverses_t(rsd_ctx* ctx, int n, const T* U, int64_t ldu, const char* tag, T** Wout);
+int rsd_wide_inverses_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const char* tag, float** W2out);
+int rsd_potrs_wide_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const float* W2, float* X, int64_t ldx,
+                     int nrhs, float* Y);
 
 namespace {
 
@@ -196,11 +199,11 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   float* M32 = (float*)rsd_scratch(ctx, "mixed_M32", sizeof(float) * n * n);
   float* A32 = (float*)rsd_scratch(ctx, "mixed_A32", sizeof(float) * P * P);
   double* V = (double*)rsd_scratch(ctx, "mixed_vec", sizeof(double) * (size_t)nr * (7 * n + 2 * P) + 64 * 8);
-  float* V32 = (float*)rsd_scratch(ctx, "mixed_vec32", sizeof(float) * (size_t)nr * (n + P));
+  float* V32 = (float*)rsd_scratch(ctx, "mixed_vec32", sizeof(float) * (size_t)nr * (2 * n + 2 * P));
   if (!L || !M32 || !A32 || !V || !V32) return RSD_ENOMEM;
   double *f = V, *U = f + nr * n, *w = U + nr * P, *r1 = w + nr * n, *Lw = r1 + nr * n, *r2 = Lw + nr * n,
          *y = r2 + nr * P, *y2 = y + nr * n, *dv = y2 + nr * n, *nrm = dv + nr * n;
-  float *t32 = V32, *u32 = V32 + nr * n;
+  float *t32 = V32, *u32 = V32 + nr * n, *ywork = u32 + nr * P;
   // dense FP64 lubrication matrix (R_lub - R_2B in the grand layout)
   int nc = 0;
   if (p->use_lub) {
@@ -219,7 +222,7 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
     return rsd_fail(ctx, inf, "FP32 factor of the grand mobility: leading minor %d not positive", inf);
   }
   float* W_m = nullptr;
-  RSD_TRY(rsd_diag_inverses_t<float>(ctx, (int)n, M32, n, "m32", &W_m));
+  RSD_TRY(rsd_wide_inverses_s(ctx, (int)n, M32, n, "m32", &W_m));
   // A^-1 from the trailing factor block, then RPP32 = A^-1 + rfu and its factor
   copy_block_f<<<nblk(P * P), 256, 0, s>>>(P, P, M32 + Q + Q * n, n, A32, P); RSD_LAUNCH_NOTE();
   RSD_TRY(rsd_potri_upper_t<float>(ctx, (int)P, A32, P, "a32"));
@@ -231,7 +234,7 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
     return rsd_fail(ctx, inf, "FP32 factor of RPP: leading minor %d not positive", inf);
   }
   float* W_r = nullptr;
-  RSD_TRY(rsd_diag_inverses_t<float>(ctx, (int)P, A32, P, "rpp32", &W_r));
+  RSD_TRY(rsd_wide_inverses_s(ctx, (int)P, A32, P, "rpp32", &W_r));
   // refinement
   cudaEventRecord(ctx->ev[7], s);
   RSD_CUDA(ctx, cudaMemsetAsync(f, 0, sizeof(double) * nr * n, s));
@@ -257,15 +260,15 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
     if (worst <= tol || it >= maxit) break;
     // y = M^-1 r1
     to32_perm<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, r1, n, 0, t32); RSD_LAUNCH_NOTE();
-    RSD_TRY(rsd_potrs_upper_t<float>(ctx, (int)n, M32, n, t32, n, nr, "m32", W_m));
+    RSD_TRY(rsd_potrs_wide_s(ctx, (int)n, M32, n, W_m, t32, n, nr, ywork));
     from32_perm<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, t32, y, 0); RSD_LAUNCH_NOTE();
     // dU = RPP^-1 (r2 - y_P)
     rhs_u<<<nblk(P * nr), 256, 0, s>>>(P, n, nr, r2, y, u32); RSD_LAUNCH_NOTE();
-    RSD_TRY(rsd_potrs_upper_t<float>(ctx, (int)P, A32, P, u32, P, nr, "rpp32", W_r));
+    RSD_TRY(rsd_potrs_wide_s(ctx, (int)P, A32, P, W_r, u32, P, nr, ywork));
     // df = y + M^-1 [dU; 0]
     du_vec<<<nblk(n * nr), 256, 0, s>>>(P, n, nr, u32, dv); RSD_LAUNCH_NOTE();
     to32_perm<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, dv, n, 1, t32); RSD_LAUNCH_NOTE();
-    RSD_TRY(rsd_potrs_upper_t<float>(ctx, (int)n, M32, n, t32, n, nr, "m32", W_m));
+    RSD_TRY(rsd_potrs_wide_s(ctx, (int)n, M32, n, W_m, t32, n, nr, ywork));
     from32_perm<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, t32, y, 1); RSD_LAUNCH_NOTE();
     update_fu<<<nblk(n * nr), 256, 0, s>>>(P, n, nr, y, u32, f, U); RSD_LAUNCH_NOTE();
   }
