@@ -71,6 +71,11 @@ int rsd_ctx_phase_ms(const rsd_ctx* ctx, double ms[4]);
 /* Diagnostic (no counterpart in the reference): kernel launches issued by
  * this library since it was loaded, over all contexts. */
 long long rsd_launch_count(void);
+/* Selects the trailing-update kernel of the FP32 factorisations used by the
+ * mixed-precision form: 1 (the default) = tcgen05 TF32 tensor cores wherever
+ * the layout allows (16-byte aligned blocks, leading dimension a multiple of
+ * 4), 0 = the FP32 SIMT GEMM.  The FP64 form is unaffected. */
+int rsd_ctx_set_tensor_cores(rsd_ctx* ctx, int enable);
 
 /* ---------------------------------------------------------------- lattice */
 /* SET_LATTICE_SKEW (src/csd_post.f90:105-136) with MAT_INV3
@@ -212,6 +217,18 @@ int rsd_stepper_stokesian(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_step_pa
 int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_step_params* p, double* d_conf,
                               const double* d_radii, const double* d_Fe, double* d_U_pos, double* d_SijN,
                               double yeta_mu[5], rsd_step_info* info);
+
+/* ------------------------------------------ FP32 blocks of the mixed form */
+/* The reference solves in FP64 only (LAPACK DPOTRF/DPOTRI); these are the
+ * single-precision building blocks that the mixed form's refinement uses as a
+ * preconditioner, exported for testing and for callers that build their own
+ * refinement.  Device pointers, column-major. */
+/* C (n x n, the 128 x 128 tiles on and above the diagonal) -= P^T P with P
+ * k x n (ld ldp); k <= 128 for the tensor-core path. */
+int rsd_syrk_f32_dev(rsd_ctx* ctx, int32_t n, int32_t k, const float* d_P, int64_t ldp, float* d_C, int64_t ldc);
+/* Upper Cholesky factor in place (lower triangle left as scratch); info as
+ * DPOTRF. */
+int rsd_potrf_f32_dev(rsd_ctx* ctx, int32_t n, float* d_A, int64_t lda, int32_t* info);
 
 #ifdef __cplusplus
 }

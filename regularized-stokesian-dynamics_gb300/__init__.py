@@ -92,6 +92,9 @@ _sig("rsd_stepper_stokesian", _i, [_vp, _vp, ctypes.POINTER(StepParams), _dp, _d
                                    ctypes.POINTER(StepInfo)])
 _sig("rsd_stepper_stokesian_dev", _i, [_vp, _vp, ctypes.POINTER(StepParams), _vp, _vp, _vp, _vp, _vp, _dp,
                                        ctypes.POINTER(StepInfo)])
+_sig("rsd_ctx_set_tensor_cores", _i, [_vp, _i])
+_sig("rsd_syrk_f32_dev", _i, [_vp, _i32, _i32, _vp, _i64, _vp, _i64])
+_sig("rsd_potrf_f32_dev", _i, [_vp, _i32, _vp, _i64, _ip])
 
 EXPORTED = [n for n in dir(_lib) if n.startswith("rsd_")]
 
@@ -140,6 +143,11 @@ class Context:
     @property
     def stream(self):
         return _lib.rsd_ctx_stream(self.h)
+
+    def set_tensor_cores(self, enable: bool):
+        """tcgen05 TF32 (True, the default) or FP32 SIMT trailing updates in
+        the FP32 factorisations of the mixed-precision form."""
+        self.check(_lib.rsd_ctx_set_tensor_cores(self.h, 1 if enable else 0))
 
     def close(self):
         if self.h:
@@ -216,6 +224,30 @@ def per_grpery_inv_fri_dev(ctx: Context, pos, radii, lattice: Lattice, ews_err, 
                                               ews_err, mu_f, correction_method, buf.data_ptr(), n))
     _sync_ctx(ctx)
     return buf.t()
+
+
+def syrk_f32_dev(ctx: Context, P, C):
+    """C -= P^T P on the 128 x 128 tiles on and above the diagonal.  P (k, n)
+    and C (n, n) are column-major FP32 device matrices passed as the
+    transpose views of contiguous torch tensors (P.t() of an (n, k) tensor)."""
+    import torch
+    k, n = P.shape
+    assert C.shape == (n, n) and P.stride(0) == 1 and C.stride(0) == 1
+    torch.cuda.synchronize(P.device)
+    ctx.check(_lib.rsd_syrk_f32_dev(ctx.h, n, k, P.data_ptr(), P.stride(1), C.data_ptr(), C.stride(1)))
+    return C
+
+
+def potrf_f32_dev(ctx: Context, A):
+    """Upper Cholesky factor in place of a column-major FP32 device matrix
+    (a transpose view, as syrk_f32_dev); returns info."""
+    import torch
+    n = A.shape[0]
+    assert A.shape == (n, n) and A.stride(0) == 1
+    info = ctypes.c_int32(0)
+    torch.cuda.synchronize(A.device)
+    ctx.check(_lib.rsd_potrf_f32_dev(ctx.h, n, A.data_ptr(), A.stride(1), ctypes.byref(info)))
+    return info.value
 
 
 def _sync_ctx(ctx):

@@ -109,6 +109,12 @@ extern "C" int rsd_ctx_destroy(rsd_ctx* c) {
 
 extern "C" const char* rsd_ctx_last_error(const rsd_ctx* c) { return c ? c->err.c_str() : "no context"; }
 extern "C" void* rsd_ctx_stream(rsd_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+extern "C" int rsd_ctx_set_tensor_cores(rsd_ctx* c, int enable) {
+  if (!c) return RSD_EARG;
+  c->use_tc = enable ? 1 : 0;
+  return RSD_OK;
+}
 extern "C" int rsd_ctx_phase_ms(const rsd_ctx* c, double ms[4]) {
   if (!c || !ms) return RSD_EARG;
   for (int i = 0; i < 4; i++) ms[i] = c->phase_ms[i];

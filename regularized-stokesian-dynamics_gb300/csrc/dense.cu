@@ -21,6 +21,8 @@
 
 #include <string>
 
+#include <type_traits>
+
 #include "rsd_internal.cuh"
 
 namespace {
@@ -371,6 +373,7 @@ __global__ void __launch_bounds__(256) potf2_upper(T* __restrict__ A, int64_t ld
                                                    int j0) {
   extern __shared__ unsigned char smraw[];
   T* S = (T*)smraw;  // jb x jb, column-major, ld = jb
+  T* rowk = S + jb * jb;  // scaled pivot row, read without bank conflicts
   __shared__ int failed;
   const int t = threadIdx.x, tx = t % 16, ty = t / 16;
   for (int e = t; e < jb * jb; e += blockDim.x) {
@@ -392,17 +395,163 @@ __global__ void __launch_bounds__(256) potf2_upper(T* __restrict__ A, int64_t ld
     __syncthreads();
     if (failed) break;
     const T rk = T(1) / S[k + k * jb];
-    for (int j = k + 1 + t; j < jb; j += blockDim.x) S[k + j * jb] *= rk;
+    for (int j = k + 1 + t; j < jb; j += blockDim.x) {
+      const T v = S[k + j * jb] * rk;
+      S[k + j * jb] = v;
+      rowk[j] = v;
+    }
     __syncthreads();
     for (int j = k + 1 + ty; j < jb; j += 16) {
-      const T skj = S[k + j * jb];
-      for (int i = k + 1 + tx; i <= j; i += 16) S[i + j * jb] -= S[k + i * jb] * skj;
+      const T skj = rowk[j];
+      for (int i = k + 1 + tx; i <= j; i += 16) S[i + j * jb] -= rowk[i] * skj;
     }
     __syncthreads();
   }
   for (int e = t; e < jb * jb; e += blockDim.x) {
     const int i = e % jb, j = e / jb;
     if (i <= j) A[i + (int64_t)j * lda] = S[e];
+  }
+}
+
+// FP32 diagonal block (jb <= 128): upper Cholesky factor U and its inverse
+// W = U^-1 in one CTA, both in padded shared memory (ld 129, so that row and
+// column walks hit distinct banks).  The factor is right-looking over 32-wide
+// sub-blocks: one warp factors the 32 x 32 diagonal sub-block in registers
+// (lane = column), one thread per column solves the sub-block's row panel,
+// and all threads update the trailing block.  The inverse inverts the 32 x 32
+// diagonal sub-blocks (one warp each, back substitution in registers) and
+// then fills the off-diagonal sub-blocks level by level:
+// W_ij = -W_ii (sum_{p=i+1..j} U_ip W_pj).  U goes back to A; W goes to Wout
+// (NB x NB, lower part and rows/columns past jb zero).  info as DPOTRF.
+constexpr int PLD = NB + 1;
+constexpr int SMEM_POTF2_INV = (2 * NB * PLD + 3 * 32 * 33) * (int)sizeof(float);
+__global__ void __launch_bounds__(256) potf2_inv_f32(float* __restrict__ A, int64_t lda, int jb,
+                                                     int* __restrict__ info, int j0, float* __restrict__ Wout) {
+  extern __shared__ unsigned char smraw[];
+  float* S = (float*)smraw;   // U, NB x NB, ld PLD
+  float* Wm = S + NB * PLD;   // W, NB x NB, ld PLD
+  float* Tt = Wm + NB * PLD;  // 3 temporaries of 32 x 32, ld 33
+  __shared__ int failed;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  for (int e = t; e < NB * NB; e += 256) {
+    const int i = e % NB, j = e / NB;
+    S[i + j * PLD] = (i < jb && j < jb && i <= j) ? A[i + (int64_t)j * lda] : 0.f;
+    Wm[i + j * PLD] = 0.f;
+  }
+  if (t == 0) failed = 0;
+  __syncthreads();
+  const int nsub = (jb + 31) / 32;
+  for (int kb = 0; kb < nsub; kb++) {
+    const int k0 = kb * 32, kw = min(32, jb - k0);
+    if (warp == 0) {
+      float r[32];
+#pragma unroll
+      for (int i = 0; i < 32; i++) r[i] = S[(k0 + i) + (k0 + lane) * PLD];
+      int bad = 0;
+#pragma unroll
+      for (int k = 0; k < 32; k++) {
+        if (k < kw && !bad) {
+          const float piv = __shfl_sync(0xffffffffu, r[k], k);
+          if (!(piv > 0.f) || !isfinite(piv)) {
+            bad = k + 1;
+          } else {
+            const float d = sqrtf(piv);
+            if (lane > k) r[k] = r[k] / d;
+            else if (lane == k) r[k] = d;
+#pragma unroll
+            for (int i = k + 1; i < 32; i++) {
+              const float uki = __shfl_sync(0xffffffffu, r[k], i);
+              if (lane >= i) r[i] -= uki * r[k];
+            }
+          }
+        }
+      }
+      if (bad) {
+        if (lane == 0) {
+          failed = 1;
+          atomicCAS(info, 0, j0 + k0 + bad);
+        }
+      } else if (lane < kw) {
+#pragma unroll
+        for (int i = 0; i < 32; i++)
+          if (i <= lane) S[(k0 + i) + (k0 + lane) * PLD] = r[i];
+      }
+    }
+    __syncthreads();
+    if (failed) return;
+    const int m0 = k0 + kw, mw = jb - m0;
+    if (t < mw) {  // row panel: D^T X = R, one column per thread
+      const int c = m0 + t;
+      float x[32];
+#pragma unroll
+      for (int i = 0; i < 32; i++) {
+        float v = 0.f;
+        if (i < kw) {
+          v = S[(k0 + i) + c * PLD];
+#pragma unroll
+          for (int p = 0; p < i; p++) v -= S[(k0 + p) + (k0 + i) * PLD] * x[p];
+          v = v / S[(k0 + i) + (k0 + i) * PLD];
+        }
+        x[i] = v;
+      }
+#pragma unroll
+      for (int i = 0; i < 32; i++)
+        if (i < kw) S[(k0 + i) + c * PLD] = x[i];
+    }
+    __syncthreads();
+    for (int e = t; e < mw * mw; e += 256) {  // trailing update, upper part
+      const int i = e % mw, j = e / mw;
+      if (i <= j) {
+        float acc = 0.f;
+        for (int p = 0; p < kw; p++) acc += S[(k0 + p) + (m0 + i) * PLD] * S[(k0 + p) + (m0 + j) * PLD];
+        S[(m0 + i) + (m0 + j) * PLD] -= acc;
+      }
+    }
+    __syncthreads();
+  }
+  // inverse: diagonal 32 x 32 sub-blocks, one warp each
+  if (warp < nsub) {
+    const int k0 = warp * 32, kw = min(32, jb - k0);
+    float x[32];
+#pragma unroll
+    for (int ii = 31; ii >= 0; ii--) {
+      float v = 0.f;
+      if (ii < kw && lane < kw) {
+        v = (ii == lane) ? 1.f : 0.f;
+#pragma unroll
+        for (int p = ii + 1; p < 32; p++) v -= S[(k0 + ii) + (k0 + p) * PLD] * x[p];
+        v = v / S[(k0 + ii) + (k0 + ii) * PLD];
+      }
+      x[ii] = v;
+    }
+    if (lane < kw) {
+#pragma unroll
+      for (int i = 0; i < 32; i++) Wm[(k0 + i) + (k0 + lane) * PLD] = x[i];
+    }
+  }
+  __syncthreads();
+  for (int d = 1; d < nsub; d++) {
+    const int nb = nsub - d;
+    for (int e = t; e < nb * 1024; e += 256) {  // T_b = sum_p U_{bi,p} W_{p,bj}
+      const int r = e % 32, c = (e / 32) % 32, b = e / 1024, bi = b, bj = b + d;
+      float acc = 0.f;
+      for (int q = 32 * (bi + 1); q < 32 * (bj + 1); q++) acc += S[(32 * bi + r) + q * PLD] * Wm[q + (32 * bj + c) * PLD];
+      Tt[b * 32 * 33 + r + c * 33] = acc;
+    }
+    __syncthreads();
+    for (int e = t; e < nb * 1024; e += 256) {  // W_{bi,bj} = -W_{bi,bi} T_b
+      const int r = e % 32, c = (e / 32) % 32, b = e / 1024, bi = b, bj = b + d;
+      float acc = 0.f;
+#pragma unroll 8
+      for (int q = 0; q < 32; q++) acc += Wm[(32 * bi + r) + (32 * bi + q) * PLD] * Tt[b * 32 * 33 + q + c * 33];
+      Wm[(32 * bi + r) + (32 * bj + c) * PLD] = -acc;
+    }
+    __syncthreads();
+  }
+  for (int e = t; e < NB * NB; e += 256) {
+    const int i = e % NB, j = e / NB;
+    if (i < jb && j < jb && i <= j) A[i + (int64_t)j * lda] = S[i + j * PLD];
+    Wout[e] = (i < jb && j < jb && i <= j) ? Wm[i + j * PLD] : 0.f;
   }
 }
 
@@ -619,6 +768,7 @@ int ensure_attrs(rsd_ctx* ctx) {
   RSD_CUDA(ctx, cudaFuncSetAttribute(trsm_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_trsm<T>()));
   RSD_CUDA(ctx, cudaFuncSetAttribute(trsv_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_trsv<T>()));
   RSD_CUDA(ctx, cudaFuncSetAttribute(trtri_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_potf2<T>(NB)));
+  RSD_CUDA(ctx, cudaFuncSetAttribute(potf2_inv_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_POTF2_INV));
   done = true;
   return RSD_OK;
 }
@@ -694,36 +844,63 @@ int rsd_mirror_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda) {
 }
 
 template <typename T>
-int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const char* tag) {
+int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const char* tag, int tc) {
   if (n < 1 || lda < n) return rsd_fail(ctx, RSD_EARG, "potrf: n=%d lda=%lld", n, (long long)lda);
   RSD_TRY(ensure_attrs<T>(ctx));
   cudaStream_t s = ctx->stream;
   T* W = diag_inverses<T>(ctx, n, tag);
   if (!W) return RSD_ENOMEM;
-  RSD_CUDA(ctx, cudaMemsetAsync(ctx->d_info, 0, sizeof(int), s));
-  for (int j0 = 0; j0 < n; j0 += NB) {
+  constexpr bool F32 = std::is_same<T, float>::value;
+  T* T1 = nullptr;
+  if (F32) {
+    T1 = (T*)rsd_scratch(ctx, "potrf_panel_s", sizeof(T) * (size_t)NB * n);
+    if (!T1) return RSD_ENOMEM;
+  }
+  RSD_CUDA(ctx, cudaMemsetAsync(ctx->d_info, 0, 2 * sizeof(int), s));
+  for (int j0 = 0, b = 0; j0 < n; j0 += NB, b++) {
     const int jb = n - j0 < NB ? n - j0 : NB;
     T* Ajj = d_A + j0 + (int64_t)j0 * lda;
-    potf2_upper<T><<<1, 256, smem_potf2<T>(jb), s>>>(Ajj, lda, jb, ctx->d_info, j0); RSD_LAUNCH_NOTE();
     const int rest = n - j0 - jb;
+    T* Apan = d_A + j0 + (int64_t)(j0 + jb) * lda;
+    if constexpr (F32) {
+      // factor + inverse of the diagonal block, then the panel as W_jj^T B
+      T* Wb = W + (size_t)b * NB * NB;
+      potf2_inv_f32<<<1, 256, SMEM_POTF2_INV, s>>>(Ajj, lda, jb, ctx->d_info, j0, Wb); RSD_LAUNCH_NOTE();
+      if (rest > 0) {
+        launch_gemm<T>(s, gp(jb, rest, jb, 1.0, Wb, NB, 1, Apan, lda, 0, 0.0, T1, NB));
+        RSD_CUDA(ctx, cudaMemcpy2DAsync(Apan, lda * sizeof(T), T1, NB * sizeof(T), jb * sizeof(T), rest,
+                                        cudaMemcpyDeviceToDevice, s));
+      }
+    } else {
+      potf2_upper<T><<<1, 256, smem_potf2<T>(jb), s>>>(Ajj, lda, jb, ctx->d_info, j0); RSD_LAUNCH_NOTE();
+      if (rest > 0) {
+        trsm_panel<T><<<(rest + TRSM_COLS - 1) / TRSM_COLS, TRSM_COLS, smem_trsm<T>(), s>>>(Ajj, lda, jb, rest, Apan); RSD_LAUNCH_NOTE();
+      }
+    }
     if (rest > 0) {
-      T* Apan = d_A + j0 + (int64_t)(j0 + jb) * lda;
-      trsm_panel<T><<<(rest + TRSM_COLS - 1) / TRSM_COLS, TRSM_COLS, smem_trsm<T>(), s>>>(Ajj, lda, jb, rest, Apan); RSD_LAUNCH_NOTE();
       // trailing: A22 -= Apan^T Apan (upper tiles)
-      GemmP g = gp(rest, rest, jb, -1.0, Apan, lda, 1, Apan, lda, 0, 1.0, d_A + (j0 + jb) + (int64_t)(j0 + jb) * lda, lda);
+      T* A22 = d_A + (j0 + jb) + (int64_t)(j0 + jb) * lda;
+      if constexpr (F32) {
+        if (tc && ctx->use_tc && rsd_tc_syrk_ok(Apan, lda, A22, lda, jb)) {
+          RSD_TRY(rsd_tc_syrk(ctx, Apan, lda, jb, rest, A22, lda, ctx->d_info + 1));
+          continue;
+        }
+      }
+      GemmP g = gp(rest, rest, jb, -1.0, Apan, lda, 1, Apan, lda, 0, 1.0, A22, lda);
       g.uplo = 1;
       launch_gemm<T>(s, g);
     }
   }
-  // diagonal-block inverses for the solves
-  {
+  // diagonal-block inverses for the solves (the FP32 path made them above)
+  if (!F32) {
     const int nblk = (n + NB - 1) / NB;
     trtri_diag<T><<<nblk, 256, smem_potf2<T>(NB), s>>>(n, d_A, lda, W); RSD_LAUNCH_NOTE();
   }
   RSD_CUDA(ctx, cudaGetLastError());
-  RSD_CUDA(ctx, cudaMemcpyAsync(ctx->h_info, ctx->d_info, sizeof(int), cudaMemcpyDeviceToHost, s));
+  RSD_CUDA(ctx, cudaMemcpyAsync(ctx->h_info, ctx->d_info, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
   RSD_CUDA(ctx, cudaStreamSynchronize(s));
-  *info = *ctx->h_info;
+  *info = ctx->h_info[0];
+  if (ctx->h_info[1]) return rsd_fail(ctx, RSD_ETIMEOUT, "potrf: tensor-core update timed out (code %d)", ctx->h_info[1]);
   return RSD_OK;
 }
 
@@ -905,7 +1082,7 @@ template int rsd_gemv<float>(rsd_ctx*, int, int, int, float, const float*, int64
                              float*, int64_t);
 template int rsd_gemv<double>(rsd_ctx*, int, int, int, double, const double*, int64_t, const double*, int64_t, int,
                               double, double*, int64_t);
-template int rsd_potrf_upper_t<float>(rsd_ctx*, int, float*, int64_t, int*, const char*);
+template int rsd_potrf_upper_t<float>(rsd_ctx*, int, float*, int64_t, int*, const char*, int);
 template int rsd_potri_upper_t<float>(rsd_ctx*, int, float*, int64_t, const char*);
 template int rsd_potrs_upper_t<float>(rsd_ctx*, int, const float*, int64_t, float*, int64_t, int, const char*,
                                       const float*);
@@ -922,10 +1099,10 @@ int rsd_mirror_upper(rsd_ctx* ctx, int n, double* d_A, int64_t lda) {
   return rsd_mirror_upper_t<double>(ctx, n, d_A, lda);
 }
 int rsd_potrf_upper_tag(rsd_ctx* ctx, int n, double* d_A, int64_t lda, int* info, const char* tag) {
-  return rsd_potrf_upper_t<double>(ctx, n, d_A, lda, info, tag);
+  return rsd_potrf_upper_t<double>(ctx, n, d_A, lda, info, tag, 0);
 }
 int rsd_potrf_upper(rsd_ctx* ctx, int n, double* d_A, int64_t lda, int* info) {
-  return rsd_potrf_upper_t<double>(ctx, n, d_A, lda, info, "A");
+  return rsd_potrf_upper_t<double>(ctx, n, d_A, lda, info, "A", 0);
 }
 int rsd_potri_upper_tag(rsd_ctx* ctx, int n, double* d_A, int64_t lda, const char* tag) {
   return rsd_potri_upper_t<double>(ctx, n, d_A, lda, tag);
@@ -943,4 +1120,37 @@ int rsd_trsv_upper(rsd_ctx* ctx, int n, const double* d_U, int64_t ldu, double* 
                    int transpose) {
   (void)transpose;
   return rsd_potrs_upper_tag(ctx, n, d_U, ldu, d_X, ldx, nrhs, "A");
+}
+
+// ------------------------------------------------ FP32 exported blocks
+extern "C" int rsd_syrk_f32_dev(rsd_ctx* ctx, int32_t n, int32_t k, const float* d_P, int64_t ldp, float* d_C,
+                                int64_t ldc) {
+  if (!ctx) return RSD_EARG;
+  if (n < 1 || k < 1 || ldp < k || ldc < n || !d_P || !d_C)
+    return rsd_fail(ctx, RSD_EARG, "rsd_syrk_f32_dev: bad arguments");
+  RSD_TRY(rsd_set_device(ctx));
+  if (ctx->use_tc && k <= NB && rsd_tc_syrk_ok(d_P, ldp, d_C, ldc, k)) {
+    RSD_CUDA(ctx, cudaMemsetAsync(ctx->d_info + 1, 0, sizeof(int), ctx->stream));
+    RSD_TRY(rsd_tc_syrk(ctx, d_P, ldp, k, n, d_C, ldc, ctx->d_info + 1));
+    RSD_CUDA(ctx, cudaMemcpyAsync(ctx->h_info + 1, ctx->d_info + 1, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    RSD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->h_info[1]) return rsd_fail(ctx, RSD_ETIMEOUT, "syrk: tensor-core update timed out");
+    return RSD_OK;
+  }
+  GemmP g = gp(n, n, k, -1.0, d_P, ldp, 1, d_P, ldp, 0, 1.0, d_C, ldc);
+  g.uplo = 1;
+  launch_gemm<float>(ctx->stream, g);
+  RSD_CUDA(ctx, cudaGetLastError());
+  RSD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return RSD_OK;
+}
+
+extern "C" int rsd_potrf_f32_dev(rsd_ctx* ctx, int32_t n, float* d_A, int64_t lda, int32_t* info) {
+  if (!ctx) return RSD_EARG;
+  if (n < 1 || lda < n || !d_A || !info) return rsd_fail(ctx, RSD_EARG, "rsd_potrf_f32_dev: bad arguments");
+  RSD_TRY(rsd_set_device(ctx));
+  int inf = 0;
+  RSD_TRY(rsd_potrf_upper_t<float>(ctx, n, d_A, lda, &inf, "f32dev", 1));
+  *info = inf;
+  return RSD_OK;
 }

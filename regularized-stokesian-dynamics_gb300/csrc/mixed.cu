@@ -26,7 +26,7 @@ template <typename T>
 int rsd_gemv(rsd_ctx* ctx, int trans, int m, int k, T alpha, const T* A, int64_t lda, const T* X, int64_t ldx,
              int nrhs, T beta, T* y, int64_t ldy);
 template <typename T>
-int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const char* tag);
+int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const char* tag, int tc);
 template <typename T>
 int rsd_potri_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, const char* tag);
 template <typename T>
@@ -216,7 +216,9 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   // FP32 factor of M' (stresslets first)
   convert_perm<<<(unsigned)((n * n + 255) / 256), 256, 0, s>>>(nn, n, M, ld, M32); RSD_LAUNCH_NOTE();
   int inf = 0;
-  RSD_TRY(rsd_potrf_upper_t<float>(ctx, (int)n, M32, n, &inf, "m32"));
+  // TF32 tensor-core trailing updates here: the refinement's contraction
+  // scales with cond(M') (moderate) times the TF32 rounding
+  RSD_TRY(rsd_potrf_upper_t<float>(ctx, (int)n, M32, n, &inf, "m32", 1));
   if (inf) {
     info->info = inf;
     return rsd_fail(ctx, inf, "FP32 factor of the grand mobility: leading minor %d not positive", inf);
@@ -228,7 +230,9 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   RSD_TRY(rsd_potri_upper_t<float>(ctx, (int)P, A32, P, "a32"));
   RSD_TRY(rsd_mirror_upper_t<float>(ctx, (int)P, A32, P));
   add_lub_pp<<<nblk(P * P), 256, 0, s>>>(P, A32, L, n); RSD_LAUNCH_NOTE();
-  RSD_TRY(rsd_potrf_upper_t<float>(ctx, (int)P, A32, P, &inf, "rpp32"));
+  // FP32 SIMT updates here: cond(RPP) grows like the inverse lubrication
+  // gap, too large for TF32 rounding in the preconditioner
+  RSD_TRY(rsd_potrf_upper_t<float>(ctx, (int)P, A32, P, &inf, "rpp32", 0));
   if (inf) {
     info->info = inf;
     return rsd_fail(ctx, inf, "FP32 factor of RPP: leading minor %d not positive", inf);

@@ -31,6 +31,7 @@ struct rsd_ctx {
   std::map<std::string, rsd_buf> bufs;  // grow-only device buffers by name
   cudaEvent_t ev[8] = {};
   double phase_ms[4] = {0, 0, 0, 0};
+  int use_tc = 1;         // tcgen05 trailing updates in the FP32 factorisations
   int* d_info = nullptr;  // device-side status words
   int* h_info = nullptr;  // pinned mirror
 };
@@ -123,3 +124,8 @@ void rsd_gemm_f64(cudaStream_t s, int m, int n, int k, double alpha, const doubl
 int rsd_zero_lower(rsd_ctx* ctx, int n, double* d_A, int64_t lda);
 // A(rows x cols) += B, both column-major sub-blocks (step.cu)
 int rsd_axpy_block(rsd_ctx* ctx, int64_t rows, int64_t cols, const double* B, int64_t ldb, double* A, int64_t lda);
+
+// Tensor-core (tcgen05 TF32) trailing update of the FP32 blocked Cholesky
+// (tc_syrk.cu): C (rest x rest, upper tiles) -= P^T P, P kb x rest.
+int rsd_tc_syrk_ok(const float* panel, int64_t lda, const float* C, int64_t ldc, int kb);
+int rsd_tc_syrk(rsd_ctx* ctx, const float* panel, int64_t lda, int kb, int rest, float* C, int64_t ldc, int* d_err);
