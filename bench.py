@@ -49,7 +49,39 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-peaks", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="after the warm-up, run one step under the CUDA activity profiler and print the "
+                         "per-kernel device time instead of the JSON line")
     return ap.parse_args()
+
+
+def kernel_table(prof, top=40):
+    """Per-kernel device time of a torch.profiler run, from the kernel
+    activity records of its trace (these include the kernels this library
+    launches on its own stream)."""
+    import tempfile
+    rows = {}
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "trace.json")
+        prof.export_chrome_trace(path)
+        with open(path) as fp:
+            trace = json.load(fp)
+    for ev in trace.get("traceEvents", []):
+        if ev.get("cat") not in ("kernel", "gpu_memcpy", "gpu_memset") or "dur" not in ev:
+            continue
+        name = ev.get("name", "?")
+        for cut in ("(", " ["):
+            if cut in name and not name.startswith(cut):
+                name = name.split(cut)[0]
+        name = name.replace("(anonymous namespace)::", "").replace("void ", "")
+        c, tt = rows.get(name, (0, 0.0))
+        rows[name] = (c + 1, tt + float(ev["dur"]) / 1000.0)
+    total = sum(v[1] for v in rows.values())
+    out = ["total %.2f ms device time over %d records" % (total, sum(v[0] for v in rows.values())),
+           "%-60s %8s %12s %6s" % ("kernel", "launches", "total ms", "share")]
+    for name, (c, tt) in sorted(rows.items(), key=lambda kv: -kv[1][1])[:top]:
+        out.append("%-60s %8d %12.2f %5.1f%%" % (name[:60], c, tt, 100.0 * tt / max(total, 1e-30)))
+    return "\n".join(out)
 
 
 def dist_env():
@@ -310,6 +342,15 @@ def main():
 
     for _ in range(args.warmup):
         step()
+    if args.profile:
+        from torch.profiler import ProfilerActivity, profile
+        torch.cuda.synchronize(dev)
+        with profile(activities=[ProfilerActivity.CUDA]) as prof:
+            step()
+            torch.cuda.synchronize(dev)
+        if rank == 0:
+            print(kernel_table(prof))
+        return
     sampler = ClockSampler(local) if rank == 0 else None
     if ws > 1:
         dist.barrier()

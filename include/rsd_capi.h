@@ -71,11 +71,17 @@ int rsd_ctx_phase_ms(const rsd_ctx* ctx, double ms[4]);
 /* Diagnostic (no counterpart in the reference): kernel launches issued by
  * this library since it was loaded, over all contexts. */
 long long rsd_launch_count(void);
-/* Selects the trailing-update kernel of the FP32 factorisations used by the
- * mixed-precision form: 1 (the default) = tcgen05 TF32 tensor cores wherever
- * the layout allows (16-byte aligned blocks, leading dimension a multiple of
- * 4), 0 = the FP32 SIMT GEMM.  The FP64 form is unaffected. */
+/* Tensor cores in the FP32 factorisations of the mixed-precision form:
+ * 1 (the default) = tcgen05 kernels wherever the layout allows (16-byte
+ * aligned blocks, leading dimension a multiple of 4), at the precision the
+ * library picks per factor (TF32 or 3xTF32); 0 = FP32 SIMT kernels only.
+ * The FP64 form is unaffected. */
 int rsd_ctx_set_tensor_cores(rsd_ctx* ctx, int enable);
+/* Precision split of the mixed-precision Ewald assembly: real-space images
+ * with lammda*r < lam_r_cut and reciprocal vectors with max|n_i| <= kshell
+ * are summed in FP64, the rest in FP32.  Defaults 4.5 and 2 (every
+ * mobility block then within ~1e-11 of the all-FP64 sum). */
+int rsd_ctx_set_mixed_split(rsd_ctx* ctx, double lam_r_cut, int32_t kshell);
 
 /* ---------------------------------------------------------------- lattice */
 /* SET_LATTICE_SKEW (src/csd_post.f90:105-136) with MAT_INV3
@@ -222,13 +228,21 @@ int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_ste
 /* The reference solves in FP64 only (LAPACK DPOTRF/DPOTRI); these are the
  * single-precision building blocks that the mixed form's refinement uses as a
  * preconditioner, exported for testing and for callers that build their own
- * refinement.  Device pointers, column-major. */
+ * refinement.  Device pointers, column-major.  prec selects the product
+ * arithmetic: 0 = FP32 SIMT, 1 = TF32 tensor cores, 3 = 3xTF32 tensor cores
+ * (head/tail split, close to FP32); the tensor-core forms need 16-byte
+ * aligned pointers and leading dimensions that are multiples of 4, and fall
+ * back to SIMT otherwise. */
 /* C (n x n, the 128 x 128 tiles on and above the diagonal) -= P^T P with P
  * k x n (ld ldp); k <= 128 for the tensor-core path. */
-int rsd_syrk_f32_dev(rsd_ctx* ctx, int32_t n, int32_t k, const float* d_P, int64_t ldp, float* d_C, int64_t ldc);
+int rsd_syrk_f32_dev(rsd_ctx* ctx, int32_t n, int32_t k, const float* d_P, int64_t ldp, float* d_C, int64_t ldc,
+                     int32_t prec);
 /* Upper Cholesky factor in place (lower triangle left as scratch); info as
  * DPOTRF. */
-int rsd_potrf_f32_dev(rsd_ctx* ctx, int32_t n, float* d_A, int64_t lda, int32_t* info);
+int rsd_potrf_f32_dev(rsd_ctx* ctx, int32_t n, float* d_A, int64_t lda, int32_t prec, int32_t* info);
+/* A <- A^-1 (upper triangle; the lower triangle is scratch) from the upper
+ * factor in A, as DPOTRI. */
+int rsd_potri_f32_dev(rsd_ctx* ctx, int32_t n, float* d_A, int64_t lda, int32_t prec);
 
 #ifdef __cplusplus
 }

@@ -93,8 +93,10 @@ _sig("rsd_stepper_stokesian", _i, [_vp, _vp, ctypes.POINTER(StepParams), _dp, _d
 _sig("rsd_stepper_stokesian_dev", _i, [_vp, _vp, ctypes.POINTER(StepParams), _vp, _vp, _vp, _vp, _vp, _dp,
                                        ctypes.POINTER(StepInfo)])
 _sig("rsd_ctx_set_tensor_cores", _i, [_vp, _i])
-_sig("rsd_syrk_f32_dev", _i, [_vp, _i32, _i32, _vp, _i64, _vp, _i64])
-_sig("rsd_potrf_f32_dev", _i, [_vp, _i32, _vp, _i64, _ip])
+_sig("rsd_ctx_set_mixed_split", _i, [_vp, _d, _i32])
+_sig("rsd_syrk_f32_dev", _i, [_vp, _i32, _i32, _vp, _i64, _vp, _i64, _i32])
+_sig("rsd_potrf_f32_dev", _i, [_vp, _i32, _vp, _i64, _i32, _ip])
+_sig("rsd_potri_f32_dev", _i, [_vp, _i32, _vp, _i64, _i32])
 
 EXPORTED = [n for n in dir(_lib) if n.startswith("rsd_")]
 
@@ -144,9 +146,13 @@ class Context:
     def stream(self):
         return _lib.rsd_ctx_stream(self.h)
 
+    def set_mixed_split(self, lam_r_cut=4.5, kshell=2):
+        """FP64/FP32 split of the mixed-precision Ewald assembly."""
+        self.check(_lib.rsd_ctx_set_mixed_split(self.h, float(lam_r_cut), int(kshell)))
+
     def set_tensor_cores(self, enable: bool):
-        """tcgen05 TF32 (True, the default) or FP32 SIMT trailing updates in
-        the FP32 factorisations of the mixed-precision form."""
+        """tcgen05 kernels (True, the default) or FP32 SIMT only in the FP32
+        factorisations of the mixed-precision form."""
         self.check(_lib.rsd_ctx_set_tensor_cores(self.h, 1 if enable else 0))
 
     def close(self):
@@ -226,19 +232,20 @@ def per_grpery_inv_fri_dev(ctx: Context, pos, radii, lattice: Lattice, ews_err, 
     return buf.t()
 
 
-def syrk_f32_dev(ctx: Context, P, C):
+def syrk_f32_dev(ctx: Context, P, C, prec=1):
     """C -= P^T P on the 128 x 128 tiles on and above the diagonal.  P (k, n)
     and C (n, n) are column-major FP32 device matrices passed as the
-    transpose views of contiguous torch tensors (P.t() of an (n, k) tensor)."""
+    transpose views of contiguous torch tensors (P.t() of an (n, k) tensor).
+    prec: 0 FP32 SIMT, 1 TF32 tensor cores, 3 3xTF32 tensor cores."""
     import torch
     k, n = P.shape
     assert C.shape == (n, n) and P.stride(0) == 1 and C.stride(0) == 1
     torch.cuda.synchronize(P.device)
-    ctx.check(_lib.rsd_syrk_f32_dev(ctx.h, n, k, P.data_ptr(), P.stride(1), C.data_ptr(), C.stride(1)))
+    ctx.check(_lib.rsd_syrk_f32_dev(ctx.h, n, k, P.data_ptr(), P.stride(1), C.data_ptr(), C.stride(1), prec))
     return C
 
 
-def potrf_f32_dev(ctx: Context, A):
+def potrf_f32_dev(ctx: Context, A, prec=1):
     """Upper Cholesky factor in place of a column-major FP32 device matrix
     (a transpose view, as syrk_f32_dev); returns info."""
     import torch
@@ -246,8 +253,18 @@ def potrf_f32_dev(ctx: Context, A):
     assert A.shape == (n, n) and A.stride(0) == 1
     info = ctypes.c_int32(0)
     torch.cuda.synchronize(A.device)
-    ctx.check(_lib.rsd_potrf_f32_dev(ctx.h, n, A.data_ptr(), A.stride(1), ctypes.byref(info)))
+    ctx.check(_lib.rsd_potrf_f32_dev(ctx.h, n, A.data_ptr(), A.stride(1), prec, ctypes.byref(info)))
     return info.value
+
+
+def potri_f32_dev(ctx: Context, A, prec=3):
+    """A <- A^-1 (upper triangle) from the upper factor in A (DPOTRI)."""
+    import torch
+    n = A.shape[0]
+    assert A.shape == (n, n) and A.stride(0) == 1
+    torch.cuda.synchronize(A.device)
+    ctx.check(_lib.rsd_potri_f32_dev(ctx.h, n, A.data_ptr(), A.stride(1), prec))
+    return A
 
 
 def _sync_ctx(ctx):

@@ -110,6 +110,14 @@ extern "C" int rsd_ctx_destroy(rsd_ctx* c) {
 extern "C" const char* rsd_ctx_last_error(const rsd_ctx* c) { return c ? c->err.c_str() : "no context"; }
 extern "C" void* rsd_ctx_stream(rsd_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
+extern "C" int rsd_ctx_set_mixed_split(rsd_ctx* c, double lam_r_cut, int32_t kshell) {
+  if (!c) return RSD_EARG;
+  if (!(lam_r_cut >= 0.0) || kshell < 0) return rsd_fail(c, RSD_EARG, "mixed split: lam_r_cut >= 0, kshell >= 0");
+  c->mixed_rcut = lam_r_cut;
+  c->mixed_kshell = kshell;
+  return RSD_OK;
+}
+
 extern "C" int rsd_ctx_set_tensor_cores(rsd_ctx* c, int enable) {
   if (!c) return RSD_EARG;
   c->use_tc = enable ? 1 : 0;

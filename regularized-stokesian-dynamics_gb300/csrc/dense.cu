@@ -882,7 +882,7 @@ int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const
       T* A22 = d_A + (j0 + jb) + (int64_t)(j0 + jb) * lda;
       if constexpr (F32) {
         if (tc && ctx->use_tc && rsd_tc_syrk_ok(Apan, lda, A22, lda, jb)) {
-          RSD_TRY(rsd_tc_syrk(ctx, Apan, lda, jb, rest, A22, lda, ctx->d_info + 1));
+          RSD_TRY(rsd_tc_syrk(ctx, tc, Apan, lda, jb, rest, A22, lda, ctx->d_info + 1));
           continue;
         }
       }
@@ -938,9 +938,51 @@ int trtri_inplace_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, const T* W, T* T1,
   return RSD_OK;
 }
 
+// WT(j0:j0+jb, j0:j0+jb) = W_jj^T for the diagonal blocks
+__global__ void put_diag_transposed(int jb, const float* __restrict__ Wb, float* __restrict__ WT, int64_t ldw) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= jb * jb) return;
+  const int i = t % jb, j = t / jb;  // WT(i, j) = W(j, i)
+  WT[i + (int64_t)j * ldw] = Wb[j + (int64_t)i * NB];
+}
+
+// A <- A^-1 (upper triangle) from its upper factor U in A, on tensor cores:
+// WT = (U^-1)^T is built one block row at a time (K-major operands
+// throughout: T1^T = U(0:j0, jblk)^T WT(0:j0, 0:j0) over k >= m, then
+// WT(jblk, 0:j0) = -W_jj^T T1^T), and A^-1 = W W^T = WT^T WT over k >= the
+// tile's column.  prec 1 (TF32) or 3 (3xTF32).
+int potri_tc_s(rsd_ctx* ctx, int prec, int n, float* d_A, int64_t lda, const char* tag) {
+  cudaStream_t s = ctx->stream;
+  float* W = nullptr;
+  RSD_TRY(rsd_diag_inverses_t<float>(ctx, n, d_A, lda, tag, &W));
+  const int64_t ldw = (n + 3) / 4 * 4;
+  float* WT = (float*)rsd_scratch(ctx, "potri_WT_s", sizeof(float) * (size_t)ldw * n);
+  float* T1 = (float*)rsd_scratch(ctx, "potri_T1t_s", sizeof(float) * (size_t)NB * n);
+  if (!WT || !T1) return RSD_ENOMEM;
+  RSD_CUDA(ctx, cudaMemsetAsync(ctx->d_info + 1, 0, sizeof(int), s));
+  RSD_CUDA(ctx, cudaMemsetAsync(WT, 0, sizeof(float) * (size_t)ldw * n, s));
+  int* err = ctx->d_info + 1;
+  for (int j0 = 0, b = 0; j0 < n; j0 += NB, b++) {
+    const int jb = n - j0 < NB ? n - j0 : NB;
+    const float* Wb = W + (size_t)b * NB * NB;
+    put_diag_transposed<<<(jb * jb + 255) / 256, 256, 0, s>>>(jb, Wb, WT + j0 + (int64_t)j0 * ldw, ldw); RSD_LAUNCH_NOTE();
+    if (j0 == 0) continue;
+    RSD_TRY(rsd_tc_gemm(ctx, prec, jb, j0, j0, 1.0f, d_A + (int64_t)j0 * lda, lda, WT, ldw, T1, NB, 0, 0, 1, err));
+    RSD_TRY(rsd_tc_gemm(ctx, prec, jb, j0, jb, -1.0f, Wb, NB, T1, NB, WT + j0, ldw, 0, 0, 0, err));
+  }
+  RSD_TRY(rsd_tc_gemm(ctx, prec, n, n, n, 1.0f, WT, ldw, WT, ldw, d_A, lda, 0, 1, 1, err));
+  RSD_CUDA(ctx, cudaMemcpyAsync(ctx->h_info + 1, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  RSD_CUDA(ctx, cudaStreamSynchronize(s));
+  if (ctx->h_info[1]) return rsd_fail(ctx, RSD_ETIMEOUT, "potri: tensor-core GEMM timed out (code %d)", ctx->h_info[1]);
+  return RSD_OK;
+}
+
 // A <- A^-1 (upper triangle) from its upper Cholesky factor in A
 template <typename T>
-int rsd_potri_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, const char* tag) {
+int rsd_potri_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, const char* tag, int tc) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (tc && ctx->use_tc && rsd_tc_gemm_ok(d_A, lda, d_A, lda, d_A, lda)) return potri_tc_s(ctx, tc, n, d_A, lda, tag);
+  }
   cudaStream_t s = ctx->stream;
   T* W = nullptr;
   RSD_TRY(rsd_diag_inverses_t<T>(ctx, n, d_A, lda, tag, &W));
@@ -1083,7 +1125,7 @@ template int rsd_gemv<float>(rsd_ctx*, int, int, int, float, const float*, int64
 template int rsd_gemv<double>(rsd_ctx*, int, int, int, double, const double*, int64_t, const double*, int64_t, int,
                               double, double*, int64_t);
 template int rsd_potrf_upper_t<float>(rsd_ctx*, int, float*, int64_t, int*, const char*, int);
-template int rsd_potri_upper_t<float>(rsd_ctx*, int, float*, int64_t, const char*);
+template int rsd_potri_upper_t<float>(rsd_ctx*, int, float*, int64_t, const char*, int);
 template int rsd_potrs_upper_t<float>(rsd_ctx*, int, const float*, int64_t, float*, int64_t, int, const char*,
                                       const float*);
 template int rsd_mirror_upper_t<float>(rsd_ctx*, int, float*, int64_t);
@@ -1105,10 +1147,10 @@ int rsd_potrf_upper(rsd_ctx* ctx, int n, double* d_A, int64_t lda, int* info) {
   return rsd_potrf_upper_t<double>(ctx, n, d_A, lda, info, "A", 0);
 }
 int rsd_potri_upper_tag(rsd_ctx* ctx, int n, double* d_A, int64_t lda, const char* tag) {
-  return rsd_potri_upper_t<double>(ctx, n, d_A, lda, tag);
+  return rsd_potri_upper_t<double>(ctx, n, d_A, lda, tag, 0);
 }
 int rsd_potri_upper(rsd_ctx* ctx, int n, double* d_A, int64_t lda) {
-  return rsd_potri_upper_t<double>(ctx, n, d_A, lda, "A");
+  return rsd_potri_upper_t<double>(ctx, n, d_A, lda, "A", 0);
 }
 int rsd_potrs_upper_tag(rsd_ctx* ctx, int n, const double* d_U, int64_t ldu, double* d_X, int64_t ldx, int nrhs,
                         const char* tag) {
@@ -1123,15 +1165,21 @@ int rsd_trsv_upper(rsd_ctx* ctx, int n, const double* d_U, int64_t ldu, double* 
 }
 
 // ------------------------------------------------ FP32 exported blocks
+static int check_prec(rsd_ctx* ctx, int prec) {
+  if (prec != 0 && prec != 1 && prec != 3) return rsd_fail(ctx, RSD_EARG, "prec must be 0, 1 or 3 (got %d)", prec);
+  return RSD_OK;
+}
+
 extern "C" int rsd_syrk_f32_dev(rsd_ctx* ctx, int32_t n, int32_t k, const float* d_P, int64_t ldp, float* d_C,
-                                int64_t ldc) {
+                                int64_t ldc, int32_t prec) {
   if (!ctx) return RSD_EARG;
   if (n < 1 || k < 1 || ldp < k || ldc < n || !d_P || !d_C)
     return rsd_fail(ctx, RSD_EARG, "rsd_syrk_f32_dev: bad arguments");
+  RSD_TRY(check_prec(ctx, prec));
   RSD_TRY(rsd_set_device(ctx));
-  if (ctx->use_tc && k <= NB && rsd_tc_syrk_ok(d_P, ldp, d_C, ldc, k)) {
+  if (prec && ctx->use_tc && k <= NB && rsd_tc_syrk_ok(d_P, ldp, d_C, ldc, k)) {
     RSD_CUDA(ctx, cudaMemsetAsync(ctx->d_info + 1, 0, sizeof(int), ctx->stream));
-    RSD_TRY(rsd_tc_syrk(ctx, d_P, ldp, k, n, d_C, ldc, ctx->d_info + 1));
+    RSD_TRY(rsd_tc_syrk(ctx, prec, d_P, ldp, k, n, d_C, ldc, ctx->d_info + 1));
     RSD_CUDA(ctx, cudaMemcpyAsync(ctx->h_info + 1, ctx->d_info + 1, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     RSD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (ctx->h_info[1]) return rsd_fail(ctx, RSD_ETIMEOUT, "syrk: tensor-core update timed out");
@@ -1145,12 +1193,23 @@ extern "C" int rsd_syrk_f32_dev(rsd_ctx* ctx, int32_t n, int32_t k, const float*
   return RSD_OK;
 }
 
-extern "C" int rsd_potrf_f32_dev(rsd_ctx* ctx, int32_t n, float* d_A, int64_t lda, int32_t* info) {
+extern "C" int rsd_potrf_f32_dev(rsd_ctx* ctx, int32_t n, float* d_A, int64_t lda, int32_t prec, int32_t* info) {
   if (!ctx) return RSD_EARG;
   if (n < 1 || lda < n || !d_A || !info) return rsd_fail(ctx, RSD_EARG, "rsd_potrf_f32_dev: bad arguments");
+  RSD_TRY(check_prec(ctx, prec));
   RSD_TRY(rsd_set_device(ctx));
   int inf = 0;
-  RSD_TRY(rsd_potrf_upper_t<float>(ctx, n, d_A, lda, &inf, "f32dev", 1));
+  RSD_TRY(rsd_potrf_upper_t<float>(ctx, n, d_A, lda, &inf, "f32dev", prec));
   *info = inf;
+  return RSD_OK;
+}
+
+extern "C" int rsd_potri_f32_dev(rsd_ctx* ctx, int32_t n, float* d_A, int64_t lda, int32_t prec) {
+  if (!ctx) return RSD_EARG;
+  if (n < 1 || lda < n || !d_A) return rsd_fail(ctx, RSD_EARG, "rsd_potri_f32_dev: bad arguments");
+  RSD_TRY(check_prec(ctx, prec));
+  RSD_TRY(rsd_set_device(ctx));
+  RSD_TRY(rsd_potri_upper_t<float>(ctx, n, d_A, lda, "f32dev", prec));
+  RSD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return RSD_OK;
 }

@@ -29,10 +29,6 @@
 namespace {
 
 constexpr int KW = 3 + RSD_NMOM_KCOS + RSD_NMOM_KSIN;  // doubles per k entry
-// Mixed form: FP64 for real images with lambda r below this, and for
-// reciprocal vectors with max|n_i| up to this shell.
-#define RSD_MIXED_RCUT 4.5
-#define RSD_MIXED_KSHELL 2
 
 __host__ __device__ inline void half_space_index(int h, int NI, int* nx, int* ny, int* nz) {
   const int w = 2 * NI + 1;
@@ -221,7 +217,7 @@ __global__ void __launch_bounds__(128) ewald_pair_k(int nn, rsd_lat_dev L, int K
 }
 
 // Real-space images over the cube [-NR,NR]^3: MODE 0 all of them, MODE 1
-// those with |x| < rc (lambda r < RSD_MIXED_RCUT), MODE 2 the others.  The
+// those with |x| < rc (lambda r < the context's mixed_rcut), MODE 2 the others.  The
 // radial functions of erfc(lambda r) cancel badly in FP32 at large lambda r,
 // so FP32 is kept for images where every term is below ~1e-9 of a block.
 template <typename T, int MODE>
@@ -410,15 +406,17 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
   if (nn > 1) {
     dim3 blk(32, 4), grd((nn + 31) / 32, (nn + 3) / 4);
     if (precision == RSD_PREC_MIXED) {
-      // FP64: real images with lambda r < RSD_MIXED_RCUT and reciprocal
-      // vectors with max|n_i| <= RSD_MIXED_KSHELL; FP32 for the rest (each
-      // block then within ~1e-11 of the all-FP64 sum).
-      const double rc = RSD_MIXED_RCUT / L.lam, rc2 = rc * rc;
+      // FP64: real images with lambda r < mixed_rcut (default 4.5) and
+      // reciprocal vectors with max|n_i| <= mixed_kshell (default 2); FP32
+      // for the rest (each block then within ~1e-11 of the all-FP64 sum at
+      // the defaults).
+      const double rc = ctx->mixed_rcut / L.lam, rc2 = rc * rc;
+      const int ks = ctx->mixed_kshell;
       std::vector<int> h64, h32;
       for (int h = 0; h < Kh; h++) {
         int nx, ny, nz;
         half_space_index(h, L.NI, &nx, &ny, &nz);
-        (abs(nx) <= RSD_MIXED_KSHELL && abs(ny) <= RSD_MIXED_KSHELL && abs(nz) <= RSD_MIXED_KSHELL ? h64 : h32).push_back(h);
+        (abs(nx) <= ks && abs(ny) <= ks && abs(nz) <= ks ? h64 : h32).push_back(h);
       }
       const int K64 = (int)h64.size(), K32 = (int)h32.size();
       int* dh = (int*)rsd_scratch(ctx, "ewald_hlist", sizeof(int) * (size_t)Kh);

@@ -28,7 +28,7 @@ int rsd_gemv(rsd_ctx* ctx, int trans, int m, int k, T alpha, const T* A, int64_t
 template <typename T>
 int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const char* tag, int tc);
 template <typename T>
-int rsd_potri_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, const char* tag);
+int rsd_potri_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, const char* tag, int tc);
 template <typename T>
 int rsd_potrs_upper_t(rsd_ctx* ctx, int n, const T* d_U, int64_t ldu, T* d_X, int64_t ldx, int nrhs, const char* tag,
                       const T* W);
@@ -216,8 +216,12 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   // FP32 factor of M' (stresslets first)
   convert_perm<<<(unsigned)((n * n + 255) / 256), 256, 0, s>>>(nn, n, M, ld, M32); RSD_LAUNCH_NOTE();
   int inf = 0;
-  // TF32 tensor-core trailing updates here: the refinement's contraction
-  // scales with cond(M') (moderate) times the TF32 rounding
+  // Tensor-core precision per factor.  The refinement contracts by about the
+  // preconditioner's relative error times the condition number it meets:
+  // cond(M') is moderate, so TF32 (2^-11) suffices for the factor of M';
+  // the inverse A^-1 meets cond(A)^2 and the factor of RPP meets cond(RPP),
+  // which grows like the inverse lubrication gap, so those use 3xTF32
+  // (about 2^-21, close to FP32).
   RSD_TRY(rsd_potrf_upper_t<float>(ctx, (int)n, M32, n, &inf, "m32", 1));
   if (inf) {
     info->info = inf;
@@ -227,12 +231,10 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   RSD_TRY(rsd_wide_inverses_s(ctx, (int)n, M32, n, "m32", &W_m));
   // A^-1 from the trailing factor block, then RPP32 = A^-1 + rfu and its factor
   copy_block_f<<<nblk(P * P), 256, 0, s>>>(P, P, M32 + Q + Q * n, n, A32, P); RSD_LAUNCH_NOTE();
-  RSD_TRY(rsd_potri_upper_t<float>(ctx, (int)P, A32, P, "a32"));
+  RSD_TRY(rsd_potri_upper_t<float>(ctx, (int)P, A32, P, "a32", 3));
   RSD_TRY(rsd_mirror_upper_t<float>(ctx, (int)P, A32, P));
   add_lub_pp<<<nblk(P * P), 256, 0, s>>>(P, A32, L, n); RSD_LAUNCH_NOTE();
-  // FP32 SIMT updates here: cond(RPP) grows like the inverse lubrication
-  // gap, too large for TF32 rounding in the preconditioner
-  RSD_TRY(rsd_potrf_upper_t<float>(ctx, (int)P, A32, P, &inf, "rpp32", 0));
+  RSD_TRY(rsd_potrf_upper_t<float>(ctx, (int)P, A32, P, &inf, "rpp32", 3));
   if (inf) {
     info->info = inf;
     return rsd_fail(ctx, inf, "FP32 factor of RPP: leading minor %d not positive", inf);

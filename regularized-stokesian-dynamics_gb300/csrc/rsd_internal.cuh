@@ -31,7 +31,9 @@ struct rsd_ctx {
   std::map<std::string, rsd_buf> bufs;  // grow-only device buffers by name
   cudaEvent_t ev[8] = {};
   double phase_ms[4] = {0, 0, 0, 0};
-  int use_tc = 1;         // tcgen05 trailing updates in the FP32 factorisations
+  int use_tc = 1;         // tcgen05 GEMMs in the FP32 factorisations (0: SIMT only)
+  double mixed_rcut = 4.5;  // mixed assembly: FP64 real images below this lambda r
+  int mixed_kshell = 2;     // mixed assembly: FP64 reciprocal shells max|n_i| <= this
   int* d_info = nullptr;  // device-side status words
   int* h_info = nullptr;  // pinned mirror
 };
@@ -125,7 +127,12 @@ int rsd_zero_lower(rsd_ctx* ctx, int n, double* d_A, int64_t lda);
 // A(rows x cols) += B, both column-major sub-blocks (step.cu)
 int rsd_axpy_block(rsd_ctx* ctx, int64_t rows, int64_t cols, const double* B, int64_t ldb, double* A, int64_t lda);
 
-// Tensor-core (tcgen05 TF32) trailing update of the FP32 blocked Cholesky
-// (tc_syrk.cu): C (rest x rest, upper tiles) -= P^T P, P kb x rest.
+// Tensor-core (tcgen05) GEMM on K-major FP32 operands (tc_gemm.cu):
+// C = alpha A^T B (store) or C += alpha A^T B (reduce) on 128-tiles, prec 1
+// (TF32) or 3 (3xTF32); and the blocked-Cholesky trailing update on top of it.
+int rsd_tc_gemm_ok(const float* A, int64_t lda, const float* B, int64_t ldb, const float* C, int64_t ldc);
+int rsd_tc_gemm(rsd_ctx* ctx, int prec, int m, int n, int K, float alpha, const float* A, int64_t lda,
+                const float* B, int64_t ldb, float* C, int64_t ldc, int reduce, int tri, int klo_col, int* d_err);
 int rsd_tc_syrk_ok(const float* panel, int64_t lda, const float* C, int64_t ldc, int kb);
-int rsd_tc_syrk(rsd_ctx* ctx, const float* panel, int64_t lda, int kb, int rest, float* C, int64_t ldc, int* d_err);
+int rsd_tc_syrk(rsd_ctx* ctx, int prec, const float* panel, int64_t lda, int kb, int rest, float* C, int64_t ldc,
+                int* d_err);
