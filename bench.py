@@ -49,39 +49,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-peaks", action="store_true")
-    ap.add_argument("--profile", action="store_true",
-                    help="after the warm-up, run one step under the CUDA activity profiler and print the "
-                         "per-kernel device time instead of the JSON line")
     return ap.parse_args()
-
-
-def kernel_table(prof, top=40):
-    """Per-kernel device time of a torch.profiler run, from the kernel
-    activity records of its trace (these include the kernels this library
-    launches on its own stream)."""
-    import tempfile
-    rows = {}
-    with tempfile.TemporaryDirectory() as d:
-        path = os.path.join(d, "trace.json")
-        prof.export_chrome_trace(path)
-        with open(path) as fp:
-            trace = json.load(fp)
-    for ev in trace.get("traceEvents", []):
-        if ev.get("cat") not in ("kernel", "gpu_memcpy", "gpu_memset") or "dur" not in ev:
-            continue
-        name = ev.get("name", "?")
-        for cut in ("(", " ["):
-            if cut in name and not name.startswith(cut):
-                name = name.split(cut)[0]
-        name = name.replace("(anonymous namespace)::", "").replace("void ", "")
-        c, tt = rows.get(name, (0, 0.0))
-        rows[name] = (c + 1, tt + float(ev["dur"]) / 1000.0)
-    total = sum(v[1] for v in rows.values())
-    out = ["total %.2f ms device time over %d records" % (total, sum(v[0] for v in rows.values())),
-           "%-60s %8s %12s %6s" % ("kernel", "launches", "total ms", "share")]
-    for name, (c, tt) in sorted(rows.items(), key=lambda kv: -kv[1][1])[:top]:
-        out.append("%-60s %8d %12.2f %5.1f%%" % (name[:60], c, tt, 100.0 * tt / max(total, 1e-30)))
-    return "\n".join(out)
 
 
 def dist_env():
@@ -89,6 +57,26 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def replica_seed(rank):
+    """Seed of rank `rank`'s packing: every replica steps its own system."""
+    return SEED_BASE + 5000 + rank
+
+
+def max_over_ranks(x, ws, dist, torch, device):
+    """Largest per-rank duration over all ranks.  Replicas exchange nothing
+    on the data path; only the clock is reduced."""
+    if ws <= 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(ws, steps, seconds):
+    """Whole-job steps/s: every rank's steps over the slowest rank's time."""
+    return ws * steps / seconds
 
 
 def measured_peaks():
@@ -270,7 +258,7 @@ def reference_arm(args):
     from oracle import oracle as o
     o.build()
     rsd_cfg = _configs()
-    pos, radii, L = rsd_cfg.packing(args.N, args.phi, args.gmin, SEED_BASE + 5000, sweeps=args.sweeps)
+    pos, radii, L = rsd_cfg.packing(args.N, args.phi, args.gmin, replica_seed(0), sweeps=args.sweeps)
     threads = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
     for _ in range(args.warmup):
@@ -319,7 +307,7 @@ def main():
     torch.cuda.set_device(dev)
     rsd = ge.load_package()
     prec = rsd.PREC_MIXED if args.precision == "mixed" else rsd.PREC_FP64
-    pos, radii, L = rsd.configs.packing(args.N, args.phi, args.gmin, SEED_BASE + 5000 + rank, sweeps=args.sweeps)
+    pos, radii, L = rsd.configs.packing(args.N, args.phi, args.gmin, replica_seed(rank), sweeps=args.sweeps)
     N = args.N
     mu = rsd.mu_f_dimensionless(1.0)
     ctx = rsd.Context(local)
@@ -342,15 +330,6 @@ def main():
 
     for _ in range(args.warmup):
         step()
-    if args.profile:
-        from torch.profiler import ProfilerActivity, profile
-        torch.cuda.synchronize(dev)
-        with profile(activities=[ProfilerActivity.CUDA]) as prof:
-            step()
-            torch.cuda.synchronize(dev)
-        if rank == 0:
-            print(kernel_table(prof))
-        return
     sampler = ClockSampler(local) if rank == 0 else None
     if ws > 1:
         dist.barrier()
@@ -371,12 +350,9 @@ def main():
     launches = (lib.rsd_launch_count() - n0) if hasattr(lib, "rsd_launch_count") else None
     ms = e0.elapsed_time(e1)
     clocks = sampler.stop() if sampler else None
-    if ws > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, ws, dist, torch, dev)
     ms_per_step = ms / args.steps
-    value = ws * args.steps / (ms * 1e-3)
+    value = replica_throughput(ws, args.steps, ms * 1e-3)
     # end to end through the host C-ABI call (H2D of the inputs, D2H of the results)
     e2e = None
     if not args.no_e2e:
@@ -388,12 +364,8 @@ def main():
                                         precision=prec)
             conf_h = out["conf"]
             Te += args.dt
-        te = time.perf_counter() - t0
-        if ws > 1:
-            t = torch.tensor([te], dtype=torch.float64, device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            te = float(t.item())
-        e2e = {"value": ws * args.steps / te, "unit": "steps/s", "h2d_bytes_per_step": 8 * (3 * N + N),
+        te = max_over_ranks(time.perf_counter() - t0, ws, dist, torch, dev)
+        e2e = {"value": replica_throughput(ws, args.steps, te), "unit": "steps/s", "h2d_bytes_per_step": 8 * (3 * N + N),
                "d2h_bytes_per_step": 8 * (3 * N + 6 * N + 5 * N)}
     # the plain FP64 form on the same start configuration: its steps/s and the
     # mixed form's velocity / stresslet error against it
