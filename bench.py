@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-peaks", action="store_true")
+    ap.add_argument("--tensor-cores", type=int, default=1, choices=[0, 1, 3],
+                    help="FP32 factorisations of the mixed form: 1 TF32/3xTF32 per factor, 3 all 3xTF32, 0 SIMT")
     return ap.parse_args()
 
 
@@ -311,6 +313,7 @@ def main():
     N = args.N
     mu = rsd.mu_f_dimensionless(1.0)
     ctx = rsd.Context(local)
+    ctx.set_tensor_cores(args.tensor_cores)
     tab = rsd.LubTab(rsd.lubdat_dir())
     conf_t = torch.tensor(pos, dtype=torch.float64, device=dev)
     radii_t = torch.tensor(radii, dtype=torch.float64, device=dev)
@@ -436,7 +439,7 @@ def main():
             "data": "synthetic (seeded sphere packing, no dataset)",
             "config": {"workload": "STEPPER_Stokesian step, N=%d phi=%.2f gap>=%g, shear 1, dt %g, Ewald 1e-10, lub on"
                                    % (N, args.phi, args.gmin, args.dt),
-                       "precision": args.precision, "NR": NR, "NI": NI,
+                       "precision": args.precision, "tensor_cores": args.tensor_cores, "NR": NR, "NI": NI,
                        "l2": "inputs larger than L2 (grand mobility %.2f GB)" % (8 * (11 * N) ** 2 / 1e9),
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "phases_ms": {"assembly": ph[0], "lub": ph[1], "solve": ph[2], "refinement": ph[3]},

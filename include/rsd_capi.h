@@ -73,14 +73,17 @@ int rsd_ctx_phase_ms(const rsd_ctx* ctx, double ms[4]);
 long long rsd_launch_count(void);
 /* Tensor cores in the FP32 factorisations of the mixed-precision form:
  * 1 (the default) = tcgen05 kernels wherever the layout allows (16-byte
- * aligned blocks, leading dimension a multiple of 4), at the precision the
- * library picks per factor (TF32 or 3xTF32); 0 = FP32 SIMT kernels only.
- * The FP64 form is unaffected. */
-int rsd_ctx_set_tensor_cores(rsd_ctx* ctx, int enable);
+ * aligned blocks, leading dimension a multiple of 4), TF32 for the factor of
+ * the grand mobility and 3xTF32 (close to FP32) for the inverse and the
+ * factor of RPP; 3 = 3xTF32 for all three (fewer refinement iterations);
+ * 0 = FP32 SIMT kernels only.  The FP64 form is unaffected. */
+int rsd_ctx_set_tensor_cores(rsd_ctx* ctx, int mode);
 /* Precision split of the mixed-precision Ewald assembly: real-space images
  * with lammda*r < lam_r_cut and reciprocal vectors with max|n_i| <= kshell
- * are summed in FP64, the rest in FP32.  Defaults 4.5 and 2 (every
- * mobility block then within ~1e-11 of the all-FP64 sum). */
+ * are summed in FP64, the rest in FP32.  Defaults 4.0 and 1: a step's
+ * velocities then agree with the FP64 form to ~3e-12 and its stresslets to
+ * ~6e-11 relative (3.5 gives ~5e-11 and ~1e-9 at 0.85x the assembly time,
+ * 4.5 ~1e-13 and ~2e-12 at 1.2x). */
 int rsd_ctx_set_mixed_split(rsd_ctx* ctx, double lam_r_cut, int32_t kshell);
 
 /* ---------------------------------------------------------------- lattice */

@@ -146,14 +146,15 @@ class Context:
     def stream(self):
         return _lib.rsd_ctx_stream(self.h)
 
-    def set_mixed_split(self, lam_r_cut=4.5, kshell=2):
+    def set_mixed_split(self, lam_r_cut=4.0, kshell=1):
         """FP64/FP32 split of the mixed-precision Ewald assembly."""
         self.check(_lib.rsd_ctx_set_mixed_split(self.h, float(lam_r_cut), int(kshell)))
 
-    def set_tensor_cores(self, enable: bool):
-        """tcgen05 kernels (True, the default) or FP32 SIMT only in the FP32
-        factorisations of the mixed-precision form."""
-        self.check(_lib.rsd_ctx_set_tensor_cores(self.h, 1 if enable else 0))
+    def set_tensor_cores(self, mode=1):
+        """FP32 factorisations of the mixed form: 1 (or True, the default)
+        tcgen05 TF32/3xTF32 per factor, 3 all 3xTF32, 0 (or False) SIMT."""
+        mode = int(mode)
+        self.check(_lib.rsd_ctx_set_tensor_cores(self.h, mode))
 
     def close(self):
         if self.h:

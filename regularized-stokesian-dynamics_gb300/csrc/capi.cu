@@ -92,10 +92,26 @@ extern "C" int rsd_ctx_create(rsd_ctx** out, int device) {
   return RSD_OK;
 }
 
+int rsd_side_stream(rsd_ctx* c) {
+  if (c->side) return RSD_OK;
+  int lo = 0, hi = 0;
+  RSD_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
+  RSD_CUDA(c, cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, hi));
+  RSD_CUDA(c, cudaEventCreateWithFlags(&c->ev_panel, cudaEventDisableTiming));
+  RSD_CUDA(c, cudaEventCreateWithFlags(&c->ev_next, cudaEventDisableTiming));
+  return RSD_OK;
+}
+
 extern "C" int rsd_ctx_destroy(rsd_ctx* c) {
   if (!c) return RSD_OK;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->side) {
+    cudaStreamSynchronize(c->side);
+    cudaStreamDestroy(c->side);
+  }
+  if (c->ev_panel) cudaEventDestroy(c->ev_panel);
+  if (c->ev_next) cudaEventDestroy(c->ev_next);
   for (auto& kv : c->bufs)
     if (kv.second.p) cudaFree(kv.second.p);
   for (int i = 0; i < 8; i++)
@@ -118,9 +134,10 @@ extern "C" int rsd_ctx_set_mixed_split(rsd_ctx* c, double lam_r_cut, int32_t ksh
   return RSD_OK;
 }
 
-extern "C" int rsd_ctx_set_tensor_cores(rsd_ctx* c, int enable) {
+extern "C" int rsd_ctx_set_tensor_cores(rsd_ctx* c, int mode) {
   if (!c) return RSD_EARG;
-  c->use_tc = enable ? 1 : 0;
+  if (mode != 0 && mode != 1 && mode != 3) return rsd_fail(c, RSD_EARG, "tensor-core mode must be 0, 1 or 3");
+  c->use_tc = mode;
   return RSD_OK;
 }
 extern "C" int rsd_ctx_phase_ms(const rsd_ctx* c, double ms[4]) {

@@ -414,23 +414,31 @@ __global__ void __launch_bounds__(256) potf2_upper(T* __restrict__ A, int64_t ld
 }
 
 // FP32 diagonal block (jb <= 128): upper Cholesky factor U and its inverse
-// W = U^-1 in one CTA, both in padded shared memory (ld 129, so that row and
-// column walks hit distinct banks).  The factor is right-looking over 32-wide
-// sub-blocks: one warp factors the 32 x 32 diagonal sub-block in registers
-// (lane = column), one thread per column solves the sub-block's row panel,
-// and all threads update the trailing block.  The inverse inverts the 32 x 32
-// diagonal sub-blocks (one warp each, back substitution in registers) and
-// then fills the off-diagonal sub-blocks level by level:
-// W_ij = -W_ii (sum_{p=i+1..j} U_ip W_pj).  U goes back to A; W goes to Wout
-// (NB x NB, lower part and rows/columns past jb zero).  info as DPOTRF.
+// W = U^-1 in one CTA of 8 warps, in padded shared memory (ld 129, so that
+// row and column walks hit distinct banks).  Right-looking over 32-wide
+// sub-blocks D:
+//   - warp 0 factors D in registers (lane = column) and inverts the factor
+//     by back substitution, also in registers; D^-1 is the sub-block's
+//     diagonal block of W;
+//   - the row panel R next to D becomes D^-T R (a 32-deep product, one warp
+//     per column, lane = row), kept also transposed for the update;
+//   - the trailing block loses R^T R: lane = row, 8 columns per warp task,
+//     so each 32-row x 8-column task reads 9 values per 8 FMAs.
+// The off-diagonal W blocks follow level by level,
+// W_ij = -W_ii (sum_{p=i+1..j} U_ip W_pj), one warp per (block, 4 columns).
+// U goes back to A; W goes to Wout (NB x NB, lower part and rows/columns
+// past jb zero).  info as DPOTRF.
 constexpr int PLD = NB + 1;
-constexpr int SMEM_POTF2_INV = (2 * NB * PLD + 3 * 32 * 33) * (int)sizeof(float);
+constexpr int RTLD = 33;
+constexpr int SMEM_POTF2_INV = (2 * NB * PLD + NB * RTLD + 32 * 33 + 3 * 32 * 33) * (int)sizeof(float);
 __global__ void __launch_bounds__(256) potf2_inv_f32(float* __restrict__ A, int64_t lda, int jb,
                                                      int* __restrict__ info, int j0, float* __restrict__ Wout) {
   extern __shared__ unsigned char smraw[];
-  float* S = (float*)smraw;   // U, NB x NB, ld PLD
-  float* Wm = S + NB * PLD;   // W, NB x NB, ld PLD
-  float* Tt = Wm + NB * PLD;  // 3 temporaries of 32 x 32, ld 33
+  float* S = (float*)smraw;       // U, NB x NB, ld PLD
+  float* Wm = S + NB * PLD;       // W, NB x NB, ld PLD
+  float* RT = Wm + NB * PLD;      // D^-T R transposed: trailing column c, row p at RT[c * RTLD + p]
+  float* Dinv = RT + NB * RTLD;   // D^-1 (32 x 32): (p, i) at Dinv[p * 33 + i]
+  float* Tt = Dinv + 32 * 33;     // 3 temporaries of 32 x 32: (r, c) at r * 33 + c
   __shared__ int failed;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   for (int e = t; e < NB * NB; e += 256) {
@@ -471,80 +479,93 @@ __global__ void __launch_bounds__(256) potf2_inv_f32(float* __restrict__ A, int6
           failed = 1;
           atomicCAS(info, 0, j0 + k0 + bad);
         }
-      } else if (lane < kw) {
+      } else {
+        // column `lane` of D^-1: back substitution against the rows of U_D,
+        // whose entry (ii, p) lane p holds in r[ii]
+        float x[32];
 #pragma unroll
-        for (int i = 0; i < 32; i++)
-          if (i <= lane) S[(k0 + i) + (k0 + lane) * PLD] = r[i];
+        for (int ii = 31; ii >= 0; ii--) {
+          float v = (ii == lane) ? 1.f : 0.f;
+#pragma unroll
+          for (int p = ii + 1; p < 32; p++) v -= __shfl_sync(0xffffffffu, r[ii], p) * x[p];
+          const float dii = __shfl_sync(0xffffffffu, r[ii], ii);
+          x[ii] = (ii < kw && lane < kw && ii <= lane) ? v / dii : 0.f;
+        }
+        if (lane < kw) {
+#pragma unroll
+          for (int i = 0; i < 32; i++) {
+            if (i <= lane) S[(k0 + i) + (k0 + lane) * PLD] = r[i];
+            Wm[(k0 + i) + (k0 + lane) * PLD] = x[i];
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < 32; i++) Dinv[i * 33 + lane] = x[i];
       }
     }
     __syncthreads();
     if (failed) return;
     const int m0 = k0 + kw, mw = jb - m0;
-    if (t < mw) {  // row panel: D^T X = R, one column per thread
-      const int c = m0 + t;
-      float x[32];
-#pragma unroll
-      for (int i = 0; i < 32; i++) {
-        float v = 0.f;
-        if (i < kw) {
-          v = S[(k0 + i) + c * PLD];
-#pragma unroll
-          for (int p = 0; p < i; p++) v -= S[(k0 + p) + (k0 + i) * PLD] * x[p];
-          v = v / S[(k0 + i) + (k0 + i) * PLD];
-        }
-        x[i] = v;
-      }
-#pragma unroll
-      for (int i = 0; i < 32; i++)
-        if (i < kw) S[(k0 + i) + c * PLD] = x[i];
-    }
-    __syncthreads();
-    for (int e = t; e < mw * mw; e += 256) {  // trailing update, upper part
-      const int i = e % mw, j = e / mw;
-      if (i <= j) {
-        float acc = 0.f;
-        for (int p = 0; p < kw; p++) acc += S[(k0 + p) + (m0 + i) * PLD] * S[(k0 + p) + (m0 + j) * PLD];
-        S[(m0 + i) + (m0 + j) * PLD] -= acc;
-      }
-    }
-    __syncthreads();
-  }
-  // inverse: diagonal 32 x 32 sub-blocks, one warp each
-  if (warp < nsub) {
-    const int k0 = warp * 32, kw = min(32, jb - k0);
-    float x[32];
-#pragma unroll
-    for (int ii = 31; ii >= 0; ii--) {
+    // row panel: R <- D^-T R, one warp per column, lane = row
+    for (int c = warp; c < mw; c += 8) {
       float v = 0.f;
-      if (ii < kw && lane < kw) {
-        v = (ii == lane) ? 1.f : 0.f;
+#pragma unroll 8
+      for (int p = 0; p < 32; p++) v += Dinv[p * 33 + lane] * S[(k0 + p) + (m0 + c) * PLD];
+      __syncwarp();
+      if (lane < kw) S[(k0 + lane) + (m0 + c) * PLD] = v;
+      RT[c * RTLD + lane] = (lane < kw) ? v : 0.f;
+    }
+    __syncthreads();
+    // trailing update of the upper part: lane = row i of a 32-row block,
+    // 8 columns per task
+    const int nrb = (mw + 31) / 32, ncg = (mw + 7) / 8;
+    for (int task = warp; task < nrb * ncg; task += 8) {
+      const int rb = task % nrb, cg = task / nrb;
+      const int i = rb * 32 + lane, c0 = cg * 8;
+      if (rb * 32 > c0 + 7) continue;  // entirely below the diagonal
+      float acc[8];
 #pragma unroll
-        for (int p = ii + 1; p < 32; p++) v -= S[(k0 + ii) + (k0 + p) * PLD] * x[p];
-        v = v / S[(k0 + ii) + (k0 + ii) * PLD];
+      for (int q = 0; q < 8; q++) acc[q] = 0.f;
+      const int ir = min(i, NB - 1);
+#pragma unroll 4
+      for (int p = 0; p < 32; p++) {
+        const float a = RT[ir * RTLD + p];
+#pragma unroll
+        for (int q = 0; q < 8; q++) acc[q] += a * RT[min(c0 + q, NB - 1) * RTLD + p];
       }
-      x[ii] = v;
-    }
-    if (lane < kw) {
+      if (i < mw) {
 #pragma unroll
-      for (int i = 0; i < 32; i++) Wm[(k0 + i) + (k0 + lane) * PLD] = x[i];
+        for (int q = 0; q < 8; q++)
+          if (c0 + q < mw && i <= c0 + q) S[(m0 + i) + (m0 + c0 + q) * PLD] -= acc[q];
+      }
     }
+    __syncthreads();
   }
-  __syncthreads();
+  // off-diagonal W blocks, level by level: warp per (block, 4 columns)
   for (int d = 1; d < nsub; d++) {
     const int nb = nsub - d;
-    for (int e = t; e < nb * 1024; e += 256) {  // T_b = sum_p U_{bi,p} W_{p,bj}
-      const int r = e % 32, c = (e / 32) % 32, b = e / 1024, bi = b, bj = b + d;
-      float acc = 0.f;
-      for (int q = 32 * (bi + 1); q < 32 * (bj + 1); q++) acc += S[(32 * bi + r) + q * PLD] * Wm[q + (32 * bj + c) * PLD];
-      Tt[b * 32 * 33 + r + c * 33] = acc;
+    for (int task = warp; task < nb * 8; task += 8) {  // T_b = sum_p U_{bi,p} W_{p,bj}
+      const int b = task / 8, c0 = (task % 8) * 4, bi = b, bj = b + d;
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int q = 32 * (bi + 1); q < 32 * (bj + 1); q++) {
+        const float u = S[(32 * bi + lane) + q * PLD];
+#pragma unroll
+        for (int cc = 0; cc < 4; cc++) acc[cc] += u * Wm[q + (32 * bj + c0 + cc) * PLD];
+      }
+#pragma unroll
+      for (int cc = 0; cc < 4; cc++) Tt[b * 32 * 33 + lane * 33 + c0 + cc] = acc[cc];
     }
     __syncthreads();
-    for (int e = t; e < nb * 1024; e += 256) {  // W_{bi,bj} = -W_{bi,bi} T_b
-      const int r = e % 32, c = (e / 32) % 32, b = e / 1024, bi = b, bj = b + d;
-      float acc = 0.f;
+    for (int task = warp; task < nb * 8; task += 8) {  // W_{bi,bj} = -W_{bi,bi} T_b
+      const int b = task / 8, c0 = (task % 8) * 4, bi = b, bj = b + d;
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 8
-      for (int q = 0; q < 32; q++) acc += Wm[(32 * bi + r) + (32 * bi + q) * PLD] * Tt[b * 32 * 33 + q + c * 33];
-      Wm[(32 * bi + r) + (32 * bj + c) * PLD] = -acc;
+      for (int q = 0; q < 32; q++) {
+        const float w = Wm[(32 * bi + lane) + (32 * bi + q) * PLD];
+#pragma unroll
+        for (int cc = 0; cc < 4; cc++) acc[cc] += w * Tt[b * 32 * 33 + q * 33 + c0 + cc];
+      }
+#pragma unroll
+      for (int cc = 0; cc < 4; cc++) Wm[(32 * bi + lane) + (32 * bj + c0 + cc) * PLD] = -acc[cc];
     }
     __syncthreads();
   }
@@ -843,11 +864,32 @@ int rsd_mirror_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda) {
   return RSD_OK;
 }
 
+// C (m x nc, ld ldc) -= P(:, 0:m)^T P(:, 0:nc) for a kb-row panel P (ld ldp);
+// uplo: only the tiles on and above the diagonal.  Tensor cores (prec tc)
+// where the layout allows, else the SIMT GEMM.
+template <typename T>
+int trailing_update(rsd_ctx* ctx, int tc, const T* P, int64_t ldp, int kb, int m, int nc, T* C, int64_t ldc,
+                    int uplo) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (tc && ctx->use_tc && rsd_tc_syrk_ok(P, ldp, C, ldc, kb))
+      return rsd_tc_gemm(ctx, tc, m, nc, kb, -1.0f, P, ldp, P, ldp, C, ldc, 1, uplo, 0, ctx->d_info + 1);
+  }
+  GemmP g = gp(m, nc, kb, -1.0, P, ldp, 1, P, ldp, 0, 1.0, C, ldc);
+  g.uplo = uplo;
+  launch_gemm<T>(ctx->stream, g);
+  return RSD_OK;
+}
+
+// Blocked right-looking upper Cholesky with one step of look-ahead: the
+// diagonal block and row panel of step j+1 are factored on a second,
+// higher-priority stream as soon as the first tile row of step j's trailing
+// update has landed, while the rest of that update runs on the main stream.
 template <typename T>
 int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const char* tag, int tc) {
   if (n < 1 || lda < n) return rsd_fail(ctx, RSD_EARG, "potrf: n=%d lda=%lld", n, (long long)lda);
   RSD_TRY(ensure_attrs<T>(ctx));
-  cudaStream_t s = ctx->stream;
+  RSD_TRY(rsd_side_stream(ctx));
+  cudaStream_t s = ctx->stream, s2 = ctx->side;
   T* W = diag_inverses<T>(ctx, n, tag);
   if (!W) return RSD_ENOMEM;
   constexpr bool F32 = std::is_same<T, float>::value;
@@ -857,38 +899,40 @@ int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const
     if (!T1) return RSD_ENOMEM;
   }
   RSD_CUDA(ctx, cudaMemsetAsync(ctx->d_info, 0, 2 * sizeof(int), s));
+  RSD_CUDA(ctx, cudaEventRecord(ctx->ev_next, s));
   for (int j0 = 0, b = 0; j0 < n; j0 += NB, b++) {
     const int jb = n - j0 < NB ? n - j0 : NB;
     T* Ajj = d_A + j0 + (int64_t)j0 * lda;
     const int rest = n - j0 - jb;
     T* Apan = d_A + j0 + (int64_t)(j0 + jb) * lda;
+    // panel j on the side stream, after the first tile row of step j-1's update
+    RSD_CUDA(ctx, cudaStreamWaitEvent(s2, ctx->ev_next, 0));
     if constexpr (F32) {
       // factor + inverse of the diagonal block, then the panel as W_jj^T B
       T* Wb = W + (size_t)b * NB * NB;
-      potf2_inv_f32<<<1, 256, SMEM_POTF2_INV, s>>>(Ajj, lda, jb, ctx->d_info, j0, Wb); RSD_LAUNCH_NOTE();
+      potf2_inv_f32<<<1, 256, SMEM_POTF2_INV, s2>>>(Ajj, lda, jb, ctx->d_info, j0, Wb); RSD_LAUNCH_NOTE();
       if (rest > 0) {
-        launch_gemm<T>(s, gp(jb, rest, jb, 1.0, Wb, NB, 1, Apan, lda, 0, 0.0, T1, NB));
+        launch_gemm<T>(s2, gp(jb, rest, jb, 1.0, Wb, NB, 1, Apan, lda, 0, 0.0, T1, NB));
         RSD_CUDA(ctx, cudaMemcpy2DAsync(Apan, lda * sizeof(T), T1, NB * sizeof(T), jb * sizeof(T), rest,
-                                        cudaMemcpyDeviceToDevice, s));
+                                        cudaMemcpyDeviceToDevice, s2));
       }
     } else {
-      potf2_upper<T><<<1, 256, smem_potf2<T>(jb), s>>>(Ajj, lda, jb, ctx->d_info, j0); RSD_LAUNCH_NOTE();
+      potf2_upper<T><<<1, 256, smem_potf2<T>(jb), s2>>>(Ajj, lda, jb, ctx->d_info, j0); RSD_LAUNCH_NOTE();
       if (rest > 0) {
-        trsm_panel<T><<<(rest + TRSM_COLS - 1) / TRSM_COLS, TRSM_COLS, smem_trsm<T>(), s>>>(Ajj, lda, jb, rest, Apan); RSD_LAUNCH_NOTE();
+        trsm_panel<T><<<(rest + TRSM_COLS - 1) / TRSM_COLS, TRSM_COLS, smem_trsm<T>(), s2>>>(Ajj, lda, jb, rest, Apan); RSD_LAUNCH_NOTE();
       }
     }
+    RSD_CUDA(ctx, cudaEventRecord(ctx->ev_panel, s2));
+    RSD_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_panel, 0));
     if (rest > 0) {
-      // trailing: A22 -= Apan^T Apan (upper tiles)
+      // trailing A22 -= Apan^T Apan: first tile row (the next panel's input), then the rest
       T* A22 = d_A + (j0 + jb) + (int64_t)(j0 + jb) * lda;
-      if constexpr (F32) {
-        if (tc && ctx->use_tc && rsd_tc_syrk_ok(Apan, lda, A22, lda, jb)) {
-          RSD_TRY(rsd_tc_syrk(ctx, tc, Apan, lda, jb, rest, A22, lda, ctx->d_info + 1));
-          continue;
-        }
-      }
-      GemmP g = gp(rest, rest, jb, -1.0, Apan, lda, 1, Apan, lda, 0, 1.0, A22, lda);
-      g.uplo = 1;
-      launch_gemm<T>(s, g);
+      const int m1 = rest < NB ? rest : NB;
+      RSD_TRY(trailing_update<T>(ctx, tc, Apan, lda, jb, m1, rest, A22, lda, 0));
+      RSD_CUDA(ctx, cudaEventRecord(ctx->ev_next, s));
+      if (rest > NB)
+        RSD_TRY(trailing_update<T>(ctx, tc, Apan + (int64_t)NB * lda, lda, jb, rest - NB, rest - NB,
+                                   A22 + NB + (int64_t)NB * lda, lda, 1));
     }
   }
   // diagonal-block inverses for the solves (the FP32 path made them above)
@@ -903,6 +947,9 @@ int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const
   if (ctx->h_info[1]) return rsd_fail(ctx, RSD_ETIMEOUT, "potrf: tensor-core update timed out (code %d)", ctx->h_info[1]);
   return RSD_OK;
 }
+
+// the diagonal-block inverses that the FP32 potrf with this tag left
+const float* rsd_potrf_inverses_s(rsd_ctx* ctx, int n, const char* tag) { return diag_inverses<float>(ctx, n, tag); }
 
 // inverses of the diagonal blocks of an upper factor U (n x n, ld ldu)
 template <typename T>
@@ -1017,7 +1064,11 @@ __global__ void copy_upper_block(int jb, const float* __restrict__ U, int64_t ld
   D[t] = (i < jb && j < jb && i <= j) ? U[i + (int64_t)j * ldu] : (i == j ? 1.0f : 0.0f);
 }
 
-int rsd_wide_inverses_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const char* tag, float** W2out) {
+// W128 (optional): the NB x NB diagonal-block inverses that the FP32 potrf
+// of U left (NB-block b at W128 + b NB^2); full NB2 blocks then start from
+// them instead of inverting their NB blocks again.
+int rsd_wide_inverses_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const char* tag, const float* W128,
+                        float** W2out) {
   const int nblk2 = (n + NB2 - 1) / NB2;
   std::string name = std::string("wide_W_") + tag;
   float* W2 = (float*)rsd_scratch(ctx, name.c_str(), sizeof(float) * (size_t)nblk2 * NB2 * NB2);
@@ -1029,8 +1080,13 @@ int rsd_wide_inverses_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const 
     const int j0 = b * NB2, jb = n - j0 < NB2 ? n - j0 : NB2;
     float* D = W2 + (size_t)b * NB2 * NB2;
     copy_upper_block<<<(NB2 * NB2 + 255) / 256, 256, 0, ctx->stream>>>(jb, U + j0 + (int64_t)j0 * ldu, ldu, D); RSD_LAUNCH_NOTE();
-    trtri_diag<float><<<NB2 / NB, 256, smem_potf2<float>(NB), ctx->stream>>>(NB2, D, NB2, Wt); RSD_LAUNCH_NOTE();
-    RSD_TRY(trtri_inplace_t<float>(ctx, NB2, D, NB2, Wt, T1, NB2));
+    const float* Wb = Wt;
+    if (W128 && jb == NB2) {
+      Wb = W128 + (size_t)(j0 / NB) * NB * NB;
+    } else {
+      trtri_diag<float><<<NB2 / NB, 256, smem_potf2<float>(NB), ctx->stream>>>(NB2, D, NB2, Wt); RSD_LAUNCH_NOTE();
+    }
+    RSD_TRY(trtri_inplace_t<float>(ctx, NB2, D, NB2, Wb, T1, NB2));
   }
   RSD_CUDA(ctx, cudaGetLastError());
   *W2out = W2;

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "ewald_gen.cuh"
+#include "dsf.cuh"
 #include "rsd_internal.cuh"
 
 namespace {
@@ -216,10 +217,63 @@ __global__ void __launch_bounds__(128) ewald_pair_k(int nn, rsd_lat_dev L, int K
   store_pair(M, ldm, nn, a, b, o, add);
 }
 
-// Real-space images over the cube [-NR,NR]^3: MODE 0 all of them, MODE 1
-// those with |x| < rc (lambda r < the context's mixed_rcut), MODE 2 the others.  The
-// radial functions of erfc(lambda r) cancel badly in FP32 at large lambda r,
-// so FP32 is kept for images where every term is below ~1e-9 of a block.
+// Near/far split of the real-space images for the mixed form.  For one
+// lattice column p + a3 nz (p = R + nx a1 + ny a2) the images with
+// |p + a3 nz| < rc are those with nz strictly between the roots zlo, zhi of
+// |a3|^2 z^2 + 2 (p.a3) z + |p|^2 - rc^2.  An integer nz further than
+// COL_MARGIN from both roots is classified by the interval alone; the rare
+// ones closer than that take the direct FP64 distance test.  Every step uses
+// explicitly rounded FP64 operations, so the FP64 (near) and FP32 (far)
+// kernels classify every image identically: each is summed exactly once.
+// (The root errors are below ~1e-7 in nz, far inside the margin.)
+constexpr double COL_MARGIN = 1e-6;
+
+struct ColumnSplit {
+  double p[3];
+  double zlo, zhi;
+};
+
+__device__ inline ColumnSplit column_split(const double R[3], const double* LR, int nx, int ny, double rc2) {
+  ColumnSplit c;
+  for (int k = 0; k < 3; k++) c.p[k] = __fma_rn(LR[3 + k], (double)ny, __fma_rn(LR[k], (double)nx, R[k]));
+  const double* a3 = LR + 6;
+  const double a33 = __fma_rn(a3[0], a3[0], __fma_rn(a3[1], a3[1], __dmul_rn(a3[2], a3[2])));
+  const double pa = __fma_rn(c.p[0], a3[0], __fma_rn(c.p[1], a3[1], __dmul_rn(c.p[2], a3[2])));
+  const double pp = __fma_rn(c.p[0], c.p[0], __fma_rn(c.p[1], c.p[1], __dmul_rn(c.p[2], c.p[2])));
+  const double D = __fma_rn(pa, pa, -__dmul_rn(a33, __dsub_rn(pp, rc2)));
+  const double zc = __ddiv_rn(-pa, a33);
+  if (D > 0.0) {
+    const double h = __ddiv_rn(__dsqrt_rn(D), a33);
+    c.zlo = __dsub_rn(zc, h);
+    c.zhi = __dadd_rn(zc, h);
+  } else {
+    c.zlo = c.zhi = zc;  // empty (or tangent): only integers within the margin get the direct test
+  }
+  return c;
+}
+
+// image nz of the column: FP64 coordinates
+__device__ inline void column_point(const ColumnSplit& c, const double* LR, int nz, double d[3]) {
+  for (int k = 0; k < 3; k++) d[k] = __fma_rn(LR[6 + k], (double)nz, c.p[k]);
+}
+
+// 1 near, 0 far, decided by the interval or by the direct test
+__device__ inline bool column_near(const ColumnSplit& c, const double* LR, int nz, double rc2) {
+  const double z = (double)nz;
+  if (z > c.zlo + COL_MARGIN && z < c.zhi - COL_MARGIN) return true;
+  if (z < c.zlo - COL_MARGIN || z > c.zhi + COL_MARGIN) return false;
+  double d[3];
+  column_point(c, LR, nz, d);
+  return __fma_rn(d[0], d[0], __fma_rn(d[1], d[1], __dmul_rn(d[2], d[2]))) < rc2;
+}
+
+// Real-space images of the mixed form: MODE 1 sums the near images
+// (lambda r below the context's mixed_rcut) in FP64, visiting only the nz
+// range of each column that can hold them; MODE 2 sums the others in FP32,
+// with FP32 coordinates p + a3 nz from the column's FP64 base point.  The
+// radial functions of erfc(lambda r) feed moments that the epilogue combines
+// with 2-3 orders of cancellation, so FP32 is kept for images whose terms
+// are below ~1e-10 of a block.
 template <typename T, int MODE>
 __global__ void __launch_bounds__(128) ewald_pair_real_t(int nn, rsd_lat_dev L, const double* __restrict__ pos,
                                                          const double* __restrict__ radii, double inv_pimu,
@@ -235,19 +289,31 @@ __global__ void __launch_bounds__(128) ewald_pair_real_t(int nn, rsd_lat_dev L, 
   const T lam = (T)L.lam, lam2 = lam * lam, cd = T(2.0 * RSD_PIP5) * lam;
   const int NR = L.NR;
   for (int nx = -NR; nx <= NR; nx++)
-    for (int ny = -NR; ny <= NR; ny++)
-      for (int nz = -NR; nz <= NR; nz++) {
-        const double d0 = R[0] + L.LR[0] * nx + L.LR[3] * ny + L.LR[6] * nz;
-        const double d1 = R[1] + L.LR[1] * nx + L.LR[4] * ny + L.LR[7] * nz;
-        const double d2 = R[2] + L.LR[2] * nx + L.LR[5] * ny + L.LR[8] * nz;
-        const bool near = d0 * d0 + d1 * d1 + d2 * d2 < rc2;
-        if ((MODE == 1 && !near) || (MODE == 2 && near)) continue;
-        const T x0 = (T)d0, x1 = (T)d1, x2 = (T)d2;
-        const T r2 = x0 * x0 + x1 * x1 + x2 * x2;
-        const T r = sqrt(r2), ir = T(1) / r;
-        const T E0 = erfc(lam * r), Ed = cd * exp(-r2 * lam2);
-        rsd_real_image<T>(x0, x1, x2, r, ir, E0, Ed, lam, acc);
+    for (int ny = -NR; ny <= NR; ny++) {
+      const ColumnSplit col = column_split(R, L.LR, nx, ny, rc2);
+      if constexpr (MODE == 1) {
+        const int lo = max(-NR, (int)ceil(col.zlo - COL_MARGIN)), hi = min(NR, (int)floor(col.zhi + COL_MARGIN));
+        for (int nz = lo; nz <= hi; nz++) {
+          if (!column_near(col, L.LR, nz, rc2)) continue;
+          double d[3];
+          column_point(col, L.LR, nz, d);
+          const T r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+          const T r = sqrt(r2), ir = T(1) / r;
+          rsd_real_image<T>(d[0], d[1], d[2], r, ir, erfc(lam * r), cd * exp(-r2 * lam2), lam, acc);
+        }
+      } else {
+        const float p0 = (float)col.p[0], p1 = (float)col.p[1], p2 = (float)col.p[2];
+        const float a0 = (float)L.LR[6], a1 = (float)L.LR[7], a2 = (float)L.LR[8];
+        for (int nz = -NR; nz <= NR; nz++) {
+          if (column_near(col, L.LR, nz, rc2)) continue;
+          const T x0 = fmaf(a0, (float)nz, p0), x1 = fmaf(a1, (float)nz, p1), x2 = fmaf(a2, (float)nz, p2);
+          const T r2 = x0 * x0 + x1 * x1 + x2 * x2;
+          const T r = sqrt(r2), ir = T(1) / r;
+          const T E0 = erfc(lam * r), Ed = cd * exp(-r2 * lam2);
+          rsd_real_image<T>(x0, x1, x2, r, ir, E0, Ed, lam, acc);
+        }
       }
+    }
   T v[60];
   rsd_real_epilogue<T>(acc, (T)radii[a], (T)radii[b], (T)L.phix, v);
   double o[60];
@@ -255,6 +321,49 @@ __global__ void __launch_bounds__(128) ewald_pair_real_t(int nn, rsd_lat_dev L, 
   for (int q = 0; q < 60; q++) o[q] = (double)v[q];
   scale_block(o, radii[a], inv_pimu);
   store_pair(M, ldm, nn, a, b, o, 1);
+}
+
+// Near images of the mixed form in double-single arithmetic: coordinates,
+// r, 1/r, erfc(lambda r) and the Gaussian come from FP64 (as in the FP64
+// kernel), the moments are evaluated and accumulated in double-single on the
+// FP32 pipe (~4e-15 relative per operation, so even after the epilogue's
+// 2-3 orders of cancellation a block stays within ~1e-12 of FP64), and the
+// epilogue runs in FP64.  Same image set as ewald_pair_real_t<double, 1>.
+__global__ void __launch_bounds__(128) ewald_pair_real_near_ds(int nn, rsd_lat_dev L, const double* __restrict__ pos,
+                                                               const double* __restrict__ radii, double inv_pimu,
+                                                               double rc2, double* __restrict__ M, int64_t ldm) {
+  int a, b;
+  if (!pair_of(nn, &a, &b)) return;
+  double R[3] = {pos[3 * a] - pos[3 * b], pos[3 * a + 1] - pos[3 * b + 1], pos[3 * a + 2] - pos[3 * b + 2]};
+  double dmin;
+  rsd_skew_correction(L.LR, L.LI, R, &dmin);
+  dsf acc[RSD_NMOM_REAL];
+#pragma unroll
+  for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = dsf(0);
+  const double lam = L.lam, lam2 = lam * lam, cd = 2.0 * RSD_PIP5 * lam;
+  const dsf lam_s = dsf_from(lam);
+  const int NR = L.NR;
+  for (int nx = -NR; nx <= NR; nx++)
+    for (int ny = -NR; ny <= NR; ny++) {
+      const ColumnSplit col = column_split(R, L.LR, nx, ny, rc2);
+      const int lo = max(-NR, (int)ceil(col.zlo - COL_MARGIN)), hi = min(NR, (int)floor(col.zhi + COL_MARGIN));
+      for (int nz = lo; nz <= hi; nz++) {
+        if (!column_near(col, L.LR, nz, rc2)) continue;
+        double d[3];
+        column_point(col, L.LR, nz, d);
+        const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        const double r = sqrt(r2), ir = 1.0 / r;
+        rsd_real_image<dsf>(dsf_from(d[0]), dsf_from(d[1]), dsf_from(d[2]), dsf_from(r), dsf_from(ir),
+                            dsf_from(erfc(lam * r)), dsf_from(cd * exp(-r2 * lam2)), lam_s, acc);
+      }
+    }
+  double accd[RSD_NMOM_REAL];
+#pragma unroll
+  for (int m = 0; m < RSD_NMOM_REAL; m++) accd[m] = dsf_to(acc[m]);
+  double v[60];
+  rsd_real_epilogue<double>(accd, radii[a], radii[b], L.phix, v);
+  scale_block(v, radii[a], inv_pimu);
+  store_pair(M, ldm, nn, a, b, v, 1);
 }
 
 __global__ void __launch_bounds__(128) ewald_pair_real(int nn, rsd_lat_dev L, const double* __restrict__ pos,
@@ -406,10 +515,12 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
   if (nn > 1) {
     dim3 blk(32, 4), grd((nn + 31) / 32, (nn + 3) / 4);
     if (precision == RSD_PREC_MIXED) {
-      // FP64: real images with lambda r < mixed_rcut (default 4.5) and
-      // reciprocal vectors with max|n_i| <= mixed_kshell (default 2); FP32
-      // for the rest (each block then within ~1e-11 of the all-FP64 sum at
-      // the defaults).
+      // FP64: real images with lambda r < mixed_rcut (default 4.0) and
+      // reciprocal vectors with max|n_i| <= mixed_kshell (default 1); FP32
+      // for the rest.  The FP32 part is limited by the epilogue, which
+      // combines moments that cancel by 2-3 orders of magnitude: images at
+      // lambda r >= 4.0 then change a block by ~1e-10 of its largest entry
+      // (a step's stresslets by ~6e-11, velocities by ~3e-12).
       const double rc = ctx->mixed_rcut / L.lam, rc2 = rc * rc;
       const int ks = ctx->mixed_kshell;
       std::vector<int> h64, h32;
@@ -439,7 +550,7 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
       }
       ewald_pair_k<double, double2><<<grd, blk, 0, s>>>(nn, L, K64, t64, c64, d_radii, inv_pimu, d_M, ldm, 0); RSD_LAUNCH_NOTE();
       ewald_pair_k<float, float2><<<grd, blk, 0, s>>>(nn, L, K32, t32, c32, d_radii, inv_pimu, d_M, ldm, 1); RSD_LAUNCH_NOTE();
-      ewald_pair_real_t<double, 1><<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, d_M, ldm); RSD_LAUNCH_NOTE();
+      ewald_pair_real_near_ds<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, d_M, ldm); RSD_LAUNCH_NOTE();
       ewald_pair_real_t<float, 2><<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, d_M, ldm); RSD_LAUNCH_NOTE();
     } else {
       ewald_pair_k<double, double2><<<grd, blk, 0, s>>>(nn, L, Kh, tab, cs, d_radii, inv_pimu, d_M, ldm, 0); RSD_LAUNCH_NOTE();

@@ -239,6 +239,40 @@ __device__ inline void lput(double* L, int64_t ld, int r, int c, double v, int a
   *p = acc ? *p + v : v;
 }
 
+// grand-layout index of component k (0..10) of particle part
+__device__ inline int gidx(int N, int part, int k) {
+  return k < 3 ? 3 * part + k : (k < 6 ? 3 * N + 3 * part + k - 3 : 6 * N + 5 * part + k - 6);
+}
+
+// Entry (r, c) of the (a,b) particle block (ab = true) or of the (b,a)
+// block (ab = false) of pair block B, r and c in 0..10.
+__device__ inline double pair_entry(const double* B, int r, int c, bool ab) {
+  if (r < 3 && c < 3) return ab ? B[O_A12 + r + 3 * c] : B[O_A12 + c + 3 * r];  // TT, (b,a) mirrored
+  if (r >= 3 && r < 6 && c >= 3 && c < 6)                                          // RR
+    return ab ? B[O_C12 + (r - 3) + 3 * (c - 3)] : B[O_C12 + (c - 3) + 3 * (r - 3)];
+  if (r >= 3 && r < 6 && c < 3) return (ab ? 1.0 : -1.0) * B[O_B12 + (r - 3) + 3 * c];   // RT: b12, b21 = -b12
+  if (r < 3 && c >= 3 && c < 6) return (ab ? -1.0 : 1.0) * B[O_B12 + (c - 3) + 3 * r];   // TR = RT^T
+  if (r >= 6 && c < 3) return (ab ? 1.0 : -1.0) * B[O_G12 + (r - 6) + 5 * c];            // G: g12, -g12
+  if (r < 3 && c >= 6) return (ab ? -1.0 : 1.0) * B[O_G12 + (c - 6) + 5 * r];            // rfe = QP^T
+  if (r >= 6 && c >= 3 && c < 6) return B[O_H12 + (r - 6) + 5 * (c - 3)];               // H: h12 both ways
+  if (r >= 3 && r < 6 && c >= 6) return B[O_H12 + (c - 6) + 5 * (r - 3)];
+  return B[O_M + (r - 6) + 5 * (c - 6)];                                                 // QQ: mmx both ways
+}
+
+// Entry (r, c) of a particle's own block contributed by pair block B;
+// sgn = +1 when the particle is the pair's first, -1 when its second.
+__device__ inline double self_entry(const double* B, int r, int c, double sgn) {
+  if (r < 3 && c < 3) return B[O_A11 + r + 3 * c];
+  if (r >= 3 && r < 6 && c >= 3 && c < 6) return B[O_C11 + (r - 3) + 3 * (c - 3)];
+  if (r >= 3 && r < 6 && c < 3) return sgn * B[O_B11 + (r - 3) + 3 * c];
+  if (r < 3 && c >= 3 && c < 6) return sgn * B[O_B11 + (c - 3) + 3 * r];
+  if (r >= 6 && c < 3) return sgn * B[O_G11 + (r - 6) + 5 * c];
+  if (r < 3 && c >= 6) return sgn * B[O_G11 + (c - 6) + 5 * r];
+  if (r >= 6 && c >= 3 && c < 6) return B[O_H11 + (r - 6) + 5 * (c - 3)];
+  if (r >= 3 && r < 6 && c >= 6) return B[O_H11 + (c - 6) + 5 * (r - 3)];
+  return B[O_M + (r - 6) + 5 * (c - 6)];
+}
+
 // 121 entries of the (a,b) block and 121 of the (b,a) block per pair
 __global__ void lub_cross(int npair, int N, const int2* __restrict__ pairs, const double* __restrict__ blk,
                           double scale, double* __restrict__ L, int64_t ld, int acc) {
@@ -248,39 +282,8 @@ __global__ void lub_cross(int npair, int N, const int2* __restrict__ pairs, cons
   const int a = pairs[p].x, b = pairs[p].y;
   const double* B = blk + (size_t)p * PB;
   const int r = e % 11, c = e / 11;  // position inside an 11x11 particle block
-  // particle block (u,v): row index rr(u, r), col index cc(v, c)
-  auto gidx = [N](int part, int k) { return k < 3 ? 3 * part + k : (k < 6 ? 3 * N + 3 * part + k - 3 : 6 * N + 5 * part + k - 6); };
-  double vab = 0.0, vba = 0.0;
-  if (r < 3 && c < 3) {  // TT
-    vab = B[O_A12 + r + 3 * c];
-    vba = B[O_A12 + c + 3 * r];  // mirrored from the upper triangle
-  } else if (r >= 3 && r < 6 && c >= 3 && c < 6) {  // RR
-    vab = B[O_C12 + (r - 3) + 3 * (c - 3)];
-    vba = B[O_C12 + (c - 3) + 3 * (r - 3)];
-  } else if (r >= 3 && r < 6 && c < 3) {  // RT: b12 at (a,b), b21 = -b12 at (b,a)
-    vab = B[O_B12 + (r - 3) + 3 * c];
-    vba = -B[O_B12 + (r - 3) + 3 * c];
-  } else if (r < 3 && c >= 3 && c < 6) {  // TR = RT^T
-    vab = -B[O_B12 + (c - 3) + 3 * r];  // = RT(b-rows, a-cols)^T = b21^T
-    vba = B[O_B12 + (c - 3) + 3 * r];
-  } else if (r >= 6 && c < 3) {  // G: QP(5a+i, 3b+j) = g12, QP(5b+i,3a+j) = -g12
-    vab = B[O_G12 + (r - 6) + 5 * c];
-    vba = -B[O_G12 + (r - 6) + 5 * c];
-  } else if (r < 3 && c >= 6) {  // rfe = QP^T
-    vab = -B[O_G12 + (c - 6) + 5 * r];
-    vba = B[O_G12 + (c - 6) + 5 * r];
-  } else if (r >= 6 && c >= 3 && c < 6) {  // H: h12 both ways
-    vab = B[O_H12 + (r - 6) + 5 * (c - 3)];
-    vba = vab;
-  } else if (r >= 3 && r < 6 && c >= 6) {
-    vab = B[O_H12 + (c - 6) + 5 * (r - 3)];
-    vba = vab;
-  } else {  // QQ: mmx at (a,b) and (b,a)
-    vab = B[O_M + (r - 6) + 5 * (c - 6)];
-    vba = vab;
-  }
-  lput(L, ld, gidx(a, r), gidx(b, c), vab * scale, acc);
-  lput(L, ld, gidx(b, r), gidx(a, c), vba * scale, acc);
+  lput(L, ld, gidx(N, a, r), gidx(N, b, c), pair_entry(B, r, c, true) * scale, acc);
+  lput(L, ld, gidx(N, b, r), gidx(N, a, c), pair_entry(B, r, c, false) * scale, acc);
 }
 
 // Second-particle lists: for each particle u, the pairs (a,u) with a < u,
@@ -313,31 +316,77 @@ __global__ void lub_second_sort(int nn, const int* __restrict__ off2, int* __res
 }
 
 // self block of particle u: its pairs as second particle, then as first,
-// in the order lubmxcalc visits them
+// in the order lubmxcalc visits them.  Written into L (grand layout) or,
+// when L is null, into self[u * 121 + r + 11 c].
 __global__ void lub_self(int N, const int* __restrict__ off, const int* __restrict__ off2,
                          const int* __restrict__ list2, const double* __restrict__ blk, double scale,
-                         double* __restrict__ L, int64_t ld, int acc) {
+                         double* __restrict__ L, int64_t ld, int acc, double* __restrict__ self) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)N * 121) return;
   const int u = (int)(t / 121), e = (int)(t % 121);
   const int r = e % 11, c = e / 11;
-  auto entry = [&](const double* B, double sgn) -> double {
-    // sgn = +1 when u is the first particle of the pair, -1 when second
-    if (r < 3 && c < 3) return B[O_A11 + r + 3 * c];
-    if (r >= 3 && r < 6 && c >= 3 && c < 6) return B[O_C11 + (r - 3) + 3 * (c - 3)];
-    if (r >= 3 && r < 6 && c < 3) return sgn * B[O_B11 + (r - 3) + 3 * c];
-    if (r < 3 && c >= 3 && c < 6) return sgn * B[O_B11 + (c - 3) + 3 * r];
-    if (r >= 6 && c < 3) return sgn * B[O_G11 + (r - 6) + 5 * c];
-    if (r < 3 && c >= 6) return sgn * B[O_G11 + (c - 6) + 5 * r];
-    if (r >= 6 && c >= 3 && c < 6) return B[O_H11 + (r - 6) + 5 * (c - 3)];
-    if (r >= 3 && r < 6 && c >= 6) return B[O_H11 + (c - 6) + 5 * (r - 3)];
-    return B[O_M + (r - 6) + 5 * (c - 6)];
-  };
   double v = 0.0;
-  for (int q = off2[u]; q < off2[u + 1]; q++) v += entry(blk + (size_t)list2[q] * PB, -1.0);
-  for (int q = off[u]; q < off[u + 1]; q++) v += entry(blk + (size_t)q * PB, 1.0);
-  auto gidx = [N](int part, int k) { return k < 3 ? 3 * part + k : (k < 6 ? 3 * N + 3 * part + k - 3 : 6 * N + 5 * part + k - 6); };
-  lput(L, ld, gidx(u, r), gidx(u, c), v * scale, acc);
+  for (int q = off2[u]; q < off2[u + 1]; q++) v += self_entry(blk + (size_t)list2[q] * PB, r, c, -1.0);
+  for (int q = off[u]; q < off[u + 1]; q++) v += self_entry(blk + (size_t)q * PB, r, c, 1.0);
+  if (L)
+    lput(L, ld, gidx(N, u, r), gidx(N, u, c), v * scale, acc);
+  else
+    self[t] = v * scale;
+}
+
+// y = L w for the sparse operator, one thread per (row, right-hand side):
+// the particle's self block, then its pairs as first and as second particle.
+__global__ void lub_spmv_k(int N, const int* __restrict__ off, const int* __restrict__ off2,
+                           const int* __restrict__ list2, const int2* __restrict__ pairs,
+                           const double* __restrict__ blk, const double* __restrict__ self, double scale, int nr,
+                           const double* __restrict__ w, int64_t ldw, double* __restrict__ y, int64_t ldy) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t rows = 11LL * N;
+  if (t >= rows * nr) return;
+  const int i = (int)(t % rows), col = (int)(t / rows);
+  const int u = i / 11, r = i % 11;
+  const double* wc = w + col * ldw;
+  double vs = 0.0, vp = 0.0;
+  const double* S = self + (size_t)u * 121;
+#pragma unroll
+  for (int c = 0; c < 11; c++) vs += S[r + 11 * c] * wc[gidx(N, u, c)];
+  for (int p = off[u]; p < off[u + 1]; p++) {
+    const double* B = blk + (size_t)p * PB;
+    const int b = pairs[p].y;
+#pragma unroll
+    for (int c = 0; c < 11; c++) vp += pair_entry(B, r, c, true) * wc[gidx(N, b, c)];
+  }
+  for (int q = off2[u]; q < off2[u + 1]; q++) {
+    const int p = list2[q];
+    const double* B = blk + (size_t)p * PB;
+    const int a = pairs[p].x;
+#pragma unroll
+    for (int c = 0; c < 11; c++) vp += pair_entry(B, r, c, false) * wc[gidx(N, a, c)];
+  }
+  y[gidx(N, u, r) + col * ldy] = vs + vp * scale;
+}
+
+// A (FP32, ld lda) += the force/torque-velocity part L_PP of the sparse
+// operator: pair blocks (each entry of A is touched by at most one pair or
+// self block, so no two threads add to the same entry)
+__global__ void lub_pp_pairs(int npair, int N, const int2* __restrict__ pairs, const double* __restrict__ blk,
+                             double scale, float* __restrict__ A, int64_t lda) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)npair * 36) return;
+  const int p = (int)(t / 36), e = (int)(t % 36);
+  const int r = e % 6, c = e / 6;
+  const int a = pairs[p].x, b = pairs[p].y;
+  const double* B = blk + (size_t)p * PB;
+  A[gidx(N, a, r) + gidx(N, b, c) * lda] += (float)(pair_entry(B, r, c, true) * scale);
+  A[gidx(N, b, r) + gidx(N, a, c) * lda] += (float)(pair_entry(B, r, c, false) * scale);
+}
+
+__global__ void lub_pp_self(int N, const double* __restrict__ self, float* __restrict__ A, int64_t lda) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)N * 36) return;
+  const int u = (int)(t / 36), e = (int)(t % 36);
+  const int r = e % 6, c = e / 6;
+  A[gidx(N, u, r) + gidx(N, u, c) * lda] += (float)self[(size_t)u * 121 + r + 11 * c];
 }
 
 __global__ void zero_matrix(int64_t rows, int64_t cols, double* __restrict__ A, int64_t ld) {
@@ -362,11 +411,10 @@ static double* lubtab_device(rsd_ctx* ctx, const rsd_lubtab* tab) {
   return d;
 }
 
-int rsd_lub_assemble(rsd_ctx* ctx, const rsd_lubtab* tab, int nn, int nb, int is_period, const double* d_pos,
-                     const double* d_radii, const rsd_lattice* lat, double mu_f, double* d_L, int64_t ldl,
-                     int accumulate, int* n_contact) {
-  if (!tab) return rsd_fail(ctx, RSD_EARG, "no lubrication tables");
-  if (nn < 1 || ldl < 11LL * nn) return rsd_fail(ctx, RSD_EARG, "bad size nn=%d ldl=%lld", nn, (long long)ldl);
+// The pair stage shared by the dense and the sparse assembly: near-pair
+// list, pair blocks (unscaled), second-particle lists and contact count.
+static int lub_pair_stage(rsd_ctx* ctx, const rsd_lubtab* tab, int nn, int nb, int is_period, const double* d_pos,
+                          const double* d_radii, const rsd_lattice* lat, rsd_lub_sparse* sp, int* dcon) {
   static bool y2_ready = false;
   if (!y2_ready) {
     double Y[45] = {0};
@@ -389,8 +437,7 @@ int rsd_lub_assemble(rsd_ctx* ctx, const rsd_lubtab* tab, int nn, int nb, int is
   cudaStream_t s = ctx->stream;
   int* cnt = (int*)rsd_scratch(ctx, "lub_count", sizeof(int) * (nn + 1));
   int* off = (int*)rsd_scratch(ctx, "lub_off", sizeof(int) * (nn + 1));
-  int* dcon = (int*)rsd_scratch(ctx, "lub_contacts", sizeof(int) * 2);
-  if (!cnt || !off || !dcon) return RSD_ENOMEM;
+  if (!cnt || !off) return RSD_ENOMEM;
   const int wpb = 8;
   lub_count<<<(nn + wpb - 1) / wpb, 32 * wpb, 0, s>>>(nn, nb, is_period, Ld, d_pos, d_radii, cnt); RSD_LAUNCH_NOTE();
   lub_scan<<<1, 1024, 0, s>>>(nn, cnt, off); RSD_LAUNCH_NOTE();
@@ -399,40 +446,110 @@ int rsd_lub_assemble(rsd_ctx* ctx, const rsd_lubtab* tab, int nn, int nb, int is
   RSD_CUDA(ctx, cudaStreamSynchronize(s));
   int2* pairs = (int2*)rsd_scratch(ctx, "lub_pairs", sizeof(int2) * (size_t)(npair > 0 ? npair : 1));
   double* blk = (double*)rsd_scratch(ctx, "lub_blocks", sizeof(double) * PB * (size_t)(npair > 0 ? npair : 1));
-  if (!pairs || !blk) return RSD_ENOMEM;
+  int* cnt2 = (int*)rsd_scratch(ctx, "lub_count2", sizeof(int) * (nn + 1));
+  int* off2 = (int*)rsd_scratch(ctx, "lub_off2", sizeof(int) * (nn + 1));
+  int* cur = (int*)rsd_scratch(ctx, "lub_cur", sizeof(int) * (nn + 1));
+  int* list2 = (int*)rsd_scratch(ctx, "lub_list2", sizeof(int) * (size_t)(npair > 0 ? npair : 1));
+  if (!pairs || !blk || !cnt2 || !off2 || !cur || !list2) return RSD_ENOMEM;
   RSD_CUDA(ctx, cudaMemsetAsync(dcon, 0, sizeof(int), s));
+  RSD_CUDA(ctx, cudaMemsetAsync(cnt2, 0, sizeof(int) * (nn + 1), s));
+  RSD_CUDA(ctx, cudaMemsetAsync(cur, 0, sizeof(int) * (nn + 1), s));
+  if (npair > 0) {
+    lub_list<<<(nn + wpb - 1) / wpb, 32 * wpb, 0, s>>>(nn, nb, is_period, Ld, d_pos, d_radii, off, pairs); RSD_LAUNCH_NOTE();
+    lub_pairs<<<(npair + 127) / 128, 128, 0, s>>>(npair, T, is_period, Ld, d_pos, d_radii, pairs, blk, dcon); RSD_LAUNCH_NOTE();
+    lub_second_count<<<(npair + 255) / 256, 256, 0, s>>>(npair, pairs, cnt2); RSD_LAUNCH_NOTE();
+    lub_scan<<<1, 1024, 0, s>>>(nn, cnt2, off2); RSD_LAUNCH_NOTE();
+    lub_second_fill<<<(npair + 255) / 256, 256, 0, s>>>(npair, pairs, off2, cur, list2); RSD_LAUNCH_NOTE();
+    lub_second_sort<<<(nn + 127) / 128, 128, 0, s>>>(nn, off2, list2); RSD_LAUNCH_NOTE();
+  } else {
+    RSD_CUDA(ctx, cudaMemsetAsync(off2, 0, sizeof(int) * (nn + 1), s));
+  }
+  sp->nn = nn;
+  sp->npair = npair;
+  sp->pairs = pairs;
+  sp->blk = blk;
+  sp->off = off;
+  sp->off2 = off2;
+  sp->list2 = list2;
+  return RSD_OK;
+}
+
+int rsd_lub_assemble(rsd_ctx* ctx, const rsd_lubtab* tab, int nn, int nb, int is_period, const double* d_pos,
+                     const double* d_radii, const rsd_lattice* lat, double mu_f, double* d_L, int64_t ldl,
+                     int accumulate, int* n_contact) {
+  if (!tab) return rsd_fail(ctx, RSD_EARG, "no lubrication tables");
+  if (nn < 1 || ldl < 11LL * nn) return rsd_fail(ctx, RSD_EARG, "bad size nn=%d ldl=%lld", nn, (long long)ldl);
+  int* dcon = (int*)rsd_scratch(ctx, "lub_contacts", sizeof(int) * 2);
+  if (!dcon) return RSD_ENOMEM;
+  cudaStream_t s = ctx->stream;
   if (!accumulate) {
     const int64_t tot = 121LL * nn * nn;
     zero_matrix<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(11LL * nn, 11LL * nn, d_L, ldl); RSD_LAUNCH_NOTE();
   }
+  rsd_lub_sparse sp;
+  RSD_TRY(lub_pair_stage(ctx, tab, nn, nb, is_period, d_pos, d_radii, lat, &sp, dcon));
   const double scale = 6.0 * (RSD_PI * mu_f);
-  if (npair > 0) {
-    lub_list<<<(nn + wpb - 1) / wpb, 32 * wpb, 0, s>>>(nn, nb, is_period, Ld, d_pos, d_radii, off, pairs); RSD_LAUNCH_NOTE();
-    lub_pairs<<<(npair + 127) / 128, 128, 0, s>>>(npair, T, is_period, Ld, d_pos, d_radii, pairs, blk, dcon); RSD_LAUNCH_NOTE();
-    const int64_t tc = 121LL * npair;
-    lub_cross<<<(unsigned)((tc + 255) / 256), 256, 0, s>>>(npair, nn, pairs, blk, scale, d_L, ldl, 1); RSD_LAUNCH_NOTE();
-  }
-  {
-    int* cnt2 = (int*)rsd_scratch(ctx, "lub_count2", sizeof(int) * (nn + 1));
-    int* off2 = (int*)rsd_scratch(ctx, "lub_off2", sizeof(int) * (nn + 1));
-    int* cur = (int*)rsd_scratch(ctx, "lub_cur", sizeof(int) * (nn + 1));
-    int* list2 = (int*)rsd_scratch(ctx, "lub_list2", sizeof(int) * (size_t)(npair > 0 ? npair : 1));
-    if (!cnt2 || !off2 || !cur || !list2) return RSD_ENOMEM;
-    RSD_CUDA(ctx, cudaMemsetAsync(cnt2, 0, sizeof(int) * (nn + 1), s));
-    RSD_CUDA(ctx, cudaMemsetAsync(cur, 0, sizeof(int) * (nn + 1), s));
-    if (npair > 0) {
-      lub_second_count<<<(npair + 255) / 256, 256, 0, s>>>(npair, pairs, cnt2); RSD_LAUNCH_NOTE();
-      lub_scan<<<1, 1024, 0, s>>>(nn, cnt2, off2); RSD_LAUNCH_NOTE();
-      lub_second_fill<<<(npair + 255) / 256, 256, 0, s>>>(npair, pairs, off2, cur, list2); RSD_LAUNCH_NOTE();
-      lub_second_sort<<<(nn + 127) / 128, 128, 0, s>>>(nn, off2, list2); RSD_LAUNCH_NOTE();
-      const int64_t ts = 121LL * nn;
-      lub_self<<<(unsigned)((ts + 255) / 256), 256, 0, s>>>(nn, off, off2, list2, blk, scale, d_L, ldl, 1); RSD_LAUNCH_NOTE();
-    }
+  if (sp.npair > 0) {
+    const int64_t tc = 121LL * sp.npair;
+    lub_cross<<<(unsigned)((tc + 255) / 256), 256, 0, s>>>(sp.npair, nn, sp.pairs, sp.blk, scale, d_L, ldl, 1); RSD_LAUNCH_NOTE();
+    const int64_t ts = 121LL * nn;
+    lub_self<<<(unsigned)((ts + 255) / 256), 256, 0, s>>>(nn, sp.off, sp.off2, sp.list2, sp.blk, scale, d_L, ldl, 1,
+                                                            nullptr); RSD_LAUNCH_NOTE();
   }
   RSD_CUDA(ctx, cudaGetLastError());
   if (n_contact) {
     RSD_CUDA(ctx, cudaMemcpyAsync(n_contact, dcon, sizeof(int), cudaMemcpyDeviceToHost, s));
     RSD_CUDA(ctx, cudaStreamSynchronize(s));
   }
+  return RSD_OK;
+}
+
+// Sparse form for the mixed-precision refinement: the same pair blocks and
+// the per-particle self blocks (scaled), no dense 11N x 11N matrix.
+int rsd_lub_build_sparse(rsd_ctx* ctx, const rsd_lubtab* tab, int nn, int nb, int is_period, const double* d_pos,
+                         const double* d_radii, const rsd_lattice* lat, double mu_f, rsd_lub_sparse* sp,
+                         int* n_contact) {
+  if (!tab) return rsd_fail(ctx, RSD_EARG, "no lubrication tables");
+  if (nn < 1) return rsd_fail(ctx, RSD_EARG, "bad size nn=%d", nn);
+  int* dcon = (int*)rsd_scratch(ctx, "lub_contacts", sizeof(int) * 2);
+  double* self = (double*)rsd_scratch(ctx, "lub_self_blocks", sizeof(double) * 121 * (size_t)nn);
+  if (!dcon || !self) return RSD_ENOMEM;
+  cudaStream_t s = ctx->stream;
+  RSD_TRY(lub_pair_stage(ctx, tab, nn, nb, is_period, d_pos, d_radii, lat, sp, dcon));
+  sp->scale = 6.0 * (RSD_PI * mu_f);
+  sp->self = self;
+  const int64_t ts = 121LL * nn;
+  lub_self<<<(unsigned)((ts + 255) / 256), 256, 0, s>>>(nn, sp->off, sp->off2, sp->list2, sp->blk, sp->scale,
+                                                          nullptr, 0, 0, self); RSD_LAUNCH_NOTE();
+  RSD_CUDA(ctx, cudaGetLastError());
+  if (n_contact) {
+    RSD_CUDA(ctx, cudaMemcpyAsync(n_contact, dcon, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RSD_CUDA(ctx, cudaStreamSynchronize(s));
+  }
+  return RSD_OK;
+}
+
+// y (11N x nr, grand layout, ld ldy) = L w
+int rsd_lub_spmv(rsd_ctx* ctx, const rsd_lub_sparse* sp, int nr, const double* w, int64_t ldw, double* y,
+                 int64_t ldy) {
+  const int64_t tot = 11LL * sp->nn * nr;
+  lub_spmv_k<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(sp->nn, sp->off, sp->off2, sp->list2, sp->pairs,
+                                                                      sp->blk, sp->self, sp->scale, nr, w, ldw, y,
+                                                                      ldy); RSD_LAUNCH_NOTE();
+  RSD_CUDA(ctx, cudaGetLastError());
+  return RSD_OK;
+}
+
+// A (6N x 6N FP32, ld lda) += L_PP
+int rsd_lub_add_pp_f32(rsd_ctx* ctx, const rsd_lub_sparse* sp, float* A, int64_t lda) {
+  cudaStream_t s = ctx->stream;
+  if (sp->npair > 0) {
+    const int64_t tp = 36LL * sp->npair;
+    lub_pp_pairs<<<(unsigned)((tp + 255) / 256), 256, 0, s>>>(sp->npair, sp->nn, sp->pairs, sp->blk, sp->scale, A,
+                                                              lda); RSD_LAUNCH_NOTE();
+  }
+  const int64_t ts = 36LL * sp->nn;
+  lub_pp_self<<<(unsigned)((ts + 255) / 256), 256, 0, s>>>(sp->nn, sp->self, A, lda); RSD_LAUNCH_NOTE();
+  RSD_CUDA(ctx, cudaGetLastError());
   return RSD_OK;
 }

@@ -6,9 +6,10 @@
 // Augmented system in (f, U), with w = [U; -EIN]:
 //     M f = w                    (f = R_inf w, the far-field forces)
 //     f_P + (L w)_P = Fe          (force balance with lubrication)
-// and then SijN_hyd = f_Q + (L w)_Q.  Its FP64 residual needs only the dense
-// FP64 products M f and L w (HBM-bound GEMVs).  The correction is solved
-// with FP32 factors:
+// and then SijN_hyd = f_Q + (L w)_Q.  Its FP64 residual needs only the FP64
+// products M f (an HBM-bound dense GEMV) and L w (a block-sparse product
+// over the near pairs, L is never formed densely here).  The correction is
+// solved with FP32 factors:
 //   M' = [M_QQ M_QP; M_PQ M_PP] = U'^T U'  (stresslets ordered first), so the
 //   trailing block U'_PP is the Cholesky factor of the Schur complement
 //   A = M_PP - M_PQ M_QQ^-1 M_QP and (M^-1)_PP = A^-1 = U'_PP^-1 U'_PP^-T;
@@ -36,7 +37,9 @@ template <typename T>
 int rsd_mirror_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda);
 template <typename T>
 int rsd_diag_inverses_t(rsd_ctx* ctx, int n, const T* U, int64_t ldu, const char* tag, T** Wout);
-int rsd_wide_inverses_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const char* tag, float** W2out);
+int rsd_wide_inverses_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const char* tag, const float* W128,
+                        float** W2out);
+const float* rsd_potrf_inverses_s(rsd_ctx* ctx, int n, const char* tag);
 int rsd_potrs_wide_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const float* W2, float* X, int64_t ldx,
                      int nrhs, float* Y);
 
@@ -58,13 +61,6 @@ __global__ void copy_block_f(int64_t rows, int64_t cols, const float* __restrict
   if (t >= rows * cols) return;
   const int64_t i = t % rows, j = t / rows;
   D[i + j * ldd] = S[i + j * lds];
-}
-
-__global__ void add_lub_pp(int64_t P, float* __restrict__ A, const double* __restrict__ L, int64_t ldl) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= P * P) return;
-  const int64_t i = t % P, j = t / P;
-  A[i + j * P] += (float)L[i + j * ldl];
 }
 
 // w = [U; -EIN] per column
@@ -195,22 +191,18 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   const int nr = have_fe ? 2 : 1;
   const double tol = p->tol > 0 ? p->tol : 1e-12;
   const int maxit = p->max_iter > 0 ? p->max_iter : 50;
-  double* L = (double*)rsd_scratch(ctx, "mixed_L", sizeof(double) * n * n);
   float* M32 = (float*)rsd_scratch(ctx, "mixed_M32", sizeof(float) * n * n);
   float* A32 = (float*)rsd_scratch(ctx, "mixed_A32", sizeof(float) * P * P);
   double* V = (double*)rsd_scratch(ctx, "mixed_vec", sizeof(double) * (size_t)nr * (7 * n + 2 * P) + 64 * 8);
   float* V32 = (float*)rsd_scratch(ctx, "mixed_vec32", sizeof(float) * (size_t)nr * (2 * n + 2 * P));
-  if (!L || !M32 || !A32 || !V || !V32) return RSD_ENOMEM;
+  if (!M32 || !A32 || !V || !V32) return RSD_ENOMEM;
   double *f = V, *U = f + nr * n, *w = U + nr * P, *r1 = w + nr * n, *Lw = r1 + nr * n, *r2 = Lw + nr * n,
          *y = r2 + nr * P, *y2 = y + nr * n, *dv = y2 + nr * n, *nrm = dv + nr * n;
   float *t32 = V32, *u32 = V32 + nr * n, *ywork = u32 + nr * P;
-  // dense FP64 lubrication matrix (R_lub - R_2B in the grand layout)
+  // sparse FP64 lubrication operator (R_lub - R_2B in the grand layout)
   int nc = 0;
-  if (p->use_lub) {
-    RSD_TRY(rsd_lub_assemble(ctx, tab, nn, p->nb, 1, d_pos, d_radii, lat, p->mu_f, L, n, 0, &nc));
-  } else {
-    RSD_CUDA(ctx, cudaMemsetAsync(L, 0, sizeof(double) * n * n, s));
-  }
+  rsd_lub_sparse lub;
+  if (p->use_lub) RSD_TRY(rsd_lub_build_sparse(ctx, tab, nn, p->nb, 1, d_pos, d_radii, lat, p->mu_f, &lub, &nc));
   info->n_contact = nc;
   cudaEventRecord(ctx->ev[6], s);
   // FP32 factor of M' (stresslets first)
@@ -222,25 +214,25 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   // the inverse A^-1 meets cond(A)^2 and the factor of RPP meets cond(RPP),
   // which grows like the inverse lubrication gap, so those use 3xTF32
   // (about 2^-21, close to FP32).
-  RSD_TRY(rsd_potrf_upper_t<float>(ctx, (int)n, M32, n, &inf, "m32", 1));
+  RSD_TRY(rsd_potrf_upper_t<float>(ctx, (int)n, M32, n, &inf, "m32", ctx->use_tc == 3 ? 3 : 1));
   if (inf) {
     info->info = inf;
     return rsd_fail(ctx, inf, "FP32 factor of the grand mobility: leading minor %d not positive", inf);
   }
   float* W_m = nullptr;
-  RSD_TRY(rsd_wide_inverses_s(ctx, (int)n, M32, n, "m32", &W_m));
+  RSD_TRY(rsd_wide_inverses_s(ctx, (int)n, M32, n, "m32", rsd_potrf_inverses_s(ctx, (int)n, "m32"), &W_m));
   // A^-1 from the trailing factor block, then RPP32 = A^-1 + rfu and its factor
   copy_block_f<<<nblk(P * P), 256, 0, s>>>(P, P, M32 + Q + Q * n, n, A32, P); RSD_LAUNCH_NOTE();
   RSD_TRY(rsd_potri_upper_t<float>(ctx, (int)P, A32, P, "a32", 3));
   RSD_TRY(rsd_mirror_upper_t<float>(ctx, (int)P, A32, P));
-  add_lub_pp<<<nblk(P * P), 256, 0, s>>>(P, A32, L, n); RSD_LAUNCH_NOTE();
+  if (p->use_lub) RSD_TRY(rsd_lub_add_pp_f32(ctx, &lub, A32, P));
   RSD_TRY(rsd_potrf_upper_t<float>(ctx, (int)P, A32, P, &inf, "rpp32", 3));
   if (inf) {
     info->info = inf;
     return rsd_fail(ctx, inf, "FP32 factor of RPP: leading minor %d not positive", inf);
   }
   float* W_r = nullptr;
-  RSD_TRY(rsd_wide_inverses_s(ctx, (int)P, A32, P, "rpp32", &W_r));
+  RSD_TRY(rsd_wide_inverses_s(ctx, (int)P, A32, P, "rpp32", rsd_potrf_inverses_s(ctx, (int)P, "rpp32"), &W_r));
   // refinement
   cudaEventRecord(ctx->ev[7], s);
   RSD_CUDA(ctx, cudaMemsetAsync(f, 0, sizeof(double) * nr * n, s));
@@ -252,7 +244,11 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
     build_w<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, U, ein, w); RSD_LAUNCH_NOTE();
     RSD_CUDA(ctx, cudaMemcpyAsync(r1, w, sizeof(double) * nr * n, cudaMemcpyDeviceToDevice, s));
     RSD_TRY(rsd_gemv<double>(ctx, 0, (int)n, (int)n, -1.0, M, ld, f, n, nr, 1.0, r1, n));
-    RSD_TRY(rsd_gemv<double>(ctx, 0, (int)n, (int)n, 1.0, L, n, w, n, nr, 0.0, Lw, n));
+    if (p->use_lub) {
+      RSD_TRY(rsd_lub_spmv(ctx, &lub, nr, w, n, Lw, n));
+    } else {
+      RSD_CUDA(ctx, cudaMemsetAsync(Lw, 0, sizeof(double) * nr * n, s));
+    }
     build_r2<<<nblk(P * nr), 256, 0, s>>>(P, n, nr, Fe, have_fe, f, Lw, r2); RSD_LAUNCH_NOTE();
     norms<<<nr, 256, 0, s>>>(P, n, nr, r1, r2, ein, Fe, have_fe, nrm); RSD_LAUNCH_NOTE();
     RSD_CUDA(ctx, cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 2 * nr, cudaMemcpyDeviceToHost, s));

@@ -31,9 +31,11 @@ struct rsd_ctx {
   std::map<std::string, rsd_buf> bufs;  // grow-only device buffers by name
   cudaEvent_t ev[8] = {};
   double phase_ms[4] = {0, 0, 0, 0};
-  int use_tc = 1;         // tcgen05 GEMMs in the FP32 factorisations (0: SIMT only)
-  double mixed_rcut = 4.5;  // mixed assembly: FP64 real images below this lambda r
-  int mixed_kshell = 2;     // mixed assembly: FP64 reciprocal shells max|n_i| <= this
+  int use_tc = 1;         // FP32 factorisations: 0 SIMT, 1 per-factor TF32/3xTF32, 3 all 3xTF32
+  double mixed_rcut = 4.0;  // mixed assembly: FP64 real images below this lambda r
+  int mixed_kshell = 1;     // mixed assembly: FP64 reciprocal shells max|n_i| <= this
+  cudaStream_t side = nullptr;  // higher-priority stream for look-ahead panels
+  cudaEvent_t ev_panel = nullptr, ev_next = nullptr;
   int* d_info = nullptr;  // device-side status words
   int* h_info = nullptr;  // pinned mirror
 };
@@ -65,6 +67,8 @@ int rsd_cuda_check(rsd_ctx* ctx, cudaError_t e, const char* what);
 // allocation failure.
 void* rsd_scratch(rsd_ctx* ctx, const char* name, size_t bytes);
 int rsd_set_device(rsd_ctx* ctx);
+// creates ctx->side, ev_panel and ev_next on first use
+int rsd_side_stream(rsd_ctx* ctx);
 
 // ------------------------------------------------------------ lattice
 struct rsd_lat_dev {
@@ -109,6 +113,23 @@ int rsd_count_overlaps(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
 int rsd_lub_assemble(rsd_ctx* ctx, const rsd_lubtab* tab, int nn, int nb, int is_period, const double* d_pos,
                      const double* d_radii, const rsd_lattice* lat, double mu_f, double* d_L, int64_t ldl,
                      int accumulate, int* n_contact);
+// Sparse lubrication operator of the mixed-precision refinement (lub.cu):
+// the near-pair blocks (139 unscaled values each) and the per-particle self
+// blocks (121 scaled values each, entry (r, c) at r + 11 c).
+struct rsd_lub_sparse {
+  int nn = 0, npair = 0;
+  const int2* pairs = nullptr;
+  const double* blk = nullptr;
+  const int *off = nullptr, *off2 = nullptr, *list2 = nullptr;
+  const double* self = nullptr;
+  double scale = 0.0;
+};
+int rsd_lub_build_sparse(rsd_ctx* ctx, const rsd_lubtab* tab, int nn, int nb, int is_period, const double* d_pos,
+                         const double* d_radii, const rsd_lattice* lat, double mu_f, rsd_lub_sparse* sp,
+                         int* n_contact);
+int rsd_lub_spmv(rsd_ctx* ctx, const rsd_lub_sparse* sp, int nr, const double* w, int64_t ldw, double* y,
+                 int64_t ldy);
+int rsd_lub_add_pp_f32(rsd_ctx* ctx, const rsd_lub_sparse* sp, float* A, int64_t lda);
 // Dense linear algebra (dense.cu)
 int rsd_potrf_upper(rsd_ctx* ctx, int n, double* d_A, int64_t lda, int* info);
 int rsd_potri_upper(rsd_ctx* ctx, int n, double* d_A, int64_t lda);  // after potrf; result upper
