@@ -79,12 +79,20 @@ long long rsd_launch_count(void);
  * 0 = FP32 SIMT kernels only.  The FP64 form is unaffected. */
 int rsd_ctx_set_tensor_cores(rsd_ctx* ctx, int mode);
 /* Precision split of the mixed-precision Ewald assembly: real-space images
- * with lammda*r < lam_r_cut and reciprocal vectors with max|n_i| <= kshell
- * are summed in FP64, the rest in FP32.  Defaults 4.0 and 1: a step's
+ * with lammda*r < lam_r_cut (at most 6) and reciprocal vectors with
+ * max|n_i| <= kshell are summed in double-single / FP64 (~1e-14), the rest
+ * in FP32.  Defaults 4.0 and 1: a step's
  * velocities then agree with the FP64 form to ~3e-12 and its stresslets to
  * ~6e-11 relative (3.5 gives ~5e-11 and ~1e-9 at 0.85x the assembly time,
  * 4.5 ~1e-13 and ~2e-12 at 1.2x). */
 int rsd_ctx_set_mixed_split(rsd_ctx* ctx, double lam_r_cut, int32_t kshell);
+/* Truncation of the mixed-precision Ewald sums inside the reference's image
+ * cubes: real-space images with lammda*r >= lam_r_max and reciprocal vectors
+ * with k^2/(4 lammda^2) >= k2_over_4lam2_max are dropped.  Defaults 6.0 and
+ * 10 pi: each changes a mobility block by less than ~1e-12 of its largest
+ * entry (the reference's cubes reach lammda*r ~ 10 and k^2/(4 lammda^2) ~
+ * 85 at zero strain).  The FP64 form always sums the whole cubes. */
+int rsd_ctx_set_mixed_truncation(rsd_ctx* ctx, double lam_r_max, double k2_over_4lam2_max);
 
 /* ---------------------------------------------------------------- lattice */
 /* SET_LATTICE_SKEW (src/csd_post.f90:105-136) with MAT_INV3

@@ -94,6 +94,7 @@ _sig("rsd_stepper_stokesian_dev", _i, [_vp, _vp, ctypes.POINTER(StepParams), _vp
                                        ctypes.POINTER(StepInfo)])
 _sig("rsd_ctx_set_tensor_cores", _i, [_vp, _i])
 _sig("rsd_ctx_set_mixed_split", _i, [_vp, _d, _i32])
+_sig("rsd_ctx_set_mixed_truncation", _i, [_vp, _d, _d])
 _sig("rsd_syrk_f32_dev", _i, [_vp, _i32, _i32, _vp, _i64, _vp, _i64, _i32])
 _sig("rsd_potrf_f32_dev", _i, [_vp, _i32, _vp, _i64, _i32, _ip])
 _sig("rsd_potri_f32_dev", _i, [_vp, _i32, _vp, _i64, _i32])
@@ -149,6 +150,10 @@ class Context:
     def set_mixed_split(self, lam_r_cut=4.0, kshell=1):
         """FP64/FP32 split of the mixed-precision Ewald assembly."""
         self.check(_lib.rsd_ctx_set_mixed_split(self.h, float(lam_r_cut), int(kshell)))
+
+    def set_mixed_truncation(self, lam_r_max=6.0, k2_over_4lam2_max=10.0 * np.pi):
+        """Truncation of the mixed-precision Ewald sums."""
+        self.check(_lib.rsd_ctx_set_mixed_truncation(self.h, float(lam_r_max), float(k2_over_4lam2_max)))
 
     def set_tensor_cores(self, mode=1):
         """FP32 factorisations of the mixed form: 1 (or True, the default)

@@ -128,9 +128,19 @@ extern "C" void* rsd_ctx_stream(rsd_ctx* c) { return c ? (void*)c->stream : null
 
 extern "C" int rsd_ctx_set_mixed_split(rsd_ctx* c, double lam_r_cut, int32_t kshell) {
   if (!c) return RSD_EARG;
-  if (!(lam_r_cut >= 0.0) || kshell < 0) return rsd_fail(c, RSD_EARG, "mixed split: lam_r_cut >= 0, kshell >= 0");
+  if (!(lam_r_cut >= 0.0 && lam_r_cut <= 6.0) || kshell < 0)
+    return rsd_fail(c, RSD_EARG, "mixed split: 0 <= lam_r_cut <= 6, kshell >= 0");
   c->mixed_rcut = lam_r_cut;
   c->mixed_kshell = kshell;
+  return RSD_OK;
+}
+
+extern "C" int rsd_ctx_set_mixed_truncation(rsd_ctx* c, double lam_r_max, double k2_over_4lam2_max) {
+  if (!c) return RSD_EARG;
+  if (!(lam_r_max > 0.0) || !(k2_over_4lam2_max > 0.0))
+    return rsd_fail(c, RSD_EARG, "mixed truncation: both limits must be positive");
+  c->mixed_rmax = lam_r_max;
+  c->mixed_kexp = k2_over_4lam2_max;
   return RSD_OK;
 }
 

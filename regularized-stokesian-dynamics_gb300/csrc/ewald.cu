@@ -183,28 +183,71 @@ __device__ inline bool pair_of(int nn, int* a, int* b) {
   return *a < nn && *b < nn && *a < *b;
 }
 
+template <typename T>
+struct Vec2;
+template <>
+struct Vec2<float> {
+  using type = float4;  // four weights per shared-memory load
+  static constexpr int W = 4;
+};
+template <>
+struct Vec2<double> {
+  using type = double2;
+  static constexpr int W = 2;
+};
+
+// Reciprocal-space pair sums: per half-space vector, cos and sin of k.(x_a -
+// x_b) from the per-particle trig table, times the vector's 80 moment
+// weights.  The weights are staged in shared memory 16 vectors at a time and
+// read as 16-byte vectors (the same address for every thread of a warp).
 template <typename T, typename T2>
 __global__ void __launch_bounds__(128) ewald_pair_k(int nn, rsd_lat_dev L, int Kh, const T* __restrict__ tab,
                                                     const T2* __restrict__ cs, const double* __restrict__ radii,
                                                     double inv_pimu, double* __restrict__ M, int64_t ldm, int add) {
   constexpr int KWT = 3 + RSD_NMOM_KCOS + RSD_NMOM_KSIN;
+  constexpr int NW = RSD_NMOM_KCOS + RSD_NMOM_KSIN;  // 80
+  constexpr int KC = 16;
+  using V = typename Vec2<T>::type;
+  constexpr int VW = Vec2<T>::W;
+  static_assert(NW % VW == 0, "weights per vector");
+  __shared__ __align__(16) T sw[KC * NW];
+  // blocks entirely on or below the diagonal (a >= b everywhere) have no work
+  if ((int)(blockIdx.x * blockDim.x) >= (int)(blockIdx.y * blockDim.y + blockDim.y - 1)) return;
   int a, b;
-  if (!pair_of(nn, &a, &b)) return;
+  const bool valid = pair_of(nn, &a, &b);
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
   T ac[RSD_NMOM_KCOS], as[RSD_NMOM_KSIN];
 #pragma unroll
   for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] = T(0);
 #pragma unroll
   for (int m = 0; m < RSD_NMOM_KSIN; m++) as[m] = T(0);
-  for (int h = 0; h < Kh; h++) {
-    const T2 ua = cs[(size_t)h * nn + a], ub = cs[(size_t)h * nn + b];
-    const T c = ua.x * ub.x + ua.y * ub.y;  // cos(k.(x_a - x_b))
-    const T s = ua.y * ub.x - ua.x * ub.y;  // sin(k.(x_a - x_b))
-    const T* e = tab + (size_t)h * KWT + 3;
+  for (int h0 = 0; h0 < Kh; h0 += KC) {
+    const int kc = min(KC, Kh - h0);
+    __syncthreads();
+    for (int e = tid; e < kc * NW; e += nthr) sw[e] = tab[(size_t)(h0 + e / NW) * KWT + 3 + e % NW];
+    __syncthreads();
+    if (!valid) continue;
+    for (int hh = 0; hh < kc; hh++) {
+      const T2 ua = cs[(size_t)(h0 + hh) * nn + a], ub = cs[(size_t)(h0 + hh) * nn + b];
+      const T c = ua.x * ub.x + ua.y * ub.y;  // cos(k.(x_a - x_b))
+      const T sn = ua.y * ub.x - ua.x * ub.y;  // sin(k.(x_a - x_b))
+      const V* e = reinterpret_cast<const V*>(sw + hh * NW);
 #pragma unroll
-    for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] = fma(__ldg(e + m), c, ac[m]);
+      for (int m4 = 0; m4 < NW / VW; m4++) {
+        const V w = e[m4];
+        const T* wq = reinterpret_cast<const T*>(&w);
 #pragma unroll
-    for (int m = 0; m < RSD_NMOM_KSIN; m++) as[m] = fma(__ldg(e + RSD_NMOM_KCOS + m), s, as[m]);
+        for (int q = 0; q < VW; q++) {
+          const int m = m4 * VW + q;
+          if (m < RSD_NMOM_KCOS)
+            ac[m] = fma(wq[q], c, ac[m]);
+          else
+            as[m - RSD_NMOM_KCOS] = fma(wq[q], sn, as[m - RSD_NMOM_KCOS]);
+        }
+      }
+    }
   }
+  if (!valid) return;
   const T ai = (T)radii[a], aj = (T)radii[b], phix = (T)L.phix;
   T v[60], w[60];
   rsd_kcos_epilogue<T>(ac, ai, aj, phix, v);
@@ -217,105 +260,65 @@ __global__ void __launch_bounds__(128) ewald_pair_k(int nn, rsd_lat_dev L, int K
   store_pair(M, ldm, nn, a, b, o, add);
 }
 
-// Near/far split of the real-space images for the mixed form.  For one
-// lattice column p + a3 nz (p = R + nx a1 + ny a2) the images with
-// |p + a3 nz| < rc are those with nz strictly between the roots zlo, zhi of
-// |a3|^2 z^2 + 2 (p.a3) z + |p|^2 - rc^2.  An integer nz further than
-// COL_MARGIN from both roots is classified by the interval alone; the rare
-// ones closer than that take the direct FP64 distance test.  Every step uses
-// explicitly rounded FP64 operations, so the FP64 (near) and FP32 (far)
-// kernels classify every image identically: each is summed exactly once.
-// (The root errors are below ~1e-7 in nz, far inside the margin.)
-constexpr double COL_MARGIN = 1e-6;
-
-struct ColumnSplit {
-  double p[3];
-  double zlo, zhi;
-};
-
-__device__ inline ColumnSplit column_split(const double R[3], const double* LR, int nx, int ny, double rc2) {
-  ColumnSplit c;
-  for (int k = 0; k < 3; k++) c.p[k] = __fma_rn(LR[3 + k], (double)ny, __fma_rn(LR[k], (double)nx, R[k]));
-  const double* a3 = LR + 6;
-  const double a33 = __fma_rn(a3[0], a3[0], __fma_rn(a3[1], a3[1], __dmul_rn(a3[2], a3[2])));
-  const double pa = __fma_rn(c.p[0], a3[0], __fma_rn(c.p[1], a3[1], __dmul_rn(c.p[2], a3[2])));
-  const double pp = __fma_rn(c.p[0], c.p[0], __fma_rn(c.p[1], c.p[1], __dmul_rn(c.p[2], c.p[2])));
-  const double D = __fma_rn(pa, pa, -__dmul_rn(a33, __dsub_rn(pp, rc2)));
-  const double zc = __ddiv_rn(-pa, a33);
-  if (D > 0.0) {
-    const double h = __ddiv_rn(__dsqrt_rn(D), a33);
-    c.zlo = __dsub_rn(zc, h);
-    c.zhi = __dadd_rn(zc, h);
-  } else {
-    c.zlo = c.zhi = zc;  // empty (or tangent): only integers within the margin get the direct test
-  }
-  return c;
+// Near/far split of the real-space images for the mixed form.  Image nz of
+// lattice column (nx, ny) has FP32 coordinates p + a3 nz, where p = R + nx a1
+// + ny a2 is formed in FP64 and rounded once; it is "near" when its FP32
+// squared distance, computed by exactly the sequence below, is below rc^2.
+// The near (double-single) and far (FP32) kernels evaluate the same sequence
+// on the same inputs, so every image is summed by exactly one of them.  An
+// image within a rounding of the boundary may fall on either side; both
+// sides are accurate there.
+__device__ __forceinline__ void column_base(const double R[3], const double* LR, int nx, int ny, double p[3]) {
+  for (int k = 0; k < 3; k++) p[k] = __fma_rn(LR[3 + k], (double)ny, __fma_rn(LR[k], (double)nx, R[k]));
 }
 
-// image nz of the column: FP64 coordinates
-__device__ inline void column_point(const ColumnSplit& c, const double* LR, int nz, double d[3]) {
-  for (int k = 0; k < 3; k++) d[k] = __fma_rn(LR[6 + k], (double)nz, c.p[k]);
+__device__ __forceinline__ float image_r2f(float p0, float p1, float p2, float a0, float a1, float a2, int nz,
+                                           float* x0, float* x1, float* x2) {
+  const float z = (float)nz;
+  *x0 = __fmaf_rn(a0, z, p0);
+  *x1 = __fmaf_rn(a1, z, p1);
+  *x2 = __fmaf_rn(a2, z, p2);
+  return __fmaf_rn(*x2, *x2, __fmaf_rn(*x1, *x1, __fmul_rn(*x0, *x0)));
 }
 
-// 1 near, 0 far, decided by the interval or by the direct test
-__device__ inline bool column_near(const ColumnSplit& c, const double* LR, int nz, double rc2) {
-  const double z = (double)nz;
-  if (z > c.zlo + COL_MARGIN && z < c.zhi - COL_MARGIN) return true;
-  if (z < c.zlo - COL_MARGIN || z > c.zhi + COL_MARGIN) return false;
-  double d[3];
-  column_point(c, LR, nz, d);
-  return __fma_rn(d[0], d[0], __fma_rn(d[1], d[1], __dmul_rn(d[2], d[2]))) < rc2;
-}
-
-// Real-space images of the mixed form: MODE 1 sums the near images
-// (lambda r below the context's mixed_rcut) in FP64, visiting only the nz
-// range of each column that can hold them; MODE 2 sums the others in FP32,
-// with FP32 coordinates p + a3 nz from the column's FP64 base point.  The
-// radial functions of erfc(lambda r) feed moments that the epilogue combines
-// with 2-3 orders of cancellation, so FP32 is kept for images whose terms
-// are below ~1e-10 of a block.
-template <typename T, int MODE>
-__global__ void __launch_bounds__(128) ewald_pair_real_t(int nn, rsd_lat_dev L, const double* __restrict__ pos,
-                                                         const double* __restrict__ radii, double inv_pimu,
-                                                         double rc2, double* __restrict__ M, int64_t ldm) {
+// Far real-space images of the mixed form in FP32: lambda r from the
+// context's mixed_rcut up to mixed_rmax (beyond which the terms change a
+// block by less than ~1e-12 of its largest entry), with FP32 coordinates
+// p + a3 nz from each column's FP64 base point.  The radial functions of
+// erfc(lambda r) feed moments that the epilogue combines with 2-3 orders of
+// cancellation, so FP32 is kept for images whose terms are below ~1e-6 of a
+// block (a few 1e-11 of a block after the epilogue).
+__global__ void __launch_bounds__(128) ewald_pair_real_far(int nn, rsd_lat_dev L, const double* __restrict__ pos,
+                                                           const double* __restrict__ radii, double inv_pimu,
+                                                           double rc2, double rmax2, double* __restrict__ M,
+                                                           int64_t ldm) {
   int a, b;
   if (!pair_of(nn, &a, &b)) return;
   double R[3] = {pos[3 * a] - pos[3 * b], pos[3 * a + 1] - pos[3 * b + 1], pos[3 * a + 2] - pos[3 * b + 2]};
   double dmin;
   rsd_skew_correction(L.LR, L.LI, R, &dmin);
-  T acc[RSD_NMOM_REAL];
+  float acc[RSD_NMOM_REAL];
 #pragma unroll
-  for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = T(0);
-  const T lam = (T)L.lam, lam2 = lam * lam, cd = T(2.0 * RSD_PIP5) * lam;
+  for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = 0.f;
+  const float lam = (float)L.lam, lam2 = lam * lam, cd = (float)(2.0 * RSD_PIP5) * lam;
+  const float a0 = __double2float_rn(L.LR[6]), a1 = __double2float_rn(L.LR[7]), a2 = __double2float_rn(L.LR[8]);
+  const float rc2f = __double2float_rn(rc2), rmax2f = __double2float_rn(rmax2);
   const int NR = L.NR;
   for (int nx = -NR; nx <= NR; nx++)
     for (int ny = -NR; ny <= NR; ny++) {
-      const ColumnSplit col = column_split(R, L.LR, nx, ny, rc2);
-      if constexpr (MODE == 1) {
-        const int lo = max(-NR, (int)ceil(col.zlo - COL_MARGIN)), hi = min(NR, (int)floor(col.zhi + COL_MARGIN));
-        for (int nz = lo; nz <= hi; nz++) {
-          if (!column_near(col, L.LR, nz, rc2)) continue;
-          double d[3];
-          column_point(col, L.LR, nz, d);
-          const T r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-          const T r = sqrt(r2), ir = T(1) / r;
-          rsd_real_image<T>(d[0], d[1], d[2], r, ir, erfc(lam * r), cd * exp(-r2 * lam2), lam, acc);
-        }
-      } else {
-        const float p0 = (float)col.p[0], p1 = (float)col.p[1], p2 = (float)col.p[2];
-        const float a0 = (float)L.LR[6], a1 = (float)L.LR[7], a2 = (float)L.LR[8];
-        for (int nz = -NR; nz <= NR; nz++) {
-          if (column_near(col, L.LR, nz, rc2)) continue;
-          const T x0 = fmaf(a0, (float)nz, p0), x1 = fmaf(a1, (float)nz, p1), x2 = fmaf(a2, (float)nz, p2);
-          const T r2 = x0 * x0 + x1 * x1 + x2 * x2;
-          const T r = sqrt(r2), ir = T(1) / r;
-          const T E0 = erfc(lam * r), Ed = cd * exp(-r2 * lam2);
-          rsd_real_image<T>(x0, x1, x2, r, ir, E0, Ed, lam, acc);
-        }
+      double p[3];
+      column_base(R, L.LR, nx, ny, p);
+      const float p0 = __double2float_rn(p[0]), p1 = __double2float_rn(p[1]), p2 = __double2float_rn(p[2]);
+      for (int nz = -NR; nz <= NR; nz++) {
+        float x0, x1, x2;
+        const float r2 = image_r2f(p0, p1, p2, a0, a1, a2, nz, &x0, &x1, &x2);
+        if (r2 < rc2f || r2 >= rmax2f) continue;  // near (the other kernel) or truncated
+        const float r = sqrtf(r2), ir = 1.f / r;
+        rsd_real_image<float>(x0, x1, x2, r, ir, erfcf(lam * r), cd * expf(-r2 * lam2), lam, acc);
       }
     }
-  T v[60];
-  rsd_real_epilogue<T>(acc, (T)radii[a], (T)radii[b], (T)L.phix, v);
+  float v[60];
+  rsd_real_epilogue<float>(acc, (float)radii[a], (float)radii[b], (float)L.phix, v);
   double o[60];
 #pragma unroll
   for (int q = 0; q < 60; q++) o[q] = (double)v[q];
@@ -323,15 +326,20 @@ __global__ void __launch_bounds__(128) ewald_pair_real_t(int nn, rsd_lat_dev L, 
   store_pair(M, ldm, nn, a, b, o, 1);
 }
 
-// Near images of the mixed form in double-single arithmetic: coordinates,
-// r, 1/r, erfc(lambda r) and the Gaussian come from FP64 (as in the FP64
-// kernel), the moments are evaluated and accumulated in double-single on the
-// FP32 pipe (~4e-15 relative per operation, so even after the epilogue's
-// 2-3 orders of cancellation a block stays within ~1e-12 of FP64), and the
-// epilogue runs in FP64.  Same image set as ewald_pair_real_t<double, 1>.
+// Near images of the mixed form (lambda r below the context's mixed_rcut) in
+// double-single arithmetic on the FP32 pipe: coordinates p + a3 nz, r, 1/r,
+// erfc(lambda r) and the Gaussian (dsf.cuh), the moments and their sums all
+// carry ~48 bits (so even after the epilogue's 2-3 orders of cancellation a
+// block stays within ~1e-12 of FP64); FP64 is left for the per-column set-up
+// and the FP64 epilogue.  Same image set as the FP32 far kernel's complement.
 __global__ void __launch_bounds__(128) ewald_pair_real_near_ds(int nn, rsd_lat_dev L, const double* __restrict__ pos,
                                                                const double* __restrict__ radii, double inv_pimu,
                                                                double rc2, double* __restrict__ M, int64_t ldm) {
+  __shared__ dsf_tables T;
+  // blocks entirely on or below the diagonal (a >= b everywhere) have no work
+  if ((int)(blockIdx.x * blockDim.x) >= (int)(blockIdx.y * blockDim.y + blockDim.y - 1)) return;
+  dsf_tables_fill(T, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y);
+  __syncthreads();
   int a, b;
   if (!pair_of(nn, &a, &b)) return;
   double R[3] = {pos[3 * a] - pos[3 * b], pos[3 * a + 1] - pos[3 * b + 1], pos[3 * a + 2] - pos[3 * b + 2]};
@@ -340,21 +348,26 @@ __global__ void __launch_bounds__(128) ewald_pair_real_near_ds(int nn, rsd_lat_d
   dsf acc[RSD_NMOM_REAL];
 #pragma unroll
   for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = dsf(0);
-  const double lam = L.lam, lam2 = lam * lam, cd = 2.0 * RSD_PIP5 * lam;
-  const dsf lam_s = dsf_from(lam);
+  const dsf lam_s = dsf_from(L.lam), cd_s = dsf_from(2.0 * RSD_PIP5 * L.lam);
+  const dsf a30 = dsf_from(L.LR[6]), a31 = dsf_from(L.LR[7]), a32 = dsf_from(L.LR[8]);
+  const float a0 = __double2float_rn(L.LR[6]), a1 = __double2float_rn(L.LR[7]), a2 = __double2float_rn(L.LR[8]);
+  const float rc2f = __double2float_rn(rc2);
   const int NR = L.NR;
   for (int nx = -NR; nx <= NR; nx++)
     for (int ny = -NR; ny <= NR; ny++) {
-      const ColumnSplit col = column_split(R, L.LR, nx, ny, rc2);
-      const int lo = max(-NR, (int)ceil(col.zlo - COL_MARGIN)), hi = min(NR, (int)floor(col.zhi + COL_MARGIN));
-      for (int nz = lo; nz <= hi; nz++) {
-        if (!column_near(col, L.LR, nz, rc2)) continue;
-        double d[3];
-        column_point(col, L.LR, nz, d);
-        const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-        const double r = sqrt(r2), ir = 1.0 / r;
-        rsd_real_image<dsf>(dsf_from(d[0]), dsf_from(d[1]), dsf_from(d[2]), dsf_from(r), dsf_from(ir),
-                            dsf_from(erfc(lam * r)), dsf_from(cd * exp(-r2 * lam2)), lam_s, acc);
+      double p[3];
+      column_base(R, L.LR, nx, ny, p);
+      const float f0 = __double2float_rn(p[0]), f1 = __double2float_rn(p[1]), f2 = __double2float_rn(p[2]);
+      const dsf p0 = dsf_from(p[0]), p1 = dsf_from(p[1]), p2 = dsf_from(p[2]);
+      for (int nz = -NR; nz <= NR; nz++) {
+        float y0, y1, y2;
+        if (!(image_r2f(f0, f1, f2, a0, a1, a2, nz, &y0, &y1, &y2) < rc2f)) continue;
+        const dsf x0 = p0 + nz * a30, x1 = p1 + nz * a31, x2 = p2 + nz * a32;
+        const dsf r = dsf_sqrt(x0 * x0 + x1 * x1 + x2 * x2);
+        const dsf ir = dsf_rcp(r);
+        dsf E0, G;
+        dsf_erfc_gauss(lam_s * r, T, &E0, &G);
+        rsd_real_image<dsf>(x0, x1, x2, r, ir, E0, cd_s * G, lam_s, acc);
       }
     }
   double accd[RSD_NMOM_REAL];
@@ -510,7 +523,9 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
   const double inv_pimu = 1.0 / (RSD_PI * mu_f);
   cudaStream_t s = ctx->stream;
   ewald_ktable<<<(Kh + 127) / 128, 128, 0, s>>>(L, Kh, tab); RSD_LAUNCH_NOTE();
-  ewald_trig<<<dim3((nn + 127) / 128, Kh), 128, 0, s>>>(nn, Kh, tab, d_pos, cs); RSD_LAUNCH_NOTE();
+  if (precision != RSD_PREC_MIXED) {
+    ewald_trig<<<dim3((nn + 127) / 128, Kh), 128, 0, s>>>(nn, Kh, tab, d_pos, cs); RSD_LAUNCH_NOTE();
+  }
   ewald_self<<<(nn + 63) / 64, 64, 0, s>>>(nn, L, Kh, tab, d_radii, inv_pimu, d_M, ldm); RSD_LAUNCH_NOTE();
   if (nn > 1) {
     dim3 blk(32, 4), grd((nn + 31) / 32, (nn + 3) / 4);
@@ -521,13 +536,27 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
       // combines moments that cancel by 2-3 orders of magnitude: images at
       // lambda r >= 4.0 then change a block by ~1e-10 of its largest entry
       // (a step's stresslets by ~6e-11, velocities by ~3e-12).
+      // Truncation: real images with lambda r >= mixed_rmax and reciprocal
+      // vectors with k^2 / (4 lambda^2) >= mixed_kexp are dropped (each
+      // changes a block by less than ~1e-12 of its largest entry at the
+      // defaults 6.0 and 10 pi; the FP64 form keeps the whole cube).
       const double rc = ctx->mixed_rcut / L.lam, rc2 = rc * rc;
+      const double rm = ctx->mixed_rmax / L.lam, rmax2 = rm * rm;
       const int ks = ctx->mixed_kshell;
+      const double k2max = 4.0 * L.lam * L.lam * ctx->mixed_kexp;
       std::vector<int> h64, h32;
       for (int h = 0; h < Kh; h++) {
         int nx, ny, nz;
         half_space_index(h, L.NI, &nx, &ny, &nz);
-        (abs(nx) <= ks && abs(ny) <= ks && abs(nz) <= ks ? h64 : h32).push_back(h);
+        double k2 = 0.0;
+        for (int j = 0; j < 3; j++) {
+          const double kj = 2.0 * RSD_PI * (nx * L.LI[3 * j] + ny * L.LI[1 + 3 * j] + nz * L.LI[2 + 3 * j]);
+          k2 += kj * kj;
+        }
+        if (abs(nx) <= ks && abs(ny) <= ks && abs(nz) <= ks)
+          h64.push_back(h);
+        else if (k2 < k2max)
+          h32.push_back(h);
       }
       const int K64 = (int)h64.size(), K32 = (int)h32.size();
       int* dh = (int*)rsd_scratch(ctx, "ewald_hlist", sizeof(int) * (size_t)Kh);
@@ -551,7 +580,7 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
       ewald_pair_k<double, double2><<<grd, blk, 0, s>>>(nn, L, K64, t64, c64, d_radii, inv_pimu, d_M, ldm, 0); RSD_LAUNCH_NOTE();
       ewald_pair_k<float, float2><<<grd, blk, 0, s>>>(nn, L, K32, t32, c32, d_radii, inv_pimu, d_M, ldm, 1); RSD_LAUNCH_NOTE();
       ewald_pair_real_near_ds<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, d_M, ldm); RSD_LAUNCH_NOTE();
-      ewald_pair_real_t<float, 2><<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, d_M, ldm); RSD_LAUNCH_NOTE();
+      ewald_pair_real_far<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, rmax2, d_M, ldm); RSD_LAUNCH_NOTE();
     } else {
       ewald_pair_k<double, double2><<<grd, blk, 0, s>>>(nn, L, Kh, tab, cs, d_radii, inv_pimu, d_M, ldm, 0); RSD_LAUNCH_NOTE();
       ewald_pair_real<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, d_M, ldm); RSD_LAUNCH_NOTE();
