@@ -1096,6 +1096,179 @@ int rsd_wide_inverses_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const 
 // (U^T U) X = B with the NB2 block inverses: per block two wide GEMVs
 // (diagonal block by its inverse, then the update of the remaining rows).
 // X holds B on entry; Y is a work vector of the same shape.
+// ------------------------------------------- block-scaled factor solves
+// U = D Uh with D = blockdiag(U_bb) over NB2 blocks, so Uh_bb = I and
+// Uh_bc = W_b U_bc (W_b = U_bb^-1).  Then U^T U x = r is solved as
+//   forward   z_b = r_b - sum_{c<b} Uh_cb^T z_c        (unit diagonal blocks)
+//   middle    w_b = G_b z_b,  G_b = W_b W_b^T = (U_bb^T U_bb)^-1
+//   backward  x_b = w_b - sum_{c>b} Uh_bc x_c
+// Each direction is one streaming launch per block (the strip of Uh next to
+// the block), with no diagonal solve in between.  Uh and G are formed once
+// per factor on tensor cores (3xTF32).
+namespace {
+
+__global__ void transpose_block(int nb2, const float* __restrict__ W, float* __restrict__ WT) {
+  __shared__ float t[32][33];
+  const int b = blockIdx.z;
+  const float* Wb = W + (size_t)b * nb2 * nb2;
+  float* Tb = WT + (size_t)b * nb2 * nb2;
+  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) t[k][threadIdx.x] = Wb[(i0 + threadIdx.x) + (size_t)(j0 + k) * nb2];
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) Tb[(j0 + threadIdx.x) + (size_t)(i0 + k) * nb2] = t[threadIdx.x][k];
+}
+
+// forward strip: z_rest[c] -= sum_k S(k, c) z_b[k], one warp per column c
+template <int NR>
+__global__ void __launch_bounds__(256) strip_t_update(int kb, int rest, const float* __restrict__ S, int64_t lds,
+                                                      const float* __restrict__ zb, float* __restrict__ zr,
+                                                      int64_t ldx) {
+  __shared__ __align__(16) float sz[NR][NB2];
+  for (int k = threadIdx.x; k < kb; k += blockDim.x)
+    for (int r = 0; r < NR; r++) sz[r][k] = zb[k + r * ldx];
+  __syncthreads();
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int c = warp; c < rest; c += nwarps) {
+    const float* col = S + (int64_t)c * lds;
+    float acc[NR];
+    for (int r = 0; r < NR; r++) acc[r] = 0.f;
+#pragma unroll 4
+    for (int k = lane * 4; k < kb; k += 128) {  // kb is a multiple of 4
+      const float4 v = *reinterpret_cast<const float4*>(col + k);
+      for (int r = 0; r < NR; r++) {
+        const float4 zz = *reinterpret_cast<const float4*>(&sz[r][k]);
+        acc[r] += v.x * zz.x + v.y * zz.y + v.z * zz.z + v.w * zz.w;
+      }
+    }
+    for (int r = 0; r < NR; r++) {
+      float a = acc[r];
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      if (lane == 0) zr[c + r * ldx] -= a;
+    }
+  }
+}
+
+// backward strip: w[i] -= sum_k S(i, k) x_b[k], i < rows; a CTA takes 64
+// rows and splits the k range over four warp pairs, reduced in shared memory
+template <int NR>
+__global__ void __launch_bounds__(256) strip_n_update(int rows, int kb, const float* __restrict__ S, int64_t lds,
+                                                      const float* __restrict__ xb, float* __restrict__ w,
+                                                      int64_t ldx) {
+  __shared__ float sx[NR][NB2];
+  __shared__ float part[NR][4][64];
+  for (int k = threadIdx.x; k < kb; k += blockDim.x)
+    for (int r = 0; r < NR; r++) sx[r][k] = xb[k + r * ldx];
+  __syncthreads();
+  const int il = threadIdx.x & 63, g = threadIdx.x >> 6;
+  const int i = blockIdx.x * 64 + il;
+  const int kq = (kb + 3) / 4, k0 = g * kq, k1 = min(kb, k0 + kq);
+  float acc[NR];
+  for (int r = 0; r < NR; r++) acc[r] = 0.f;
+  if (i < rows) {
+#pragma unroll 8
+    for (int k = k0; k < k1; k++) {
+      const float v = S[i + (int64_t)k * lds];
+      for (int r = 0; r < NR; r++) acc[r] += v * sx[r][k];
+    }
+  }
+  for (int r = 0; r < NR; r++) part[r][g][il] = acc[r];
+  __syncthreads();
+  if (g == 0 && i < rows)
+    for (int r = 0; r < NR; r++)
+      w[i + r * ldx] -= (part[r][0][il] + part[r][1][il]) + (part[r][2][il] + part[r][3][il]);
+}
+
+// w_b = G_b z_b for every block, one thread per row
+template <int NR>
+__global__ void __launch_bounds__(256) blockdiag_gemv(int n, const float* __restrict__ G, const float* __restrict__ z,
+                                                      float* __restrict__ w, int64_t ldx) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int b = i / NB2, il = i % NB2, j0 = b * NB2, jb = min(NB2, n - j0);
+  const float* Gb = G + (size_t)b * NB2 * NB2;
+  float acc[NR];
+  for (int r = 0; r < NR; r++) acc[r] = 0.f;
+  for (int k = 0; k < jb; k++) {
+    const float g = Gb[il + (size_t)k * NB2];
+    for (int r = 0; r < NR; r++) acc[r] += g * z[j0 + k + r * ldx];
+  }
+  for (int r = 0; r < NR; r++) w[i + r * ldx] = acc[r];
+}
+
+}  // namespace
+
+// Builds Uh (strict upper block strips, ld ldu, in a buffer of its own) and
+// the G_b blocks from the factor U and its NB2 block inverses W2.
+int rsd_uhat_build(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const float* W2, const char* tag,
+                   rsd_uhat* out) {
+  if (ldu % 4 != 0 || ((uintptr_t)U & 15)) return rsd_fail(ctx, RSD_EARG, "uhat: unsupported layout");
+  const int nblk2 = (n + NB2 - 1) / NB2;
+  std::string nu = std::string("uhat_U_") + tag, ng = std::string("uhat_G_") + tag;
+  float* Uh = (float*)rsd_scratch(ctx, nu.c_str(), sizeof(float) * (size_t)ldu * n);
+  float* G = (float*)rsd_scratch(ctx, ng.c_str(), sizeof(float) * (size_t)nblk2 * NB2 * NB2);
+  float* WT = (float*)rsd_scratch(ctx, "uhat_WT", sizeof(float) * (size_t)nblk2 * NB2 * NB2);
+  if (!Uh || !G || !WT) return RSD_ENOMEM;
+  cudaStream_t s = ctx->stream;
+  transpose_block<<<dim3(NB2 / 32, NB2 / 32, nblk2), dim3(32, 8), 0, s>>>(NB2, W2, WT); RSD_LAUNCH_NOTE();
+  RSD_CUDA(ctx, cudaMemsetAsync(ctx->d_info + 1, 0, sizeof(int), s));
+  int* err = ctx->d_info + 1;
+  for (int b = 0; b < nblk2; b++) {
+    const int j0 = b * NB2, jb = n - j0 < NB2 ? n - j0 : NB2, rest = n - j0 - jb;
+    const float* WTb = WT + (size_t)b * NB2 * NB2;
+    RSD_TRY(rsd_tc_gemm(ctx, 3, NB2, NB2, NB2, 1.0f, WTb, NB2, WTb, NB2, G + (size_t)b * NB2 * NB2, NB2, 0, 0, 0, err));
+    if (rest > 0)
+      RSD_TRY(rsd_tc_gemm(ctx, 3, jb, rest, jb, 1.0f, WTb, NB2, U + j0 + (int64_t)(j0 + jb) * ldu, ldu,
+                          Uh + j0 + (int64_t)(j0 + jb) * ldu, ldu, 0, 0, 0, err));
+  }
+  RSD_CUDA(ctx, cudaMemcpyAsync(ctx->h_info + 1, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  RSD_CUDA(ctx, cudaStreamSynchronize(s));
+  if (ctx->h_info[1]) return rsd_fail(ctx, RSD_ETIMEOUT, "uhat: tensor-core GEMM timed out");
+  out->n = n;
+  out->Uh = Uh;
+  out->ld = ldu;
+  out->G = G;
+  return RSD_OK;
+}
+
+// X (n x nrhs, ld ldx) <- (U^T U)^-1 X with the block-scaled factor; Y is
+// n x nrhs scratch (ld ldx).
+int rsd_uhat_solve(rsd_ctx* ctx, const rsd_uhat* h, float* X, int64_t ldx, int nrhs, float* Y) {
+  if (nrhs < 1 || nrhs > 2) return rsd_fail(ctx, RSD_EARG, "uhat solve: 1 or 2 right-hand sides");
+  const int n = h->n, nblk2 = (n + NB2 - 1) / NB2;
+  cudaStream_t s = ctx->stream;
+  const int gsm = ctx->sm_count > 0 ? ctx->sm_count : 148;
+  for (int b = 0; b < nblk2; b++) {  // forward, in place on X
+    const int j0 = b * NB2, jb = n - j0 < NB2 ? n - j0 : NB2, rest = n - j0 - jb;
+    if (rest <= 0) break;
+    const float* S = h->Uh + j0 + (int64_t)(j0 + jb) * h->ld;
+    const int blocks = min(4 * gsm, (rest + 7) / 8);
+    if (nrhs == 1)
+      strip_t_update<1><<<blocks, 256, 0, s>>>(jb, rest, S, h->ld, X + j0, X + j0 + jb, ldx);
+    else
+      strip_t_update<2><<<blocks, 256, 0, s>>>(jb, rest, S, h->ld, X + j0, X + j0 + jb, ldx);
+    RSD_LAUNCH_NOTE();
+  }
+  if (nrhs == 1)
+    blockdiag_gemv<1><<<(n + 255) / 256, 256, 0, s>>>(n, h->G, X, Y, ldx);
+  else
+    blockdiag_gemv<2><<<(n + 255) / 256, 256, 0, s>>>(n, h->G, X, Y, ldx);
+  RSD_LAUNCH_NOTE();
+  for (int b = nblk2 - 1; b > 0; b--) {  // backward, in place on Y
+    const int j0 = b * NB2, jb = n - j0 < NB2 ? n - j0 : NB2;
+    const float* S = h->Uh + (int64_t)j0 * h->ld;  // rows 0..j0, columns of block b
+    if (nrhs == 1)
+      strip_n_update<1><<<(j0 + 63) / 64, 256, 0, s>>>(j0, jb, S, h->ld, Y + j0, Y, ldx);
+    else
+      strip_n_update<2><<<(j0 + 63) / 64, 256, 0, s>>>(j0, jb, S, h->ld, Y + j0, Y, ldx);
+    RSD_LAUNCH_NOTE();
+  }
+  for (int r = 0; r < nrhs; r++)
+    RSD_CUDA(ctx, cudaMemcpyAsync(X + r * ldx, Y + r * ldx, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+  RSD_CUDA(ctx, cudaGetLastError());
+  return RSD_OK;
+}
+
 int rsd_potrs_wide_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const float* W2, float* X, int64_t ldx,
                      int nrhs, float* Y) {
   const int nblk2 = (n + NB2 - 1) / NB2;

@@ -100,6 +100,13 @@ __global__ void ewald_ktable_list(rsd_lat_dev L, int count, const int* __restric
   for (int m = 0; m < RSD_NMOM_KSIN; m++) e[3 + RSD_NMOM_KCOS + m] = (T)ws[m];
 }
 
+__device__ __forceinline__ void put_trig(double2* p, double c, double sn) { *p = make_double2(c, sn); }
+__device__ __forceinline__ void put_trig(float2* p, double c, double sn) { *p = make_float2((float)c, (float)sn); }
+__device__ __forceinline__ void put_trig(float4* p, double c, double sn) {
+  const dsf dc = dsf_from(c), ds = dsf_from(sn);
+  *p = make_float4(dc.hi, dc.lo, ds.hi, ds.lo);
+}
+
 template <typename T2>
 __global__ void ewald_trig_list(int nn, rsd_lat_dev L, const int* __restrict__ hlist, const double* __restrict__ pos,
                                 T2* __restrict__ cs) {
@@ -114,10 +121,7 @@ __global__ void ewald_trig_list(int nn, rsd_lat_dev L, const int* __restrict__ h
   const double kr = k[0] * pos[3 * a] + k[1] * pos[3 * a + 1] + k[2] * pos[3 * a + 2];
   double sn, c;
   sincos(kr, &sn, &c);
-  T2 v;
-  v.x = c;
-  v.y = sn;
-  cs[(size_t)q * nn + a] = v;
+  put_trig(cs + (size_t)q * nn + a, c, sn);
 }
 
 // Scatter of the pair block (a,b), a < b, and its mirror (b,a) with
@@ -256,6 +260,61 @@ __global__ void __launch_bounds__(128) ewald_pair_k(int nn, rsd_lat_dev L, int K
   const double f = 2.0 / L.LV;  // half space counted twice
 #pragma unroll
   for (int q = 0; q < 60; q++) o[q] = ((double)v[q] + (double)w[q]) * f;
+  scale_block(o, radii[a], inv_pimu);
+  store_pair(M, ldm, nn, a, b, o, add);
+}
+
+// Reciprocal-space pair sums of the FP64 shells of the mixed form in
+// double-single: the trig table holds (cos, sin) as float pairs (float4 per
+// vector and particle), the weights are converted to float pairs as they are
+// staged in shared memory, and the epilogue runs in FP64.
+__global__ void __launch_bounds__(128) ewald_pair_k_ds(int nn, rsd_lat_dev L, int Kh, const double* __restrict__ tab,
+                                                       const float4* __restrict__ cs, const double* __restrict__ radii,
+                                                       double inv_pimu, double* __restrict__ M, int64_t ldm, int add) {
+  constexpr int KWT = 3 + RSD_NMOM_KCOS + RSD_NMOM_KSIN;
+  constexpr int NW = RSD_NMOM_KCOS + RSD_NMOM_KSIN;
+  constexpr int KC = 16;
+  __shared__ __align__(16) dsf sw[KC * NW];
+  if ((int)(blockIdx.x * blockDim.x) >= (int)(blockIdx.y * blockDim.y + blockDim.y - 1)) return;
+  int a, b;
+  const bool valid = pair_of(nn, &a, &b);
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  dsf ac[RSD_NMOM_KCOS], as[RSD_NMOM_KSIN];
+#pragma unroll
+  for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] = dsf(0);
+#pragma unroll
+  for (int m = 0; m < RSD_NMOM_KSIN; m++) as[m] = dsf(0);
+  for (int h0 = 0; h0 < Kh; h0 += KC) {
+    const int kc = min(KC, Kh - h0);
+    __syncthreads();
+    for (int e = tid; e < kc * NW; e += nthr) sw[e] = dsf_from(tab[(size_t)(h0 + e / NW) * KWT + 3 + e % NW]);
+    __syncthreads();
+    if (!valid) continue;
+    for (int hh = 0; hh < kc; hh++) {
+      const float4 ua = cs[(size_t)(h0 + hh) * nn + a], ub = cs[(size_t)(h0 + hh) * nn + b];
+      const dsf ca(ua.x, ua.y), sa(ua.z, ua.w), cb(ub.x, ub.y), sb(ub.z, ub.w);
+      const dsf c = ca * cb + sa * sb;   // cos(k.(x_a - x_b))
+      const dsf sn = sa * cb - ca * sb;  // sin(k.(x_a - x_b))
+      const dsf* e = sw + hh * NW;
+#pragma unroll
+      for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] = fma(e[m], c, ac[m]);
+#pragma unroll
+      for (int m = 0; m < RSD_NMOM_KSIN; m++) as[m] = fma(e[RSD_NMOM_KCOS + m], sn, as[m]);
+    }
+  }
+  if (!valid) return;
+  double acd[RSD_NMOM_KCOS], asd[RSD_NMOM_KSIN];
+#pragma unroll
+  for (int m = 0; m < RSD_NMOM_KCOS; m++) acd[m] = dsf_to(ac[m]);
+#pragma unroll
+  for (int m = 0; m < RSD_NMOM_KSIN; m++) asd[m] = dsf_to(as[m]);
+  double v[60], w[60];
+  rsd_kcos_epilogue<double>(acd, radii[a], radii[b], L.phix, v);
+  rsd_ksin_epilogue<double>(asd, radii[a], radii[b], L.phix, w);
+  double o[60];
+  const double f = 2.0 / L.LV;  // half space counted twice
+#pragma unroll
+  for (int q = 0; q < 60; q++) o[q] = (v[q] + w[q]) * f;
   scale_block(o, radii[a], inv_pimu);
   store_pair(M, ldm, nn, a, b, o, add);
 }
@@ -562,7 +621,7 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
       int* dh = (int*)rsd_scratch(ctx, "ewald_hlist", sizeof(int) * (size_t)Kh);
       double* t64 = (double*)rsd_scratch(ctx, "ewald_ktab64", sizeof(double) * (size_t)(K64 > 0 ? K64 : 1) * KW);
       float* t32 = (float*)rsd_scratch(ctx, "ewald_ktab32", sizeof(float) * (size_t)(K32 > 0 ? K32 : 1) * KW);
-      double2* c64 = (double2*)rsd_scratch(ctx, "ewald_trig64", sizeof(double2) * (size_t)(K64 > 0 ? K64 : 1) * nn);
+      float4* c64 = (float4*)rsd_scratch(ctx, "ewald_trig64", sizeof(float4) * (size_t)(K64 > 0 ? K64 : 1) * nn);
       float2* c32 = (float2*)rsd_scratch(ctx, "ewald_trig32", sizeof(float2) * (size_t)(K32 > 0 ? K32 : 1) * nn);
       if (!dh || !t64 || !t32 || !c64 || !c32) return RSD_ENOMEM;
       std::vector<int> all(h64);
@@ -571,13 +630,13 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
       RSD_CUDA(ctx, cudaStreamSynchronize(s));
       if (K64) {
         ewald_ktable_list<double><<<(K64 + 127) / 128, 128, 0, s>>>(L, K64, dh, t64); RSD_LAUNCH_NOTE();
-        ewald_trig_list<double2><<<dim3((nn + 127) / 128, K64), 128, 0, s>>>(nn, L, dh, d_pos, c64); RSD_LAUNCH_NOTE();
+        ewald_trig_list<float4><<<dim3((nn + 127) / 128, K64), 128, 0, s>>>(nn, L, dh, d_pos, c64); RSD_LAUNCH_NOTE();
       }
       if (K32) {
         ewald_ktable_list<float><<<(K32 + 127) / 128, 128, 0, s>>>(L, K32, dh + K64, t32); RSD_LAUNCH_NOTE();
         ewald_trig_list<float2><<<dim3((nn + 127) / 128, K32), 128, 0, s>>>(nn, L, dh + K64, d_pos, c32); RSD_LAUNCH_NOTE();
       }
-      ewald_pair_k<double, double2><<<grd, blk, 0, s>>>(nn, L, K64, t64, c64, d_radii, inv_pimu, d_M, ldm, 0); RSD_LAUNCH_NOTE();
+      ewald_pair_k_ds<<<grd, blk, 0, s>>>(nn, L, K64, t64, c64, d_radii, inv_pimu, d_M, ldm, 0); RSD_LAUNCH_NOTE();
       ewald_pair_k<float, float2><<<grd, blk, 0, s>>>(nn, L, K32, t32, c32, d_radii, inv_pimu, d_M, ldm, 1); RSD_LAUNCH_NOTE();
       ewald_pair_real_near_ds<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, d_M, ldm); RSD_LAUNCH_NOTE();
       ewald_pair_real_far<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, rmax2, d_M, ldm); RSD_LAUNCH_NOTE();

@@ -221,6 +221,11 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   }
   float* W_m = nullptr;
   RSD_TRY(rsd_wide_inverses_s(ctx, (int)n, M32, n, "m32", rsd_potrf_inverses_s(ctx, (int)n, "m32"), &W_m));
+  // block-scaled factors for one-launch-per-block refinement solves (the
+  // tensor-core GEMMs that form them need leading dimensions divisible by 4)
+  rsd_uhat uh_m, uh_r;
+  const bool use_uh = ctx->use_tc && n % 4 == 0 && P % 4 == 0;
+  if (use_uh) RSD_TRY(rsd_uhat_build(ctx, (int)n, M32, n, W_m, "m32", &uh_m));
   // A^-1 from the trailing factor block, then RPP32 = A^-1 + rfu and its factor
   copy_block_f<<<nblk(P * P), 256, 0, s>>>(P, P, M32 + Q + Q * n, n, A32, P); RSD_LAUNCH_NOTE();
   RSD_TRY(rsd_potri_upper_t<float>(ctx, (int)P, A32, P, "a32", 3));
@@ -233,6 +238,7 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   }
   float* W_r = nullptr;
   RSD_TRY(rsd_wide_inverses_s(ctx, (int)P, A32, P, "rpp32", rsd_potrf_inverses_s(ctx, (int)P, "rpp32"), &W_r));
+  if (use_uh) RSD_TRY(rsd_uhat_build(ctx, (int)P, A32, P, W_r, "rpp32", &uh_r));
   // refinement
   cudaEventRecord(ctx->ev[7], s);
   RSD_CUDA(ctx, cudaMemsetAsync(f, 0, sizeof(double) * nr * n, s));
@@ -262,15 +268,24 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
     if (worst <= tol || it >= maxit) break;
     // y = M^-1 r1
     to32_perm<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, r1, n, 0, t32); RSD_LAUNCH_NOTE();
-    RSD_TRY(rsd_potrs_wide_s(ctx, (int)n, M32, n, W_m, t32, n, nr, ywork));
+    if (use_uh)
+      RSD_TRY(rsd_uhat_solve(ctx, &uh_m, t32, n, nr, ywork));
+    else
+      RSD_TRY(rsd_potrs_wide_s(ctx, (int)n, M32, n, W_m, t32, n, nr, ywork));
     from32_perm<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, t32, y, 0); RSD_LAUNCH_NOTE();
     // dU = RPP^-1 (r2 - y_P)
     rhs_u<<<nblk(P * nr), 256, 0, s>>>(P, n, nr, r2, y, u32); RSD_LAUNCH_NOTE();
-    RSD_TRY(rsd_potrs_wide_s(ctx, (int)P, A32, P, W_r, u32, P, nr, ywork));
+    if (use_uh)
+      RSD_TRY(rsd_uhat_solve(ctx, &uh_r, u32, P, nr, ywork));
+    else
+      RSD_TRY(rsd_potrs_wide_s(ctx, (int)P, A32, P, W_r, u32, P, nr, ywork));
     // df = y + M^-1 [dU; 0]
     du_vec<<<nblk(n * nr), 256, 0, s>>>(P, n, nr, u32, dv); RSD_LAUNCH_NOTE();
     to32_perm<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, dv, n, 1, t32); RSD_LAUNCH_NOTE();
-    RSD_TRY(rsd_potrs_wide_s(ctx, (int)n, M32, n, W_m, t32, n, nr, ywork));
+    if (use_uh)
+      RSD_TRY(rsd_uhat_solve(ctx, &uh_m, t32, n, nr, ywork));
+    else
+      RSD_TRY(rsd_potrs_wide_s(ctx, (int)n, M32, n, W_m, t32, n, nr, ywork));
     from32_perm<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, t32, y, 1); RSD_LAUNCH_NOTE();
     update_fu<<<nblk(n * nr), 256, 0, s>>>(P, n, nr, y, u32, f, U); RSD_LAUNCH_NOTE();
   }

@@ -159,3 +159,15 @@ int rsd_tc_gemm(rsd_ctx* ctx, int prec, int m, int n, int K, float alpha, const 
 int rsd_tc_syrk_ok(const float* panel, int64_t lda, const float* C, int64_t ldc, int kb);
 int rsd_tc_syrk(rsd_ctx* ctx, int prec, const float* panel, int64_t lda, int kb, int rest, float* C, int64_t ldc,
                 int* d_err);
+
+// Block-scaled FP32 factor for the refinement solves (dense.cu): U = D Uh with
+// D = blockdiag(U_bb) over 512-blocks; Uh's strict upper block strips and the
+// blocks G_b = (U_bb^T U_bb)^-1.
+struct rsd_uhat {
+  int n = 0;
+  const float* Uh = nullptr;
+  int64_t ld = 0;
+  const float* G = nullptr;
+};
+int rsd_uhat_build(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const float* W2, const char* tag, rsd_uhat* out);
+int rsd_uhat_solve(rsd_ctx* ctx, const rsd_uhat* h, float* X, int64_t ldx, int nrhs, float* Y);
