@@ -430,6 +430,56 @@ __global__ void __launch_bounds__(256) potf2_upper(T* __restrict__ A, int64_t ld
 // past jb zero).  info as DPOTRF.
 constexpr int PLD = NB + 1;
 constexpr int RTLD = 33;
+// Loads of an FP32 tile into shared memory with many loads in flight: a
+// loop of one load per iteration serialises the DRAM round trips of a
+// single CTA (~0.7 us each), so each thread first issues a batch of 16
+// (16-byte vectors where the column starts are 16-byte aligned), then
+// writes them.  Tile: rows x cols of a column-major matrix (ld lda) into
+// S(i, j) = S[i + j * lds]; with upper = 1 only i <= j is kept (the rest 0).
+// Entries outside rows x cols up to NB x cmax are written as 0.
+__device__ __forceinline__ void load_tile_f32(const float* __restrict__ A, int64_t lda, int rows, int cols, int cmax,
+                                              float* __restrict__ S, int lds, int upper) {
+  const int t = threadIdx.x, nt = blockDim.x;
+  const bool vec = ((lda & 3) == 0) && (((uintptr_t)A & 15) == 0) && ((rows & 3) == 0);
+  if (vec) {
+    const int per_col = NB / 4, total = per_col * cmax;
+    for (int f0 = 0; f0 < total; f0 += 16 * nt) {
+      float4 v[16];
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        const int f = f0 + t + q * nt, j = f / per_col, i = (f % per_col) * 4;
+        v[q] = (f < total && j < cols && i < rows) ? *reinterpret_cast<const float4*>(A + i + (int64_t)j * lda)
+                                                   : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        const int f = f0 + t + q * nt, j = f / per_col, i = (f % per_col) * 4;
+        if (f < total) {
+          S[i + j * lds] = (!upper || i <= j) ? v[q].x : 0.f;
+          S[i + 1 + j * lds] = (!upper || i + 1 <= j) ? v[q].y : 0.f;
+          S[i + 2 + j * lds] = (!upper || i + 2 <= j) ? v[q].z : 0.f;
+          S[i + 3 + j * lds] = (!upper || i + 3 <= j) ? v[q].w : 0.f;
+        }
+      }
+    }
+  } else {
+    const int total = NB * cmax;
+    for (int e0 = 0; e0 < total; e0 += 16 * nt) {
+      float v[16];
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        const int e = e0 + t + q * nt, i = e % NB, j = e / NB;
+        v[q] = (e < total && i < rows && j < cols && (!upper || i <= j)) ? A[i + (int64_t)j * lda] : 0.f;
+      }
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        const int e = e0 + t + q * nt;
+        if (e < total) S[(e % NB) + (e / NB) * lds] = v[q];
+      }
+    }
+  }
+}
+
 constexpr int SMEM_POTF2_INV = (2 * NB * PLD + NB * RTLD + 32 * 33 + 3 * 32 * 33) * (int)sizeof(float);
 __global__ void __launch_bounds__(256) potf2_inv_f32(float* __restrict__ A, int64_t lda, int jb,
                                                      int* __restrict__ info, int j0, float* __restrict__ Wout) {
@@ -441,11 +491,8 @@ __global__ void __launch_bounds__(256) potf2_inv_f32(float* __restrict__ A, int6
   float* Tt = Dinv + 32 * 33;     // 3 temporaries of 32 x 32: (r, c) at r * 33 + c
   __shared__ int failed;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  for (int e = t; e < NB * NB; e += 256) {
-    const int i = e % NB, j = e / NB;
-    S[i + j * PLD] = (i < jb && j < jb && i <= j) ? A[i + (int64_t)j * lda] : 0.f;
-    Wm[i + j * PLD] = 0.f;
-  }
+  load_tile_f32(A, lda, jb, jb, NB, S, PLD, 1);
+  for (int e = t; e < NB * NB; e += 256) Wm[(e % NB) + (e / NB) * PLD] = 0.f;
   if (t == 0) failed = 0;
   __syncthreads();
   const int nsub = (jb + 31) / 32;
@@ -573,6 +620,163 @@ __global__ void __launch_bounds__(256) potf2_inv_f32(float* __restrict__ A, int6
     const int i = e % NB, j = e / NB;
     if (i < jb && j < jb && i <= j) A[i + (int64_t)j * lda] = S[i + j * PLD];
     Wout[e] = (i < jb && j < jb && i <= j) ? Wm[i + j * PLD] : 0.f;
+  }
+}
+
+// FP32 diagonal block (jb <= 128), factor only: as potf2_inv_f32 without
+// the inverse (the row panel of each 32-wide sub-block by substitution, one
+// thread per column), so the serial single-warp work on the critical path
+// of the blocked factorisation is the 32 x 32 factors alone.
+constexpr int SMEM_POTF2_F32 = (NB * PLD + NB * RTLD) * (int)sizeof(float);
+__global__ void __launch_bounds__(256) potf2_f32(float* __restrict__ A, int64_t lda, int jb, int* __restrict__ info,
+                                                 int j0) {
+  extern __shared__ unsigned char smraw[];
+  float* S = (float*)smraw;   // U, NB x NB, ld PLD
+  float* RT = S + NB * PLD;   // row panel transposed: trailing column c, row p at RT[c * RTLD + p]
+  __shared__ int failed;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  load_tile_f32(A, lda, jb, jb, NB, S, PLD, 1);
+  if (t == 0) failed = 0;
+  __syncthreads();
+  const int nsub = (jb + 31) / 32;
+  for (int kb = 0; kb < nsub; kb++) {
+    const int k0 = kb * 32, kw = min(32, jb - k0);
+    if (warp == 0) {
+      float r[32];
+#pragma unroll
+      for (int i = 0; i < 32; i++) r[i] = S[(k0 + i) + (k0 + lane) * PLD];
+      int bad = 0;
+#pragma unroll
+      for (int k = 0; k < 32; k++) {
+        if (k < kw && !bad) {
+          const float piv = __shfl_sync(0xffffffffu, r[k], k);
+          if (!(piv > 0.f) || !isfinite(piv)) {
+            bad = k + 1;
+          } else {
+            const float d = sqrtf(piv);
+            if (lane > k) r[k] = r[k] / d;
+            else if (lane == k) r[k] = d;
+#pragma unroll
+            for (int i = k + 1; i < 32; i++) {
+              const float uki = __shfl_sync(0xffffffffu, r[k], i);
+              if (lane >= i) r[i] -= uki * r[k];
+            }
+          }
+        }
+      }
+      if (bad) {
+        if (lane == 0) {
+          failed = 1;
+          atomicCAS(info, 0, j0 + k0 + bad);
+        }
+      } else if (lane < kw) {
+#pragma unroll
+        for (int i = 0; i < 32; i++)
+          if (i <= lane) S[(k0 + i) + (k0 + lane) * PLD] = r[i];
+      }
+    }
+    __syncthreads();
+    if (failed) return;
+    const int m0 = k0 + kw, mw = jb - m0;
+    if (t < mw) {  // row panel: U_D^T X = R by substitution, one column per thread
+      const int c = m0 + t;
+      float x[32];
+#pragma unroll
+      for (int i = 0; i < 32; i++) {
+        float v = 0.f;
+        if (i < kw) {
+          v = S[(k0 + i) + c * PLD];
+#pragma unroll
+          for (int p = 0; p < i; p++) v -= S[(k0 + p) + (k0 + i) * PLD] * x[p];
+          v = v / S[(k0 + i) + (k0 + i) * PLD];
+        }
+        x[i] = v;
+      }
+#pragma unroll
+      for (int i = 0; i < 32; i++) {
+        if (i < kw) S[(k0 + i) + c * PLD] = x[i];
+        RT[t * RTLD + i] = x[i];
+      }
+    }
+    __syncthreads();
+    const int nrb = (mw + 31) / 32, ncg = (mw + 7) / 8;
+    for (int task = warp; task < nrb * ncg; task += 8) {
+      const int rb = task % nrb, cg = task / nrb;
+      const int i = rb * 32 + lane, c0 = cg * 8;
+      if (rb * 32 > c0 + 7) continue;
+      float acc[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) acc[q] = 0.f;
+      const int ir = min(i, NB - 1);
+#pragma unroll 4
+      for (int p = 0; p < 32; p++) {
+        const float a = RT[ir * RTLD + p];
+#pragma unroll
+        for (int q = 0; q < 8; q++) acc[q] += a * RT[min(c0 + q, NB - 1) * RTLD + p];
+      }
+      if (i < mw) {
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+          if (c0 + q < mw && i <= c0 + q) S[(m0 + i) + (m0 + c0 + q) * PLD] -= acc[q];
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = t; e < NB * NB; e += 256) {
+    const int i = e % NB, j = e / NB;
+    if (i < jb && j < jb && i <= j) A[i + (int64_t)j * lda] = S[i + j * PLD];
+  }
+}
+
+// FP32 panel solve U_jj^T X = B in place (B = A(j0:j0+jb, j0+jb:n)), 256
+// columns per CTA: the tile is staged in shared memory with batched loads,
+// each thread solves its column in 32-row blocks (substitution within a
+// block, then the block's update of the rows below, whose accumulations are
+// independent), and the tile is written back coalesced.
+constexpr int TRSM_F32_COLS = 256;
+constexpr int SMEM_TRSM_F32 = (NB * PLD + PLD * TRSM_F32_COLS) * (int)sizeof(float);
+__global__ void __launch_bounds__(TRSM_F32_COLS) trsm_panel_f32(const float* __restrict__ Ujj, int64_t lda, int jb,
+                                                                int rest, float* __restrict__ B) {
+  extern __shared__ unsigned char smraw[];
+  float* U = (float*)smraw;  // jb x jb upper, ld PLD
+  float* Xt = U + NB * PLD;  // column c, row i at Xt[i + c * PLD] (odd stride: one bank per thread)
+  const int t = threadIdx.x, c0 = blockIdx.x * TRSM_F32_COLS;
+  const int ncol = min(TRSM_F32_COLS, rest - c0);
+  load_tile_f32(Ujj, lda, jb, jb, NB, U, PLD, 1);
+  load_tile_f32(B + (int64_t)c0 * lda, lda, jb, ncol, TRSM_F32_COLS, Xt, PLD, 0);
+  __syncthreads();
+  if (t < ncol) {
+    float* x = Xt + t * PLD;  // thread t owns column t
+    for (int q0 = 0; q0 < jb; q0 += 32) {
+      const int qw = min(32, jb - q0);
+      float v[32];
+#pragma unroll
+      for (int i = 0; i < 32; i++) {
+        float a = 0.f;
+        if (i < qw) {
+          a = x[q0 + i];
+#pragma unroll
+          for (int p = 0; p < i; p++) a -= U[(q0 + p) + (q0 + i) * PLD] * v[p];
+          a = a / U[(q0 + i) + (q0 + i) * PLD];
+        }
+        v[i] = a;
+      }
+#pragma unroll
+      for (int i = 0; i < 32; i++)
+        if (i < qw) x[q0 + i] = v[i];
+#pragma unroll 4
+      for (int i = q0 + qw; i < jb; i++) {
+        float a = x[i];
+#pragma unroll
+        for (int p = 0; p < 32; p++) a -= U[(q0 + p) + i * PLD] * v[p];  // U is zero past qw
+        x[i] = a;
+      }
+    }
+  }
+  __syncthreads();
+  for (int e = t; e < jb * ncol; e += TRSM_F32_COLS) {
+    const int i = e % jb, c = e / jb;
+    B[i + (int64_t)(c0 + c) * lda] = Xt[i + c * PLD];
   }
 }
 
@@ -790,6 +994,8 @@ int ensure_attrs(rsd_ctx* ctx) {
   RSD_CUDA(ctx, cudaFuncSetAttribute(trsv_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_trsv<T>()));
   RSD_CUDA(ctx, cudaFuncSetAttribute(trtri_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_potf2<T>(NB)));
   RSD_CUDA(ctx, cudaFuncSetAttribute(potf2_inv_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_POTF2_INV));
+  RSD_CUDA(ctx, cudaFuncSetAttribute(potf2_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_POTF2_F32));
+  RSD_CUDA(ctx, cudaFuncSetAttribute(trsm_panel_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TRSM_F32));
   done = true;
   return RSD_OK;
 }
@@ -880,6 +1086,52 @@ int trailing_update(rsd_ctx* ctx, int tc, const T* P, int64_t ldp, int kb, int m
   return RSD_OK;
 }
 
+// Two-level FP32 Cholesky on tensor cores: outer panels of NBO = 512 rows
+// are factored in NB = 128 steps (diagonal block, row panel by
+// substitution, and an update of the outer panel's remaining rows only),
+// then the trailing matrix takes one K = 512 update per outer panel, so it
+// is read and written a quarter as often as with 128-wide steps.  One outer
+// step of look-ahead: the next outer panel is factored on the side stream
+// once the first 512 rows of the trailing update have landed.
+constexpr int NBO = 512;
+int potrf_two_level_f32(rsd_ctx* ctx, int n, float* d_A, int64_t lda, int tc) {
+  cudaStream_t s = ctx->stream, s2 = ctx->side;
+  RSD_CUDA(ctx, cudaEventRecord(ctx->ev_next, s));
+  for (int J0 = 0; J0 < n; J0 += NBO) {
+    const int JB = n - J0 < NBO ? n - J0 : NBO;
+    RSD_CUDA(ctx, cudaStreamWaitEvent(s2, ctx->ev_next, 0));
+    for (int j0 = J0; j0 < J0 + JB; j0 += NB) {
+      const int jb = J0 + JB - j0 < NB ? J0 + JB - j0 : NB;
+      float* Ajj = d_A + j0 + (int64_t)j0 * lda;
+      const int rest = n - j0 - jb;
+      float* Apan = d_A + j0 + (int64_t)(j0 + jb) * lda;
+      potf2_f32<<<1, 256, SMEM_POTF2_F32, s2>>>(Ajj, lda, jb, ctx->d_info, j0); RSD_LAUNCH_NOTE();
+      if (rest <= 0) continue;
+      trsm_panel_f32<<<(rest + TRSM_F32_COLS - 1) / TRSM_F32_COLS, TRSM_F32_COLS, SMEM_TRSM_F32, s2>>>(
+          Ajj, lda, jb, rest, Apan); RSD_LAUNCH_NOTE();
+      const int m_in = J0 + JB - (j0 + jb);  // rows of this outer panel still to update
+      if (m_in > 0)
+        RSD_TRY(rsd_tc_gemm(ctx, tc, m_in, rest, jb, -1.0f, Apan, lda, Apan, lda, Apan + jb, lda, 1, 1, 0,
+                            ctx->d_info + 1, s2));
+    }
+    RSD_CUDA(ctx, cudaEventRecord(ctx->ev_panel, s2));
+    RSD_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_panel, 0));
+    const int restO = n - J0 - JB;
+    if (restO > 0) {
+      const float* PO = d_A + J0 + (int64_t)(J0 + JB) * lda;
+      float* C = d_A + (J0 + JB) + (int64_t)(J0 + JB) * lda;
+      const int m1 = restO < NBO ? restO : NBO;
+      RSD_TRY(rsd_tc_gemm(ctx, tc, m1, restO, JB, -1.0f, PO, lda, PO, lda, C, lda, 1, 1, 0, ctx->d_info + 1, s));
+      RSD_CUDA(ctx, cudaEventRecord(ctx->ev_next, s));
+      if (restO > NBO)
+        RSD_TRY(rsd_tc_gemm(ctx, tc, restO - NBO, restO - NBO, JB, -1.0f, PO + (int64_t)NBO * lda, lda,
+                            PO + (int64_t)NBO * lda, lda, C + NBO + (int64_t)NBO * lda, lda, 1, 1, 0,
+                            ctx->d_info + 1, s));
+    }
+  }
+  return RSD_OK;
+}
+
 // Blocked right-looking upper Cholesky with one step of look-ahead: the
 // diagonal block and row panel of step j+1 are factored on a second,
 // higher-priority stream as soon as the first tile row of step j's trailing
@@ -899,6 +1151,14 @@ int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const
     if (!T1) return RSD_ENOMEM;
   }
   RSD_CUDA(ctx, cudaMemsetAsync(ctx->d_info, 0, 2 * sizeof(int), s));
+  bool two_level = false;
+  if constexpr (F32) two_level = tc && ctx->use_tc && rsd_tc_syrk_ok(d_A, lda, d_A, lda, NB);
+  if constexpr (F32) {
+    if (two_level) {
+      RSD_TRY(potrf_two_level_f32(ctx, n, d_A, lda, tc));
+      goto done;
+    }
+  }
   RSD_CUDA(ctx, cudaEventRecord(ctx->ev_next, s));
   for (int j0 = 0, b = 0; j0 < n; j0 += NB, b++) {
     const int jb = n - j0 < NB ? n - j0 : NB;
@@ -935,8 +1195,10 @@ int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const
                                    A22 + NB + (int64_t)NB * lda, lda, 1));
     }
   }
-  // diagonal-block inverses for the solves (the FP32 path made them above)
-  if (!F32) {
+done:
+  // diagonal-block inverses for the solves; the single-level FP32 path made
+  // them with its diagonal blocks, the others take them here
+  if (!F32 || two_level) {
     const int nblk = (n + NB - 1) / NB;
     trtri_diag<T><<<nblk, 256, smem_potf2<T>(NB), s>>>(n, d_A, lda, W); RSD_LAUNCH_NOTE();
   }

@@ -370,8 +370,10 @@ int rsd_tc_gemm_ok(const float* A, int64_t lda, const float* B, int64_t ldb, con
 // ld ldb) column-major.  tri: only tiles on and above the diagonal.
 // klo_col: the K range of the tile at column col0 is [col0, K).  prec: 1
 // (TF32) or 3 (3xTF32).  d_err receives a nonzero code if a wait timed out.
+// stream: 0 for the context's stream.
 int rsd_tc_gemm(rsd_ctx* ctx, int prec, int m, int n, int K, float alpha, const float* A, int64_t lda,
-                const float* B, int64_t ldb, float* C, int64_t ldc, int reduce, int tri, int klo_col, int* d_err) {
+                const float* B, int64_t ldb, float* C, int64_t ldc, int reduce, int tri, int klo_col, int* d_err,
+                cudaStream_t stream) {
   if (m < 1 || n < 1 || K < 1 || (prec != 1 && prec != 3) || !rsd_tc_gemm_ok(A, lda, B, ldb, C, ldc))
     return rsd_fail(ctx, RSD_EARG, "tc_gemm: unsupported arguments (m=%d n=%d K=%d prec=%d)", m, n, K, prec);
   RSD_TRY(tc_init(ctx));
@@ -381,10 +383,11 @@ int rsd_tc_gemm(rsd_ctx* ctx, int prec, int m, int n, int K, float alpha, const 
   RSD_TRY(encode_2d(ctx, &tmC, C, m, n, ldc, TC_TILE, TC_TILE, CU_TENSOR_MAP_SWIZZLE_NONE));
   TcArgs a{K, tri, klo_col, reduce, alpha, d_err};
   const dim3 grid((m + TC_TILE - 1) / TC_TILE, (n + TC_TILE - 1) / TC_TILE);
+  cudaStream_t st = stream ? stream : ctx->stream;
   if (prec == 1) {
-    tc_gemm_kernel<1><<<grid, TC_THREADS, TcCfg<1>::SMEM, ctx->stream>>>(tmA, tmB, tmC, a);
+    tc_gemm_kernel<1><<<grid, TC_THREADS, TcCfg<1>::SMEM, st>>>(tmA, tmB, tmC, a);
   } else {
-    tc_gemm_kernel<3><<<grid, TC_THREADS, TcCfg<3>::SMEM, ctx->stream>>>(tmA, tmB, tmC, a);
+    tc_gemm_kernel<3><<<grid, TC_THREADS, TcCfg<3>::SMEM, st>>>(tmA, tmB, tmC, a);
   }
   RSD_LAUNCH_NOTE();
   RSD_CUDA(ctx, cudaGetLastError());
