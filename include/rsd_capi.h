@@ -80,11 +80,9 @@ long long rsd_launch_count(void);
 int rsd_ctx_set_tensor_cores(rsd_ctx* ctx, int mode);
 /* Precision split of the mixed-precision Ewald assembly: real-space images
  * with lammda*r < lam_r_cut (at most 6) and reciprocal vectors with
- * max|n_i| <= kshell are summed in double-single / FP64 (~1e-14), the rest
- * in FP32.  Defaults 4.0 and 1: a step's
- * velocities then agree with the FP64 form to ~3e-12 and its stresslets to
- * ~6e-11 relative (3.5 gives ~5e-11 and ~1e-9 at 0.85x the assembly time,
- * 4.5 ~1e-13 and ~2e-12 at 1.2x). */
+ * k^2/(4 lammda^2) <= 3 pi kshell^2 (on a cubic cell at the reference's
+ * lammda: max|n_i| <= kshell) are summed in double-single (~1e-14), the
+ * rest in FP32.  Defaults 4.0 and 1. */
 int rsd_ctx_set_mixed_split(rsd_ctx* ctx, double lam_r_cut, int32_t kshell);
 /* Truncation of the mixed-precision Ewald sums inside the reference's image
  * cubes: real-space images with lammda*r >= lam_r_max and reciprocal vectors
@@ -93,6 +91,13 @@ int rsd_ctx_set_mixed_split(rsd_ctx* ctx, double lam_r_cut, int32_t kshell);
  * entry (the reference's cubes reach lammda*r ~ 10 and k^2/(4 lammda^2) ~
  * 85 at zero strain).  The FP64 form always sums the whole cubes. */
 int rsd_ctx_set_mixed_truncation(rsd_ctx* ctx, double lam_r_max, double k2_over_4lam2_max);
+/* Ewald splitting parameter of the mixed-precision assembly relative to the
+ * reference's lammda = sqrt(pi)/LV^(1/3).  The Ewald sum does not depend on
+ * it; a larger value moves work from the real-space images to the cheaper
+ * reciprocal vectors, and the image cubes are widened to hold the
+ * truncation spheres.  1 keeps the reference's lammda, NR and NI.  The FP64
+ * form always uses the reference's values. */
+int rsd_ctx_set_mixed_lambda_scale(rsd_ctx* ctx, double scale);
 
 /* ---------------------------------------------------------------- lattice */
 /* SET_LATTICE_SKEW (src/csd_post.f90:105-136) with MAT_INV3

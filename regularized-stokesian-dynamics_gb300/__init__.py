@@ -95,6 +95,7 @@ _sig("rsd_stepper_stokesian_dev", _i, [_vp, _vp, ctypes.POINTER(StepParams), _vp
 _sig("rsd_ctx_set_tensor_cores", _i, [_vp, _i])
 _sig("rsd_ctx_set_mixed_split", _i, [_vp, _d, _i32])
 _sig("rsd_ctx_set_mixed_truncation", _i, [_vp, _d, _d])
+_sig("rsd_ctx_set_mixed_lambda_scale", _i, [_vp, _d])
 _sig("rsd_syrk_f32_dev", _i, [_vp, _i32, _i32, _vp, _i64, _vp, _i64, _i32])
 _sig("rsd_potrf_f32_dev", _i, [_vp, _i32, _vp, _i64, _i32, _ip])
 _sig("rsd_potri_f32_dev", _i, [_vp, _i32, _vp, _i64, _i32])
@@ -154,6 +155,11 @@ class Context:
     def set_mixed_truncation(self, lam_r_max=6.0, k2_over_4lam2_max=10.0 * np.pi):
         """Truncation of the mixed-precision Ewald sums."""
         self.check(_lib.rsd_ctx_set_mixed_truncation(self.h, float(lam_r_max), float(k2_over_4lam2_max)))
+
+    def set_mixed_lambda_scale(self, scale=1.0):
+        """Ewald splitting parameter of the mixed assembly relative to the
+        reference's."""
+        self.check(_lib.rsd_ctx_set_mixed_lambda_scale(self.h, float(scale)))
 
     def set_tensor_cores(self, mode=1):
         """FP32 factorisations of the mixed form: 1 (or True, the default)

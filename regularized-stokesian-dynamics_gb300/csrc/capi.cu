@@ -144,6 +144,13 @@ extern "C" int rsd_ctx_set_mixed_truncation(rsd_ctx* c, double lam_r_max, double
   return RSD_OK;
 }
 
+extern "C" int rsd_ctx_set_mixed_lambda_scale(rsd_ctx* c, double scale) {
+  if (!c) return RSD_EARG;
+  if (!(scale >= 0.5 && scale <= 4.0)) return rsd_fail(c, RSD_EARG, "mixed lambda scale must be in [0.5, 4]");
+  c->mixed_lambda_scale = scale;
+  return RSD_OK;
+}
+
 extern "C" int rsd_ctx_set_tensor_cores(rsd_ctx* c, int mode) {
   if (!c) return RSD_EARG;
   if (mode != 0 && mode != 1 && mode != 3) return rsd_fail(c, RSD_EARG, "tensor-core mode must be 0, 1 or 3");

@@ -215,11 +215,13 @@ __global__ void __launch_bounds__(128) ewald_pair_k(int nn, rsd_lat_dev L, int K
   constexpr int VW = Vec2<T>::W;
   static_assert(NW % VW == 0, "weights per vector");
   __shared__ __align__(16) T sw[KC * NW];
+  __shared__ T2 sca[KC][32], scb[KC][4];  // trig values of the CTA's 32 + 4 particles (block 32 x 4)
   // blocks entirely on or below the diagonal (a >= b everywhere) have no work
   if ((int)(blockIdx.x * blockDim.x) >= (int)(blockIdx.y * blockDim.y + blockDim.y - 1)) return;
   int a, b;
   const bool valid = pair_of(nn, &a, &b);
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  const int a0 = blockIdx.x * blockDim.x, b0 = blockIdx.y * blockDim.y;
   T ac[RSD_NMOM_KCOS], as[RSD_NMOM_KSIN];
 #pragma unroll
   for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] = T(0);
@@ -229,10 +231,20 @@ __global__ void __launch_bounds__(128) ewald_pair_k(int nn, rsd_lat_dev L, int K
     const int kc = min(KC, Kh - h0);
     __syncthreads();
     for (int e = tid; e < kc * NW; e += nthr) sw[e] = tab[(size_t)(h0 + e / NW) * KWT + 3 + e % NW];
+    for (int e = tid; e < kc * 36; e += nthr) {
+      const int hh = e / 36, q = e % 36, part = q < 32 ? a0 + q : b0 + q - 32;
+      if (part < nn) {
+        const T2 v = cs[(size_t)(h0 + hh) * nn + part];
+        if (q < 32)
+          sca[hh][q] = v;
+        else
+          scb[hh][q - 32] = v;
+      }
+    }
     __syncthreads();
     if (!valid) continue;
     for (int hh = 0; hh < kc; hh++) {
-      const T2 ua = cs[(size_t)(h0 + hh) * nn + a], ub = cs[(size_t)(h0 + hh) * nn + b];
+      const T2 ua = sca[hh][threadIdx.x], ub = scb[hh][threadIdx.y];
       const T c = ua.x * ub.x + ua.y * ub.y;  // cos(k.(x_a - x_b))
       const T sn = ua.y * ub.x - ua.x * ub.y;  // sin(k.(x_a - x_b))
       const V* e = reinterpret_cast<const V*>(sw + hh * NW);
@@ -275,10 +287,12 @@ __global__ void __launch_bounds__(128) ewald_pair_k_ds(int nn, rsd_lat_dev L, in
   constexpr int NW = RSD_NMOM_KCOS + RSD_NMOM_KSIN;
   constexpr int KC = 16;
   __shared__ __align__(16) dsf sw[KC * NW];
+  __shared__ float4 sca[KC][32], scb[KC][4];  // trig values of the CTA's 32 + 4 particles (block 32 x 4)
   if ((int)(blockIdx.x * blockDim.x) >= (int)(blockIdx.y * blockDim.y + blockDim.y - 1)) return;
   int a, b;
   const bool valid = pair_of(nn, &a, &b);
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  const int a0 = blockIdx.x * blockDim.x, b0 = blockIdx.y * blockDim.y;
   dsf ac[RSD_NMOM_KCOS], as[RSD_NMOM_KSIN];
 #pragma unroll
   for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] = dsf(0);
@@ -288,10 +302,20 @@ __global__ void __launch_bounds__(128) ewald_pair_k_ds(int nn, rsd_lat_dev L, in
     const int kc = min(KC, Kh - h0);
     __syncthreads();
     for (int e = tid; e < kc * NW; e += nthr) sw[e] = dsf_from(tab[(size_t)(h0 + e / NW) * KWT + 3 + e % NW]);
+    for (int e = tid; e < kc * 36; e += nthr) {
+      const int hh = e / 36, q = e % 36, part = q < 32 ? a0 + q : b0 + q - 32;
+      if (part < nn) {
+        const float4 v = cs[(size_t)(h0 + hh) * nn + part];
+        if (q < 32)
+          sca[hh][q] = v;
+        else
+          scb[hh][q - 32] = v;
+      }
+    }
     __syncthreads();
     if (!valid) continue;
     for (int hh = 0; hh < kc; hh++) {
-      const float4 ua = cs[(size_t)(h0 + hh) * nn + a], ub = cs[(size_t)(h0 + hh) * nn + b];
+      const float4 ua = sca[hh][threadIdx.x], ub = scb[hh][threadIdx.y];
       const dsf ca(ua.x, ua.y), sa(ua.z, ua.w), cb(ub.x, ub.y), sb(ub.z, ub.w);
       const dsf c = ca * cb + sa * sb;   // cos(k.(x_a - x_b))
       const dsf sn = sa * cb - ca * sb;  // sin(k.(x_a - x_b))
@@ -570,10 +594,42 @@ int rsd_count_overlaps(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
   return RSD_OK;
 }
 
+// The Ewald sum does not depend on its splitting parameter lambda (checked
+// with the oracle: moving lambda by 1.25-2x changes pair blocks by ~3e-15
+// when the image cubes hold the sums).  The mixed form moves it by the
+// context's mixed_lambda_scale, which trades double-single real-space
+// images for cheaper reciprocal vectors, and sizes the cubes to hold its
+// truncation spheres: lambda |x| < mixed_rmax, k^2 / (4 lambda^2) <
+// mixed_kexp.  With fractional coordinates of the minimum image within
+// [-1/2, 1/2], |n_i| <= r_max |b_i| + 1/2 in real space and |n_i| <= k_max
+// |a_i| / (2 pi) in reciprocal space (a_i the lattice vectors, b_i their
+// reciprocal vectors).  Scale 1 keeps the reference's lambda and cubes.
+static rsd_lat_dev mixed_lattice(const rsd_ctx* ctx, rsd_lat_dev L) {
+  const double f = ctx->mixed_lambda_scale;
+  if (f == 1.0) return L;
+  L.lam *= f;
+  double amax = 0.0, bmax = 0.0;
+  for (int i = 0; i < 3; i++) {
+    double a2 = 0.0, b2 = 0.0;
+    for (int j = 0; j < 3; j++) {
+      a2 += L.LR[j + 3 * i] * L.LR[j + 3 * i];  // column i of LR
+      b2 += L.LI[i + 3 * j] * L.LI[i + 3 * j];  // row i of LI
+    }
+    amax = fmax(amax, sqrt(a2));
+    bmax = fmax(bmax, sqrt(b2));
+  }
+  const double rmax = ctx->mixed_rmax / L.lam, kmax = 2.0 * L.lam * sqrt(ctx->mixed_kexp);
+  L.NR = max(L.NR, (int)ceil(rmax * bmax + 0.5));
+  L.NI = max(L.NI, (int)ceil(kmax * amax / (2.0 * RSD_PI)));
+  return L;
+}
+
 int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
                        double mu_f, int precision, double* d_M, int64_t ldm) {
   if (nn < 1 || ldm < 11LL * nn) return rsd_fail(ctx, RSD_EARG, "bad size nn=%d ldm=%lld", nn, (long long)ldm);
   rsd_lat_dev L = rsd_lat_pack(lat);
+  if (precision == RSD_PREC_MIXED) L = mixed_lattice(ctx, L);
+  if (L.NR > 40 || L.NI > 40) return rsd_fail(ctx, RSD_EARG, "image cubes too large (NR=%d NI=%d)", L.NR, L.NI);
   const int w = 2 * L.NI + 1;
   const int Kh = (w * w * w - 1) / 2;
   double* tab = (double*)rsd_scratch(ctx, "ewald_ktab", sizeof(double) * (size_t)Kh * KW);
@@ -602,6 +658,10 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
       const double rc = ctx->mixed_rcut / L.lam, rc2 = rc * rc;
       const double rm = ctx->mixed_rmax / L.lam, rmax2 = rm * rm;
       const int ks = ctx->mixed_kshell;
+      // double-single reciprocal vectors: k^2 / (4 lambda^2) <= 3 pi ks^2
+      // (at the reference's lambda on a cubic cell, ks = 1 is the shell
+      // max|n_i| <= 1); FP32 for the others below the truncation
+      const double k2ds = 4.0 * L.lam * L.lam * 3.0 * RSD_PI * ks * ks;
       const double k2max = 4.0 * L.lam * L.lam * ctx->mixed_kexp;
       std::vector<int> h64, h32;
       for (int h = 0; h < Kh; h++) {
@@ -612,7 +672,7 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
           const double kj = 2.0 * RSD_PI * (nx * L.LI[3 * j] + ny * L.LI[1 + 3 * j] + nz * L.LI[2 + 3 * j]);
           k2 += kj * kj;
         }
-        if (abs(nx) <= ks && abs(ny) <= ks && abs(nz) <= ks)
+        if (k2 <= k2ds * (1.0 + 1e-12))
           h64.push_back(h);
         else if (k2 < k2max)
           h32.push_back(h);

@@ -36,6 +36,7 @@ struct rsd_ctx {
   int mixed_kshell = 1;     // mixed assembly: FP64 reciprocal shells max|n_i| <= this
   double mixed_rmax = 6.0;  // mixed assembly: real images with lambda r beyond this dropped
   double mixed_kexp = 10.0 * 3.141592653589793;  // and reciprocal vectors with k^2/(4 lambda^2) beyond this
+  double mixed_lambda_scale = 1.0;  // mixed assembly: Ewald splitting parameter relative to the reference's
   cudaStream_t side = nullptr;  // higher-priority stream for look-ahead panels
   cudaEvent_t ev_panel = nullptr, ev_next = nullptr;
   int* d_info = nullptr;  // device-side status words
