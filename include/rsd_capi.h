@@ -82,7 +82,7 @@ int rsd_ctx_set_tensor_cores(rsd_ctx* ctx, int mode);
  * with lammda*r < lam_r_cut (at most 6) and reciprocal vectors with
  * k^2/(4 lammda^2) <= 3 pi kshell^2 (on a cubic cell at the reference's
  * lammda: max|n_i| <= kshell) are summed in double-single (~1e-14), the
- * rest in FP32.  Defaults 4.0 and 1. */
+ * rest in FP32.  Defaults 4.5 and 1. */
 int rsd_ctx_set_mixed_split(rsd_ctx* ctx, double lam_r_cut, int32_t kshell);
 /* Truncation of the mixed-precision Ewald sums inside the reference's image
  * cubes: real-space images with lammda*r >= lam_r_max and reciprocal vectors
@@ -95,8 +95,8 @@ int rsd_ctx_set_mixed_truncation(rsd_ctx* ctx, double lam_r_max, double k2_over_
  * reference's lammda = sqrt(pi)/LV^(1/3).  The Ewald sum does not depend on
  * it; a larger value moves work from the real-space images to the cheaper
  * reciprocal vectors, and the image cubes are widened to hold the
- * truncation spheres.  1 keeps the reference's lammda, NR and NI.  The FP64
- * form always uses the reference's values. */
+ * truncation spheres.  1 keeps the reference's lammda, NR and NI; the
+ * default is 1.5.  The FP64 form always uses the reference's values. */
 int rsd_ctx_set_mixed_lambda_scale(rsd_ctx* ctx, double scale);
 
 /* ---------------------------------------------------------------- lattice */

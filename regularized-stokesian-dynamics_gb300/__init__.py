@@ -148,7 +148,7 @@ class Context:
     def stream(self):
         return _lib.rsd_ctx_stream(self.h)
 
-    def set_mixed_split(self, lam_r_cut=4.0, kshell=1):
+    def set_mixed_split(self, lam_r_cut=4.5, kshell=1):
         """FP64/FP32 split of the mixed-precision Ewald assembly."""
         self.check(_lib.rsd_ctx_set_mixed_split(self.h, float(lam_r_cut), int(kshell)))
 
@@ -156,7 +156,7 @@ class Context:
         """Truncation of the mixed-precision Ewald sums."""
         self.check(_lib.rsd_ctx_set_mixed_truncation(self.h, float(lam_r_max), float(k2_over_4lam2_max)))
 
-    def set_mixed_lambda_scale(self, scale=1.0):
+    def set_mixed_lambda_scale(self, scale=1.5):
         """Ewald splitting parameter of the mixed assembly relative to the
         reference's."""
         self.check(_lib.rsd_ctx_set_mixed_lambda_scale(self.h, float(scale)))

@@ -127,48 +127,103 @@ __global__ void ewald_trig_list(int nn, rsd_lat_dev L, const int* __restrict__ h
 // Scatter of the pair block (a,b), a < b, and its mirror (b,a) with
 // b -> -b, g -> -g (per_GRPY_YZD.f90:123-151,160-188).  v holds the 60
 // unique values (order of gen_ewald.py) already scaled; add != 0 adds.
+// Stores (add = 0) or read-modify-writes (add = 1) K entries of M.  All K
+// loads are issued before the first store, so a thread waits for one memory
+// round trip per group rather than one per entry (the addresses of a group
+// are distinct).
+template <int K>
+__device__ __forceinline__ void put_group(double* const* p, const double* x, int add) {
+  if (add) {
+    double o[K];
+#pragma unroll
+    for (int i = 0; i < K; i++) o[i] = *p[i];
+#pragma unroll
+    for (int i = 0; i < K; i++) *p[i] = o[i] + x[i];
+  } else {
+#pragma unroll
+    for (int i = 0; i < K; i++) *p[i] = x[i];
+  }
+}
+
+// Writes the pair blocks (a, b) and (b, a), a != b, of the grand mobility
+// from the 60 values of a pair (TT 0-5, RR 6-11, TR 12-14, QQ 15-29, G
+// 30-44, H 45-59), in 14 groups of at most 25 entries.
 __device__ inline void store_pair(double* __restrict__ M, int64_t ld, int N, int a, int b, const double* v, int add) {
-  auto put = [&](int r, int c, double x) {
-    double* p = M + (int64_t)r + (int64_t)c * ld;
-    *p = add ? *p + x : x;
-  };
-  const int sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
-  for (int i = 0; i < 3; i++)
-    for (int j = 0; j < 3; j++) {
-      const double tt = v[sym[i][j]], rr = v[6 + sym[i][j]];
-      double tr = 0.0;
-      if (i < j) tr = v[12 + (i == 0 ? j - 1 : 2)];
-      if (i > j) tr = -v[12 + (j == 0 ? i - 1 : 2)];
-      put(3 * a + i, 3 * b + j, tt);
-      put(3 * b + i, 3 * a + j, tt);
-      put(3 * N + 3 * a + i, 3 * N + 3 * b + j, rr);
-      put(3 * N + 3 * b + i, 3 * N + 3 * a + j, rr);
-      put(3 * a + i, 3 * N + 3 * b + j, tr);
-      put(3 * N + 3 * b + j, 3 * a + i, tr);
-      put(3 * b + i, 3 * N + 3 * a + j, -tr);
-      put(3 * N + 3 * a + j, 3 * b + i, -tr);
-    }
-  for (int i = 0; i < 3; i++)
-    for (int m = 0; m < 5; m++) {
-      const double g = v[30 + 5 * i + m], h = v[45 + 5 * i + m];
-      put(3 * a + i, 6 * N + 5 * b + m, g);
-      put(3 * N + 3 * a + i, 6 * N + 5 * b + m, h);
-      put(6 * N + 5 * b + m, 3 * a + i, g);
-      put(6 * N + 5 * b + m, 3 * N + 3 * a + i, h);
-      put(3 * b + i, 6 * N + 5 * a + m, -g);
-      put(3 * N + 3 * b + i, 6 * N + 5 * a + m, h);
-      put(6 * N + 5 * a + m, 3 * b + i, -g);
-      put(6 * N + 5 * a + m, 3 * N + 3 * b + i, h);
-    }
-  int q = 15;
-  double qq[5][5];
-  for (int x = 0; x < 5; x++)
-    for (int y = x; y < 5; y++) qq[x][y] = qq[y][x] = v[q++];
-  for (int x = 0; x < 5; x++)
-    for (int y = 0; y < 5; y++) {
-      put(6 * N + 5 * a + x, 6 * N + 5 * b + y, qq[x][y]);
-      put(6 * N + 5 * b + x, 6 * N + 5 * a + y, qq[x][y]);
-    }
+  auto at = [&](int r, int c) { return M + (int64_t)r + (int64_t)c * ld; };
+  constexpr int sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+  // TT and RR, both orders
+#pragma unroll
+  for (int blk = 0; blk < 2; blk++) {
+    const int o = blk ? 3 * N : 0;
+    double* p[18];
+    double x[18];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        const double t = v[6 * blk + sym[i][j]];
+        p[6 * i + 2 * j] = at(o + 3 * a + i, o + 3 * b + j);
+        p[6 * i + 2 * j + 1] = at(o + 3 * b + i, o + 3 * a + j);
+        x[6 * i + 2 * j] = x[6 * i + 2 * j + 1] = t;
+      }
+    put_group<18>(p, x, add);
+  }
+  // TR: translation of one particle against rotation of the other, both
+  // placements (upper and lower triangle) of each
+#pragma unroll
+  for (int side = 0; side < 2; side++) {
+    const int t = side ? b : a, r = side ? a : b;
+    double* p[18];
+    double x[18];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        double tr = 0.0;
+        if (i < j) tr = v[12 + (i == 0 ? j - 1 : 2)];
+        if (i > j) tr = -v[12 + (j == 0 ? i - 1 : 2)];
+        if (side) tr = -tr;
+        p[6 * i + 2 * j] = at(3 * t + i, 3 * N + 3 * r + j);
+        p[6 * i + 2 * j + 1] = at(3 * N + 3 * r + j, 3 * t + i);
+        x[6 * i + 2 * j] = x[6 * i + 2 * j + 1] = tr;
+      }
+    put_group<18>(p, x, add);
+  }
+  // G (translation-stresslet, odd under a <-> b) and H (rotation-stresslet)
+#pragma unroll
+  for (int grp = 0; grp < 8; grp++) {
+    const int side = grp >> 2, h = (grp >> 1) & 1, lower = grp & 1;
+    const int u = side ? b : a, s = side ? a : b;  // velocity row particle, stresslet column particle
+    const int ro = h ? 3 * N : 0;
+    double* p[15];
+    double x[15];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int m = 0; m < 5; m++) {
+        double g = v[(h ? 45 : 30) + 5 * i + m];
+        if (side && !h) g = -g;
+        p[5 * i + m] = lower ? at(6 * N + 5 * s + m, ro + 3 * u + i) : at(ro + 3 * u + i, 6 * N + 5 * s + m);
+        x[5 * i + m] = g;
+      }
+    put_group<15>(p, x, add);
+  }
+  // QQ, both orders
+#pragma unroll
+  for (int side = 0; side < 2; side++) {
+    const int r = side ? b : a, c = side ? a : b;
+    double* p[25];
+    double x[25];
+#pragma unroll
+    for (int xi = 0; xi < 5; xi++)
+#pragma unroll
+      for (int y = 0; y < 5; y++) {
+        const int lo = xi < y ? xi : y, hi = xi < y ? y : xi;
+        p[5 * xi + y] = at(6 * N + 5 * r + xi, 6 * N + 5 * c + y);
+        x[5 * xi + y] = v[15 + lo * 5 - lo * (lo - 1) / 2 + (hi - lo)];
+      }
+    put_group<25>(p, x, add);
+  }
 }
 
 // scale by nondim (1/(6 a_i) for TT, TR, G; 1/(6 a_i^3) for RR, QQ, H) and
@@ -343,6 +398,122 @@ __global__ void __launch_bounds__(128) ewald_pair_k_ds(int nn, rsd_lat_dev L, in
   store_pair(M, ldm, nn, a, b, o, add);
 }
 
+// ---------------------------------------------------- equal radii, k space
+// With one radius for every particle, the reciprocal-space epilogue (linear
+// in the moments) can be applied per vector instead of per pair: each of
+// the 60 block entries is then sum_k W_q(k) cos(k.R) (41 entries: TT, RR,
+// QQ, H) or sum_k W_q(k) sin(k.R) (the 18 TR and G entries), with the block
+// weights W_q(k) = epilogue(moment weights of k) formed once per vector in
+// FP64.  A pair then costs 60 multiply-adds per vector instead of 80, and
+// its FP32 rounding is no longer amplified by the epilogue's cancellation
+// between moments.
+__host__ __device__ constexpr bool kblock_is_sin(int q) { return (q >= 12 && q < 15) || (q >= 30 && q < 45); }
+constexpr int KBW = 64;  // weights per vector (60 used, padded for 16-byte rows)
+
+template <typename T>
+__device__ __forceinline__ void put_weight(T* p, double v) { *p = (T)v; }
+template <>
+__device__ __forceinline__ void put_weight<dsf>(dsf* p, double v) { *p = dsf_from(v); }
+
+template <typename T>
+__global__ void ewald_kblock_list(rsd_lat_dev L, int count, const int* __restrict__ hlist, double a,
+                                  T* __restrict__ W) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= count) return;
+  int nx, ny, nz;
+  half_space_index(hlist[q], L.NI, &nx, &ny, &nz);
+  double k[3];
+  for (int j = 0; j < 3; j++)
+    k[j] = 2.0 * RSD_PI * (nx * L.LI[0 + 3 * j] + ny * L.LI[1 + 3 * j] + nz * L.LI[2 + 3 * j]);
+  const double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+  const double S = kernel_S<double>(k2, L.lam);
+  double wc[RSD_NMOM_KCOS], ws[RSD_NMOM_KSIN], v[60], w[60];
+  rsd_kcos_weights<double>(k[0], k[1], k[2], S, L.lam, wc);
+  rsd_ksin_weights<double>(k[0], k[1], k[2], S, L.lam, ws);
+  rsd_kcos_epilogue<double>(wc, a, a, L.phix, v);
+  rsd_ksin_epilogue<double>(ws, a, a, L.phix, w);
+  const double f = 2.0 / L.LV;  // half space counted twice
+  T* e = W + (size_t)q * KBW;
+  for (int i = 0; i < 60; i++) put_weight<T>(e + i, (kblock_is_sin(i) ? w[i] : v[i]) * f);
+  for (int i = 60; i < KBW; i++) put_weight<T>(e + i, 0.0);
+}
+
+__device__ __forceinline__ float trig_c(float2 v) { return v.x; }
+__device__ __forceinline__ float trig_s(float2 v) { return v.y; }
+__device__ __forceinline__ dsf trig_c(float4 v) { return dsf(v.x, v.y); }
+__device__ __forceinline__ dsf trig_s(float4 v) { return dsf(v.z, v.w); }
+
+// Accumulates sum_k W_q(k) {cos, sin}(k.(x_a - x_b)) over Kh vectors into
+// acc, for the pair (a, b) of the calling thread (block 32 x 4).  The
+// weights of 16 vectors and the trig values of the CTA's 32 + 4 particles
+// are staged in shared memory (sw: 16 x KBW, sca: 16 x 32, scb: 16 x 4).
+template <typename T, typename TT>
+__device__ __forceinline__ void kblock_accumulate(int nn, int Kh, const T* __restrict__ W, const TT* __restrict__ cs,
+                                                  T* sw, TT* sca, TT* scb, bool valid, T (&acc)[60]) {
+  constexpr int KC = 16;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  const int a0 = blockIdx.x * blockDim.x, b0 = blockIdx.y * blockDim.y;
+  for (int h0 = 0; h0 < Kh; h0 += KC) {
+    const int kc = min(KC, Kh - h0);
+    __syncthreads();
+    for (int e = tid; e < kc * KBW; e += nthr) sw[e] = W[(size_t)h0 * KBW + e];
+    for (int e = tid; e < kc * 36; e += nthr) {
+      const int hh = e / 36, q = e % 36, part = q < 32 ? a0 + q : b0 + q - 32;
+      if (part < nn) {
+        const TT v = cs[(size_t)(h0 + hh) * nn + part];
+        if (q < 32)
+          sca[hh * 32 + q] = v;
+        else
+          scb[hh * 4 + q - 32] = v;
+      }
+    }
+    __syncthreads();
+    if (!valid) continue;
+    for (int hh = 0; hh < kc; hh++) {
+      const TT ua = sca[hh * 32 + threadIdx.x], ub = scb[hh * 4 + threadIdx.y];
+      const T ca = trig_c(ua), sa = trig_s(ua), cb = trig_c(ub), sb = trig_s(ub);
+      const T c = ca * cb + sa * sb;   // cos(k.(x_a - x_b))
+      const T sn = sa * cb - ca * sb;  // sin(k.(x_a - x_b))
+      const T* e = sw + hh * KBW;
+#pragma unroll
+      for (int q = 0; q < 60; q++) acc[q] = fma(e[q], kblock_is_sin(q) ? sn : c, acc[q]);
+    }
+  }
+}
+
+// Reciprocal-space pair blocks with per-vector block weights (equal radii):
+// the K32 FP32 vectors first, then the K64 double-single ones on top of the
+// FP32 sums; the blocks are written (add = 0) or added (add = 1) once.
+__global__ void __launch_bounds__(128) ewald_pair_kblock(int nn, int K32, const float* __restrict__ W32,
+                                                         const float2* __restrict__ c32, int K64,
+                                                         const dsf* __restrict__ W64, const float4* __restrict__ c64,
+                                                         const double* __restrict__ radii, double inv_pimu,
+                                                         double* __restrict__ M, int64_t ldm, int add) {
+  constexpr int KC = 16;
+  __shared__ __align__(16) dsf sw[KC * KBW];  // the FP32 phase uses the first half as floats
+  __shared__ __align__(16) float4 sca[KC * 32], scb[KC * 4];
+  if ((int)(blockIdx.x * blockDim.x) >= (int)(blockIdx.y * blockDim.y + blockDim.y - 1)) return;
+  int a, b;
+  const bool valid = pair_of(nn, &a, &b);
+  dsf acc[60];
+  {
+    float f[60];
+#pragma unroll
+    for (int q = 0; q < 60; q++) f[q] = 0.f;
+    kblock_accumulate<float, float2>(nn, K32, W32, c32, reinterpret_cast<float*>(sw),
+                                     reinterpret_cast<float2*>(sca), reinterpret_cast<float2*>(scb), valid, f);
+#pragma unroll
+    for (int q = 0; q < 60; q++) acc[q] = dsf(f[q], 0.f);
+  }
+  kblock_accumulate<dsf, float4>(nn, K64, W64, c64, sw, sca, scb, valid, acc);
+  if (!valid) return;
+  double o[60];
+#pragma unroll
+  for (int q = 0; q < 60; q++) o[q] = dsf_to(acc[q]);
+  scale_block(o, radii[a], inv_pimu);
+  store_pair(M, ldm, nn, a, b, o, add);
+}
+
 // Near/far split of the real-space images for the mixed form.  Image nz of
 // lattice column (nx, ny) has FP32 coordinates p + a3 nz, where p = R + nx a1
 // + ny a2 is formed in FP64 and rounded once; it is "near" when its FP32
@@ -496,36 +667,85 @@ __global__ void __launch_bounds__(128) ewald_pair_real(int nn, rsd_lat_dev L, co
   store_pair(M, ldm, nn, a, b, v, 1);
 }
 
-__global__ void __launch_bounds__(64) ewald_self(int nn, rsd_lat_dev L, int Kh, const double* __restrict__ tab,
+// Self-image moments.  The real-space images n != 0 of a particle and the
+// cos weights of the half space do not depend on the particle (only the
+// epilogue does, through its radius), so one CTA sums them once in FP64:
+// out[0..96] = real moments, out[97..145] = kcos weights.
+constexpr int SELF_NMOM = RSD_NMOM_REAL + RSD_NMOM_KCOS;
+constexpr int SELF_THREADS = 128;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__global__ void __launch_bounds__(SELF_THREADS) ewald_self_moments(rsd_lat_dev L, int Kh,
+                                                                   const double* __restrict__ tab,
+                                                                   double* __restrict__ out) {
+  __shared__ double part[SELF_THREADS / 32][SELF_NMOM];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const double lam = L.lam, lam2 = lam * lam, cd = 2.0 * RSD_PIP5 * lam;
+  {
+    double acc[RSD_NMOM_REAL];
+#pragma unroll
+    for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = 0.0;
+    const int NR = L.NR, w = 2 * NR + 1, nimg = w * w * w;
+    for (int i = tid; i < nimg; i += SELF_THREADS) {
+      const int nx = i / (w * w) - NR, ny = (i / w) % w - NR, nz = i % w - NR;
+      if (!nx && !ny && !nz) continue;  // PER_ROTNE_PRAGER_SELF 61
+      const double x0 = L.LR[0] * nx + L.LR[3] * ny + L.LR[6] * nz;
+      const double x1 = L.LR[1] * nx + L.LR[4] * ny + L.LR[7] * nz;
+      const double x2 = L.LR[2] * nx + L.LR[5] * ny + L.LR[8] * nz;
+      const double r2 = x0 * x0 + x1 * x1 + x2 * x2, r = sqrt(r2);
+      rsd_real_image<double>(x0, x1, x2, r, 1.0 / r, erfc(lam * r), cd * exp(-r2 * lam2), lam, acc);
+    }
+#pragma unroll
+    for (int m = 0; m < RSD_NMOM_REAL; m++) {
+      const double v = warp_sum(acc[m]);
+      if (lane == 0) part[warp][m] = v;
+    }
+  }
+  {
+    double ac[RSD_NMOM_KCOS];
+#pragma unroll
+    for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] = 0.0;
+    for (int h = tid; h < Kh; h += SELF_THREADS) {
+      const double* e = tab + (size_t)h * KW + 3;
+#pragma unroll
+      for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] += e[m];
+    }
+#pragma unroll
+    for (int m = 0; m < RSD_NMOM_KCOS; m++) {
+      const double v = warp_sum(ac[m]);
+      if (lane == 0) part[warp][RSD_NMOM_REAL + m] = v;
+    }
+  }
+  __syncthreads();
+  for (int m = tid; m < SELF_NMOM; m += SELF_THREADS) {
+    double t = 0.0;
+    for (int q = 0; q < SELF_THREADS / 32; q++) t += part[q][m];
+    out[m] = t;
+  }
+}
+
+// Diagonal blocks from the self moments (ewald_self_moments) and the
+// particle's radius.
+__global__ void __launch_bounds__(64) ewald_self(int nn, rsd_lat_dev L, const double* __restrict__ mom,
                                                  const double* __restrict__ radii, double inv_pimu,
                                                  double* __restrict__ M, int64_t ldm) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= nn) return;
-  const double ai = radii[a], lam = L.lam, lam2 = lam * lam, cd = 2.0 * RSD_PIP5 * lam;
+  const double ai = radii[a], lam = L.lam;
   double v[60], w[60];
   {
     double acc[RSD_NMOM_REAL];
-    for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = 0.0;
-    const int NR = L.NR;
-    for (int nx = -NR; nx <= NR; nx++)
-      for (int ny = -NR; ny <= NR; ny++)
-        for (int nz = -NR; nz <= NR; nz++) {
-          if (!nx && !ny && !nz) continue;  // PER_ROTNE_PRAGER_SELF 61
-          const double x0 = L.LR[0] * nx + L.LR[3] * ny + L.LR[6] * nz;
-          const double x1 = L.LR[1] * nx + L.LR[4] * ny + L.LR[7] * nz;
-          const double x2 = L.LR[2] * nx + L.LR[5] * ny + L.LR[8] * nz;
-          const double r2 = x0 * x0 + x1 * x1 + x2 * x2, r = sqrt(r2);
-          rsd_real_image<double>(x0, x1, x2, r, 1.0 / r, erfc(lam * r), cd * exp(-r2 * lam2), lam, acc);
-        }
+    for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = mom[m];
     rsd_real_epilogue<double>(acc, ai, ai, L.phix, v);
   }
   {
     double ac[RSD_NMOM_KCOS];
-    for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] = 0.0;
-    for (int h = 0; h < Kh; h++) {
-      const double* e = tab + (size_t)h * KW + 3;
-      for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] += __ldg(e + m);
-    }
+    for (int m = 0; m < RSD_NMOM_KCOS; m++) ac[m] = mom[RSD_NMOM_REAL + m];
     rsd_kcos_epilogue<double>(ac, ai, ai, L.phix, w);
   }
   // analytic self terms (Ewald_summation.f90:179-188)
@@ -641,16 +861,18 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
   if (precision != RSD_PREC_MIXED) {
     ewald_trig<<<dim3((nn + 127) / 128, Kh), 128, 0, s>>>(nn, Kh, tab, d_pos, cs); RSD_LAUNCH_NOTE();
   }
-  ewald_self<<<(nn + 63) / 64, 64, 0, s>>>(nn, L, Kh, tab, d_radii, inv_pimu, d_M, ldm); RSD_LAUNCH_NOTE();
+  double* mom = (double*)rsd_scratch(ctx, "ewald_self_mom", sizeof(double) * SELF_NMOM);
+  if (!mom) return RSD_ENOMEM;
+  ewald_self_moments<<<1, SELF_THREADS, 0, s>>>(L, Kh, tab, mom); RSD_LAUNCH_NOTE();
+  ewald_self<<<(nn + 63) / 64, 64, 0, s>>>(nn, L, mom, d_radii, inv_pimu, d_M, ldm); RSD_LAUNCH_NOTE();
   if (nn > 1) {
     dim3 blk(32, 4), grd((nn + 31) / 32, (nn + 3) / 4);
     if (precision == RSD_PREC_MIXED) {
-      // FP64: real images with lambda r < mixed_rcut (default 4.0) and
-      // reciprocal vectors with max|n_i| <= mixed_kshell (default 1); FP32
-      // for the rest.  The FP32 part is limited by the epilogue, which
-      // combines moments that cancel by 2-3 orders of magnitude: images at
-      // lambda r >= 4.0 then change a block by ~1e-10 of its largest entry
-      // (a step's stresslets by ~6e-11, velocities by ~3e-12).
+      // Double-single: real images with lambda r < mixed_rcut (default 4.5)
+      // and reciprocal vectors with k^2/(4 lambda^2) <= 3 pi mixed_kshell^2
+      // (default 1); FP32 for the rest.  The FP32 error of a block follows
+      // the largest FP32 term: at the defaults (with lambda x 1.5) a step's
+      // velocities move by ~3e-11 and its stresslets by ~3e-10 relative.
       // Truncation: real images with lambda r >= mixed_rmax and reciprocal
       // vectors with k^2 / (4 lambda^2) >= mixed_kexp are dropped (each
       // changes a block by less than ~1e-12 of its largest entry at the
@@ -688,16 +910,38 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
       all.insert(all.end(), h32.begin(), h32.end());
       RSD_CUDA(ctx, cudaMemcpyAsync(dh, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice, s));
       RSD_CUDA(ctx, cudaStreamSynchronize(s));
+      // equal radii: per-vector block weights (ewald_pair_kblock)
+      std::vector<double> hr((size_t)nn);
+      RSD_CUDA(ctx, cudaMemcpy(hr.data(), d_radii, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+      bool equal = true;
+      for (int i = 1; i < nn && equal; i++) equal = hr[i] == hr[0];
       if (K64) {
-        ewald_ktable_list<double><<<(K64 + 127) / 128, 128, 0, s>>>(L, K64, dh, t64); RSD_LAUNCH_NOTE();
         ewald_trig_list<float4><<<dim3((nn + 127) / 128, K64), 128, 0, s>>>(nn, L, dh, d_pos, c64); RSD_LAUNCH_NOTE();
       }
       if (K32) {
-        ewald_ktable_list<float><<<(K32 + 127) / 128, 128, 0, s>>>(L, K32, dh + K64, t32); RSD_LAUNCH_NOTE();
         ewald_trig_list<float2><<<dim3((nn + 127) / 128, K32), 128, 0, s>>>(nn, L, dh + K64, d_pos, c32); RSD_LAUNCH_NOTE();
       }
-      ewald_pair_k_ds<<<grd, blk, 0, s>>>(nn, L, K64, t64, c64, d_radii, inv_pimu, d_M, ldm, 0); RSD_LAUNCH_NOTE();
-      ewald_pair_k<float, float2><<<grd, blk, 0, s>>>(nn, L, K32, t32, c32, d_radii, inv_pimu, d_M, ldm, 1); RSD_LAUNCH_NOTE();
+      if (equal) {
+        dsf* w64 = (dsf*)rsd_scratch(ctx, "ewald_kblock64", sizeof(dsf) * (size_t)(K64 > 0 ? K64 : 1) * KBW);
+        float* w32 = (float*)rsd_scratch(ctx, "ewald_kblock32", sizeof(float) * (size_t)(K32 > 0 ? K32 : 1) * KBW);
+        if (!w64 || !w32) return RSD_ENOMEM;
+        if (K64) {
+          ewald_kblock_list<dsf><<<(K64 + 127) / 128, 128, 0, s>>>(L, K64, dh, hr[0], w64); RSD_LAUNCH_NOTE();
+        }
+        if (K32) {
+          ewald_kblock_list<float><<<(K32 + 127) / 128, 128, 0, s>>>(L, K32, dh + K64, hr[0], w32); RSD_LAUNCH_NOTE();
+        }
+        ewald_pair_kblock<<<grd, blk, 0, s>>>(nn, K32, w32, c32, K64, w64, c64, d_radii, inv_pimu, d_M, ldm, 0); RSD_LAUNCH_NOTE();
+      } else {
+        if (K64) {
+          ewald_ktable_list<double><<<(K64 + 127) / 128, 128, 0, s>>>(L, K64, dh, t64); RSD_LAUNCH_NOTE();
+        }
+        if (K32) {
+          ewald_ktable_list<float><<<(K32 + 127) / 128, 128, 0, s>>>(L, K32, dh + K64, t32); RSD_LAUNCH_NOTE();
+        }
+        ewald_pair_k_ds<<<grd, blk, 0, s>>>(nn, L, K64, t64, c64, d_radii, inv_pimu, d_M, ldm, 0); RSD_LAUNCH_NOTE();
+        ewald_pair_k<float, float2><<<grd, blk, 0, s>>>(nn, L, K32, t32, c32, d_radii, inv_pimu, d_M, ldm, 1); RSD_LAUNCH_NOTE();
+      }
       ewald_pair_real_near_ds<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, d_M, ldm); RSD_LAUNCH_NOTE();
       ewald_pair_real_far<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, rmax2, d_M, ldm); RSD_LAUNCH_NOTE();
     } else {

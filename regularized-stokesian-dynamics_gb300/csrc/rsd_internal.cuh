@@ -32,11 +32,11 @@ struct rsd_ctx {
   cudaEvent_t ev[8] = {};
   double phase_ms[4] = {0, 0, 0, 0};
   int use_tc = 1;         // FP32 factorisations: 0 SIMT, 1 per-factor TF32/3xTF32, 3 all 3xTF32
-  double mixed_rcut = 4.0;  // mixed assembly: FP64 real images below this lambda r
+  double mixed_rcut = 4.5;  // mixed assembly: FP64 real images below this lambda r
   int mixed_kshell = 1;     // mixed assembly: FP64 reciprocal shells max|n_i| <= this
   double mixed_rmax = 6.0;  // mixed assembly: real images with lambda r beyond this dropped
   double mixed_kexp = 10.0 * 3.141592653589793;  // and reciprocal vectors with k^2/(4 lambda^2) beyond this
-  double mixed_lambda_scale = 1.0;  // mixed assembly: Ewald splitting parameter relative to the reference's
+  double mixed_lambda_scale = 1.5;  // mixed assembly: Ewald splitting parameter relative to the reference's
   cudaStream_t side = nullptr;  // higher-priority stream for look-ahead panels
   cudaEvent_t ev_panel = nullptr, ev_next = nullptr;
   int* d_info = nullptr;  // device-side status words
