@@ -480,6 +480,116 @@ __device__ __forceinline__ void load_tile_f32(const float* __restrict__ A, int64
   }
 }
 
+// Step K of the 32 x 32 register factor of diag32_factor_inv (lane =
+// column), then steps K+1..31.  Template recursion keeps every index of r
+// and dinv a compile-time constant, so both stay in registers.
+template <int K>
+__device__ __forceinline__ void chol32_step(float (&r)[32], float (&dinv)[32], int lane, int& bad) {
+  if constexpr (K < 32) {
+    const float pv = __shfl_sync(0xffffffffu, r[K], K);
+    bad = (bad == 0 && !(pv > 0.f && pv <= 3.402823466e38f)) ? K + 1 : bad;
+    const float inv = rsqrtf(pv);  // every lane forms the pivot's 1/sqrt itself
+    dinv[K] = inv;
+    r[K] = lane >= K ? r[K] * inv : r[K];
+#pragma unroll
+    for (int i = K + 1; i < 32; i++) {
+      const float u = __shfl_sync(0xffffffffu, r[K], i);
+      r[i] = lane >= i ? fmaf(-u, r[K], r[i]) : r[i];
+    }
+    chol32_step<K + 1>(r, dinv, lane, bad);
+  }
+}
+
+// A full 32 x 32 diagonal sub-block (warp-wide, no branches): the factor in
+// registers (written to S), then D^-1 column `lane` by back substitution in
+// axpy form, U's rows read from shared memory at the same address for every
+// lane (written to Wm and Dinv, (p, i) at Dinv[p * 33 + i]).  Returns the
+// 1-based index of the first pivot that is not positive and finite, 0 if
+// none.
+__device__ __forceinline__ int diag32_factor_inv(float* S, float* Wm, float* Dinv, int k0, int lane) {
+  float r[32], dinv[32];
+#pragma unroll
+  for (int i = 0; i < 32; i++) r[i] = S[(k0 + i) + (k0 + lane) * PLD];
+  int bad = 0;
+  chol32_step<0>(r, dinv, lane, bad);
+  if (bad) return bad;
+#pragma unroll
+  for (int i = 0; i < 32; i++)
+    if (i <= lane) S[(k0 + i) + (k0 + lane) * PLD] = r[i];
+  __syncwarp();
+  float x[32], acc[32];
+#pragma unroll
+  for (int i = 0; i < 32; i++) acc[i] = 0.f;
+#pragma unroll
+  for (int q = 0; q < 32; q++) {
+    const int p = 31 - q;
+    const float v = ((p == lane ? 1.f : 0.f) - acc[p]) * dinv[p];
+    x[p] = p <= lane ? v : 0.f;
+#pragma unroll
+    for (int i = 0; i < p; i++) acc[i] = fmaf(S[(k0 + i) + (k0 + p) * PLD], x[p], acc[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < 32; i++) {
+    Wm[(k0 + i) + (k0 + lane) * PLD] = x[i];
+    Dinv[i * 33 + lane] = x[i];
+  }
+  return 0;
+}
+
+// The trailing sub-block of kw < 32 columns (zero-padded to 32), as
+// diag32_factor_inv with IEEE square roots and divisions.
+__device__ __forceinline__ int diag_partial_factor_inv(float* S, float* Wm, float* Dinv, int k0, int kw, int lane) {
+  float r[32];
+#pragma unroll
+  for (int i = 0; i < 32; i++) r[i] = S[(k0 + i) + (k0 + lane) * PLD];
+  int bad = 0;
+#pragma unroll
+  for (int k = 0; k < 32; k++) {
+    if (k < kw && !bad) {
+      const float piv = __shfl_sync(0xffffffffu, r[k], k);
+      if (!(piv > 0.f) || !isfinite(piv)) {
+        bad = k + 1;
+      } else {
+        const float d = sqrtf(piv);
+        if (lane > k) r[k] = r[k] / d;
+        else if (lane == k) r[k] = d;
+#pragma unroll
+        for (int i = k + 1; i < 32; i++) {
+          const float uki = __shfl_sync(0xffffffffu, r[k], i);
+          if (lane >= i) r[i] -= uki * r[k];
+        }
+      }
+    }
+  }
+  if (bad) return bad;
+  // column `lane` of D^-1: back substitution against the rows of U_D, whose
+  // entry (ii, p) lane p holds in r[ii]
+  float x[32];
+#pragma unroll
+  for (int ii = 31; ii >= 0; ii--) {
+    float v = (ii == lane) ? 1.f : 0.f;
+#pragma unroll
+    for (int p = ii + 1; p < 32; p++) v -= __shfl_sync(0xffffffffu, r[ii], p) * x[p];
+    const float dii = __shfl_sync(0xffffffffu, r[ii], ii);
+    x[ii] = (ii < kw && lane < kw && ii <= lane) ? v / dii : 0.f;
+  }
+  if (lane < kw) {
+#pragma unroll
+    for (int i = 0; i < 32; i++) {
+      if (i <= lane) S[(k0 + i) + (k0 + lane) * PLD] = r[i];
+      Wm[(k0 + i) + (k0 + lane) * PLD] = x[i];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 32; i++) Dinv[i * 33 + lane] = x[i];
+  return 0;
+}
+
+// FP32 diagonal block (jb <= 128) of the blocked Cholesky: its upper factor
+// U in place and W = U^-1 into Wout (NB x NB, zero below the diagonal).  In
+// 32-wide sub-blocks: warp 0 factors and inverts the diagonal sub-block D,
+// all warps form the row panel D^-T R and the trailing update; at the end
+// W's off-diagonal blocks are filled level by level from the D^-1.
 constexpr int SMEM_POTF2_INV = (2 * NB * PLD + NB * RTLD + 32 * 33 + 3 * 32 * 33) * (int)sizeof(float);
 __global__ void __launch_bounds__(256) potf2_inv_f32(float* __restrict__ A, int64_t lda, int jb,
                                                      int* __restrict__ info, int j0, float* __restrict__ Wout) {
@@ -499,67 +609,35 @@ __global__ void __launch_bounds__(256) potf2_inv_f32(float* __restrict__ A, int6
   for (int kb = 0; kb < nsub; kb++) {
     const int k0 = kb * 32, kw = min(32, jb - k0);
     if (warp == 0) {
-      float r[32];
-#pragma unroll
-      for (int i = 0; i < 32; i++) r[i] = S[(k0 + i) + (k0 + lane) * PLD];
-      int bad = 0;
-#pragma unroll
-      for (int k = 0; k < 32; k++) {
-        if (k < kw && !bad) {
-          const float piv = __shfl_sync(0xffffffffu, r[k], k);
-          if (!(piv > 0.f) || !isfinite(piv)) {
-            bad = k + 1;
-          } else {
-            const float d = sqrtf(piv);
-            if (lane > k) r[k] = r[k] / d;
-            else if (lane == k) r[k] = d;
-#pragma unroll
-            for (int i = k + 1; i < 32; i++) {
-              const float uki = __shfl_sync(0xffffffffu, r[k], i);
-              if (lane >= i) r[i] -= uki * r[k];
-            }
-          }
-        }
-      }
-      if (bad) {
-        if (lane == 0) {
-          failed = 1;
-          atomicCAS(info, 0, j0 + k0 + bad);
-        }
-      } else {
-        // column `lane` of D^-1: back substitution against the rows of U_D,
-        // whose entry (ii, p) lane p holds in r[ii]
-        float x[32];
-#pragma unroll
-        for (int ii = 31; ii >= 0; ii--) {
-          float v = (ii == lane) ? 1.f : 0.f;
-#pragma unroll
-          for (int p = ii + 1; p < 32; p++) v -= __shfl_sync(0xffffffffu, r[ii], p) * x[p];
-          const float dii = __shfl_sync(0xffffffffu, r[ii], ii);
-          x[ii] = (ii < kw && lane < kw && ii <= lane) ? v / dii : 0.f;
-        }
-        if (lane < kw) {
-#pragma unroll
-          for (int i = 0; i < 32; i++) {
-            if (i <= lane) S[(k0 + i) + (k0 + lane) * PLD] = r[i];
-            Wm[(k0 + i) + (k0 + lane) * PLD] = x[i];
-          }
-        }
-#pragma unroll
-        for (int i = 0; i < 32; i++) Dinv[i * 33 + lane] = x[i];
+      const int bad = kw == 32 ? diag32_factor_inv(S, Wm, Dinv, k0, lane)
+                               : diag_partial_factor_inv(S, Wm, Dinv, k0, kw, lane);
+      if (bad && lane == 0) {
+        failed = 1;
+        atomicCAS(info, 0, j0 + k0 + bad);
       }
     }
     __syncthreads();
     if (failed) return;
     const int m0 = k0 + kw, mw = jb - m0;
-    // row panel: R <- D^-T R, one warp per column, lane = row
-    for (int c = warp; c < mw; c += 8) {
-      float v = 0.f;
+    // row panel: R <- D^-T R, four columns per warp, lane = row
+    for (int c0 = 4 * warp; c0 < mw; c0 += 32) {
+      float v[4] = {0.f, 0.f, 0.f, 0.f};
+      int col[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) col[q] = m0 + min(c0 + q, mw - 1);
 #pragma unroll 8
-      for (int p = 0; p < 32; p++) v += Dinv[p * 33 + lane] * S[(k0 + p) + (m0 + c) * PLD];
+      for (int p = 0; p < 32; p++) {
+        const float d = Dinv[p * 33 + lane];
+#pragma unroll
+        for (int q = 0; q < 4; q++) v[q] = fmaf(d, S[(k0 + p) + col[q] * PLD], v[q]);
+      }
       __syncwarp();
-      if (lane < kw) S[(k0 + lane) + (m0 + c) * PLD] = v;
-      RT[c * RTLD + lane] = (lane < kw) ? v : 0.f;
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (c0 + q < mw) {
+          if (lane < kw) S[(k0 + lane) + col[q] * PLD] = v[q];
+          RT[(c0 + q) * RTLD + lane] = (lane < kw) ? v[q] : 0.f;
+        }
     }
     __syncthreads();
     // trailing update of the upper part: lane = row i of a 32-row block,
@@ -620,163 +698,6 @@ __global__ void __launch_bounds__(256) potf2_inv_f32(float* __restrict__ A, int6
     const int i = e % NB, j = e / NB;
     if (i < jb && j < jb && i <= j) A[i + (int64_t)j * lda] = S[i + j * PLD];
     Wout[e] = (i < jb && j < jb && i <= j) ? Wm[i + j * PLD] : 0.f;
-  }
-}
-
-// FP32 diagonal block (jb <= 128), factor only: as potf2_inv_f32 without
-// the inverse (the row panel of each 32-wide sub-block by substitution, one
-// thread per column), so the serial single-warp work on the critical path
-// of the blocked factorisation is the 32 x 32 factors alone.
-constexpr int SMEM_POTF2_F32 = (NB * PLD + NB * RTLD) * (int)sizeof(float);
-__global__ void __launch_bounds__(256) potf2_f32(float* __restrict__ A, int64_t lda, int jb, int* __restrict__ info,
-                                                 int j0) {
-  extern __shared__ unsigned char smraw[];
-  float* S = (float*)smraw;   // U, NB x NB, ld PLD
-  float* RT = S + NB * PLD;   // row panel transposed: trailing column c, row p at RT[c * RTLD + p]
-  __shared__ int failed;
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  load_tile_f32(A, lda, jb, jb, NB, S, PLD, 1);
-  if (t == 0) failed = 0;
-  __syncthreads();
-  const int nsub = (jb + 31) / 32;
-  for (int kb = 0; kb < nsub; kb++) {
-    const int k0 = kb * 32, kw = min(32, jb - k0);
-    if (warp == 0) {
-      float r[32];
-#pragma unroll
-      for (int i = 0; i < 32; i++) r[i] = S[(k0 + i) + (k0 + lane) * PLD];
-      int bad = 0;
-#pragma unroll
-      for (int k = 0; k < 32; k++) {
-        if (k < kw && !bad) {
-          const float piv = __shfl_sync(0xffffffffu, r[k], k);
-          if (!(piv > 0.f) || !isfinite(piv)) {
-            bad = k + 1;
-          } else {
-            const float d = sqrtf(piv);
-            if (lane > k) r[k] = r[k] / d;
-            else if (lane == k) r[k] = d;
-#pragma unroll
-            for (int i = k + 1; i < 32; i++) {
-              const float uki = __shfl_sync(0xffffffffu, r[k], i);
-              if (lane >= i) r[i] -= uki * r[k];
-            }
-          }
-        }
-      }
-      if (bad) {
-        if (lane == 0) {
-          failed = 1;
-          atomicCAS(info, 0, j0 + k0 + bad);
-        }
-      } else if (lane < kw) {
-#pragma unroll
-        for (int i = 0; i < 32; i++)
-          if (i <= lane) S[(k0 + i) + (k0 + lane) * PLD] = r[i];
-      }
-    }
-    __syncthreads();
-    if (failed) return;
-    const int m0 = k0 + kw, mw = jb - m0;
-    if (t < mw) {  // row panel: U_D^T X = R by substitution, one column per thread
-      const int c = m0 + t;
-      float x[32];
-#pragma unroll
-      for (int i = 0; i < 32; i++) {
-        float v = 0.f;
-        if (i < kw) {
-          v = S[(k0 + i) + c * PLD];
-#pragma unroll
-          for (int p = 0; p < i; p++) v -= S[(k0 + p) + (k0 + i) * PLD] * x[p];
-          v = v / S[(k0 + i) + (k0 + i) * PLD];
-        }
-        x[i] = v;
-      }
-#pragma unroll
-      for (int i = 0; i < 32; i++) {
-        if (i < kw) S[(k0 + i) + c * PLD] = x[i];
-        RT[t * RTLD + i] = x[i];
-      }
-    }
-    __syncthreads();
-    const int nrb = (mw + 31) / 32, ncg = (mw + 7) / 8;
-    for (int task = warp; task < nrb * ncg; task += 8) {
-      const int rb = task % nrb, cg = task / nrb;
-      const int i = rb * 32 + lane, c0 = cg * 8;
-      if (rb * 32 > c0 + 7) continue;
-      float acc[8];
-#pragma unroll
-      for (int q = 0; q < 8; q++) acc[q] = 0.f;
-      const int ir = min(i, NB - 1);
-#pragma unroll 4
-      for (int p = 0; p < 32; p++) {
-        const float a = RT[ir * RTLD + p];
-#pragma unroll
-        for (int q = 0; q < 8; q++) acc[q] += a * RT[min(c0 + q, NB - 1) * RTLD + p];
-      }
-      if (i < mw) {
-#pragma unroll
-        for (int q = 0; q < 8; q++)
-          if (c0 + q < mw && i <= c0 + q) S[(m0 + i) + (m0 + c0 + q) * PLD] -= acc[q];
-      }
-    }
-    __syncthreads();
-  }
-  for (int e = t; e < NB * NB; e += 256) {
-    const int i = e % NB, j = e / NB;
-    if (i < jb && j < jb && i <= j) A[i + (int64_t)j * lda] = S[i + j * PLD];
-  }
-}
-
-// FP32 panel solve U_jj^T X = B in place (B = A(j0:j0+jb, j0+jb:n)), 256
-// columns per CTA: the tile is staged in shared memory with batched loads,
-// each thread solves its column in 32-row blocks (substitution within a
-// block, then the block's update of the rows below, whose accumulations are
-// independent), and the tile is written back coalesced.
-constexpr int TRSM_F32_COLS = 256;
-constexpr int SMEM_TRSM_F32 = (NB * PLD + PLD * TRSM_F32_COLS) * (int)sizeof(float);
-__global__ void __launch_bounds__(TRSM_F32_COLS) trsm_panel_f32(const float* __restrict__ Ujj, int64_t lda, int jb,
-                                                                int rest, float* __restrict__ B) {
-  extern __shared__ unsigned char smraw[];
-  float* U = (float*)smraw;  // jb x jb upper, ld PLD
-  float* Xt = U + NB * PLD;  // column c, row i at Xt[i + c * PLD] (odd stride: one bank per thread)
-  const int t = threadIdx.x, c0 = blockIdx.x * TRSM_F32_COLS;
-  const int ncol = min(TRSM_F32_COLS, rest - c0);
-  load_tile_f32(Ujj, lda, jb, jb, NB, U, PLD, 1);
-  load_tile_f32(B + (int64_t)c0 * lda, lda, jb, ncol, TRSM_F32_COLS, Xt, PLD, 0);
-  __syncthreads();
-  if (t < ncol) {
-    float* x = Xt + t * PLD;  // thread t owns column t
-    for (int q0 = 0; q0 < jb; q0 += 32) {
-      const int qw = min(32, jb - q0);
-      float v[32];
-#pragma unroll
-      for (int i = 0; i < 32; i++) {
-        float a = 0.f;
-        if (i < qw) {
-          a = x[q0 + i];
-#pragma unroll
-          for (int p = 0; p < i; p++) a -= U[(q0 + p) + (q0 + i) * PLD] * v[p];
-          a = a / U[(q0 + i) + (q0 + i) * PLD];
-        }
-        v[i] = a;
-      }
-#pragma unroll
-      for (int i = 0; i < 32; i++)
-        if (i < qw) x[q0 + i] = v[i];
-#pragma unroll 4
-      for (int i = q0 + qw; i < jb; i++) {
-        float a = x[i];
-#pragma unroll
-        for (int p = 0; p < 32; p++) a -= U[(q0 + p) + i * PLD] * v[p];  // U is zero past qw
-        x[i] = a;
-      }
-    }
-  }
-  __syncthreads();
-  for (int e = t; e < jb * ncol; e += TRSM_F32_COLS) {
-    const int i = e % jb, c = e / jb;
-    B[i + (int64_t)(c0 + c) * lda] = Xt[i + c * PLD];
   }
 }
 
@@ -994,8 +915,6 @@ int ensure_attrs(rsd_ctx* ctx) {
   RSD_CUDA(ctx, cudaFuncSetAttribute(trsv_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_trsv<T>()));
   RSD_CUDA(ctx, cudaFuncSetAttribute(trtri_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_potf2<T>(NB)));
   RSD_CUDA(ctx, cudaFuncSetAttribute(potf2_inv_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_POTF2_INV));
-  RSD_CUDA(ctx, cudaFuncSetAttribute(potf2_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_POTF2_F32));
-  RSD_CUDA(ctx, cudaFuncSetAttribute(trsm_panel_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TRSM_F32));
   done = true;
   return RSD_OK;
 }
@@ -1094,7 +1013,7 @@ int trailing_update(rsd_ctx* ctx, int tc, const T* P, int64_t ldp, int kb, int m
 // step of look-ahead: the next outer panel is factored on the side stream
 // once the first 512 rows of the trailing update have landed.
 constexpr int NBO = 512;
-int potrf_two_level_f32(rsd_ctx* ctx, int n, float* d_A, int64_t lda, int tc) {
+int potrf_two_level_f32(rsd_ctx* ctx, int n, float* d_A, int64_t lda, int tc, float* W) {
   cudaStream_t s = ctx->stream, s2 = ctx->side;
   RSD_CUDA(ctx, cudaEventRecord(ctx->ev_next, s));
   for (int J0 = 0; J0 < n; J0 += NBO) {
@@ -1105,10 +1024,12 @@ int potrf_two_level_f32(rsd_ctx* ctx, int n, float* d_A, int64_t lda, int tc) {
       float* Ajj = d_A + j0 + (int64_t)j0 * lda;
       const int rest = n - j0 - jb;
       float* Apan = d_A + j0 + (int64_t)(j0 + jb) * lda;
-      potf2_f32<<<1, 256, SMEM_POTF2_F32, s2>>>(Ajj, lda, jb, ctx->d_info, j0); RSD_LAUNCH_NOTE();
+      float* Wb = W + (size_t)(j0 / NB) * NB * NB;
+      potf2_inv_f32<<<1, 256, SMEM_POTF2_INV, s2>>>(Ajj, lda, jb, ctx->d_info, j0, Wb); RSD_LAUNCH_NOTE();
       if (rest <= 0) continue;
-      trsm_panel_f32<<<(rest + TRSM_F32_COLS - 1) / TRSM_F32_COLS, TRSM_F32_COLS, SMEM_TRSM_F32, s2>>>(
-          Ajj, lda, jb, rest, Apan); RSD_LAUNCH_NOTE();
+      // row panel U_jj^-T B = W_jj^T B in place on tensor cores (each output
+      // tile reads only its own columns of B)
+      RSD_TRY(rsd_tc_gemm(ctx, tc, jb, rest, jb, 1.0f, Wb, NB, Apan, lda, Apan, lda, 0, 0, 0, ctx->d_info + 1, s2));
       const int m_in = J0 + JB - (j0 + jb);  // rows of this outer panel still to update
       if (m_in > 0)
         RSD_TRY(rsd_tc_gemm(ctx, tc, m_in, rest, jb, -1.0f, Apan, lda, Apan, lda, Apan + jb, lda, 1, 1, 0,
@@ -1155,7 +1076,7 @@ int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const
   if constexpr (F32) two_level = tc && ctx->use_tc && rsd_tc_syrk_ok(d_A, lda, d_A, lda, NB);
   if constexpr (F32) {
     if (two_level) {
-      RSD_TRY(potrf_two_level_f32(ctx, n, d_A, lda, tc));
+      RSD_TRY(potrf_two_level_f32(ctx, n, d_A, lda, tc, W));
       goto done;
     }
   }
@@ -1196,9 +1117,9 @@ int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const
     }
   }
 done:
-  // diagonal-block inverses for the solves; the single-level FP32 path made
-  // them with its diagonal blocks, the others take them here
-  if (!F32 || two_level) {
+  // diagonal-block inverses for the solves; the FP32 paths made them with
+  // their diagonal blocks, the FP64 one takes them here
+  if (!F32) {
     const int nblk = (n + NB - 1) / NB;
     trtri_diag<T><<<nblk, 256, smem_potf2<T>(NB), s>>>(n, d_A, lda, W); RSD_LAUNCH_NOTE();
   }

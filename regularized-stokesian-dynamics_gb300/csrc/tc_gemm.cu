@@ -40,9 +40,13 @@ constexpr int TC_CHUNK = TC_TILE * TC_KC * 4;  // one operand chunk: 16 KB
 constexpr int TC_THREADS = 192;
 constexpr unsigned long long TC_WAIT_NS = 500ull * 1000 * 1000;  // 0.5 s per wait
 
+// PREC 1: three 32 KB stages, so that two CTAs share an SM and one CTA's
+// epilogue (TMEM -> shared -> TMA store) overlaps the other's main loop;
+// PREC 3: three 64 KB stages (heads and tails), one CTA per SM.
 template <int PREC>
 struct TcCfg {
-  static constexpr int STAGES = PREC == 1 ? 6 : 3;
+  static constexpr int STAGES = 3;
+  static constexpr int MIN_CTAS = PREC == 1 ? 2 : 1;
   static constexpr int STAGE_BYTES = (PREC == 1 ? 2 : 4) * TC_CHUNK;
   static constexpr int BAR_BYTES = (3 * STAGES + 1) * 8 + 16;
   static constexpr int SMEM = STAGES * STAGE_BYTES + BAR_BYTES + 1024;
@@ -141,7 +145,7 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
 }
 
 template <int PREC>
-__global__ void __launch_bounds__(TC_THREADS, 1)
+__global__ void __launch_bounds__(TC_THREADS, TcCfg<PREC>::MIN_CTAS)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    const __grid_constant__ CUtensorMap tmC, const TcArgs a) {
   using Cfg = TcCfg<PREC>;
