@@ -1181,6 +1181,7 @@ __global__ void put_diag_transposed(int jb, const float* __restrict__ Wb, float*
 // throughout: T1^T = U(0:j0, jblk)^T WT(0:j0, 0:j0) over k >= m, then
 // WT(jblk, 0:j0) = -W_jj^T T1^T), and A^-1 = W W^T = WT^T WT over k >= the
 // tile's column.  prec 1 (TF32) or 3 (3xTF32).
+constexpr int POTRI_KSPLIT = 1024;
 int potri_tc_s(rsd_ctx* ctx, int prec, int n, float* d_A, int64_t lda, const char* tag) {
   cudaStream_t s = ctx->stream;
   float* W = nullptr;
@@ -1197,7 +1198,15 @@ int potri_tc_s(rsd_ctx* ctx, int prec, int n, float* d_A, int64_t lda, const cha
     const float* Wb = W + (size_t)b * NB * NB;
     put_diag_transposed<<<(jb * jb + 255) / 256, 256, 0, s>>>(jb, Wb, WT + j0 + (int64_t)j0 * ldw, ldw); RSD_LAUNCH_NOTE();
     if (j0 == 0) continue;
-    RSD_TRY(rsd_tc_gemm(ctx, prec, jb, j0, j0, 1.0f, d_A + (int64_t)j0 * lda, lda, WT, ldw, T1, NB, 0, 0, 1, err));
+    // long K ranges are split across CTAs (their partial products added
+    // into the zeroed T1), so that a step does not wait on its longest tile
+    if (j0 > POTRI_KSPLIT) {
+      RSD_CUDA(ctx, cudaMemsetAsync(T1, 0, sizeof(float) * (size_t)NB * j0, s));
+      RSD_TRY(rsd_tc_gemm(ctx, prec, jb, j0, j0, 1.0f, d_A + (int64_t)j0 * lda, lda, WT, ldw, T1, NB, 1, 0, 1, err, s,
+                          POTRI_KSPLIT));
+    } else {
+      RSD_TRY(rsd_tc_gemm(ctx, prec, jb, j0, j0, 1.0f, d_A + (int64_t)j0 * lda, lda, WT, ldw, T1, NB, 0, 0, 1, err));
+    }
     RSD_TRY(rsd_tc_gemm(ctx, prec, jb, j0, jb, -1.0f, Wb, NB, T1, NB, WT + j0, ldw, 0, 0, 0, err));
   }
   RSD_TRY(rsd_tc_gemm(ctx, prec, n, n, n, 1.0f, WT, ldw, WT, ldw, d_A, lda, 0, 1, 1, err));

@@ -157,7 +157,7 @@ int rsd_axpy_block(rsd_ctx* ctx, int64_t rows, int64_t cols, const double* B, in
 int rsd_tc_gemm_ok(const float* A, int64_t lda, const float* B, int64_t ldb, const float* C, int64_t ldc);
 int rsd_tc_gemm(rsd_ctx* ctx, int prec, int m, int n, int K, float alpha, const float* A, int64_t lda,
                 const float* B, int64_t ldb, float* C, int64_t ldc, int reduce, int tri, int klo_col, int* d_err,
-                cudaStream_t stream = 0);
+                cudaStream_t stream = 0, int ksplit = 0);
 int rsd_tc_syrk_ok(const float* panel, int64_t lda, const float* C, int64_t ldc, int kb);
 int rsd_tc_syrk(rsd_ctx* ctx, int prec, const float* panel, int64_t lda, int kb, int rest, float* C, int64_t ldc,
                 int* d_err);

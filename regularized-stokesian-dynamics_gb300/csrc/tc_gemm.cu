@@ -59,6 +59,7 @@ struct TcArgs {
   int tri;       // skip tiles with row0 > col0
   int klo_col;   // K range of a tile starts at its first column
   int reduce;    // 1: C += alpha D (reduce-add), 0: C = alpha D (store)
+  int ksplit;    // > 0: CTA z sums K in [z ksplit, (z + 1) ksplit) (a multiple of TC_KC; reduce = 1)
   float alpha;
   int* err;
 };
@@ -152,8 +153,12 @@ __global__ void __launch_bounds__(TC_THREADS, TcCfg<PREC>::MIN_CTAS)
   constexpr int ST = Cfg::STAGES, SB = Cfg::STAGE_BYTES;
   const int row0 = blockIdx.x * TC_TILE, col0 = blockIdx.y * TC_TILE;
   if (a.tri && row0 > col0) return;
-  const int klo = a.klo_col ? col0 : 0;
-  const int nch = a.K > klo ? (a.K - klo + TC_KC - 1) / TC_KC : 0;
+  int klo = a.klo_col ? col0 : 0, khi = a.K;
+  if (a.ksplit > 0) {
+    klo = max(klo, (int)blockIdx.z * a.ksplit);
+    khi = min(khi, ((int)blockIdx.z + 1) * a.ksplit);
+  }
+  const int nch = khi > klo ? (khi - klo + TC_KC - 1) / TC_KC : 0;
 
   extern __shared__ unsigned char smraw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
@@ -373,20 +378,23 @@ int rsd_tc_gemm_ok(const float* A, int64_t lda, const float* B, int64_t ldb, con
 // (reduce = 1) on the 128-tiles of C, with A (K x m, ld lda) and B (K x n,
 // ld ldb) column-major.  tri: only tiles on and above the diagonal.
 // klo_col: the K range of the tile at column col0 is [col0, K).  prec: 1
-// (TF32) or 3 (3xTF32).  d_err receives a nonzero code if a wait timed out.
-// stream: 0 for the context's stream.
+// (TF32) or 3 (3xTF32).  ksplit > 0 (a multiple of 32, reduce = 1 only):
+// the K range is cut into slices of that length, one CTA per tile and
+// slice, each adding its partial product into C.  d_err receives a nonzero
+// code if a wait timed out.  stream: 0 for the context's stream.
 int rsd_tc_gemm(rsd_ctx* ctx, int prec, int m, int n, int K, float alpha, const float* A, int64_t lda,
                 const float* B, int64_t ldb, float* C, int64_t ldc, int reduce, int tri, int klo_col, int* d_err,
-                cudaStream_t stream) {
-  if (m < 1 || n < 1 || K < 1 || (prec != 1 && prec != 3) || !rsd_tc_gemm_ok(A, lda, B, ldb, C, ldc))
+                cudaStream_t stream, int ksplit) {
+  if (m < 1 || n < 1 || K < 1 || (prec != 1 && prec != 3) || !rsd_tc_gemm_ok(A, lda, B, ldb, C, ldc) ||
+      ksplit < 0 || ksplit % TC_KC != 0 || (ksplit > 0 && !reduce))
     return rsd_fail(ctx, RSD_EARG, "tc_gemm: unsupported arguments (m=%d n=%d K=%d prec=%d)", m, n, K, prec);
   RSD_TRY(tc_init(ctx));
   CUtensorMap tmA, tmB, tmC;
   RSD_TRY(encode_2d(ctx, &tmA, A, K, m, lda, TC_KC, TC_TILE, CU_TENSOR_MAP_SWIZZLE_128B));
   RSD_TRY(encode_2d(ctx, &tmB, B, K, n, ldb, TC_KC, TC_TILE, CU_TENSOR_MAP_SWIZZLE_128B));
   RSD_TRY(encode_2d(ctx, &tmC, C, m, n, ldc, TC_TILE, TC_TILE, CU_TENSOR_MAP_SWIZZLE_NONE));
-  TcArgs a{K, tri, klo_col, reduce, alpha, d_err};
-  const dim3 grid((m + TC_TILE - 1) / TC_TILE, (n + TC_TILE - 1) / TC_TILE);
+  TcArgs a{K, tri, klo_col, reduce, ksplit, alpha, d_err};
+  const dim3 grid((m + TC_TILE - 1) / TC_TILE, (n + TC_TILE - 1) / TC_TILE, ksplit > 0 ? (K + ksplit - 1) / ksplit : 1);
   cudaStream_t st = stream ? stream : ctx->stream;
   if (prec == 1) {
     tc_gemm_kernel<1><<<grid, TC_THREADS, TcCfg<1>::SMEM, st>>>(tmA, tmB, tmC, a);
