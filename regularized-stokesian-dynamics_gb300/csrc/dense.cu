@@ -43,6 +43,8 @@ struct GemmP {
   int offA;
   int kB_col;  // op(B)(p,c) = 0 for p < c + offB: start k at col0 + offB
   int offB;
+  int batch;              // > 1: blockIdx.z = b runs the same product on A + b sA, B + b sB, C + b sC
+  int64_t sA, sB, sC;     // batch strides in elements
 };
 
 // C = alpha op(A) op(B) + beta C, one BM x BN tile per CTA of 256 threads
@@ -61,8 +63,8 @@ __global__ void __launch_bounds__(256) gemm_kernel(GemmP g) {
   __shared__ T As[2][BK][BM + 1];
   __shared__ T Bs[2][BK][BN + 1];
   const int t = threadIdx.x, tx = t % 16, ty = t / 16;
-  const T* A = (const T*)g.A;
-  const T* B = (const T*)g.B;
+  const T* A = (const T*)g.A + blockIdx.z * g.sA;
+  const T* B = (const T*)g.B + blockIdx.z * g.sB;
   T ra[LA], rb[LB];
   auto load = [&](int k0) {
 #pragma unroll
@@ -142,7 +144,7 @@ __global__ void __launch_bounds__(256) gemm_kernel(GemmP g) {
     __syncthreads();
     buf ^= 1;
   }
-  T* C = (T*)g.C;
+  T* C = (T*)g.C + blockIdx.z * g.sC;
   const T alpha = (T)g.alpha, beta = (T)g.beta;
 #pragma unroll
   for (int i = 0; i < TM; i++)
@@ -173,8 +175,8 @@ __global__ void __launch_bounds__(256) sgemm_vec(GemmP g) {
   __shared__ __align__(16) float As[2][BK][BM];
   __shared__ __align__(16) float Bs[2][BK][BN];
   const int t = threadIdx.x, tx = t % 16, ty = t / 16;
-  const float* A = (const float*)g.A;
-  const float* B = (const float*)g.B;
+  const float* A = (const float*)g.A + blockIdx.z * g.sA;
+  const float* B = (const float*)g.B + blockIdx.z * g.sB;
   float4 ra, rb;
   // op(A) tile element coordinates of this thread's float4
   int ai, ap, bc, bp;
@@ -289,7 +291,7 @@ __global__ void __launch_bounds__(256) sgemm_vec(GemmP g) {
     __syncthreads();
     buf ^= 1;
   }
-  float* C = (float*)g.C;
+  float* C = (float*)g.C + blockIdx.z * g.sC;
   const float alpha = (float)g.alpha, beta = (float)g.beta;
 #pragma unroll
   for (int j = 0; j < 8; j++) {
@@ -334,13 +336,15 @@ struct Tile<float> {
 template <typename T>
 void launch_gemm(cudaStream_t s, const GemmP& g) {
   if (g.m <= 0 || g.n <= 0) return;
-  if (sizeof(T) == 4 && aligned16(g.A, g.lda) && aligned16(g.B, g.ldb) && aligned16(g.C, g.ldc)) {
-    dim3 grd((g.m + 127) / 128, (g.n + 127) / 128);
+  const unsigned nb = g.batch > 1 ? (unsigned)g.batch : 1u;
+  const bool strides16 = (g.sA % 4 == 0) && (g.sB % 4 == 0) && (g.sC % 4 == 0);
+  if (sizeof(T) == 4 && strides16 && aligned16(g.A, g.lda) && aligned16(g.B, g.ldb) && aligned16(g.C, g.ldc)) {
+    dim3 grd((g.m + 127) / 128, (g.n + 127) / 128, nb);
     sgemm_vec<<<grd, 256, 0, s>>>(g); RSD_LAUNCH_NOTE();
     return;
   }
   constexpr int BM = Tile<T>::BM, BN = Tile<T>::BN, BK = Tile<T>::BK;
-  dim3 grd((g.m + BM - 1) / BM, (g.n + BN - 1) / BN);
+  dim3 grd((g.m + BM - 1) / BM, (g.n + BN - 1) / BN, nb);
   gemm_kernel<T, BM, BN, BK><<<grd, 256, 0, s>>>(g); RSD_LAUNCH_NOTE();
 }
 
@@ -1256,9 +1260,55 @@ __global__ void copy_upper_block(int jb, const float* __restrict__ U, int64_t ld
   D[t] = (i < jb && j < jb && i <= j) ? U[i + (int64_t)j * ldu] : (i == j ? 1.0f : 0.0f);
 }
 
+// The full NB2 diagonal blocks of U (blockIdx.z = block) into D (one
+// NB2 x NB2 block each, lower part zero).
+__global__ void copy_upper_blocks(const float* __restrict__ U, int64_t ldu, float* __restrict__ D) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.z;
+  if (t >= NB2 * NB2) return;
+  const int i = t % NB2, j = t / NB2;
+  const int64_t o = (int64_t)b * NB2;
+  D[(size_t)b * NB2 * NB2 + t] = i <= j ? U[(o + i) + (o + j) * ldu] : 0.0f;
+}
+
+// D_b(j0:j0+NB, j0:j0+NB) = W_{b NB2/NB + j0/NB} for every block b = blockIdx.z
+__global__ void put_diag_blocks(int j0, const float* __restrict__ W, float* __restrict__ D) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.z;
+  if (t >= NB * NB) return;
+  const int i = t % NB, j = t / NB;
+  D[(size_t)b * NB2 * NB2 + (j0 + i) + (int64_t)(j0 + j) * NB2] = W[((size_t)b * (NB2 / NB) + j0 / NB) * NB * NB + t];
+}
+
+// In-place inverses of nblk upper triangular NB2 x NB2 blocks D_b (ld NB2,
+// stride NB2^2) from their NB diagonal-block inverses: trtri_inplace_t on
+// all blocks at once, one batched GEMM pair per NB column block.
+int trtri_wide_batched_s(rsd_ctx* ctx, int nblk, float* D, const float* W, float* T1) {
+  cudaStream_t s = ctx->stream;
+  for (int j0 = 0; j0 < NB2; j0 += NB) {
+    if (j0 > 0) {
+      GemmP g = gp(j0, NB, j0, 1.0, D, NB2, 0, D + (int64_t)j0 * NB2, NB2, 0, 0.0, T1, NB2);
+      g.kA_row = 1;
+      g.offA = 0;
+      g.batch = nblk;
+      g.sA = g.sB = (int64_t)NB2 * NB2;
+      g.sC = (int64_t)NB2 * NB;
+      launch_gemm<float>(s, g);
+      GemmP g2 = gp(j0, NB, NB, -1.0, T1, NB2, 0, W + (size_t)(j0 / NB) * NB * NB, NB, 0, 0.0,
+                    D + (int64_t)j0 * NB2, NB2);
+      g2.batch = nblk;
+      g2.sA = (int64_t)NB2 * NB;
+      g2.sB = (int64_t)(NB2 / NB) * NB * NB;
+      g2.sC = (int64_t)NB2 * NB2;
+      launch_gemm<float>(s, g2);
+    }
+    put_diag_blocks<<<dim3(NB * NB / 256, 1, nblk), 256, 0, s>>>(j0, W, D); RSD_LAUNCH_NOTE();
+  }
+  return RSD_OK;
+}
+
 // W128 (optional): the NB x NB diagonal-block inverses that the FP32 potrf
-// of U left (NB-block b at W128 + b NB^2); full NB2 blocks then start from
-// them instead of inverting their NB blocks again.
+// of U left (NB-block b at W128 + b NB^2); the full NB2 blocks then start
+// from them (all blocks in one batched pass) instead of inverting their NB
+// blocks again.
 int rsd_wide_inverses_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const char* tag, const float* W128,
                         float** W2out) {
   const int nblk2 = (n + NB2 - 1) / NB2;
@@ -1268,7 +1318,16 @@ int rsd_wide_inverses_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const 
   float* T1 = (float*)rsd_scratch(ctx, "wide_T1", sizeof(float) * (size_t)NB * NB2);
   if (!W2 || !Wt || !T1) return RSD_ENOMEM;
   RSD_TRY(ensure_attrs<float>(ctx));
-  for (int b = 0; b < nblk2; b++) {
+  int b0 = 0;
+  if (W128 && n >= NB2) {
+    const int full = n / NB2;
+    float* Tb = (float*)rsd_scratch(ctx, "wide_T1b", sizeof(float) * (size_t)full * NB * NB2);
+    if (!Tb) return RSD_ENOMEM;
+    copy_upper_blocks<<<dim3(NB2 * NB2 / 256, 1, full), 256, 0, ctx->stream>>>(U, ldu, W2); RSD_LAUNCH_NOTE();
+    RSD_TRY(trtri_wide_batched_s(ctx, full, W2, W128, Tb));
+    b0 = full;
+  }
+  for (int b = b0; b < nblk2; b++) {
     const int j0 = b * NB2, jb = n - j0 < NB2 ? n - j0 : NB2;
     float* D = W2 + (size_t)b * NB2 * NB2;
     copy_upper_block<<<(NB2 * NB2 + 255) / 256, 256, 0, ctx->stream>>>(jb, U + j0 + (int64_t)j0 * ldu, ldu, D); RSD_LAUNCH_NOTE();
