@@ -105,6 +105,48 @@ DSF_FN dsf& operator+=(dsf& a, dsf b) {
 
 DSF_FN dsf fma(dsf a, dsf b, dsf c) { return a * b + c; }
 
+// Unnormalised double-single accumulator: hi is the FP32 running sum and lo
+// collects the exact rounding error of every addition into hi (Knuth's
+// two-sum) and the error of every product (Dekker's product through FMAs),
+// so an accumulate costs 12 FP32 operations instead of 18.  lo is a plain
+// FP32 sum, so it grows by about ulp(hi) per step and its own rounding with
+// it: renormalise (dsacc_norm, 3 operations) every few steps (at most 16)
+// to keep hi + lo within ~2^-47 of the exact sum of the magnitudes added.
+struct dsacc {
+  float hi, lo;
+  DSF_FN dsacc() {}
+  DSF_FN dsacc(float h, float l) : hi(h), lo(l) {}
+  DSF_FN dsacc(int v) : hi((float)v), lo(0.f) {}
+};
+
+// c + a b
+DSF_FN dsacc fma(dsf a, dsf b, dsacc c) {
+  const float p = DSF_MUL(a.hi, b.hi);
+  float pe = DSF_FMA(a.hi, b.hi, -p);
+  pe = DSF_FMA(a.hi, b.lo, DSF_FMA(a.lo, b.hi, pe));
+  const float s = DSF_ADD(c.hi, p);
+  const float bb = DSF_SUB(s, c.hi);
+  const float e = DSF_ADD(DSF_SUB(c.hi, DSF_SUB(s, bb)), DSF_SUB(p, bb));
+  return dsacc(s, DSF_ADD(c.lo, DSF_ADD(e, pe)));
+}
+
+DSF_FN dsacc& operator+=(dsacc& c, dsf v) {
+  const float s = DSF_ADD(c.hi, v.hi);
+  const float bb = DSF_SUB(s, c.hi);
+  const float e = DSF_ADD(DSF_SUB(c.hi, DSF_SUB(s, bb)), DSF_SUB(v.hi, bb));
+  c.lo = DSF_ADD(c.lo, DSF_ADD(e, v.lo));
+  c.hi = s;
+  return c;
+}
+
+DSF_FN void dsacc_norm(dsacc& c) {
+  const float s = DSF_ADD(c.hi, c.lo);
+  c.lo = DSF_SUB(c.lo, DSF_SUB(s, c.hi));
+  c.hi = s;
+}
+
+DSF_FN double dsacc_to(dsacc a) { return (double)a.hi + (double)a.lo; }
+
 // sqrt(a), a > 0
 DSF_FN dsf dsf_sqrt(dsf a) {
   const float s = DSF_SQRT(a.hi);

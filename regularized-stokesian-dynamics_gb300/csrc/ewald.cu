@@ -438,6 +438,9 @@ __global__ void ewald_kblock_list(rsd_lat_dev L, int count, const int* __restric
   for (int i = 60; i < KBW; i++) put_weight<T>(e + i, 0.0);
 }
 
+__device__ __forceinline__ void acc_norm(float&) {}
+__device__ __forceinline__ void acc_norm(dsacc& a) { dsacc_norm(a); }
+
 __device__ __forceinline__ float trig_c(float2 v) { return v.x; }
 __device__ __forceinline__ float trig_s(float2 v) { return v.y; }
 __device__ __forceinline__ dsf trig_c(float4 v) { return dsf(v.x, v.y); }
@@ -447,9 +450,9 @@ __device__ __forceinline__ dsf trig_s(float4 v) { return dsf(v.z, v.w); }
 // acc, for the pair (a, b) of the calling thread (block 32 x 4).  The
 // weights of 16 vectors and the trig values of the CTA's 32 + 4 particles
 // are staged in shared memory (sw: 16 x KBW, sca: 16 x 32, scb: 16 x 4).
-template <typename T, typename TT>
+template <typename T, typename TT, typename A>
 __device__ __forceinline__ void kblock_accumulate(int nn, int Kh, const T* __restrict__ W, const TT* __restrict__ cs,
-                                                  T* sw, TT* sca, TT* scb, bool valid, T (&acc)[60]) {
+                                                  T* sw, TT* sca, TT* scb, bool valid, A (&acc)[60]) {
   constexpr int KC = 16;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
   const int a0 = blockIdx.x * blockDim.x, b0 = blockIdx.y * blockDim.y;
@@ -478,6 +481,8 @@ __device__ __forceinline__ void kblock_accumulate(int nn, int Kh, const T* __res
 #pragma unroll
       for (int q = 0; q < 60; q++) acc[q] = fma(e[q], kblock_is_sin(q) ? sn : c, acc[q]);
     }
+#pragma unroll
+    for (int q = 0; q < 60; q++) acc_norm(acc[q]);  // at most 16 steps between renormalisations
   }
 }
 
@@ -495,7 +500,7 @@ __global__ void __launch_bounds__(128) ewald_pair_kblock(int nn, int K32, const 
   if ((int)(blockIdx.x * blockDim.x) >= (int)(blockIdx.y * blockDim.y + blockDim.y - 1)) return;
   int a, b;
   const bool valid = pair_of(nn, &a, &b);
-  dsf acc[60];
+  dsacc acc[60];
   {
     float f[60];
 #pragma unroll
@@ -503,13 +508,13 @@ __global__ void __launch_bounds__(128) ewald_pair_kblock(int nn, int K32, const 
     kblock_accumulate<float, float2>(nn, K32, W32, c32, reinterpret_cast<float*>(sw),
                                      reinterpret_cast<float2*>(sca), reinterpret_cast<float2*>(scb), valid, f);
 #pragma unroll
-    for (int q = 0; q < 60; q++) acc[q] = dsf(f[q], 0.f);
+    for (int q = 0; q < 60; q++) acc[q] = dsacc(f[q], 0.f);
   }
   kblock_accumulate<dsf, float4>(nn, K64, W64, c64, sw, sca, scb, valid, acc);
   if (!valid) return;
   double o[60];
 #pragma unroll
-  for (int q = 0; q < 60; q++) o[q] = dsf_to(acc[q]);
+  for (int q = 0; q < 60; q++) o[q] = dsacc_to(acc[q]);
   scale_block(o, radii[a], inv_pimu);
   store_pair(M, ldm, nn, a, b, o, add);
 }
@@ -599,9 +604,10 @@ __global__ void __launch_bounds__(128) ewald_pair_real_near_ds(int nn, rsd_lat_d
   double R[3] = {pos[3 * a] - pos[3 * b], pos[3 * a + 1] - pos[3 * b + 1], pos[3 * a + 2] - pos[3 * b + 2]};
   double dmin;
   rsd_skew_correction(L.LR, L.LI, R, &dmin);
-  dsf acc[RSD_NMOM_REAL];
+  dsacc acc[RSD_NMOM_REAL];
 #pragma unroll
-  for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = dsf(0);
+  for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = dsacc(0);
+  int since_norm = 0;
   const dsf lam_s = dsf_from(L.lam), cd_s = dsf_from(2.0 * RSD_PIP5 * L.lam);
   const dsf a30 = dsf_from(L.LR[6]), a31 = dsf_from(L.LR[7]), a32 = dsf_from(L.LR[8]);
   const float a0 = __double2float_rn(L.LR[6]), a1 = __double2float_rn(L.LR[7]), a2 = __double2float_rn(L.LR[8]);
@@ -621,12 +627,17 @@ __global__ void __launch_bounds__(128) ewald_pair_real_near_ds(int nn, rsd_lat_d
         const dsf ir = dsf_rcp(r);
         dsf E0, G;
         dsf_erfc_gauss(lam_s * r, T, &E0, &G);
-        rsd_real_image<dsf>(x0, x1, x2, r, ir, E0, cd_s * G, lam_s, acc);
+        rsd_real_image<dsf, dsacc>(x0, x1, x2, r, ir, E0, cd_s * G, lam_s, acc);
+        if (++since_norm == 4) {  // keep the accumulators' lo parts small
+#pragma unroll
+          for (int m = 0; m < RSD_NMOM_REAL; m++) dsacc_norm(acc[m]);
+          since_norm = 0;
+        }
       }
     }
   double accd[RSD_NMOM_REAL];
 #pragma unroll
-  for (int m = 0; m < RSD_NMOM_REAL; m++) accd[m] = dsf_to(acc[m]);
+  for (int m = 0; m < RSD_NMOM_REAL; m++) accd[m] = dsacc_to(acc[m]);
   double v[60];
   rsd_real_epilogue<double>(accd, radii[a], radii[b], L.phix, v);
   scale_block(v, radii[a], inv_pimu);

@@ -326,10 +326,11 @@ def gen():
     monos = sorted({xm for _, xm in mom_r if sum(xm) > 0}, key=lambda t: (sum(t), t))
     L.append("")
     L.append("// Adds one real-space image at separation (x0,x1,x2), r = |x|, E0 = erfc(lam r),")
-    L.append("// Ed = 2 lam exp(-lam^2 r^2)/sqrt(pi); lam2..lam10 are powers of lam.")
-    L.append("template <typename T>")
+    L.append("// Ed = 2 lam exp(-lam^2 r^2)/sqrt(pi); lam2..lam10 are powers of lam.  A is the")
+    L.append("// accumulator type (T, or a wider accumulator with fma(T, T, A) and A += T).")
+    L.append("template <typename T, typename A = T>")
     L.append("__device__ __forceinline__ void rsd_real_image(T x0, T x1, T x2, T r, T ir, T E0, T Ed, T lam,")
-    L.append("                                               T* __restrict__ acc) {")
+    L.append("                                               A* __restrict__ acc) {")
     irs = sp.Symbol("ir")
     fexprs = []
     used = set()

@@ -38,3 +38,20 @@ extern "C" void dsf_check_ops(double a, double b, double c, double out[2]) {
   out[0] = dsf_to(fma(dsf_from(a), dsf_from(b), dsf_from(c)));
   out[1] = dsf_to(dsf_from(a) - dsf_from(b));
 }
+
+// sum_i a_i b_i + sum_i c_i, n terms each, through the unnormalised
+// accumulator (the products first, then the plain additions), renormalised
+// every `every` steps
+extern "C" double dsf_check_accumulate(int n, const double* a, const double* b, const double* c, int every) {
+  dsacc s(0);
+  int k = 0;
+  for (int i = 0; i < n; i++) {
+    s = fma(dsf_from(a[i]), dsf_from(b[i]), s);
+    if (++k == every) dsacc_norm(s), k = 0;
+  }
+  for (int i = 0; i < n; i++) {
+    s += dsf_from(c[i]);
+    if (++k == every) dsacc_norm(s), k = 0;
+  }
+  return dsacc_to(s);
+}

@@ -1,7 +1,9 @@
 """Double-single arithmetic and elementary functions (csrc/dsf.cuh) against
 40-digit mpmath, on the host build of the same header.
 
-Tolerances (relative): products/sums and sqrt, 1/x 2e-14 (a handful of
+Tolerances (relative): products/sums and sqrt, 1/x 2e-14; the unnormalised
+accumulator (dsacc, renormalised every 4 or 16 steps) 1e-14 of the sum of
+the magnitudes added (a handful of
 roundings at 2^-48 in the worst case; the median is ~5e-16); exp(y) on [-36, 0] 8e-15 (1 + |y|)
 and erfc(x), exp(-x^2) on [0, 6) 1.5e-14 (1 + x^2): exp amplifies the
 double-single rounding of its argument by |y| (the near-image Ewald sums use
@@ -33,6 +35,9 @@ def lib(tmp_path_factory):
     L.dsf_check_exp_neg.restype = ctypes.c_double
     L.dsf_check_sqrt_rcp.argtypes = [ctypes.c_double, d2]
     L.dsf_check_ops.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, d2]
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.dsf_check_accumulate.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_int]
+    L.dsf_check_accumulate.restype = ctypes.c_double
     L.d2 = d2
     return L
 
@@ -84,3 +89,27 @@ def test_sqrt_rcp_and_ops(lib):
         wd = max(wd, float(abs(mp.mpf(out[1]) - (q(a) - q(b))) / (abs(q(a)) + abs(q(b)))))
     assert ws <= 2e-14 and wr <= 2e-14, (ws, wr)
     assert wf <= 2e-14 and wd <= 2e-14, (wf, wd)
+
+
+@pytest.mark.parametrize("every", [4, 16])
+@pytest.mark.parametrize("n", [1, 7, 300, 5000])
+def test_unnormalised_accumulator(lib, n, every):
+    """sum a_i b_i + sum c_i through dsacc renormalised every 4 (the
+    near-image sums) or 16 (the reciprocal sums) steps: error below 1e-14 of
+    sum |terms|, also when the sum cancels to a small fraction of its
+    terms."""
+    mp.mp.dps = 50
+    rng = np.random.default_rng(11 + n)
+    for trial in range(4):
+        a = rng.normal(size=n) * np.exp(rng.uniform(-6, 6, n))
+        b = rng.normal(size=n)
+        c = rng.normal(size=n) * np.exp(rng.uniform(-6, 6, n))
+        if trial == 3:  # cancelling sum
+            c = -a * b + 1e-9 * rng.normal(size=n)
+        q = lambda v: mp.mpf(float(np.float32(v))) + mp.mpf(float(np.float32(v - float(np.float32(v)))))
+        terms = [q(x) * q(y) for x, y in zip(a, b)] + [q(z) for z in c]
+        exact = mp.fsum(terms)
+        scale = mp.fsum(abs(t) for t in terms)
+        ptr = lambda v: np.ascontiguousarray(v, dtype=np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        got = lib.dsf_check_accumulate(n, ptr(a), ptr(b), ptr(c), every)
+        assert float(abs(mp.mpf(got) - exact) / scale) <= 1e-14
