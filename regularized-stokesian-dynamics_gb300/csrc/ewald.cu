@@ -127,59 +127,99 @@ __global__ void ewald_trig_list(int nn, rsd_lat_dev L, const int* __restrict__ h
 // Scatter of the pair block (a,b), a < b, and its mirror (b,a) with
 // b -> -b, g -> -g (per_GRPY_YZD.f90:123-151,160-188).  v holds the 60
 // unique values (order of gen_ewald.py) already scaled; add != 0 adds.
-// Stores (add = 0) or read-modify-writes (add = 1) K entries of M.  All K
+// Destinations of the pair blocks.  DenseSink: the FP64 grand mobility
+// (column-major, ld).  PlaneSink: the mixed form's grand mobility as two
+// FP32 planes, M = hi + lo with |lo| <= ulp(hi)/2 (~48 bits, the precision
+// the mixed assembly computes in), read by the FP32 factorisation (hi) and
+// by the double-single residual products of the refinement (both).
+// put<K> stores (add = 0) or read-modify-writes (add = 1) K entries; all K
 // loads are issued before the first store, so a thread waits for one memory
-// round trip per group rather than one per entry (the addresses of a group
-// are distinct).
-template <int K>
-__device__ __forceinline__ void put_group(double* const* p, const double* x, int add) {
-  if (add) {
-    double o[K];
+// round trip per group rather than one per entry (the offsets of a group are
+// distinct).
+struct DenseSink {
+  double* M;
+  int64_t ld;
+  template <int K>
+  __device__ __forceinline__ void put(const int64_t* o, const double* x, int add) const {
+    if (add) {
+      double v[K];
 #pragma unroll
-    for (int i = 0; i < K; i++) o[i] = *p[i];
+      for (int i = 0; i < K; i++) v[i] = M[o[i]];
 #pragma unroll
-    for (int i = 0; i < K; i++) *p[i] = o[i] + x[i];
-  } else {
+      for (int i = 0; i < K; i++) M[o[i]] = v[i] + x[i];
+    } else {
 #pragma unroll
-    for (int i = 0; i < K; i++) *p[i] = x[i];
+      for (int i = 0; i < K; i++) M[o[i]] = x[i];
+    }
   }
-}
+};
+
+struct PlaneSink {
+  float* hi;
+  float* lo;
+  int64_t ld;
+  template <int K>
+  __device__ __forceinline__ void put(const int64_t* o, const dsf* x, int add) const {
+    if (add) {
+      float h[K], l[K];
+#pragma unroll
+      for (int i = 0; i < K; i++) {
+        h[i] = hi[o[i]];
+        l[i] = lo[o[i]];
+      }
+#pragma unroll
+      for (int i = 0; i < K; i++) {
+        const dsf v = dsf(h[i], l[i]) + x[i];
+        hi[o[i]] = v.hi;
+        lo[o[i]] = v.lo;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < K; i++) {
+        hi[o[i]] = x[i].hi;
+        lo[o[i]] = x[i].lo;
+      }
+    }
+  }
+};
 
 // Writes the pair blocks (a, b) and (b, a), a != b, of the grand mobility
 // from the 60 values of a pair (TT 0-5, RR 6-11, TR 12-14, QQ 15-29, G
-// 30-44, H 45-59), in 14 groups of at most 25 entries.
-__device__ inline void store_pair(double* __restrict__ M, int64_t ld, int N, int a, int b, const double* v, int add) {
-  auto at = [&](int r, int c) { return M + (int64_t)r + (int64_t)c * ld; };
+// 30-44, H 45-59), in 14 groups of at most 25 entries.  V: double
+// (DenseSink) or dsf (PlaneSink).
+template <typename V, typename S>
+__device__ inline void store_pair_t(const S& sk, int N, int a, int b, const V* v, int add) {
+  auto at = [&](int r, int c) { return (int64_t)r + (int64_t)c * sk.ld; };
   constexpr int sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
   // TT and RR, both orders
 #pragma unroll
   for (int blk = 0; blk < 2; blk++) {
     const int o = blk ? 3 * N : 0;
-    double* p[18];
-    double x[18];
+    int64_t p[18];
+    V x[18];
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int j = 0; j < 3; j++) {
-        const double t = v[6 * blk + sym[i][j]];
+        const V t = v[6 * blk + sym[i][j]];
         p[6 * i + 2 * j] = at(o + 3 * a + i, o + 3 * b + j);
         p[6 * i + 2 * j + 1] = at(o + 3 * b + i, o + 3 * a + j);
         x[6 * i + 2 * j] = x[6 * i + 2 * j + 1] = t;
       }
-    put_group<18>(p, x, add);
+    sk.template put<18>(p, x, add);
   }
   // TR: translation of one particle against rotation of the other, both
   // placements (upper and lower triangle) of each
 #pragma unroll
   for (int side = 0; side < 2; side++) {
     const int t = side ? b : a, r = side ? a : b;
-    double* p[18];
-    double x[18];
+    int64_t p[18];
+    V x[18];
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int j = 0; j < 3; j++) {
-        double tr = 0.0;
+        V tr = V(0);
         if (i < j) tr = v[12 + (i == 0 ? j - 1 : 2)];
         if (i > j) tr = -v[12 + (j == 0 ? i - 1 : 2)];
         if (side) tr = -tr;
@@ -187,33 +227,33 @@ __device__ inline void store_pair(double* __restrict__ M, int64_t ld, int N, int
         p[6 * i + 2 * j + 1] = at(3 * N + 3 * r + j, 3 * t + i);
         x[6 * i + 2 * j] = x[6 * i + 2 * j + 1] = tr;
       }
-    put_group<18>(p, x, add);
+    sk.template put<18>(p, x, add);
   }
   // G (translation-stresslet, odd under a <-> b) and H (rotation-stresslet)
 #pragma unroll
   for (int grp = 0; grp < 8; grp++) {
     const int side = grp >> 2, h = (grp >> 1) & 1, lower = grp & 1;
-    const int u = side ? b : a, s = side ? a : b;  // velocity row particle, stresslet column particle
+    const int u = side ? b : a, sp = side ? a : b;  // velocity row particle, stresslet column particle
     const int ro = h ? 3 * N : 0;
-    double* p[15];
-    double x[15];
+    int64_t p[15];
+    V x[15];
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int m = 0; m < 5; m++) {
-        double g = v[(h ? 45 : 30) + 5 * i + m];
+        V g = v[(h ? 45 : 30) + 5 * i + m];
         if (side && !h) g = -g;
-        p[5 * i + m] = lower ? at(6 * N + 5 * s + m, ro + 3 * u + i) : at(ro + 3 * u + i, 6 * N + 5 * s + m);
+        p[5 * i + m] = lower ? at(6 * N + 5 * sp + m, ro + 3 * u + i) : at(ro + 3 * u + i, 6 * N + 5 * sp + m);
         x[5 * i + m] = g;
       }
-    put_group<15>(p, x, add);
+    sk.template put<15>(p, x, add);
   }
   // QQ, both orders
 #pragma unroll
   for (int side = 0; side < 2; side++) {
     const int r = side ? b : a, c = side ? a : b;
-    double* p[25];
-    double x[25];
+    int64_t p[25];
+    V x[25];
 #pragma unroll
     for (int xi = 0; xi < 5; xi++)
 #pragma unroll
@@ -222,8 +262,19 @@ __device__ inline void store_pair(double* __restrict__ M, int64_t ld, int N, int
         p[5 * xi + y] = at(6 * N + 5 * r + xi, 6 * N + 5 * c + y);
         x[5 * xi + y] = v[15 + lo * 5 - lo * (lo - 1) / 2 + (hi - lo)];
       }
-    put_group<25>(p, x, add);
+    sk.template put<25>(p, x, add);
   }
+}
+
+// A pair block computed in FP64 into either destination.
+__device__ __forceinline__ void store_pair_d(const DenseSink& sk, int N, int a, int b, const double* o, int add) {
+  store_pair_t<double>(sk, N, a, b, o, add);
+}
+__device__ __forceinline__ void store_pair_d(const PlaneSink& sk, int N, int a, int b, const double* o, int add) {
+  dsf v[60];
+#pragma unroll
+  for (int q = 0; q < 60; q++) v[q] = dsf_from(o[q]);
+  store_pair_t<dsf>(sk, N, a, b, v, add);
 }
 
 // scale by nondim (1/(6 a_i) for TT, TR, G; 1/(6 a_i^3) for RR, QQ, H) and
@@ -259,10 +310,10 @@ struct Vec2<double> {
 // x_b) from the per-particle trig table, times the vector's 80 moment
 // weights.  The weights are staged in shared memory 16 vectors at a time and
 // read as 16-byte vectors (the same address for every thread of a warp).
-template <typename T, typename T2>
+template <typename T, typename T2, typename S>
 __global__ void __launch_bounds__(128) ewald_pair_k(int nn, rsd_lat_dev L, int Kh, const T* __restrict__ tab,
                                                     const T2* __restrict__ cs, const double* __restrict__ radii,
-                                                    double inv_pimu, double* __restrict__ M, int64_t ldm, int add) {
+                                                    double inv_pimu, S sk, int add) {
   constexpr int KWT = 3 + RSD_NMOM_KCOS + RSD_NMOM_KSIN;
   constexpr int NW = RSD_NMOM_KCOS + RSD_NMOM_KSIN;  // 80
   constexpr int KC = 16;
@@ -328,16 +379,17 @@ __global__ void __launch_bounds__(128) ewald_pair_k(int nn, rsd_lat_dev L, int K
 #pragma unroll
   for (int q = 0; q < 60; q++) o[q] = ((double)v[q] + (double)w[q]) * f;
   scale_block(o, radii[a], inv_pimu);
-  store_pair(M, ldm, nn, a, b, o, add);
+  store_pair_d(sk, nn, a, b, o, add);
 }
 
 // Reciprocal-space pair sums of the FP64 shells of the mixed form in
 // double-single: the trig table holds (cos, sin) as float pairs (float4 per
 // vector and particle), the weights are converted to float pairs as they are
 // staged in shared memory, and the epilogue runs in FP64.
+template <typename S>
 __global__ void __launch_bounds__(128) ewald_pair_k_ds(int nn, rsd_lat_dev L, int Kh, const double* __restrict__ tab,
                                                        const float4* __restrict__ cs, const double* __restrict__ radii,
-                                                       double inv_pimu, double* __restrict__ M, int64_t ldm, int add) {
+                                                       double inv_pimu, S sk, int add) {
   constexpr int KWT = 3 + RSD_NMOM_KCOS + RSD_NMOM_KSIN;
   constexpr int NW = RSD_NMOM_KCOS + RSD_NMOM_KSIN;
   constexpr int KC = 16;
@@ -395,7 +447,7 @@ __global__ void __launch_bounds__(128) ewald_pair_k_ds(int nn, rsd_lat_dev L, in
 #pragma unroll
   for (int q = 0; q < 60; q++) o[q] = (v[q] + w[q]) * f;
   scale_block(o, radii[a], inv_pimu);
-  store_pair(M, ldm, nn, a, b, o, add);
+  store_pair_d(sk, nn, a, b, o, add);
 }
 
 // ---------------------------------------------------- equal radii, k space
@@ -417,7 +469,7 @@ __device__ __forceinline__ void put_weight<dsf>(dsf* p, double v) { *p = dsf_fro
 
 template <typename T>
 __global__ void ewald_kblock_list(rsd_lat_dev L, int count, const int* __restrict__ hlist, double a,
-                                  T* __restrict__ W) {
+                                  double inv_pimu, T* __restrict__ W) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= count) return;
   int nx, ny, nz;
@@ -432,9 +484,13 @@ __global__ void ewald_kblock_list(rsd_lat_dev L, int count, const int* __restric
   rsd_ksin_weights<double>(k[0], k[1], k[2], S, L.lam, ws);
   rsd_kcos_epilogue<double>(wc, a, a, L.phix, v);
   rsd_ksin_epilogue<double>(ws, a, a, L.phix, w);
-  const double f = 2.0 / L.LV;  // half space counted twice
+  // half space counted twice, and the non-dimensionalisation of scale_block
+  const double f = 2.0 / L.LV, na = f * inv_pimu / (6.0 * a), na3 = na / (a * a);
   T* e = W + (size_t)q * KBW;
-  for (int i = 0; i < 60; i++) put_weight<T>(e + i, (kblock_is_sin(i) ? w[i] : v[i]) * f);
+  for (int i = 0; i < 60; i++) {
+    const bool a3 = (i >= 6 && i < 12) || (i >= 15 && i < 30) || i >= 45;
+    put_weight<T>(e + i, (kblock_is_sin(i) ? w[i] : v[i]) * (a3 ? na3 : na));
+  }
   for (int i = 60; i < KBW; i++) put_weight<T>(e + i, 0.0);
 }
 
@@ -492,8 +548,7 @@ __device__ __forceinline__ void kblock_accumulate(int nn, int Kh, const T* __res
 __global__ void __launch_bounds__(128) ewald_pair_kblock(int nn, int K32, const float* __restrict__ W32,
                                                          const float2* __restrict__ c32, int K64,
                                                          const dsf* __restrict__ W64, const float4* __restrict__ c64,
-                                                         const double* __restrict__ radii, double inv_pimu,
-                                                         double* __restrict__ M, int64_t ldm, int add) {
+                                                         PlaneSink sk, int add) {
   constexpr int KC = 16;
   __shared__ __align__(16) dsf sw[KC * KBW];  // the FP32 phase uses the first half as floats
   __shared__ __align__(16) float4 sca[KC * 32], scb[KC * 4];
@@ -512,11 +567,13 @@ __global__ void __launch_bounds__(128) ewald_pair_kblock(int nn, int K32, const 
   }
   kblock_accumulate<dsf, float4>(nn, K64, W64, c64, sw, sca, scb, valid, acc);
   if (!valid) return;
-  double o[60];
+  dsf o[60];
 #pragma unroll
-  for (int q = 0; q < 60; q++) o[q] = dsacc_to(acc[q]);
-  scale_block(o, radii[a], inv_pimu);
-  store_pair(M, ldm, nn, a, b, o, add);
+  for (int q = 0; q < 60; q++) {
+    dsacc_norm(acc[q]);
+    o[q] = dsf(acc[q].hi, acc[q].lo);
+  }
+  store_pair_t<dsf>(sk, nn, a, b, o, add);
 }
 
 // Near/far split of the real-space images for the mixed form.  Image nz of
@@ -547,10 +604,10 @@ __device__ __forceinline__ float image_r2f(float p0, float p1, float p2, float a
 // erfc(lambda r) feed moments that the epilogue combines with 2-3 orders of
 // cancellation, so FP32 is kept for images whose terms are below ~1e-6 of a
 // block (a few 1e-11 of a block after the epilogue).
+template <typename S>
 __global__ void __launch_bounds__(128) ewald_pair_real_far(int nn, rsd_lat_dev L, const double* __restrict__ pos,
                                                            const double* __restrict__ radii, double inv_pimu,
-                                                           double rc2, double rmax2, double* __restrict__ M,
-                                                           int64_t ldm) {
+                                                           double rc2, double rmax2, S sk) {
   int a, b;
   if (!pair_of(nn, &a, &b)) return;
   double R[3] = {pos[3 * a] - pos[3 * b], pos[3 * a + 1] - pos[3 * b + 1], pos[3 * a + 2] - pos[3 * b + 2]};
@@ -582,7 +639,7 @@ __global__ void __launch_bounds__(128) ewald_pair_real_far(int nn, rsd_lat_dev L
 #pragma unroll
   for (int q = 0; q < 60; q++) o[q] = (double)v[q];
   scale_block(o, radii[a], inv_pimu);
-  store_pair(M, ldm, nn, a, b, o, 1);
+  store_pair_d(sk, nn, a, b, o, 1);
 }
 
 // Near images of the mixed form (lambda r below the context's mixed_rcut) in
@@ -591,9 +648,10 @@ __global__ void __launch_bounds__(128) ewald_pair_real_far(int nn, rsd_lat_dev L
 // carry ~48 bits (so even after the epilogue's 2-3 orders of cancellation a
 // block stays within ~1e-12 of FP64); FP64 is left for the per-column set-up
 // and the FP64 epilogue.  Same image set as the FP32 far kernel's complement.
+template <typename S>
 __global__ void __launch_bounds__(128) ewald_pair_real_near_ds(int nn, rsd_lat_dev L, const double* __restrict__ pos,
                                                                const double* __restrict__ radii, double inv_pimu,
-                                                               double rc2, double* __restrict__ M, int64_t ldm) {
+                                                               double rc2, S sk) {
   __shared__ dsf_tables T;
   // blocks entirely on or below the diagonal (a >= b everywhere) have no work
   if ((int)(blockIdx.x * blockDim.x) >= (int)(blockIdx.y * blockDim.y + blockDim.y - 1)) return;
@@ -641,12 +699,190 @@ __global__ void __launch_bounds__(128) ewald_pair_real_near_ds(int nn, rsd_lat_d
   double v[60];
   rsd_real_epilogue<double>(accd, radii[a], radii[b], L.phix, v);
   scale_block(v, radii[a], inv_pimu);
-  store_pair(M, ldm, nn, a, b, v, 1);
+  store_pair_d(sk, nn, a, b, v, 1);
+}
+
+// ------------------------------------------ equal radii, real space, mixed
+// One kernel for both real-space image sets of a pair, all in FP32 and
+// double-single arithmetic (the FP64 pipe of GB300 runs at ~1/60 of the
+// FP32 rate, so no FP64 is left in the image loops or the epilogue):
+//   - images are classified in FP32: column base p = R + nx a1 + ny a2 and
+//     image p + nz a3 (fused multiply-adds in a fixed order), near when its
+//     squared distance is below rc^2, far up to rmax^2, so every image lands
+//     in exactly one set;
+//   - each set is processed from a per-thread list of image indices in
+//     shared memory (REAL_CAP at a time), so the lanes of a warp run their
+//     own images together instead of idling through each other's;
+//   - far images: FP32 moments; near images: double-single coordinates
+//     R + nx a1 + ny a2 + nz a3, r, erfc, exp and moments (dsacc);
+//   - the epilogues apply the coefficient table of the common radius
+//     (rsd_real_epi_coef_scaled, formed once in FP64), output by output, and
+//     the pair blocks are added to M's planes once.
+constexpr int REAL_CAP = 32;
+constexpr int REAL_THREADS = 128;
+struct RealEqShared {
+  dsf_tables T;
+  dsf cr[RSD_REAL_EPI_NC];
+  float cf[RSD_REAL_EPI_NC];
+  int list[REAL_CAP][REAL_THREADS];
+  float oh[60][REAL_THREADS];  // the pair block: far part, then hi of the sum
+  float ol[60][REAL_THREADS];  // lo of the sum
+};
+constexpr int SMEM_REAL_EQ = (int)sizeof(RealEqShared);
+
+// The coefficient tables for radius a (double-single and FP32).
+__global__ void ewald_real_epi_table(double a, double phix, double inv_pimu, dsf* __restrict__ cr,
+                                     float* __restrict__ cf) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double c[RSD_REAL_EPI_NC];
+  const double s1 = inv_pimu / (6.0 * a), s3 = s1 / (a * a);
+  rsd_real_epi_coef_scaled<double>(a, a, phix, s1, s3, c);
+  for (int k = 0; k < RSD_REAL_EPI_NC; k++) {
+    cr[k] = dsf_from(c[k]);
+    cf[k] = (float)c[k];
+  }
+}
+
+__device__ __forceinline__ int pack_image(int nx, int ny, int nz, int NR) {
+  return (nx + NR) | ((ny + NR) << 8) | ((nz + NR) << 16);
+}
+
+// FP32 column base of the classification (the same sequence for both sets)
+__device__ __forceinline__ void column_base_f(const float* Rf, const float* A, int nx, int ny, float* p) {
+  for (int k = 0; k < 3; k++) p[k] = __fmaf_rn(A[3 + k], (float)ny, __fmaf_rn(A[k], (float)nx, Rf[k]));
+}
+
+// Lists the next images of the set (near: r2 < rc2; far: rc2 <= r2 < rmax2)
+// from the resumable position (col, nz) into list[.][t], at most REAL_CAP;
+// returns the count.
+template <bool NEAR>
+__device__ __forceinline__ int list_images(RealEqShared& sh, int t, const float* Rf, const float* A, int NR, int& col,
+                                           int& nz, float rc2, float rmax2) {
+  const int w = 2 * NR + 1, ncol = w * w;
+  int cnt = 0, nx = 0, ny = 0;
+  float p[3];
+  bool base = false;
+  while (col < ncol && cnt < REAL_CAP) {
+    if (!base) {
+      nx = col / w - NR;
+      ny = col % w - NR;
+      column_base_f(Rf, A, nx, ny, p);
+      base = true;
+    }
+    float y0, y1, y2;
+    const float r2 = image_r2f(p[0], p[1], p[2], A[6], A[7], A[8], nz, &y0, &y1, &y2);
+    if (NEAR ? (r2 < rc2) : (r2 >= rc2 && r2 < rmax2)) sh.list[cnt++][t] = pack_image(nx, ny, nz, NR);
+    if (++nz > NR) {
+      nz = -NR;
+      col++;
+      base = false;
+    }
+  }
+  return cnt;
+}
+
+__global__ void __launch_bounds__(REAL_THREADS) ewald_pair_real_eq(int nn, rsd_lat_dev L,
+                                                                  const double* __restrict__ pos,
+                                                                  const dsf* __restrict__ cr_g,
+                                                                  const float* __restrict__ cf_g, float rc2,
+                                                                  float rmax2, PlaneSink sk) {
+  extern __shared__ __align__(16) unsigned char smraw_real[];
+  RealEqShared& sh = *reinterpret_cast<RealEqShared*>(smraw_real);
+  // blocks entirely on or below the diagonal (a >= b everywhere) have no work
+  if ((int)(blockIdx.x * blockDim.x) >= (int)(blockIdx.y * blockDim.y + blockDim.y - 1)) return;
+  const int t = threadIdx.y * blockDim.x + threadIdx.x;
+  dsf_tables_fill(sh.T, t, REAL_THREADS);
+  for (int k = t; k < RSD_REAL_EPI_NC; k += REAL_THREADS) {
+    sh.cr[k] = cr_g[k];
+    sh.cf[k] = cf_g[k];
+  }
+  __syncthreads();
+  int a, b;
+  if (!pair_of(nn, &a, &b)) return;
+  double R[3] = {pos[3 * a] - pos[3 * b], pos[3 * a + 1] - pos[3 * b + 1], pos[3 * a + 2] - pos[3 * b + 2]};
+  double dmin;
+  rsd_skew_correction(L.LR, L.LI, R, &dmin);
+  const dsf Rs[3] = {dsf_from(R[0]), dsf_from(R[1]), dsf_from(R[2])};
+  const float Rf[3] = {Rs[0].hi, Rs[1].hi, Rs[2].hi};
+  float A[9];
+  dsf As[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    As[k] = dsf_from(L.LR[k]);
+    A[k] = As[k].hi;
+  }
+  const int NR = L.NR;
+  const float lamf = (float)L.lam, lam2f = lamf * lamf, cdf = (float)(2.0 * RSD_PIP5 * L.lam);
+  // far images, FP32
+  {
+    float acc[RSD_NMOM_REAL];
+#pragma unroll
+    for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = 0.f;
+    int col = 0, nz = -NR;
+    do {
+      const int cnt = list_images<false>(sh, t, Rf, A, NR, col, nz, rc2, rmax2);
+      for (int q = 0; q < cnt; q++) {
+        const int e = sh.list[q][t];
+        const int ix = (e & 255) - NR, iy = ((e >> 8) & 255) - NR, iz = (e >> 16) - NR;
+        float p[3], x0, x1, x2;
+        column_base_f(Rf, A, ix, iy, p);
+        const float r2 = image_r2f(p[0], p[1], p[2], A[6], A[7], A[8], iz, &x0, &x1, &x2);
+        const float r = sqrtf(r2), ir = 1.f / r;
+        rsd_real_image<float>(x0, x1, x2, r, ir, erfcf(lamf * r), cdf * expf(-r2 * lam2f), lamf, acc);
+      }
+    } while (col < (2 * NR + 1) * (2 * NR + 1));
+#pragma unroll
+    for (int q = 0; q < 60; q++) sh.oh[q][t] = rsd_real_epi_row<float, float, float>(q, acc, sh.cf);
+  }
+  // near images, double-single
+  {
+    dsacc acc[RSD_NMOM_REAL];
+#pragma unroll
+    for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = dsacc(0);
+    const dsf lam_s = dsf_from(L.lam), cd_s = dsf_from(2.0 * RSD_PIP5 * L.lam);
+    int col = 0, nz = -NR;
+    do {
+      const int cnt = list_images<true>(sh, t, Rf, A, NR, col, nz, rc2, rmax2);
+      for (int q = 0; q < cnt; q++) {
+        const int e = sh.list[q][t];
+        const int ix = (e & 255) - NR, iy = ((e >> 8) & 255) - NR, iz = (e >> 16) - NR;
+        const dsf x0 = Rs[0] + ix * As[0] + iy * As[3] + iz * As[6];
+        const dsf x1 = Rs[1] + ix * As[1] + iy * As[4] + iz * As[7];
+        const dsf x2 = Rs[2] + ix * As[2] + iy * As[5] + iz * As[8];
+        const dsf r = dsf_sqrt(x0 * x0 + x1 * x1 + x2 * x2);
+        const dsf ir = dsf_rcp(r);
+        dsf E0, G;
+        dsf_erfc_gauss(lam_s * r, sh.T, &E0, &G);
+        rsd_real_image<dsf, dsacc>(x0, x1, x2, r, ir, E0, cd_s * G, lam_s, acc);
+        if ((q & 3) == 3) {  // keep the accumulators' lo parts small
+#pragma unroll
+          for (int m = 0; m < RSD_NMOM_REAL; m++) dsacc_norm(acc[m]);
+        }
+      }
+#pragma unroll
+      for (int m = 0; m < RSD_NMOM_REAL; m++) dsacc_norm(acc[m]);
+    } while (col < (2 * NR + 1) * (2 * NR + 1));
+    dsf accn[RSD_NMOM_REAL];
+#pragma unroll
+    for (int m = 0; m < RSD_NMOM_REAL; m++) accn[m] = dsf(acc[m].hi, acc[m].lo);
+#pragma unroll
+    for (int q = 0; q < 60; q++) {
+      dsacc o = rsd_real_epi_row<dsf, dsf, dsacc>(q, accn, sh.cr);
+      o += dsf(sh.oh[q][t], 0.f);
+      dsacc_norm(o);
+      sh.oh[q][t] = o.hi;
+      sh.ol[q][t] = o.lo;
+    }
+  }
+  dsf v[60];
+#pragma unroll
+  for (int q = 0; q < 60; q++) v[q] = dsf(sh.oh[q][t], sh.ol[q][t]);
+  store_pair_t<dsf>(sk, nn, a, b, v, 1);
 }
 
 __global__ void __launch_bounds__(128) ewald_pair_real(int nn, rsd_lat_dev L, const double* __restrict__ pos,
                                                        const double* __restrict__ radii, double inv_pimu,
-                                                       double* __restrict__ M, int64_t ldm) {
+                                                       DenseSink sk) {
   int a, b;
   if (!pair_of(nn, &a, &b)) return;
   double R[3] = {pos[3 * a] - pos[3 * b], pos[3 * a + 1] - pos[3 * b + 1], pos[3 * a + 2] - pos[3 * b + 2]};
@@ -675,7 +911,7 @@ __global__ void __launch_bounds__(128) ewald_pair_real(int nn, rsd_lat_dev L, co
   double v[60];
   rsd_real_epilogue<double>(acc, radii[a], radii[b], L.phix, v);
   scale_block(v, radii[a], inv_pimu);
-  store_pair(M, ldm, nn, a, b, v, 1);
+  store_pair_d(sk, nn, a, b, v, 1);
 }
 
 // Self-image moments.  The real-space images n != 0 of a particle and the
@@ -742,9 +978,18 @@ __global__ void __launch_bounds__(SELF_THREADS) ewald_self_moments(rsd_lat_dev L
 
 // Diagonal blocks from the self moments (ewald_self_moments) and the
 // particle's radius.
+__device__ __forceinline__ void sink_put(const DenseSink& sk, int64_t o, double x) { sk.M[o] = x; }
+__device__ __forceinline__ void sink_put(const PlaneSink& sk, int64_t o, double x) {
+  const dsf d = dsf_from(x);
+  sk.hi[o] = d.hi;
+  sk.lo[o] = d.lo;
+}
+
+template <typename S>
 __global__ void __launch_bounds__(64) ewald_self(int nn, rsd_lat_dev L, const double* __restrict__ mom,
-                                                 const double* __restrict__ radii, double inv_pimu,
-                                                 double* __restrict__ M, int64_t ldm) {
+                                                 const double* __restrict__ radii, double inv_pimu, S sk) {
+  const int64_t ldm = sk.ld;
+  auto M = [&](int64_t o, double x) { sink_put(sk, o, x); };
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= nn) return;
   const double ai = radii[a], lam = L.lam;
@@ -779,24 +1024,24 @@ __global__ void __launch_bounds__(64) ewald_self(int nn, rsd_lat_dev L, const do
   const int sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) {
-      M[(3 * a + i) + (int64_t)(3 * a + j) * ldm] = v[sym[i][j]];
-      M[(3 * N + 3 * a + i) + (int64_t)(3 * N + 3 * a + j) * ldm] = v[6 + sym[i][j]];
-      M[(3 * a + i) + (int64_t)(3 * N + 3 * a + j) * ldm] = 0.0;
-      M[(3 * N + 3 * a + j) + (int64_t)(3 * a + i) * ldm] = 0.0;
+      M((3 * a + i) + (int64_t)(3 * a + j) * ldm, v[sym[i][j]]);
+      M((3 * N + 3 * a + i) + (int64_t)(3 * N + 3 * a + j) * ldm, v[6 + sym[i][j]]);
+      M((3 * a + i) + (int64_t)(3 * N + 3 * a + j) * ldm, 0.0);
+      M((3 * N + 3 * a + j) + (int64_t)(3 * a + i) * ldm, 0.0);
     }
   for (int i = 0; i < 3; i++)
     for (int m = 0; m < 5; m++) {
-      M[(3 * a + i) + (int64_t)(6 * N + 5 * a + m) * ldm] = 0.0;
-      M[(3 * N + 3 * a + i) + (int64_t)(6 * N + 5 * a + m) * ldm] = 0.0;
-      M[(6 * N + 5 * a + m) + (int64_t)(3 * a + i) * ldm] = 0.0;
-      M[(6 * N + 5 * a + m) + (int64_t)(3 * N + 3 * a + i) * ldm] = 0.0;
+      M((3 * a + i) + (int64_t)(6 * N + 5 * a + m) * ldm, 0.0);
+      M((3 * N + 3 * a + i) + (int64_t)(6 * N + 5 * a + m) * ldm, 0.0);
+      M((6 * N + 5 * a + m) + (int64_t)(3 * a + i) * ldm, 0.0);
+      M((6 * N + 5 * a + m) + (int64_t)(3 * N + 3 * a + i) * ldm, 0.0);
     }
   int q = 15;
   double qq[5][5];
   for (int x = 0; x < 5; x++)
     for (int y = x; y < 5; y++) qq[x][y] = qq[y][x] = v[q++];
   for (int x = 0; x < 5; x++)
-    for (int y = 0; y < 5; y++) M[(6 * N + 5 * a + x) + (int64_t)(6 * N + 5 * a + y) * ldm] = qq[x][y];
+    for (int y = 0; y < 5; y++) M((6 * N + 5 * a + x) + (int64_t)(6 * N + 5 * a + y) * ldm, qq[x][y]);
 }
 
 __global__ void overlap_count(int nn, rsd_lat_dev L, const double* __restrict__ pos, const double* __restrict__ radii,
@@ -875,7 +1120,14 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
   double* mom = (double*)rsd_scratch(ctx, "ewald_self_mom", sizeof(double) * SELF_NMOM);
   if (!mom) return RSD_ENOMEM;
   ewald_self_moments<<<1, SELF_THREADS, 0, s>>>(L, Kh, tab, mom); RSD_LAUNCH_NOTE();
-  ewald_self<<<(nn + 63) / 64, 64, 0, s>>>(nn, L, mom, d_radii, inv_pimu, d_M, ldm); RSD_LAUNCH_NOTE();
+  // mixed form: M as FP32 planes hi + lo (PlaneSink), in the buffer of the FP64 matrix
+  const DenseSink dsk{d_M, ldm};
+  const PlaneSink psk{reinterpret_cast<float*>(d_M), reinterpret_cast<float*>(d_M) + (size_t)ldm * (11LL * nn), ldm};
+  if (precision == RSD_PREC_MIXED) {
+    ewald_self<<<(nn + 63) / 64, 64, 0, s>>>(nn, L, mom, d_radii, inv_pimu, psk); RSD_LAUNCH_NOTE();
+  } else {
+    ewald_self<<<(nn + 63) / 64, 64, 0, s>>>(nn, L, mom, d_radii, inv_pimu, dsk); RSD_LAUNCH_NOTE();
+  }
   if (nn > 1) {
     dim3 blk(32, 4), grd((nn + 31) / 32, (nn + 3) / 4);
     if (precision == RSD_PREC_MIXED) {
@@ -937,12 +1189,12 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
         float* w32 = (float*)rsd_scratch(ctx, "ewald_kblock32", sizeof(float) * (size_t)(K32 > 0 ? K32 : 1) * KBW);
         if (!w64 || !w32) return RSD_ENOMEM;
         if (K64) {
-          ewald_kblock_list<dsf><<<(K64 + 127) / 128, 128, 0, s>>>(L, K64, dh, hr[0], w64); RSD_LAUNCH_NOTE();
+          ewald_kblock_list<dsf><<<(K64 + 127) / 128, 128, 0, s>>>(L, K64, dh, hr[0], inv_pimu, w64); RSD_LAUNCH_NOTE();
         }
         if (K32) {
-          ewald_kblock_list<float><<<(K32 + 127) / 128, 128, 0, s>>>(L, K32, dh + K64, hr[0], w32); RSD_LAUNCH_NOTE();
+          ewald_kblock_list<float><<<(K32 + 127) / 128, 128, 0, s>>>(L, K32, dh + K64, hr[0], inv_pimu, w32); RSD_LAUNCH_NOTE();
         }
-        ewald_pair_kblock<<<grd, blk, 0, s>>>(nn, K32, w32, c32, K64, w64, c64, d_radii, inv_pimu, d_M, ldm, 0); RSD_LAUNCH_NOTE();
+        ewald_pair_kblock<<<grd, blk, 0, s>>>(nn, K32, w32, c32, K64, w64, c64, psk, 0); RSD_LAUNCH_NOTE();
       } else {
         if (K64) {
           ewald_ktable_list<double><<<(K64 + 127) / 128, 128, 0, s>>>(L, K64, dh, t64); RSD_LAUNCH_NOTE();
@@ -950,14 +1202,28 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
         if (K32) {
           ewald_ktable_list<float><<<(K32 + 127) / 128, 128, 0, s>>>(L, K32, dh + K64, t32); RSD_LAUNCH_NOTE();
         }
-        ewald_pair_k_ds<<<grd, blk, 0, s>>>(nn, L, K64, t64, c64, d_radii, inv_pimu, d_M, ldm, 0); RSD_LAUNCH_NOTE();
-        ewald_pair_k<float, float2><<<grd, blk, 0, s>>>(nn, L, K32, t32, c32, d_radii, inv_pimu, d_M, ldm, 1); RSD_LAUNCH_NOTE();
+        ewald_pair_k_ds<<<grd, blk, 0, s>>>(nn, L, K64, t64, c64, d_radii, inv_pimu, psk, 0); RSD_LAUNCH_NOTE();
+        ewald_pair_k<float, float2><<<grd, blk, 0, s>>>(nn, L, K32, t32, c32, d_radii, inv_pimu, psk, 1); RSD_LAUNCH_NOTE();
       }
-      ewald_pair_real_near_ds<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, d_M, ldm); RSD_LAUNCH_NOTE();
-      ewald_pair_real_far<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, rmax2, d_M, ldm); RSD_LAUNCH_NOTE();
+      if (equal) {
+        dsf* cr = (dsf*)rsd_scratch(ctx, "ewald_real_cr", sizeof(dsf) * RSD_REAL_EPI_NC);
+        float* cf = (float*)rsd_scratch(ctx, "ewald_real_cf", sizeof(float) * RSD_REAL_EPI_NC);
+        if (!cr || !cf) return RSD_ENOMEM;
+        static bool attr = false;
+        if (!attr) {
+          RSD_CUDA(ctx, cudaFuncSetAttribute(ewald_pair_real_eq, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             SMEM_REAL_EQ));
+          attr = true;
+        }
+        ewald_real_epi_table<<<1, 32, 0, s>>>(hr[0], L.phix, inv_pimu, cr, cf); RSD_LAUNCH_NOTE();
+        ewald_pair_real_eq<<<grd, blk, SMEM_REAL_EQ, s>>>(nn, L, d_pos, cr, cf, (float)rc2, (float)rmax2, psk); RSD_LAUNCH_NOTE();
+      } else {
+        ewald_pair_real_near_ds<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, psk); RSD_LAUNCH_NOTE();
+        ewald_pair_real_far<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, rmax2, psk); RSD_LAUNCH_NOTE();
+      }
     } else {
-      ewald_pair_k<double, double2><<<grd, blk, 0, s>>>(nn, L, Kh, tab, cs, d_radii, inv_pimu, d_M, ldm, 0); RSD_LAUNCH_NOTE();
-      ewald_pair_real<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, d_M, ldm); RSD_LAUNCH_NOTE();
+      ewald_pair_k<double, double2><<<grd, blk, 0, s>>>(nn, L, Kh, tab, cs, d_radii, inv_pimu, dsk, 0); RSD_LAUNCH_NOTE();
+      ewald_pair_real<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, dsk); RSD_LAUNCH_NOTE();
     }
   }
   RSD_CUDA(ctx, cudaGetLastError());

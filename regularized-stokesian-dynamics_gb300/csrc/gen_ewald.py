@@ -403,6 +403,75 @@ def gen():
         L.append("")
 
     epilogue("rsd_real_epilogue", dec_r, "Real-space pair block from the accumulated moments.")
+
+    # the same epilogue as a sparse table: coefficients c[k] of the
+    # (output, moment) pairs, formed once for given radii, then applied as
+    # 60 chains of multiply-adds
+    pairs = {}
+    for q, terms in enumerate(dec_r):
+        for const, rm, m in terms:
+            pairs.setdefault((q, m), []).append((const, rm))
+    keys = sorted(pairs)
+    L.append("// The real-space epilogue as a table: c[k] (rsd_real_epi_coef) is the")
+    L.append("// coefficient of moment m_k in output q_k (rsd_real_epi_apply).")
+    L.append("#define RSD_REAL_EPI_NC %d" % len(keys))
+    L.append("template <typename T>")
+    L.append("__host__ __device__ inline void rsd_real_epi_coef(T ai, T aj, T phix, T* __restrict__ c) {")
+    L.append("  const T ai2 = ai * ai, ai3 = ai2 * ai, ai4 = ai2 * ai2, ai5 = ai4 * ai, aj2 = aj * aj;")
+    L.append("  const T aj3 = aj2 * aj, aj4 = aj2 * aj2, phix2 = phix * phix; (void)aj3; (void)aj4; (void)phix2;")
+    L.append("  (void)ai4; (void)ai5;")
+    for kk, key in enumerate(keys):
+        parts = []
+        for const, rm in pairs[key]:
+            parts.append(" * ".join(["T(%s)" % sp.ccode(sp.N(const, 20))] + radius_poly(rm)))
+        L.append("  c[%d] = %s;" % (kk, " + ".join(parts)))
+    L.append("}")
+    L.append("")
+    # the same coefficients times the block scale of their output: s1 for
+    # TT, TR, G and s3 for RR, QQ, H (the radius powers of scale_block)
+    L.append("// rsd_real_epi_coef with each coefficient times the scale of its output:")
+    L.append("// s3 for RR, QQ and H (outputs 6-11, 15-29, 45-59), s1 for the others.")
+    L.append("template <typename T>")
+    L.append("__host__ __device__ inline void rsd_real_epi_coef_scaled(T ai, T aj, T phix, T s1, T s3, T* __restrict__ c) {")
+    L.append("  rsd_real_epi_coef<T>(ai, aj, phix, c);")
+    for kk, (q, m) in enumerate(keys):
+        a3 = (6 <= q < 12) or (15 <= q < 30) or q >= 45
+        L.append("  c[%d] *= %s;" % (kk, "s3" if a3 else "s1"))
+    L.append("}")
+    L.append("")
+    L.append("// Output q alone (q a compile-time constant after unrolling): the sum over")
+    L.append("// its table entries of c[k] acc[m_k].")
+    L.append("template <typename CT, typename A, typename O>")
+    L.append("__device__ __forceinline__ O rsd_real_epi_row(int q, const A* __restrict__ acc, const CT* __restrict__ c) {")
+    L.append("  O o = O(0);")
+    L.append("  switch (q) {")
+    byq = {}
+    for kk, (q, m) in enumerate(keys):
+        byq.setdefault(q, []).append((kk, m))
+    for q in range(60):
+        if q not in byq:
+            continue
+        L.append("    case %d:" % q)
+        for kk, m in byq[q]:
+            L.append("      o = fma(c[%d], acc[%d], o);" % (kk, m))
+        L.append("      break;")
+    L.append("    default:")
+    L.append("      break;")
+    L.append("  }")
+    L.append("  return o;")
+    L.append("}")
+    L.append("")
+    L.append("// out[q] = sum over the table entries of output q of c[k] acc[m_k]; CT, A and O")
+    L.append("// are the coefficient, moment and output types (fma(CT, A, O) -> O).")
+    L.append("template <typename CT, typename A, typename O>")
+    L.append("__device__ __forceinline__ void rsd_real_epi_apply(const A* __restrict__ acc, const CT* __restrict__ c,")
+    L.append("                                                   O* __restrict__ out) {")
+    L.append("#pragma unroll")
+    L.append("  for (int q = 0; q < 60; q++) out[q] = O(0);")
+    for kk, (q, m) in enumerate(keys):
+        L.append("  out[%d] = fma(c[%d], acc[%d], out[%d]);" % (q, kk, m, q))
+    L.append("}")
+    L.append("")
     # ---- reciprocal-space weights: w[m] = S k^alpha for each moment
     for tag, mom, dec in (("kcos", mom_c, dec_c), ("ksin", mom_s, dec_s)):
         L.append("// Per-k weights of the %s moments: w[m] = g_m(S, lam) * k^alpha." % tag)

@@ -6,9 +6,10 @@
 // Augmented system in (f, U), with w = [U; -EIN]:
 //     M f = w                    (f = R_inf w, the far-field forces)
 //     f_P + (L w)_P = Fe          (force balance with lubrication)
-// and then SijN_hyd = f_Q + (L w)_Q.  Its FP64 residual needs only the FP64
-// products M f (an HBM-bound dense GEMV) and L w (a block-sparse product
-// over the near pairs, L is never formed densely here).  The correction is
+// and then SijN_hyd = f_Q + (L w)_Q.  Its residual needs only the products
+// M f (an HBM-bound dense GEMV in double-single arithmetic over M's two
+// FP32 planes, ~FP64 accuracy for the sums) and L w (an FP64 block-sparse
+// product over the near pairs, L is never formed densely here).  The correction is
 // solved with FP32 factors:
 //   M' = [M_QQ M_QP; M_PQ M_PP] = U'^T U'  (stresslets ordered first), so the
 //   trailing block U'_PP is the Cholesky factor of the Schur complement
@@ -21,6 +22,7 @@
 #include <cmath>
 #include <vector>
 
+#include "dsf.cuh"
 #include "rsd_internal.cuh"
 
 template <typename T>
@@ -45,14 +47,64 @@ int rsd_potrs_wide_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const flo
 
 namespace {
 
-// M32 = M in [Q, P] order, FP32
-__global__ void convert_perm(int N, int64_t n, const double* __restrict__ M, int64_t ld, float* __restrict__ M32) {
+// M32 = M in [Q, P] order, FP32: the hi plane of the double-single M
+__global__ void convert_perm(int N, int64_t n, const float* __restrict__ Mh, int64_t ld, float* __restrict__ M32) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * n) return;
   const int64_t i = t % n, j = t / n;
   const int64_t Q = 5LL * N;
   const int64_t si = i < Q ? 6LL * N + i : i - Q, sj = j < Q ? 6LL * N + j : j - Q;
-  M32[i + j * n] = (float)M[si + sj * ld];
+  M32[i + j * n] = Mh[si + sj * ld];
+}
+
+// x (FP64) as float pairs
+__global__ void to_dsf_vec(int64_t n, const double* __restrict__ x, float2* __restrict__ xs) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const dsf d = dsf_from(x[t]);
+  xs[t] = make_float2(d.hi, d.lo);
+}
+
+// part[c][r][i] = sum over the chunk c of columns p of M(i, p) x(p, r), with
+// M = hi + lo and x as float pairs, in double-single arithmetic on the FP32
+// pipe (the FP64 pipe of GB300 would bound an FP64 product at ~1/60 of the
+// FP32 rate; this one is bound by HBM).  Chunks of GEMV_PL_CHUNK columns
+// keep the double-single rounding of each partial near 2^-48 sqrt(chunk).
+constexpr int GEMV_PL_CHUNK = 512;
+template <int R>
+__global__ void gemv_planes_part(int m, int k, const float* __restrict__ Mh, const float* __restrict__ Ml, int64_t ld,
+                                 const float2* __restrict__ xs, double* __restrict__ part) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  const int p0 = c * GEMV_PL_CHUNK, p1 = min(k, p0 + GEMV_PL_CHUNK);
+  if (i >= m) return;
+  dsf acc[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) acc[r] = dsf(0);
+#pragma unroll 4
+  for (int p = p0; p < p1; p++) {
+    const int64_t o = i + (int64_t)p * ld;
+    const dsf a(Mh[o], Ml[o]);
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const float2 x = xs[p + (int64_t)r * k];
+      acc[r] = fma(a, dsf(x.x, x.y), acc[r]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < R; r++) part[((size_t)c * R + r) * m + i] = dsf_to(acc[r]);
+}
+
+// y(:, r) += alpha * sum_c part[c][r]
+__global__ void gemv_planes_reduce(int m, int nr, int nchunk, const double* __restrict__ part, double alpha,
+                                   double* __restrict__ y, int64_t ldy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  for (int r = 0; r < nr; r++) {
+    double s = 0.0;
+    for (int c = 0; c < nchunk; c++) s += part[((size_t)c * nr + r) * m + i];
+    y[i + (int64_t)r * ldy] += alpha * s;
+  }
 }
 
 __global__ void copy_block_f(int64_t rows, int64_t cols, const float* __restrict__ S, int64_t lds,
@@ -191,6 +243,13 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   const int nr = have_fe ? 2 : 1;
   const double tol = p->tol > 0 ? p->tol : 1e-12;
   const int maxit = p->max_iter > 0 ? p->max_iter : 50;
+  // M as FP32 planes hi + lo in the buffer of the FP64 matrix (rsd_ewald_assemble)
+  const float* Mh = reinterpret_cast<const float*>(M);
+  const float* Ml = Mh + (size_t)ld * n;
+  const unsigned gchunks = (unsigned)((n + GEMV_PL_CHUNK - 1) / GEMV_PL_CHUNK);
+  float2* fs = (float2*)rsd_scratch(ctx, "mixed_fs", sizeof(float2) * (size_t)nr * n);
+  double* gpart = (double*)rsd_scratch(ctx, "mixed_gemv_part", sizeof(double) * (size_t)gchunks * nr * n);
+  if (!fs || !gpart) return RSD_ENOMEM;
   float* M32 = (float*)rsd_scratch(ctx, "mixed_M32", sizeof(float) * n * n);
   float* A32 = (float*)rsd_scratch(ctx, "mixed_A32", sizeof(float) * P * P);
   double* V = (double*)rsd_scratch(ctx, "mixed_vec", sizeof(double) * (size_t)nr * (7 * n + 2 * P) + 64 * 8);
@@ -206,7 +265,7 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   info->n_contact = nc;
   cudaEventRecord(ctx->ev[6], s);
   // FP32 factor of M' (stresslets first)
-  convert_perm<<<(unsigned)((n * n + 255) / 256), 256, 0, s>>>(nn, n, M, ld, M32); RSD_LAUNCH_NOTE();
+  convert_perm<<<(unsigned)((n * n + 255) / 256), 256, 0, s>>>(nn, n, Mh, ld, M32); RSD_LAUNCH_NOTE();
   int inf = 0;
   // Tensor-core precision per factor.  The refinement contracts by about the
   // preconditioner's relative error times the condition number it meets:
@@ -249,7 +308,14 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   for (;; it++) {
     build_w<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, U, ein, w); RSD_LAUNCH_NOTE();
     RSD_CUDA(ctx, cudaMemcpyAsync(r1, w, sizeof(double) * nr * n, cudaMemcpyDeviceToDevice, s));
-    RSD_TRY(rsd_gemv<double>(ctx, 0, (int)n, (int)n, -1.0, M, ld, f, n, nr, 1.0, r1, n));
+    // r1 -= M f, double-single products of the two planes
+    to_dsf_vec<<<nblk(n * nr), 256, 0, s>>>(n * nr, f, fs); RSD_LAUNCH_NOTE();
+    if (nr == 1) {
+      gemv_planes_part<1><<<dim3((unsigned)((n + 255) / 256), gchunks), 256, 0, s>>>((int)n, (int)n, Mh, Ml, ld, fs, gpart); RSD_LAUNCH_NOTE();
+    } else {
+      gemv_planes_part<2><<<dim3((unsigned)((n + 255) / 256), gchunks), 256, 0, s>>>((int)n, (int)n, Mh, Ml, ld, fs, gpart); RSD_LAUNCH_NOTE();
+    }
+    gemv_planes_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>((int)n, nr, gchunks, gpart, -1.0, r1, n); RSD_LAUNCH_NOTE();
     if (p->use_lub) {
       RSD_TRY(rsd_lub_spmv(ctx, &lub, nr, w, n, Lw, n));
     } else {

@@ -28,13 +28,16 @@ __global__ void fill_ein(int nn, const double* __restrict__ ei5, double* __restr
 
 // averageU (src/matrices.f90:230-253): U_ave = sum_i (APP F)(3i) / N with
 // F(3j) = 6 pi mu_f radii_test; out[0] accumulates sum_ij APP(3i,3j)
-__global__ void sum_app_xx(int nn, const double* __restrict__ M, int64_t ld, double* __restrict__ out) {
+// Mh, Ml: the mixed form's M as FP32 planes (hi + lo); null for FP64 M
+__global__ void sum_app_xx(int nn, const double* __restrict__ M, const float* __restrict__ Mh,
+                           const float* __restrict__ Ml, int64_t ld, double* __restrict__ out) {
   __shared__ double red[256];
   double s = 0.0;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)nn * nn;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(t % nn), j = (int)(t / nn);
-    s += M[3 * i + (int64_t)(3 * j) * ld];
+    const int64_t o = 3 * i + (int64_t)(3 * j) * ld;
+    s += Mh ? (double)Mh[o] + (double)Ml[o] : M[o];
   }
   red[threadIdx.x] = s;
   __syncthreads();
@@ -227,7 +230,9 @@ extern "C" int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, co
   RSD_TRY(rsd_ewald_assemble(ctx, nn, d_conf, d_radii, &lat, p->mu_f, p->precision, M, n));
   cudaEventRecord(ctx->ev[1], s);
   // averageU on APP before it is overwritten
-  sum_app_xx<<<256, 256, 0, s>>>(nn, M, n, red); RSD_LAUNCH_NOTE();
+  const bool planes = p->precision == RSD_PREC_MIXED;
+  const float* Mh = planes ? reinterpret_cast<const float*>(M) : nullptr;
+  sum_app_xx<<<256, 256, 0, s>>>(nn, M, Mh, planes ? Mh + (size_t)n * n : nullptr, n, red); RSD_LAUNCH_NOTE();
   std::vector<double> hred(256);
   RSD_CUDA(ctx, cudaMemcpyAsync(hred.data(), red, 256 * sizeof(double), cudaMemcpyDeviceToHost, s));
   int info_m = 0;

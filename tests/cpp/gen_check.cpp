@@ -137,3 +137,13 @@ extern "C" void gen_pair_block_mixed(const double R[3], const double LR[9], cons
     out[q] = v * (a3 ? na3 : na);
   }
 }
+
+// The real-space epilogue as a coefficient table (rsd_real_epi_coef +
+// rsd_real_epi_apply) against the generated epilogue, for given moments.
+extern "C" void gen_real_epilogue_both(const double acc[RSD_NMOM_REAL], double ai, double aj, double phix,
+                                       double direct[60], double table[60]) {
+  rsd_real_epilogue<double>(acc, ai, aj, phix, direct);
+  double c[RSD_REAL_EPI_NC];
+  rsd_real_epi_coef<double>(ai, aj, phix, c);
+  rsd_real_epi_apply<double, double, double>(acc, c, table);
+}

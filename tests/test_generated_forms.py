@@ -79,3 +79,19 @@ def test_generated_free_space_block_matches_oracle(genlib):
         got = gen_block(genlib, lat, R, 1.0, 1.0, include_k=False)
         for a, b in zip(ref, got):
             assert np.abs(a - b).max() <= 1e-13 * max(np.abs(a).max(), 1e-300)
+
+
+@pytest.mark.parametrize("ai,aj", [(1.0, 1.0), (1.0, 0.6), (0.7, 1.3)])
+def test_real_epilogue_table_matches_direct(genlib, ai, aj):
+    """The table form of the real-space epilogue (coefficients per
+    (output, moment) pair, as the equal-radius mixed kernel applies it)
+    equals the generated epilogue to rounding."""
+    rng = np.random.default_rng(int(100 * ai + 10 * aj))
+    d = lambda a: np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    for _ in range(5):
+        acc = rng.normal(size=97) * np.exp(rng.uniform(-3, 3, 97))
+        direct, table = np.zeros(60), np.zeros(60)
+        genlib.gen_real_epilogue_both(d(acc), ctypes.c_double(ai), ctypes.c_double(aj), ctypes.c_double(0.9),
+                                      d(direct), d(table))
+        assert np.abs(direct - table).max() <= 1e-13 * max(np.abs(direct).max(), 1.0)
+        assert np.abs(direct).max() > 0
