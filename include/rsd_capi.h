@@ -98,6 +98,11 @@ int rsd_ctx_set_mixed_truncation(rsd_ctx* ctx, double lam_r_max, double k2_over_
  * truncation spheres.  1 keeps the reference's lammda, NR and NI; the
  * default is 1.5.  The FP64 form always uses the reference's values. */
 int rsd_ctx_set_mixed_lambda_scale(rsd_ctx* ctx, double scale);
+/* Equal radii, mixed-precision assembly: the double-single near images are
+ * summed in `passes` passes (1 to 4), each over one part of the moments
+ * (fewer live accumulators and a shorter loop per pass; r, erfc and exp are
+ * evaluated once per pass).  A performance setting; the sums are the same. */
+int rsd_ctx_set_mixed_real_passes(rsd_ctx* ctx, int32_t passes);
 
 /* ---------------------------------------------------------------- lattice */
 /* SET_LATTICE_SKEW (src/csd_post.f90:105-136) with MAT_INV3

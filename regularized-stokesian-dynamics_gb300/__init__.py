@@ -96,6 +96,7 @@ _sig("rsd_ctx_set_tensor_cores", _i, [_vp, _i])
 _sig("rsd_ctx_set_mixed_split", _i, [_vp, _d, _i32])
 _sig("rsd_ctx_set_mixed_truncation", _i, [_vp, _d, _d])
 _sig("rsd_ctx_set_mixed_lambda_scale", _i, [_vp, _d])
+_sig("rsd_ctx_set_mixed_real_passes", _i, [_vp, _i32])
 _sig("rsd_syrk_f32_dev", _i, [_vp, _i32, _i32, _vp, _i64, _vp, _i64, _i32])
 _sig("rsd_potrf_f32_dev", _i, [_vp, _i32, _vp, _i64, _i32, _ip])
 _sig("rsd_potri_f32_dev", _i, [_vp, _i32, _vp, _i64, _i32])
@@ -160,6 +161,10 @@ class Context:
         """Ewald splitting parameter of the mixed assembly relative to the
         reference's."""
         self.check(_lib.rsd_ctx_set_mixed_lambda_scale(self.h, float(scale)))
+
+    def set_mixed_real_passes(self, passes=1):
+        """Passes over the near images of the equal-radius mixed assembly."""
+        self.check(_lib.rsd_ctx_set_mixed_real_passes(self.h, int(passes)))
 
     def set_tensor_cores(self, mode=1):
         """FP32 factorisations of the mixed form: 1 (or True, the default)

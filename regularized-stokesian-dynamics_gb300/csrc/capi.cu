@@ -151,6 +151,13 @@ extern "C" int rsd_ctx_set_mixed_lambda_scale(rsd_ctx* c, double scale) {
   return RSD_OK;
 }
 
+extern "C" int rsd_ctx_set_mixed_real_passes(rsd_ctx* c, int passes) {
+  if (!c) return RSD_EARG;
+  if (passes < 1 || passes > 4) return rsd_fail(c, RSD_EARG, "mixed real-space passes must be 1 to 4");
+  c->mixed_real_passes = passes;
+  return RSD_OK;
+}
+
 extern "C" int rsd_ctx_set_tensor_cores(rsd_ctx* c, int mode) {
   if (!c) return RSD_EARG;
   if (mode != 0 && mode != 1 && mode != 3) return rsd_fail(c, RSD_EARG, "tensor-core mode must be 0, 1 or 3");

@@ -1430,6 +1430,201 @@ __global__ void __launch_bounds__(256) strip_n_update(int rows, int kb, const fl
       w[i + r * ldx] -= (part[r][0][il] + part[r][1][il]) + (part[r][2][il] + part[r][3][il]);
 }
 
+// ------------------------------------------- dataflow block sweeps
+// One persistent launch per direction of the block-scaled solve instead of
+// one launch per 512-block.  A task is one 64-wide quarter-of-a-quarter
+// ("part") of a target block: its CTA walks the source blocks in order,
+// waits until each source block is published, and accumulates that tile's
+// product in registers, so every sum has a fixed order (deterministic) and
+// nothing is reduced across CTAs.  Tasks are taken from a ticket counter in
+// target order (block 1, 2, ... forward; nb-2, ..., 0 backward), so every
+// task a CTA waits for was taken earlier by a running CTA (no deadlock).  A
+// finished part is published by data, fence and a per-block counter; a
+// block is usable once all TRI_Q of its parts are in.  Waits are bounded
+// (TRI_SPIN_LIMIT polls); a timeout sets *err and every CTA leaves its loop.
+constexpr int TRI_Q = 16, TRI_QS = NB2 / TRI_Q;  // parts per block, columns/rows per part
+constexpr int TRI_THREADS = 256;
+constexpr long long TRI_SPIN_LIMIT = 1LL << 21;  // polls of >= 64 ns: a fraction of a second
+constexpr int TRI_MAX_BLOCKS = 256;              // order up to 131072
+
+struct TriArgs {
+  const float* Uh;  // strict upper block strips, ld
+  int64_t ld;
+  int n, nb;        // order, 512-blocks
+  float* V;         // in/out vector(s), ld ldv
+  int64_t ldv;
+  int* ready;       // per block: parts published
+  int* ticket;
+  int* err;
+};
+
+// waits until all parts of block blk are published (thread 0 of the CTA)
+__device__ __forceinline__ void tri_wait(const TriArgs& A, int blk, volatile int* abort_s) {
+  long long it = 0;
+  while (*((volatile int*)(A.ready + blk)) < TRI_Q) {
+    if (*((volatile int*)A.err) != 0) {
+      *abort_s = 1;
+      return;
+    }
+    if (++it > TRI_SPIN_LIMIT) {
+      atomicExch(A.err, 1);
+      *abort_s = 1;
+      return;
+    }
+    __nanosleep(64);
+  }
+  __threadfence();
+}
+
+// forward: z_j = V_j - sum_{c<j} Uh_cj^T z_c, in place on V (z_0 = V_0)
+template <int NR>
+__global__ void __launch_bounds__(TRI_THREADS) tri_forward(TriArgs A) {
+  __shared__ __align__(16) float zs[NR][NB2];
+  __shared__ int task_s;
+  __shared__ volatile int abort_s;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int nb = A.nb, total = TRI_Q * (nb - 1);
+  if (t == 0) abort_s = 0;
+  for (;;) {
+    __syncthreads();
+    if (t == 0) task_s = atomicAdd(A.ticket, 1);
+    __syncthreads();
+    const int task = task_s;
+    if (task >= total || abort_s) break;
+    const int j = 1 + task / TRI_Q, q = task % TRI_Q;
+    // columns col0 + cc of block j (TRI_QS / 8 per warp); each lane sums 16
+    // rows of each source tile per column.  A tile is loaded into registers
+    // before its source block is awaited (it does not depend on it).
+    constexpr int CPW = TRI_QS / 8;
+    const int col0 = j * NB2 + q * TRI_QS + warp * CPW;
+    float acc[CPW][NR];
+#pragma unroll
+    for (int cc = 0; cc < CPW; cc++)
+#pragma unroll
+      for (int r = 0; r < NR; r++) acc[cc][r] = 0.f;
+    for (int c = 0; c < j; c++) {
+      const int c0 = c * NB2;  // a full block: c < nb - 1
+      float4 v[CPW][NB2 / 128];
+#pragma unroll
+      for (int cc = 0; cc < CPW; cc++) {
+        const int col = min(col0 + cc, A.n - 1);
+        const float* u = A.Uh + c0 + (int64_t)col * A.ld;
+#pragma unroll
+        for (int i = 0; i < NB2 / 128; i++) v[cc][i] = __ldcs(reinterpret_cast<const float4*>(u + 4 * lane + 128 * i));
+      }
+      if (t == 0 && c > 0) tri_wait(A, c, &abort_s);
+      __syncthreads();
+      if (abort_s) break;
+      for (int e = t; e < NB2; e += TRI_THREADS)
+        for (int r = 0; r < NR; r++) zs[r][e] = __ldcg(A.V + c0 + e + r * A.ldv);
+      __syncthreads();
+#pragma unroll
+      for (int cc = 0; cc < CPW; cc++)
+#pragma unroll
+        for (int i = 0; i < NB2 / 128; i++) {
+          const int k = 4 * lane + 128 * i;
+#pragma unroll
+          for (int r = 0; r < NR; r++)
+            acc[cc][r] += v[cc][i].x * zs[r][k] + v[cc][i].y * zs[r][k + 1] + v[cc][i].z * zs[r][k + 2] +
+                          v[cc][i].w * zs[r][k + 3];
+        }
+      __syncthreads();  // zs is reloaded for the next source block
+    }
+    if (abort_s) break;
+#pragma unroll
+    for (int cc = 0; cc < CPW; cc++)
+#pragma unroll
+      for (int r = 0; r < NR; r++) {
+        float a = acc[cc][r];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        const int col = col0 + cc;
+        if (lane == 0 && col < A.n) {
+          float* v = A.V + col + r * A.ldv;
+          *v = __ldcg(v) - a;
+        }
+      }
+    __threadfence();
+    __syncthreads();
+    if (t == 0) atomicAdd(A.ready + j, 1);
+  }
+}
+
+// backward: x_b = V_b - sum_{c>b} Uh_bc x_c, in place on V (x_{nb-1} = V_{nb-1})
+template <int NR>
+__global__ void __launch_bounds__(TRI_THREADS) tri_backward(TriArgs A) {
+  __shared__ __align__(16) float xs[NR][NB2];
+  __shared__ float red[32][NR][TRI_QS];
+  __shared__ int task_s;
+  __shared__ volatile int abort_s;
+  const int t = threadIdx.x;
+  const int nb = A.nb, total = TRI_Q * (nb - 1);
+  if (t == 0) abort_s = 0;
+  for (;;) {
+    __syncthreads();
+    if (t == 0) task_s = atomicAdd(A.ticket, 1);
+    __syncthreads();
+    const int task = task_s;
+    if (task >= total || abort_s) break;
+    const int b = nb - 2 - task / TRI_Q, q = task % TRI_Q;
+    // rows r0 + rl .. + 3 of block b (a full block): 8 threads x 4 rows;
+    // 32 k streams of 16 columns.  A tile is loaded into registers before its
+    // source block is awaited.
+    constexpr int KPS = NB2 / 32;
+    const int r0 = b * NB2 + q * TRI_QS, rl = 4 * (t & 7), ks = t >> 3;
+    float acc[NR][4];
+#pragma unroll
+    for (int r = 0; r < NR; r++)
+#pragma unroll
+      for (int i = 0; i < 4; i++) acc[r][i] = 0.f;
+    for (int c = nb - 1; c > b; c--) {
+      const int cst = c * NB2, kc = min(NB2, A.n - cst);
+      const float* u = A.Uh + r0 + rl + (int64_t)cst * A.ld;
+      float4 v[KPS];
+#pragma unroll
+      for (int kk = 0; kk < KPS; kk++) {
+        const int k = min(ks * KPS + kk, kc - 1);
+        v[kk] = __ldcs(reinterpret_cast<const float4*>(u + (int64_t)k * A.ld));
+      }
+      if (t == 0 && c < nb - 1) tri_wait(A, c, &abort_s);
+      __syncthreads();
+      if (abort_s) break;
+      for (int e = t; e < NB2; e += TRI_THREADS)
+        for (int r = 0; r < NR; r++) xs[r][e] = e < kc ? __ldcg(A.V + cst + e + r * A.ldv) : 0.f;
+      __syncthreads();
+#pragma unroll
+      for (int kk = 0; kk < KPS; kk++) {
+        const int k = ks * KPS + kk;  // x is zero past kc
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+          const float x = xs[r][k];
+          acc[r][0] += v[kk].x * x;
+          acc[r][1] += v[kk].y * x;
+          acc[r][2] += v[kk].z * x;
+          acc[r][3] += v[kk].w * x;
+        }
+      }
+      __syncthreads();  // xs is reloaded for the next source block
+    }
+    if (abort_s) break;
+#pragma unroll
+    for (int r = 0; r < NR; r++)
+#pragma unroll
+      for (int i = 0; i < 4; i++) red[ks][r][rl + i] = acc[r][i];
+    __syncthreads();
+    for (int e = t; e < NR * TRI_QS; e += TRI_THREADS) {
+      const int r = e / TRI_QS, il = e % TRI_QS;
+      float v = 0.f;
+#pragma unroll
+      for (int w = 0; w < 32; w++) v += red[w][r][il];
+      float* p = A.V + r0 + il + r * A.ldv;
+      *p = __ldcg(p) - v;
+    }
+    __threadfence();
+    __syncthreads();
+    if (t == 0) atomicAdd(A.ready + b, 1);
+  }
+}
+
 // w_b = G_b z_b for every block, one thread per row
 template <int NR>
 __global__ void __launch_bounds__(256) blockdiag_gemv(int n, const float* __restrict__ G, const float* __restrict__ z,
@@ -1489,15 +1684,18 @@ int rsd_uhat_solve(rsd_ctx* ctx, const rsd_uhat* h, float* X, int64_t ldx, int n
   const int n = h->n, nblk2 = (n + NB2 - 1) / NB2;
   cudaStream_t s = ctx->stream;
   const int gsm = ctx->sm_count > 0 ? ctx->sm_count : 148;
-  for (int b = 0; b < nblk2; b++) {  // forward, in place on X
-    const int j0 = b * NB2, jb = n - j0 < NB2 ? n - j0 : NB2, rest = n - j0 - jb;
-    if (rest <= 0) break;
-    const float* S = h->Uh + j0 + (int64_t)(j0 + jb) * h->ld;
-    const int blocks = min(4 * gsm, (rest + 7) / 8);
+  if (nblk2 > TRI_MAX_BLOCKS) return rsd_fail(ctx, RSD_EUNSUP, "uhat solve: order %d above %d", n, TRI_MAX_BLOCKS * NB2);
+  int* sync = rsd_uhat_error_flag(ctx);  // [0] error (cumulative), [1] ticket, ready counts
+  if (!sync) return RSD_ENOMEM;
+  TriArgs A{h->Uh, h->ld, n, nblk2, X, ldx, sync + 2, sync + 1, sync};
+  const int tasks = TRI_Q * (nblk2 - 1);
+  const int grid = max(1, min(tasks, 4 * gsm));
+  if (tasks > 0) {  // forward, in place on X
+    RSD_CUDA(ctx, cudaMemsetAsync(sync + 1, 0, sizeof(int) * (size_t)(1 + nblk2), s));
     if (nrhs == 1)
-      strip_t_update<1><<<blocks, 256, 0, s>>>(jb, rest, S, h->ld, X + j0, X + j0 + jb, ldx);
+      tri_forward<1><<<grid, TRI_THREADS, 0, s>>>(A);
     else
-      strip_t_update<2><<<blocks, 256, 0, s>>>(jb, rest, S, h->ld, X + j0, X + j0 + jb, ldx);
+      tri_forward<2><<<grid, TRI_THREADS, 0, s>>>(A);
     RSD_LAUNCH_NOTE();
   }
   if (nrhs == 1)
@@ -1505,19 +1703,26 @@ int rsd_uhat_solve(rsd_ctx* ctx, const rsd_uhat* h, float* X, int64_t ldx, int n
   else
     blockdiag_gemv<2><<<(n + 255) / 256, 256, 0, s>>>(n, h->G, X, Y, ldx);
   RSD_LAUNCH_NOTE();
-  for (int b = nblk2 - 1; b > 0; b--) {  // backward, in place on Y
-    const int j0 = b * NB2, jb = n - j0 < NB2 ? n - j0 : NB2;
-    const float* S = h->Uh + (int64_t)j0 * h->ld;  // rows 0..j0, columns of block b
+  if (tasks > 0) {  // backward, in place on Y
+    A.V = Y;
+    RSD_CUDA(ctx, cudaMemsetAsync(sync + 1, 0, sizeof(int) * (size_t)(1 + nblk2), s));
     if (nrhs == 1)
-      strip_n_update<1><<<(j0 + 63) / 64, 256, 0, s>>>(j0, jb, S, h->ld, Y + j0, Y, ldx);
+      tri_backward<1><<<grid, TRI_THREADS, 0, s>>>(A);
     else
-      strip_n_update<2><<<(j0 + 63) / 64, 256, 0, s>>>(j0, jb, S, h->ld, Y + j0, Y, ldx);
+      tri_backward<2><<<grid, TRI_THREADS, 0, s>>>(A);
     RSD_LAUNCH_NOTE();
   }
   for (int r = 0; r < nrhs; r++)
     RSD_CUDA(ctx, cudaMemcpyAsync(X + r * ldx, Y + r * ldx, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
   RSD_CUDA(ctx, cudaGetLastError());
   return RSD_OK;
+}
+
+// The dataflow sweeps' synchronisation words; element 0 is a cumulative
+// error flag, nonzero once a sweep's wait timed out (the caller zeroes it
+// and reads it after synchronising the stream).
+int* rsd_uhat_error_flag(rsd_ctx* ctx) {
+  return (int*)rsd_scratch(ctx, "tri_sync", sizeof(int) * (size_t)(2 * TRI_MAX_BLOCKS + 2));
 }
 
 int rsd_potrs_wide_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const float* W2, float* X, int64_t ldx,

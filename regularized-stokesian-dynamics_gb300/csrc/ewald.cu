@@ -781,11 +781,68 @@ __device__ __forceinline__ int list_images(RealEqShared& sh, int t, const float*
   return cnt;
 }
 
-__global__ void __launch_bounds__(REAL_THREADS) ewald_pair_real_eq(int nn, rsd_lat_dev L,
-                                                                  const double* __restrict__ pos,
-                                                                  const dsf* __restrict__ cr_g,
-                                                                  const float* __restrict__ cf_g, float rc2,
-                                                                  float rmax2, PlaneSink sk) {
+// The near images' moments of part P (of NP, rsd_mom_part): one pass over
+// the near set, then that part's share of every output added into the pair
+// block held in shared memory (oh + ol).
+template <int NP, int P>
+__device__ __forceinline__ void near_part(RealEqShared& sh, int t, const float* Rf, const float* A, const dsf* Rs,
+                                          const dsf* As, int NR, float rc2, dsf lam_s, dsf cd_s) {
+  dsacc acc[RSD_NMOM_REAL];
+#pragma unroll
+  for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = dsacc(0);
+  int col = 0, nz = -NR;
+  do {
+    const int cnt = list_images<true>(sh, t, Rf, A, NR, col, nz, rc2, 0.f);
+    for (int q = 0; q < cnt; q++) {
+      const int e = sh.list[q][t];
+      const int ix = (e & 255) - NR, iy = ((e >> 8) & 255) - NR, iz = (e >> 16) - NR;
+      const dsf x0 = Rs[0] + ix * As[0] + iy * As[3] + iz * As[6];
+      const dsf x1 = Rs[1] + ix * As[1] + iy * As[4] + iz * As[7];
+      const dsf x2 = Rs[2] + ix * As[2] + iy * As[5] + iz * As[8];
+      const dsf r = dsf_sqrt(x0 * x0 + x1 * x1 + x2 * x2);
+      const dsf ir = dsf_rcp(r);
+      dsf E0, G;
+      dsf_erfc_gauss(lam_s * r, sh.T, &E0, &G);
+      rsd_real_image<dsf, dsacc, NP, P>(x0, x1, x2, r, ir, E0, cd_s * G, lam_s, acc);
+      if ((q & 3) == 3) {  // keep the accumulators' lo parts small
+#pragma unroll
+        for (int m = 0; m < RSD_NMOM_REAL; m++) dsacc_norm(acc[m]);
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < RSD_NMOM_REAL; m++) dsacc_norm(acc[m]);
+  } while (col < (2 * NR + 1) * (2 * NR + 1));
+  dsf accn[RSD_NMOM_REAL];
+#pragma unroll
+  for (int m = 0; m < RSD_NMOM_REAL; m++) accn[m] = dsf(acc[m].hi, acc[m].lo);
+#pragma unroll
+  for (int q = 0; q < 60; q++) {
+    dsacc o = rsd_real_epi_row<dsf, dsf, dsacc, NP, P>(q, accn, sh.cr);
+    o += dsf(sh.oh[q][t], sh.ol[q][t]);
+    dsacc_norm(o);
+    sh.oh[q][t] = o.hi;
+    sh.ol[q][t] = o.lo;
+  }
+}
+
+template <int NP, int P>
+__device__ __forceinline__ void near_parts(RealEqShared& sh, int t, const float* Rf, const float* A, const dsf* Rs,
+                                           const dsf* As, int NR, float rc2, dsf lam_s, dsf cd_s) {
+  if constexpr (P < NP) {
+    near_part<NP, P>(sh, t, Rf, A, Rs, As, NR, rc2, lam_s, cd_s);
+    near_parts<NP, P + 1>(sh, t, Rf, A, Rs, As, NR, rc2, lam_s, cd_s);
+  }
+}
+
+// NP: passes over the near images, each summing one part of the moments
+// (fewer live accumulators and a shorter loop body per pass, at the cost of
+// evaluating r, erfc and exp once per pass); MINB: CTAs per SM to fit.
+template <int NP, int MINB>
+__global__ void __launch_bounds__(REAL_THREADS, MINB) ewald_pair_real_eq(int nn, rsd_lat_dev L,
+                                                                        const double* __restrict__ pos,
+                                                                        const dsf* __restrict__ cr_g,
+                                                                        const float* __restrict__ cf_g, float rc2,
+                                                                        float rmax2, PlaneSink sk) {
   extern __shared__ __align__(16) unsigned char smraw_real[];
   RealEqShared& sh = *reinterpret_cast<RealEqShared*>(smraw_real);
   // blocks entirely on or below the diagonal (a >= b everywhere) have no work
@@ -832,53 +889,19 @@ __global__ void __launch_bounds__(REAL_THREADS) ewald_pair_real_eq(int nn, rsd_l
       }
     } while (col < (2 * NR + 1) * (2 * NR + 1));
 #pragma unroll
-    for (int q = 0; q < 60; q++) sh.oh[q][t] = rsd_real_epi_row<float, float, float>(q, acc, sh.cf);
-  }
-  // near images, double-single
-  {
-    dsacc acc[RSD_NMOM_REAL];
-#pragma unroll
-    for (int m = 0; m < RSD_NMOM_REAL; m++) acc[m] = dsacc(0);
-    const dsf lam_s = dsf_from(L.lam), cd_s = dsf_from(2.0 * RSD_PIP5 * L.lam);
-    int col = 0, nz = -NR;
-    do {
-      const int cnt = list_images<true>(sh, t, Rf, A, NR, col, nz, rc2, rmax2);
-      for (int q = 0; q < cnt; q++) {
-        const int e = sh.list[q][t];
-        const int ix = (e & 255) - NR, iy = ((e >> 8) & 255) - NR, iz = (e >> 16) - NR;
-        const dsf x0 = Rs[0] + ix * As[0] + iy * As[3] + iz * As[6];
-        const dsf x1 = Rs[1] + ix * As[1] + iy * As[4] + iz * As[7];
-        const dsf x2 = Rs[2] + ix * As[2] + iy * As[5] + iz * As[8];
-        const dsf r = dsf_sqrt(x0 * x0 + x1 * x1 + x2 * x2);
-        const dsf ir = dsf_rcp(r);
-        dsf E0, G;
-        dsf_erfc_gauss(lam_s * r, sh.T, &E0, &G);
-        rsd_real_image<dsf, dsacc>(x0, x1, x2, r, ir, E0, cd_s * G, lam_s, acc);
-        if ((q & 3) == 3) {  // keep the accumulators' lo parts small
-#pragma unroll
-          for (int m = 0; m < RSD_NMOM_REAL; m++) dsacc_norm(acc[m]);
-        }
-      }
-#pragma unroll
-      for (int m = 0; m < RSD_NMOM_REAL; m++) dsacc_norm(acc[m]);
-    } while (col < (2 * NR + 1) * (2 * NR + 1));
-    dsf accn[RSD_NMOM_REAL];
-#pragma unroll
-    for (int m = 0; m < RSD_NMOM_REAL; m++) accn[m] = dsf(acc[m].hi, acc[m].lo);
-#pragma unroll
     for (int q = 0; q < 60; q++) {
-      dsacc o = rsd_real_epi_row<dsf, dsf, dsacc>(q, accn, sh.cr);
-      o += dsf(sh.oh[q][t], 0.f);
-      dsacc_norm(o);
-      sh.oh[q][t] = o.hi;
-      sh.ol[q][t] = o.lo;
+      sh.oh[q][t] = rsd_real_epi_row<float, float, float>(q, acc, sh.cf);
+      sh.ol[q][t] = 0.f;
     }
   }
+  // near images, double-single, in NP passes
+  near_parts<NP, 0>(sh, t, Rf, A, Rs, As, NR, rc2, dsf_from(L.lam), dsf_from(2.0 * RSD_PIP5 * L.lam));
   dsf v[60];
 #pragma unroll
   for (int q = 0; q < 60; q++) v[q] = dsf(sh.oh[q][t], sh.ol[q][t]);
   store_pair_t<dsf>(sk, nn, a, b, v, 1);
 }
+
 
 __global__ void __launch_bounds__(128) ewald_pair_real(int nn, rsd_lat_dev L, const double* __restrict__ pos,
                                                        const double* __restrict__ radii, double inv_pimu,
@@ -1100,6 +1123,31 @@ static rsd_lat_dev mixed_lattice(const rsd_ctx* ctx, rsd_lat_dev L) {
   return L;
 }
 
+namespace {
+template <int NP, int MINB>
+int launch_real_eq_t(rsd_ctx* ctx, dim3 grd, dim3 blk, int nn, const rsd_lat_dev& L, const double* d_pos,
+                     const dsf* cr, const float* cf, float rc2, float rmax2, const PlaneSink& psk) {
+  static bool attr = false;
+  if (!attr) {
+    RSD_CUDA(ctx, cudaFuncSetAttribute(ewald_pair_real_eq<NP, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       SMEM_REAL_EQ));
+    attr = true;
+  }
+  ewald_pair_real_eq<NP, MINB><<<grd, blk, SMEM_REAL_EQ, ctx->stream>>>(nn, L, d_pos, cr, cf, rc2, rmax2, psk); RSD_LAUNCH_NOTE();
+  return RSD_OK;
+}
+
+int launch_real_eq(rsd_ctx* ctx, int passes, dim3 grd, dim3 blk, int nn, const rsd_lat_dev& L, const double* d_pos,
+                   const dsf* cr, const float* cf, float rc2, float rmax2, const PlaneSink& psk) {
+  switch (passes) {
+    case 1: return launch_real_eq_t<1, 2>(ctx, grd, blk, nn, L, d_pos, cr, cf, rc2, rmax2, psk);
+    case 2: return launch_real_eq_t<2, 2>(ctx, grd, blk, nn, L, d_pos, cr, cf, rc2, rmax2, psk);
+    case 3: return launch_real_eq_t<3, 2>(ctx, grd, blk, nn, L, d_pos, cr, cf, rc2, rmax2, psk);
+    default: return launch_real_eq_t<4, 2>(ctx, grd, blk, nn, L, d_pos, cr, cf, rc2, rmax2, psk);
+  }
+}
+}  // namespace
+
 int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
                        double mu_f, int precision, double* d_M, int64_t ldm) {
   if (nn < 1 || ldm < 11LL * nn) return rsd_fail(ctx, RSD_EARG, "bad size nn=%d ldm=%lld", nn, (long long)ldm);
@@ -1209,14 +1257,8 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
         dsf* cr = (dsf*)rsd_scratch(ctx, "ewald_real_cr", sizeof(dsf) * RSD_REAL_EPI_NC);
         float* cf = (float*)rsd_scratch(ctx, "ewald_real_cf", sizeof(float) * RSD_REAL_EPI_NC);
         if (!cr || !cf) return RSD_ENOMEM;
-        static bool attr = false;
-        if (!attr) {
-          RSD_CUDA(ctx, cudaFuncSetAttribute(ewald_pair_real_eq, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             SMEM_REAL_EQ));
-          attr = true;
-        }
         ewald_real_epi_table<<<1, 32, 0, s>>>(hr[0], L.phix, inv_pimu, cr, cf); RSD_LAUNCH_NOTE();
-        ewald_pair_real_eq<<<grd, blk, SMEM_REAL_EQ, s>>>(nn, L, d_pos, cr, cf, (float)rc2, (float)rmax2, psk); RSD_LAUNCH_NOTE();
+        RSD_TRY(launch_real_eq(ctx, ctx->mixed_real_passes, grd, blk, nn, L, d_pos, cr, cf, (float)rc2, (float)rmax2, psk));
       } else {
         ewald_pair_real_near_ds<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, psk); RSD_LAUNCH_NOTE();
         ewald_pair_real_far<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, rmax2, psk); RSD_LAUNCH_NOTE();

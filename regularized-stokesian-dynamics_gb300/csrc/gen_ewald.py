@@ -326,9 +326,36 @@ def gen():
     monos = sorted({xm for _, xm in mom_r if sum(xm) > 0}, key=lambda t: (sum(t), t))
     L.append("")
     L.append("// Adds one real-space image at separation (x0,x1,x2), r = |x|, E0 = erfc(lam r),")
+    # partitions of the moments into NP = 2..4 parts that share few radial
+    # functions (whole g-groups, greedily balanced), for kernels that sum the
+    # moments of one part per pass over the images
+    fidx0 = {sp.srepr(g): i for i, g in enumerate(fns)}
+    groups = {}
+    for m, (g, xm) in enumerate(mom_r):
+        groups.setdefault(fidx0[sp.srepr(g)], []).append(m)
+    tables = {}
+    for NP in (2, 3, 4):
+        load = [0] * NP
+        part = [0] * len(mom_r)
+        for gi, ms in sorted(groups.items(), key=lambda kv: -len(kv[1])):
+            pbest = min(range(NP), key=lambda p_: load[p_])
+            for m in ms:
+                part[m] = pbest
+            load[pbest] += len(ms)
+        tables[NP] = part
+    L.append("// Part of real moment m when the moments are summed in NP passes (NP = 1..4):")
+    L.append("// whole groups of moments that share a radial function, balanced by count.")
+    L.append("__host__ __device__ constexpr int rsd_mom_part(int m, int NP) {")
+    for NP in (2, 3, 4):
+        L.append("  constexpr unsigned char p%d[%d] = {%s};" % (NP, len(mom_r), ", ".join(str(v) for v in tables[NP])))
+    L.append("  return NP <= 1 ? 0 : NP == 2 ? p2[m] : NP == 3 ? p3[m] : p4[m];")
+    L.append("}")
+    L.append("")
+    L.append("// Adds one real-space image at separation (x0,x1,x2), r = |x|, E0 = erfc(lam r),")
     L.append("// Ed = 2 lam exp(-lam^2 r^2)/sqrt(pi); lam2..lam10 are powers of lam.  A is the")
     L.append("// accumulator type (T, or a wider accumulator with fma(T, T, A) and A += T).")
-    L.append("template <typename T, typename A = T>")
+    L.append("// With NP > 1 only the moments of part P (rsd_mom_part) are added.")
+    L.append("template <typename T, typename A = T, int NP = 1, int P = 0>")
     L.append("__device__ __forceinline__ void rsd_real_image(T x0, T x1, T x2, T r, T ir, T E0, T Ed, T lam,")
     L.append("                                               A* __restrict__ acc) {")
     irs = sp.Symbol("ir")
@@ -373,10 +400,11 @@ def gen():
     for m, (g, xm) in enumerate(mom_r):
         f = fnames[fidx[sp.srepr(g)]]
         mono = have.get(xm) if sum(xm) > 0 else None
+        pre = "  if constexpr (rsd_mom_part(%d, NP) == P) " % m
         if mono is None:
-            L.append("  acc[%d] += %s;" % (m, f))
+            L.append(pre + "acc[%d] += %s;" % (m, f))
         else:
-            L.append("  acc[%d] = fma(%s, %s, acc[%d]);" % (m, f, mono, m))
+            L.append(pre + "acc[%d] = fma(%s, %s, acc[%d]);" % (m, f, mono, m))
     L.append("}")
     L.append("")
 
@@ -441,7 +469,8 @@ def gen():
     L.append("")
     L.append("// Output q alone (q a compile-time constant after unrolling): the sum over")
     L.append("// its table entries of c[k] acc[m_k].")
-    L.append("template <typename CT, typename A, typename O>")
+    L.append("// With NP > 1 only the moments of part P (rsd_mom_part).")
+    L.append("template <typename CT, typename A, typename O, int NP = 1, int P = 0>")
     L.append("__device__ __forceinline__ O rsd_real_epi_row(int q, const A* __restrict__ acc, const CT* __restrict__ c) {")
     L.append("  O o = O(0);")
     L.append("  switch (q) {")
@@ -453,7 +482,7 @@ def gen():
             continue
         L.append("    case %d:" % q)
         for kk, m in byq[q]:
-            L.append("      o = fma(c[%d], acc[%d], o);" % (kk, m))
+            L.append("      if constexpr (rsd_mom_part(%d, NP) == P) o = fma(c[%d], acc[%d], o);" % (m, kk, m))
         L.append("      break;")
     L.append("    default:")
     L.append("      break;")

@@ -299,6 +299,10 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   RSD_TRY(rsd_wide_inverses_s(ctx, (int)P, A32, P, "rpp32", rsd_potrf_inverses_s(ctx, (int)P, "rpp32"), &W_r));
   if (use_uh) RSD_TRY(rsd_uhat_build(ctx, (int)P, A32, P, W_r, "rpp32", &uh_r));
   // refinement
+  int* tri_err = rsd_uhat_error_flag(ctx);
+  if (!tri_err) return RSD_ENOMEM;
+  RSD_CUDA(ctx, cudaMemsetAsync(tri_err, 0, sizeof(int), s));
+  int h_tri_err = 0;
   cudaEventRecord(ctx->ev[7], s);
   RSD_CUDA(ctx, cudaMemsetAsync(f, 0, sizeof(double) * nr * n, s));
   RSD_CUDA(ctx, cudaMemsetAsync(U, 0, sizeof(double) * nr * P, s));
@@ -324,7 +328,9 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
     build_r2<<<nblk(P * nr), 256, 0, s>>>(P, n, nr, Fe, have_fe, f, Lw, r2); RSD_LAUNCH_NOTE();
     norms<<<nr, 256, 0, s>>>(P, n, nr, r1, r2, ein, Fe, have_fe, nrm); RSD_LAUNCH_NOTE();
     RSD_CUDA(ctx, cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 2 * nr, cudaMemcpyDeviceToHost, s));
+    RSD_CUDA(ctx, cudaMemcpyAsync(&h_tri_err, tri_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     RSD_CUDA(ctx, cudaStreamSynchronize(s));
+    if (h_tri_err) return rsd_fail(ctx, RSD_ETIMEOUT, "refinement: a triangular sweep's wait timed out");
     worst = 0.0;
     for (int c = 0; c < nr; c++) {
       const double rr = sqrt(hn[2 * c]) / (sqrt(hn[2 * c + 1]) > 0 ? sqrt(hn[2 * c + 1]) : 1.0);

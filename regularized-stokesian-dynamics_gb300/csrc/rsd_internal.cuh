@@ -36,6 +36,7 @@ struct rsd_ctx {
   int mixed_kshell = 1;     // mixed assembly: FP64 reciprocal shells max|n_i| <= this
   double mixed_rmax = 6.0;  // mixed assembly: real images with lambda r beyond this dropped
   double mixed_kexp = 10.0 * 3.141592653589793;  // and reciprocal vectors with k^2/(4 lambda^2) beyond this
+  int mixed_real_passes = 1;  // mixed assembly, equal radii: passes over the near images (moment parts)
   double mixed_lambda_scale = 1.5;  // mixed assembly: Ewald splitting parameter relative to the reference's
   cudaStream_t side = nullptr;  // higher-priority stream for look-ahead panels
   cudaEvent_t ev_panel = nullptr, ev_next = nullptr;
@@ -175,3 +176,6 @@ struct rsd_uhat {
 };
 int rsd_uhat_build(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const float* W2, const char* tag, rsd_uhat* out);
 int rsd_uhat_solve(rsd_ctx* ctx, const rsd_uhat* h, float* X, int64_t ldx, int nrhs, float* Y);
+// device word that turns nonzero when a wait of the solves' dataflow sweeps
+// timed out (zero it before the solves, read it after synchronising)
+int* rsd_uhat_error_flag(rsd_ctx* ctx);
