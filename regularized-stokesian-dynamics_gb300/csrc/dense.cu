@@ -1625,21 +1625,52 @@ __global__ void __launch_bounds__(TRI_THREADS) tri_backward(TriArgs A) {
   }
 }
 
-// w_b = G_b z_b for every block, one thread per row
+// w_b = G_b z_b for every block: a CTA takes 128 rows of one block (32
+// lanes x 4 rows, float4 loads) and splits the block's columns over its 8
+// warps, reduced in shared memory
 template <int NR>
 __global__ void __launch_bounds__(256) blockdiag_gemv(int n, const float* __restrict__ G, const float* __restrict__ z,
                                                       float* __restrict__ w, int64_t ldx) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int b = i / NB2, il = i % NB2, j0 = b * NB2, jb = min(NB2, n - j0);
-  const float* Gb = G + (size_t)b * NB2 * NB2;
-  float acc[NR];
-  for (int r = 0; r < NR; r++) acc[r] = 0.f;
-  for (int k = 0; k < jb; k++) {
-    const float g = Gb[il + (size_t)k * NB2];
-    for (int r = 0; r < NR; r++) acc[r] += g * z[j0 + k + r * ldx];
+  __shared__ __align__(16) float zsh[NR][NB2];
+  __shared__ float red[8][NR][128];
+  const int b = blockIdx.x / (NB2 / 128), rq = blockIdx.x % (NB2 / 128);
+  const int j0 = b * NB2, jb = min(NB2, n - j0);
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  for (int e = t; e < NB2; e += 256)
+    for (int r = 0; r < NR; r++) zsh[r][e] = e < jb ? z[j0 + e + r * ldx] : 0.f;
+  __syncthreads();
+  const float* Gb = G + (size_t)b * NB2 * NB2 + rq * 128 + 4 * lane;  // G_b is NB2 x NB2, zero-padded
+  float acc[NR][4];
+#pragma unroll
+  for (int r = 0; r < NR; r++)
+#pragma unroll
+    for (int i = 0; i < 4; i++) acc[r][i] = 0.f;
+  const int kbeg = warp * (NB2 / 8);
+#pragma unroll 8
+  for (int kk = 0; kk < NB2 / 8; kk++) {
+    const int k = kbeg + kk;
+    const float4 g = *reinterpret_cast<const float4*>(Gb + (size_t)k * NB2);
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+      const float x = zsh[r][k];
+      acc[r][0] += g.x * x;
+      acc[r][1] += g.y * x;
+      acc[r][2] += g.z * x;
+      acc[r][3] += g.w * x;
+    }
   }
-  for (int r = 0; r < NR; r++) w[i + r * ldx] = acc[r];
+#pragma unroll
+  for (int r = 0; r < NR; r++)
+#pragma unroll
+    for (int i = 0; i < 4; i++) red[warp][r][4 * lane + i] = acc[r][i];
+  __syncthreads();
+  for (int e = t; e < NR * 128; e += 256) {
+    const int r = e / 128, il = e % 128, row = rq * 128 + il;
+    float v = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; q++) v += red[q][r][il];
+    if (row < jb) w[j0 + row + r * ldx] = v;
+  }
 }
 
 }  // namespace
@@ -1699,9 +1730,9 @@ int rsd_uhat_solve(rsd_ctx* ctx, const rsd_uhat* h, float* X, int64_t ldx, int n
     RSD_LAUNCH_NOTE();
   }
   if (nrhs == 1)
-    blockdiag_gemv<1><<<(n + 255) / 256, 256, 0, s>>>(n, h->G, X, Y, ldx);
+    blockdiag_gemv<1><<<nblk2 * (NB2 / 128), 256, 0, s>>>(n, h->G, X, Y, ldx);
   else
-    blockdiag_gemv<2><<<(n + 255) / 256, 256, 0, s>>>(n, h->G, X, Y, ldx);
+    blockdiag_gemv<2><<<nblk2 * (NB2 / 128), 256, 0, s>>>(n, h->G, X, Y, ldx);
   RSD_LAUNCH_NOTE();
   if (tasks > 0) {  // backward, in place on Y
     A.V = Y;
