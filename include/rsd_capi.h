@@ -74,9 +74,10 @@ long long rsd_launch_count(void);
 /* Tensor cores in the FP32 factorisations of the mixed-precision form:
  * 1 (the default) = tcgen05 kernels wherever the layout allows (16-byte
  * aligned blocks, leading dimension a multiple of 4), TF32 for the factor of
- * the grand mobility and 3xTF32 (close to FP32) for the inverse and the
- * factor of RPP; 3 = 3xTF32 for all three (fewer refinement iterations);
- * 0 = FP32 SIMT kernels only.  The FP64 form is unaffected. */
+ * the grand mobility and the inverse of its Schur factor, 3xTF32 (close to
+ * FP32) for the factor of RPP; 3 = 3xTF32 for all three (at most one
+ * refinement iteration fewer); 0 = FP32 SIMT kernels only.  The FP64 form
+ * is unaffected. */
 int rsd_ctx_set_tensor_cores(rsd_ctx* ctx, int mode);
 /* Precision split of the mixed-precision Ewald assembly: real-space images
  * with lammda*r < lam_r_cut (at most 6) and reciprocal vectors with

@@ -269,10 +269,11 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   int inf = 0;
   // Tensor-core precision per factor.  The refinement contracts by about the
   // preconditioner's relative error times the condition number it meets:
-  // cond(M') is moderate, so TF32 (2^-11) suffices for the factor of M';
-  // the inverse A^-1 meets cond(A)^2 and the factor of RPP meets cond(RPP),
-  // which grows like the inverse lubrication gap, so those use 3xTF32
-  // (about 2^-21, close to FP32).
+  // cond(M') is moderate, so TF32 (2^-11) suffices for the factor of M' and
+  // for the inverse A^-1 (at N = 2048, phi = 0.5: 7 iterations instead of 6
+  // with 3xTF32 there, for half the inverse's time); the factor of RPP meets
+  // cond(RPP), which grows like the inverse lubrication gap, and uses 3xTF32
+  // (about 2^-21, close to FP32; TF32 there takes ~17 iterations).
   RSD_TRY(rsd_potrf_upper_t<float>(ctx, (int)n, M32, n, &inf, "m32", ctx->use_tc == 3 ? 3 : 1));
   if (inf) {
     info->info = inf;
@@ -287,7 +288,7 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   if (use_uh) RSD_TRY(rsd_uhat_build(ctx, (int)n, M32, n, W_m, "m32", &uh_m));
   // A^-1 from the trailing factor block, then RPP32 = A^-1 + rfu and its factor
   copy_block_f<<<nblk(P * P), 256, 0, s>>>(P, P, M32 + Q + Q * n, n, A32, P); RSD_LAUNCH_NOTE();
-  RSD_TRY(rsd_potri_upper_t<float>(ctx, (int)P, A32, P, "a32", 3));
+  RSD_TRY(rsd_potri_upper_t<float>(ctx, (int)P, A32, P, "a32", ctx->use_tc == 3 ? 3 : 1));
   RSD_TRY(rsd_mirror_upper_t<float>(ctx, (int)P, A32, P));
   if (p->use_lub) RSD_TRY(rsd_lub_add_pp_f32(ctx, &lub, A32, P));
   RSD_TRY(rsd_potrf_upper_t<float>(ctx, (int)P, A32, P, &inf, "rpp32", 3));
