@@ -1690,13 +1690,17 @@ int rsd_uhat_build(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const float
   transpose_block<<<dim3(NB2 / 32, NB2 / 32, nblk2), dim3(32, 8), 0, s>>>(NB2, W2, WT); RSD_LAUNCH_NOTE();
   RSD_CUDA(ctx, cudaMemsetAsync(ctx->d_info + 1, 0, sizeof(int), s));
   int* err = ctx->d_info + 1;
-  for (int b = 0; b < nblk2; b++) {
-    const int j0 = b * NB2, jb = n - j0 < NB2 ? n - j0 : NB2, rest = n - j0 - jb;
-    const float* WTb = WT + (size_t)b * NB2 * NB2;
-    RSD_TRY(rsd_tc_gemm(ctx, 3, NB2, NB2, NB2, 1.0f, WTb, NB2, WTb, NB2, G + (size_t)b * NB2 * NB2, NB2, 0, 0, 0, err));
-    if (rest > 0)
-      RSD_TRY(rsd_tc_gemm(ctx, 3, jb, rest, jb, 1.0f, WTb, NB2, U + j0 + (int64_t)(j0 + jb) * ldu, ldu,
-                          Uh + j0 + (int64_t)(j0 + jb) * ldu, ldu, 0, 0, 0, err));
+  // all blocks in two batched launches: G_b = W_b W_b^T, and the strips
+  // Uh_b = W_b^T U(block b rows, columns after block b), whose width drops
+  // by NB2 from one block to the next
+  const int64_t nw = (int64_t)nblk2 * NB2;
+  RSD_TRY(rsd_tc_gemm_zbatch(ctx, 3, NB2, NB2, NB2, 1.0f, WT, NB2, NB2, nw, WT, NB2, NB2, nw, G, NB2, NB2, nw, nblk2,
+                             0, NB2, 0, NB2, 0, NB2, 0, err));
+  if (nblk2 > 1) {
+    const float* U1 = U + (int64_t)NB2 * ldu;  // columns from NB2 on
+    float* Uh1 = Uh + (int64_t)NB2 * ldu;
+    RSD_TRY(rsd_tc_gemm_zbatch(ctx, 3, NB2, n - NB2, NB2, 1.0f, WT, NB2, NB2, nw, U1, ldu, n, n - NB2, Uh1, ldu, n,
+                               n - NB2, nblk2 - 1, 0, NB2, NB2, NB2, NB2, NB2, NB2, err));
   }
   RSD_CUDA(ctx, cudaMemcpyAsync(ctx->h_info + 1, err, sizeof(int), cudaMemcpyDeviceToHost, s));
   RSD_CUDA(ctx, cudaStreamSynchronize(s));

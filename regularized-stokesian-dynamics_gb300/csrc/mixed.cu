@@ -57,6 +57,18 @@ __global__ void convert_perm(int N, int64_t n, const float* __restrict__ Mh, int
   M32[i + j * n] = Mh[si + sj * ld];
 }
 
+// convert_perm with 16-byte moves: four consecutive rows of one column, which
+// stay inside one part of the permutation when N is a multiple of 4
+__global__ void convert_perm4(int N, int64_t n, const float* __restrict__ Mh, int64_t ld, float* __restrict__ M32) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t n4 = n / 4;
+  if (t >= n4 * n) return;
+  const int64_t i = (t % n4) * 4, j = t / n4;
+  const int64_t Q = 5LL * N;
+  const int64_t si = i < Q ? 6LL * N + i : i - Q, sj = j < Q ? 6LL * N + j : j - Q;
+  *reinterpret_cast<float4*>(M32 + i + j * n) = *reinterpret_cast<const float4*>(Mh + si + sj * ld);
+}
+
 // x (FP64) as float pairs
 __global__ void to_dsf_vec(int64_t n, const double* __restrict__ x, float2* __restrict__ xs) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -265,7 +277,11 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   info->n_contact = nc;
   cudaEventRecord(ctx->ev[6], s);
   // FP32 factor of M' (stresslets first)
-  convert_perm<<<(unsigned)((n * n + 255) / 256), 256, 0, s>>>(nn, n, Mh, ld, M32); RSD_LAUNCH_NOTE();
+  if (nn % 4 == 0 && ld % 4 == 0 && ((uintptr_t)Mh & 15) == 0) {
+    convert_perm4<<<(unsigned)((n * n / 4 + 255) / 256), 256, 0, s>>>(nn, n, Mh, ld, M32); RSD_LAUNCH_NOTE();
+  } else {
+    convert_perm<<<(unsigned)((n * n + 255) / 256), 256, 0, s>>>(nn, n, Mh, ld, M32); RSD_LAUNCH_NOTE();
+  }
   int inf = 0;
   // Tensor-core precision per factor.  The refinement contracts by about the
   // preconditioner's relative error times the condition number it meets:

@@ -161,6 +161,10 @@ int rsd_tc_gemm_ok(const float* A, int64_t lda, const float* B, int64_t ldb, con
 int rsd_tc_gemm(rsd_ctx* ctx, int prec, int m, int n, int K, float alpha, const float* A, int64_t lda,
                 const float* B, int64_t ldb, float* C, int64_t ldc, int reduce, int tri, int klo_col, int* d_err,
                 cudaStream_t stream = 0, int ksplit = 0);
+int rsd_tc_gemm_zbatch(rsd_ctx* ctx, int prec, int m, int n, int K, float alpha, const float* A, int64_t lda,
+                       int64_t a_rows, int64_t a_cols, const float* B, int64_t ldb, int64_t b_rows, int64_t b_cols,
+                       float* C, int64_t ldc, int64_t c_rows, int64_t c_cols, int nbatch, int zak, int zam, int zbk,
+                       int zbn, int zcm, int zcn, int ndec, int* d_err);
 int rsd_tc_syrk_ok(const float* panel, int64_t lda, const float* C, int64_t ldc, int kb);
 int rsd_tc_syrk(rsd_ctx* ctx, int prec, const float* panel, int64_t lda, int kb, int rest, float* C, int64_t ldc,
                 int* d_err);

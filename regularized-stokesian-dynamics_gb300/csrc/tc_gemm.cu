@@ -62,6 +62,9 @@ struct TcArgs {
   int ksplit;    // > 0: CTA z sums K in [z ksplit, (z + 1) ksplit) (a multiple of TC_KC; reduce = 1)
   float alpha;
   int* err;
+  // batches (ksplit = 0): CTA z adds z times these to the coordinates of A
+  // (k, m), B (k, n) and C (m, n); the batch's n extent is n - z * ndec
+  int zak, zam, zbk, zbn, zcm, zcn, ncols, ndec;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -153,6 +156,10 @@ __global__ void __launch_bounds__(TC_THREADS, TcCfg<PREC>::MIN_CTAS)
   constexpr int ST = Cfg::STAGES, SB = Cfg::STAGE_BYTES;
   const int row0 = blockIdx.x * TC_TILE, col0 = blockIdx.y * TC_TILE;
   if (a.tri && row0 > col0) return;
+  const int z = a.ksplit > 0 ? 0 : (int)blockIdx.z;
+  if (a.ndec > 0 && col0 >= a.ncols - z * a.ndec) return;  // beyond this batch's columns
+  const int ak = z * a.zak, am = row0 + z * a.zam, bk = z * a.zbk, bn = col0 + z * a.zbn;
+  const int cm = row0 + z * a.zcm, cn = col0 + z * a.zcn;
   int klo = a.klo_col ? col0 : 0, khi = a.K;
   if (a.ksplit > 0) {
     klo = max(klo, (int)blockIdx.z * a.ksplit);
@@ -204,8 +211,8 @@ __global__ void __launch_bounds__(TC_THREADS, TcCfg<PREC>::MIN_CTAS)
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(TC_FULL(s)), "r"(2 * TC_CHUNK)
                      : "memory");
         const uint32_t st = sbase + s * SB;
-        tma_load(st, &tmA, klo + c * TC_KC, row0, TC_FULL(s));
-        tma_load(st + TC_CHUNK, &tmB, klo + c * TC_KC, col0, TC_FULL(s));
+        tma_load(st, &tmA, ak + klo + c * TC_KC, am, TC_FULL(s));
+        tma_load(st + TC_CHUNK, &tmB, bk + klo + c * TC_KC, bn, TC_FULL(s));
         last[s] = c;
       }
       if (abort_flag) {  // let the copies already issued land before the CTA exits
@@ -309,11 +316,11 @@ __global__ void __launch_bounds__(TC_THREADS, TcCfg<PREC>::MIN_CTAS)
       if (a.reduce) {
         asm volatile(
             "cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(tm),
-            "r"(row0), "r"(col0), "r"(sbase)
+            "r"(cm), "r"(cn), "r"(sbase)
             : "memory");
       } else {
         asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(tm),
-                     "r"(row0), "r"(col0), "r"(sbase)
+                     "r"(cm), "r"(cn), "r"(sbase)
                      : "memory");
       }
       asm volatile("cp.async.bulk.commit_group;" ::: "memory");
@@ -393,13 +400,41 @@ int rsd_tc_gemm(rsd_ctx* ctx, int prec, int m, int n, int K, float alpha, const 
   RSD_TRY(encode_2d(ctx, &tmA, A, K, m, lda, TC_KC, TC_TILE, CU_TENSOR_MAP_SWIZZLE_128B));
   RSD_TRY(encode_2d(ctx, &tmB, B, K, n, ldb, TC_KC, TC_TILE, CU_TENSOR_MAP_SWIZZLE_128B));
   RSD_TRY(encode_2d(ctx, &tmC, C, m, n, ldc, TC_TILE, TC_TILE, CU_TENSOR_MAP_SWIZZLE_NONE));
-  TcArgs a{K, tri, klo_col, reduce, ksplit, alpha, d_err};
+  TcArgs a{K, tri, klo_col, reduce, ksplit, alpha, d_err, 0, 0, 0, 0, 0, 0, 0, 0};
   const dim3 grid((m + TC_TILE - 1) / TC_TILE, (n + TC_TILE - 1) / TC_TILE, ksplit > 0 ? (K + ksplit - 1) / ksplit : 1);
   cudaStream_t st = stream ? stream : ctx->stream;
   if (prec == 1) {
     tc_gemm_kernel<1><<<grid, TC_THREADS, TcCfg<1>::SMEM, st>>>(tmA, tmB, tmC, a);
   } else {
     tc_gemm_kernel<3><<<grid, TC_THREADS, TcCfg<3>::SMEM, st>>>(tmA, tmB, tmC, a);
+  }
+  RSD_LAUNCH_NOTE();
+  RSD_CUDA(ctx, cudaGetLastError());
+  return RSD_OK;
+}
+
+// nbatch products C_z = alpha A_z^T B_z (store) of m x n x K each, one
+// launch: the operands are sub-blocks of three column-major arrays (A: a_rows
+// x a_cols, ld lda; likewise B and C) whose coordinates move by the given
+// steps per batch z (A: k, m; B: k, n; C: m, n); batch z has n - z * ndec
+// columns.  prec 1 or 3.
+int rsd_tc_gemm_zbatch(rsd_ctx* ctx, int prec, int m, int n, int K, float alpha, const float* A, int64_t lda,
+                       int64_t a_rows, int64_t a_cols, const float* B, int64_t ldb, int64_t b_rows, int64_t b_cols,
+                       float* C, int64_t ldc, int64_t c_rows, int64_t c_cols, int nbatch, int zak, int zam, int zbk,
+                       int zbn, int zcm, int zcn, int ndec, int* d_err) {
+  if (m < 1 || n < 1 || K < 1 || nbatch < 1 || (prec != 1 && prec != 3) || !rsd_tc_gemm_ok(A, lda, B, ldb, C, ldc))
+    return rsd_fail(ctx, RSD_EARG, "tc_gemm_zbatch: unsupported arguments (m=%d n=%d K=%d)", m, n, K);
+  RSD_TRY(tc_init(ctx));
+  CUtensorMap tmA, tmB, tmC;
+  RSD_TRY(encode_2d(ctx, &tmA, A, a_rows, a_cols, lda, TC_KC, TC_TILE, CU_TENSOR_MAP_SWIZZLE_128B));
+  RSD_TRY(encode_2d(ctx, &tmB, B, b_rows, b_cols, ldb, TC_KC, TC_TILE, CU_TENSOR_MAP_SWIZZLE_128B));
+  RSD_TRY(encode_2d(ctx, &tmC, C, c_rows, c_cols, ldc, TC_TILE, TC_TILE, CU_TENSOR_MAP_SWIZZLE_NONE));
+  TcArgs a{K, 0, 0, 0, 0, alpha, d_err, zak, zam, zbk, zbn, zcm, zcn, n, ndec};
+  const dim3 grid((m + TC_TILE - 1) / TC_TILE, (n + TC_TILE - 1) / TC_TILE, nbatch);
+  if (prec == 1) {
+    tc_gemm_kernel<1><<<grid, TC_THREADS, TcCfg<1>::SMEM, ctx->stream>>>(tmA, tmB, tmC, a);
+  } else {
+    tc_gemm_kernel<3><<<grid, TC_THREADS, TcCfg<3>::SMEM, ctx->stream>>>(tmA, tmB, tmC, a);
   }
   RSD_LAUNCH_NOTE();
   RSD_CUDA(ctx, cudaGetLastError());
