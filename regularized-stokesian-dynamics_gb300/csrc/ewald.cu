@@ -266,6 +266,114 @@ __device__ inline void store_pair_t(const S& sk, int N, int a, int b, const V* v
   }
 }
 
+// Mixed form: only the entries whose row belongs to particle a (a < b) of
+// each pair block are written (121 of 242: the pair's rows of the grand
+// matrix, all coalesced along a); mirror_planes fills the rest by symmetry
+// once every pair kernel is done.  Values as in store_pair_t.
+__device__ inline void store_pair_rows_a(const PlaneSink& sk, int N, int a, int b, const dsf* v, int add) {
+  auto at = [&](int r, int c) { return (int64_t)r + (int64_t)c * sk.ld; };
+  constexpr int sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+  {  // TT and RR
+    int64_t p[18];
+    dsf x[18];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        p[3 * i + j] = at(3 * a + i, 3 * b + j);
+        x[3 * i + j] = v[sym[i][j]];
+        p[9 + 3 * i + j] = at(3 * N + 3 * a + i, 3 * N + 3 * b + j);
+        x[9 + 3 * i + j] = v[6 + sym[i][j]];
+      }
+    sk.template put<18>(p, x, add);
+  }
+  {  // TR: a's translation rows against b's rotation, a's rotation rows against b's translation
+    int64_t p[18];
+    dsf x[18];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        dsf tr = dsf(0);
+        if (i < j) tr = v[12 + (i == 0 ? j - 1 : 2)];
+        if (i > j) tr = -v[12 + (j == 0 ? i - 1 : 2)];
+        p[3 * i + j] = at(3 * a + i, 3 * N + 3 * b + j);
+        x[3 * i + j] = tr;
+        p[9 + 3 * i + j] = at(3 * N + 3 * a + j, 3 * b + i);
+        x[9 + 3 * i + j] = -tr;
+      }
+    sk.template put<18>(p, x, add);
+  }
+#pragma unroll
+  for (int grp = 0; grp < 4; grp++) {  // G and H: a's velocity rows, then a's stresslet rows
+    const int h = grp & 1, srow = grp >> 1;
+    const int ro = h ? 3 * N : 0;
+    int64_t p[15];
+    dsf x[15];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int m = 0; m < 5; m++) {
+        dsf g = v[(h ? 45 : 30) + 5 * i + m];
+        if (srow && !h) g = -g;
+        p[5 * i + m] = srow ? at(6 * N + 5 * a + m, ro + 3 * b + i) : at(ro + 3 * a + i, 6 * N + 5 * b + m);
+        x[5 * i + m] = g;
+      }
+    sk.template put<15>(p, x, add);
+  }
+  {  // QQ
+    int64_t p[25];
+    dsf x[25];
+#pragma unroll
+    for (int xi = 0; xi < 5; xi++)
+#pragma unroll
+      for (int y = 0; y < 5; y++) {
+        const int lo = xi < y ? xi : y, hi = xi < y ? y : xi;
+        p[5 * xi + y] = at(6 * N + 5 * a + xi, 6 * N + 5 * b + y);
+        x[5 * xi + y] = v[15 + lo * 5 - lo * (lo - 1) / 2 + (hi - lo)];
+      }
+    sk.template put<25>(p, x, add);
+  }
+}
+
+// particle of grand-matrix index x
+__device__ __forceinline__ int grand_particle(int N, int x) {
+  return x < 3 * N ? x / 3 : (x < 6 * N ? (x - 3 * N) / 3 : (x - 6 * N) / 5);
+}
+
+// M(r, c) = M(c, r) for every entry whose row's particle is above its
+// column's (the entries store_pair_rows_a leaves out), on both planes:
+// 32 x 32 tiles through shared memory, both the read and the write
+// coalesced; tiles with nothing to fill return at once.
+__global__ void mirror_planes(int N, int64_t n, float* __restrict__ hi, float* __restrict__ lo, int64_t ld) {
+  __shared__ float th[32][33], tl[32][33];
+  __shared__ int skip;
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  if (ty == 0) {  // the particle index is monotonic only within each of the three row sections
+    const int rmax = __reduce_max_sync(0xffffffffu, grand_particle(N, (int)min((int64_t)r0 + tx, n - 1)));
+    const int cmin = __reduce_min_sync(0xffffffffu, grand_particle(N, (int)min((int64_t)c0 + tx, n - 1)));
+    if (tx == 0) skip = rmax <= cmin;
+  }
+  __syncthreads();
+  if (skip) return;
+  for (int k = ty; k < 32; k += blockDim.y) {  // source M(c0 + tx, r0 + k)
+    const int64_t c = c0 + tx, r = r0 + k;
+    if (c < n && r < n) {
+      th[k][tx] = hi[c + r * ld];
+      tl[k][tx] = lo[c + r * ld];
+    }
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += blockDim.y) {  // destination M(r0 + tx, c0 + k)
+    const int64_t r = r0 + tx, c = c0 + k;
+    if (r < n && c < n && grand_particle(N, (int)r) > grand_particle(N, (int)c)) {
+      hi[r + c * ld] = th[tx][k];
+      lo[r + c * ld] = tl[tx][k];
+    }
+  }
+}
+
 // A pair block computed in FP64 into either destination.
 __device__ __forceinline__ void store_pair_d(const DenseSink& sk, int N, int a, int b, const double* o, int add) {
   store_pair_t<double>(sk, N, a, b, o, add);
@@ -274,7 +382,7 @@ __device__ __forceinline__ void store_pair_d(const PlaneSink& sk, int N, int a, 
   dsf v[60];
 #pragma unroll
   for (int q = 0; q < 60; q++) v[q] = dsf_from(o[q]);
-  store_pair_t<dsf>(sk, N, a, b, v, add);
+  store_pair_rows_a(sk, N, a, b, v, add);
 }
 
 // scale by nondim (1/(6 a_i) for TT, TR, G; 1/(6 a_i^3) for RR, QQ, H) and
@@ -573,7 +681,7 @@ __global__ void __launch_bounds__(128) ewald_pair_kblock(int nn, int K32, const 
     dsacc_norm(acc[q]);
     o[q] = dsf(acc[q].hi, acc[q].lo);
   }
-  store_pair_t<dsf>(sk, nn, a, b, o, add);
+  store_pair_rows_a(sk, nn, a, b, o, add);
 }
 
 // Near/far split of the real-space images for the mixed form.  Image nz of
@@ -899,7 +1007,7 @@ __global__ void __launch_bounds__(REAL_THREADS, MINB) ewald_pair_real_eq(int nn,
   dsf v[60];
 #pragma unroll
   for (int q = 0; q < 60; q++) v[q] = dsf(sh.oh[q][t], sh.ol[q][t]);
-  store_pair_t<dsf>(sk, nn, a, b, v, 1);
+  store_pair_rows_a(sk, nn, a, b, v, 1);
 }
 
 
@@ -1263,6 +1371,9 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
         ewald_pair_real_near_ds<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, psk); RSD_LAUNCH_NOTE();
         ewald_pair_real_far<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, rmax2, psk); RSD_LAUNCH_NOTE();
       }
+      const int64_t n11 = 11LL * nn;
+      const dim3 mt((unsigned)((n11 + 31) / 32), (unsigned)((n11 + 31) / 32));
+      mirror_planes<<<mt, dim3(32, 8), 0, s>>>(nn, n11, psk.hi, psk.lo, ldm); RSD_LAUNCH_NOTE();
     } else {
       ewald_pair_k<double, double2><<<grd, blk, 0, s>>>(nn, L, Kh, tab, cs, d_radii, inv_pimu, dsk, 0); RSD_LAUNCH_NOTE();
       ewald_pair_real<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, dsk); RSD_LAUNCH_NOTE();
