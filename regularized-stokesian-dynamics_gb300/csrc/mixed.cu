@@ -107,6 +107,134 @@ __global__ void gemv_planes_part(int m, int k, const float* __restrict__ Mh, con
   for (int r = 0; r < R; r++) part[((size_t)c * R + r) * m + i] = dsf_to(acc[r]);
 }
 
+// particle of grand-matrix index x
+__device__ __forceinline__ int grand_pid(int N, int x) {
+  return x < 3 * N ? x / 3 : (x < 6 * N ? (x - 3 * N) / 3 : (x - 6 * N) / 5);
+}
+
+// Symmetric M f over the stored half of M's planes: the entries whose row's
+// particle is at most the column's (pair blocks in the rows of their first
+// particle, and the whole diagonal particle blocks).  A CTA takes a 128 x 128
+// tile: row products of its stored entries (-> prow[R][C]) and column
+// products of its entries strictly above the particle diagonal
+// (-> pcol[C][R]), in double-single; tiles with no stored entry write zero
+// partials.  About half of M is read.  Needs n % 4 == 0.
+constexpr int SYMV_T = 128;
+template <int NR>
+__global__ void __launch_bounds__(256) symv_planes_part(int N, int n, const float* __restrict__ Mh,
+                                                        const float* __restrict__ Ml, int64_t ld,
+                                                        const float2* __restrict__ xs, int nbt,
+                                                        double* __restrict__ prow, double* __restrict__ pcol) {
+  __shared__ dsf red[8][NR][SYMV_T];
+  __shared__ float2 colp[NR][SYMV_T][33];  // per-lane column partials, reduced after the tile
+  __shared__ int skip;
+  const int R = blockIdx.x, C = blockIdx.y, r0 = R * SYMV_T, c0 = C * SYMV_T;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  double* pr = prow + ((size_t)R * nbt + C) * NR * SYMV_T;
+  double* pc = pcol + ((size_t)C * nbt + R) * NR * SYMV_T;
+  if (warp == 0) {  // stored entries exist iff min over rows of pid <= max over columns
+    int rmin = 1 << 30, cmax = -1;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int r = r0 + 4 * lane + k, c = c0 + 4 * lane + k;
+      if (r < n) rmin = min(rmin, grand_pid(N, r));
+      if (c < n) cmax = max(cmax, grand_pid(N, c));
+    }
+    rmin = __reduce_min_sync(0xffffffffu, rmin);
+    cmax = __reduce_max_sync(0xffffffffu, cmax);
+    if (lane == 0) skip = rmin > cmax;
+  }
+  __syncthreads();
+  if (skip) {
+    for (int e = t; e < NR * SYMV_T; e += 256) pr[e] = pc[e] = 0.0;
+    return;
+  }
+  const int rb = r0 + 4 * lane;  // this lane's four rows (one section: boundaries are multiples of 4)
+  int prr[4];
+  dsf xr[NR][4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const bool ok = rb + k < n;
+    prr[k] = ok ? grand_pid(N, rb + k) : (1 << 30);
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+      const float2 v = ok ? xs[rb + k + (int64_t)r * n] : make_float2(0.f, 0.f);
+      xr[r][k] = dsf(v.x, v.y);
+    }
+  }
+  dsacc racc[NR][4];
+#pragma unroll
+  for (int r = 0; r < NR; r++)
+#pragma unroll
+    for (int k = 0; k < 4; k++) racc[r][k] = dsacc(0);
+#pragma unroll 8
+  for (int cc = 0; cc < SYMV_T / 8; cc++) {
+    const int cl = warp * (SYMV_T / 8) + cc, c = c0 + cl;
+    dsacc cacc[NR];
+#pragma unroll
+    for (int r = 0; r < NR; r++) cacc[r] = dsacc(0);
+    if (c < n) {
+      const int pcn = grand_pid(N, c);
+      if (rb < n && prr[0] <= pcn) {  // the lane's rows hold stored entries of this column
+        const int64_t o = rb + (int64_t)c * ld;
+        const float4 h = *reinterpret_cast<const float4*>(Mh + o), l = *reinterpret_cast<const float4*>(Ml + o);
+        const dsf m[4] = {dsf(h.x, l.x), dsf(h.y, l.y), dsf(h.z, l.z), dsf(h.w, l.w)};
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+          const float2 xv = xs[c + (int64_t)r * n];
+          const dsf xc(xv.x, xv.y);
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            if (prr[k] <= pcn) racc[r][k] = fma(m[k], xc, racc[r][k]);
+            if (prr[k] < pcn) cacc[r] = fma(m[k], xr[r][k], cacc[r]);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+      dsacc_norm(cacc[r]);
+      colp[r][cl][lane] = make_float2(cacc[r].hi, cacc[r].lo);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < NR; r++)
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      dsacc_norm(racc[r][k]);
+      red[warp][r][4 * lane + k] = dsf(racc[r][k].hi, racc[r][k].lo);
+    }
+  __syncthreads();
+  for (int e = t; e < NR * SYMV_T; e += 256) {
+    const int r = e / SYMV_T, il = e % SYMV_T;
+    dsf v = red[0][r][il];
+#pragma unroll
+    for (int w = 1; w < 8; w++) v = v + red[w][r][il];
+    pr[e] = dsf_to(v);
+    dsf u(colp[r][il][0].x, colp[r][il][0].y);
+#pragma unroll 8
+    for (int q = 1; q < 32; q++) u = u + dsf(colp[r][il][q].x, colp[r][il][q].y);
+    pc[e] = dsf_to(u);
+  }
+}
+
+// y(:, r) += alpha * (sum_C prow[K][C] + sum_R pcol[K][R]) for row block K, fixed order
+__global__ void symv_planes_reduce(int n, int nr, int nbt, const double* __restrict__ prow,
+                                   const double* __restrict__ pcol, double alpha, double* __restrict__ y,
+                                   int64_t ldy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int K = i / SYMV_T, e = i % SYMV_T;
+  for (int r = 0; r < nr; r++) {
+    double s0 = 0.0, s1 = 0.0;
+    for (int J = 0; J < nbt; J++) {
+      s0 += prow[(((size_t)K * nbt + J) * nr + r) * SYMV_T + e];
+      s1 += pcol[(((size_t)K * nbt + J) * nr + r) * SYMV_T + e];
+    }
+    y[i + (int64_t)r * ldy] += alpha * (s0 + s1);
+  }
+}
+
 // y(:, r) += alpha * sum_c part[c][r]
 __global__ void gemv_planes_reduce(int m, int nr, int nchunk, const double* __restrict__ part, double alpha,
                                    double* __restrict__ y, int64_t ldy) {
@@ -259,8 +387,11 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   const float* Mh = reinterpret_cast<const float*>(M);
   const float* Ml = Mh + (size_t)ld * n;
   const unsigned gchunks = (unsigned)((n + GEMV_PL_CHUNK - 1) / GEMV_PL_CHUNK);
+  const bool symv = n % 4 == 0 && ld % 4 == 0;
+  const int nbt = (int)((n + SYMV_T - 1) / SYMV_T);
   float2* fs = (float2*)rsd_scratch(ctx, "mixed_fs", sizeof(float2) * (size_t)nr * n);
-  double* gpart = (double*)rsd_scratch(ctx, "mixed_gemv_part", sizeof(double) * (size_t)gchunks * nr * n);
+  double* gpart = symv ? (double*)rsd_scratch(ctx, "mixed_symv_part", sizeof(double) * 2 * (size_t)nbt * nbt * SYMV_T)
+                       : (double*)rsd_scratch(ctx, "mixed_gemv_part", sizeof(double) * (size_t)gchunks * nr * n);
   if (!fs || !gpart) return RSD_ENOMEM;
   float* M32 = (float*)rsd_scratch(ctx, "mixed_M32", sizeof(float) * n * n);
   float* A32 = (float*)rsd_scratch(ctx, "mixed_A32", sizeof(float) * P * P);
@@ -331,12 +462,20 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
     RSD_CUDA(ctx, cudaMemcpyAsync(r1, w, sizeof(double) * nr * n, cudaMemcpyDeviceToDevice, s));
     // r1 -= M f, double-single products of the two planes
     to_dsf_vec<<<nblk(n * nr), 256, 0, s>>>(n * nr, f, fs); RSD_LAUNCH_NOTE();
-    if (nr == 1) {
-      gemv_planes_part<1><<<dim3((unsigned)((n + 255) / 256), gchunks), 256, 0, s>>>((int)n, (int)n, Mh, Ml, ld, fs, gpart); RSD_LAUNCH_NOTE();
+    if (symv) {  // one right-hand side per pass (the shared-memory budget of a tile)
+      double* pcol = gpart + (size_t)nbt * nbt * SYMV_T;
+      for (int c = 0; c < nr; c++) {
+        symv_planes_part<1><<<dim3(nbt, nbt), 256, 0, s>>>(nn, (int)n, Mh, Ml, ld, fs + (size_t)c * n, nbt, gpart, pcol); RSD_LAUNCH_NOTE();
+        symv_planes_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>((int)n, 1, nbt, gpart, pcol, -1.0, r1 + (size_t)c * n, n); RSD_LAUNCH_NOTE();
+      }
     } else {
-      gemv_planes_part<2><<<dim3((unsigned)((n + 255) / 256), gchunks), 256, 0, s>>>((int)n, (int)n, Mh, Ml, ld, fs, gpart); RSD_LAUNCH_NOTE();
+      if (nr == 1) {
+        gemv_planes_part<1><<<dim3((unsigned)((n + 255) / 256), gchunks), 256, 0, s>>>((int)n, (int)n, Mh, Ml, ld, fs, gpart); RSD_LAUNCH_NOTE();
+      } else {
+        gemv_planes_part<2><<<dim3((unsigned)((n + 255) / 256), gchunks), 256, 0, s>>>((int)n, (int)n, Mh, Ml, ld, fs, gpart); RSD_LAUNCH_NOTE();
+      }
+      gemv_planes_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>((int)n, nr, gchunks, gpart, -1.0, r1, n); RSD_LAUNCH_NOTE();
     }
-    gemv_planes_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>((int)n, nr, gchunks, gpart, -1.0, r1, n); RSD_LAUNCH_NOTE();
     if (p->use_lub) {
       RSD_TRY(rsd_lub_spmv(ctx, &lub, nr, w, n, Lw, n));
     } else {
