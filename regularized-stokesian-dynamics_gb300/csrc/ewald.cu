@@ -268,8 +268,9 @@ __device__ inline void store_pair_t(const S& sk, int N, int a, int b, const V* v
 
 // Mixed form: only the entries whose row belongs to particle a (a < b) of
 // each pair block are written (121 of 242: the pair's rows of the grand
-// matrix, all coalesced along a); mirror_planes fills the rest by symmetry
-// once every pair kernel is done.  Values as in store_pair_t.
+// matrix, all coalesced along a); the consumers read the other half at the
+// mirrored position, or mirror_planes fills it by symmetry.  Values as in
+// store_pair_t.
 __device__ inline void store_pair_rows_a(const PlaneSink& sk, int N, int a, int b, const dsf* v, int add) {
   auto at = [&](int r, int c) { return (int64_t)r + (int64_t)c * sk.ld; };
   constexpr int sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
@@ -1256,6 +1257,15 @@ int launch_real_eq(rsd_ctx* ctx, int passes, dim3 grd, dim3 blk, int nn, const r
 }
 }  // namespace
 
+int rsd_mirror_planes(rsd_ctx* ctx, int nn, double* d_M, int64_t ldm) {
+  const int64_t n11 = 11LL * nn;
+  float* hi = reinterpret_cast<float*>(d_M);
+  const dim3 mt((unsigned)((n11 + 31) / 32), (unsigned)((n11 + 31) / 32));
+  mirror_planes<<<mt, dim3(32, 8), 0, ctx->stream>>>(nn, n11, hi, hi + (size_t)ldm * n11, ldm); RSD_LAUNCH_NOTE();
+  RSD_CUDA(ctx, cudaGetLastError());
+  return RSD_OK;
+}
+
 int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
                        double mu_f, int precision, double* d_M, int64_t ldm) {
   if (nn < 1 || ldm < 11LL * nn) return rsd_fail(ctx, RSD_EARG, "bad size nn=%d ldm=%lld", nn, (long long)ldm);
@@ -1371,9 +1381,6 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
         ewald_pair_real_near_ds<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, psk); RSD_LAUNCH_NOTE();
         ewald_pair_real_far<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, rc2, rmax2, psk); RSD_LAUNCH_NOTE();
       }
-      const int64_t n11 = 11LL * nn;
-      const dim3 mt((unsigned)((n11 + 31) / 32), (unsigned)((n11 + 31) / 32));
-      mirror_planes<<<mt, dim3(32, 8), 0, s>>>(nn, n11, psk.hi, psk.lo, ldm); RSD_LAUNCH_NOTE();
     } else {
       ewald_pair_k<double, double2><<<grd, blk, 0, s>>>(nn, L, Kh, tab, cs, d_radii, inv_pimu, dsk, 0); RSD_LAUNCH_NOTE();
       ewald_pair_real<<<grd, blk, 0, s>>>(nn, L, d_pos, d_radii, inv_pimu, dsk); RSD_LAUNCH_NOTE();

@@ -47,26 +47,58 @@ int rsd_potrs_wide_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const flo
 
 namespace {
 
-// M32 = M in [Q, P] order, FP32: the hi plane of the double-single M
-__global__ void convert_perm(int N, int64_t n, const float* __restrict__ Mh, int64_t ld, float* __restrict__ M32) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n * n) return;
-  const int64_t i = t % n, j = t / n;
-  const int64_t Q = 5LL * N;
-  const int64_t si = i < Q ? 6LL * N + i : i - Q, sj = j < Q ? 6LL * N + j : j - Q;
-  M32[i + j * n] = Mh[si + sj * ld];
+// particle of grand-matrix index x
+__device__ __forceinline__ int grand_pid(int N, int x) {
+  return x < 3 * N ? x / 3 : (x < 6 * N ? (x - 3 * N) / 3 : (x - 6 * N) / 5);
 }
 
-// convert_perm with 16-byte moves: four consecutive rows of one column, which
-// stay inside one part of the permutation when N is a multiple of 4
-__global__ void convert_perm4(int N, int64_t n, const float* __restrict__ Mh, int64_t ld, float* __restrict__ M32) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t n4 = n / 4;
-  if (t >= n4 * n) return;
-  const int64_t i = (t % n4) * 4, j = t / n4;
+// M32 = M in [Q, P] order from the hi plane holding only the stored half
+// (entries whose row's particle is at most the column's; the rest is read
+// at the transposed position): 32 x 32 output tiles, the direct and the
+// transposed source tiles staged in shared memory so that reads and writes
+// stay coalesced; a tile loads only the kinds it needs.
+__device__ __forceinline__ int64_t perm_src(int N, int64_t i) {
   const int64_t Q = 5LL * N;
-  const int64_t si = i < Q ? 6LL * N + i : i - Q, sj = j < Q ? 6LL * N + j : j - Q;
-  *reinterpret_cast<float4*>(M32 + i + j * n) = *reinterpret_cast<const float4*>(Mh + si + sj * ld);
+  return i < Q ? 6LL * N + i : i - Q;
+}
+
+__global__ void convert_perm_half(int N, int64_t n, const float* __restrict__ Mh, int64_t ld,
+                                  float* __restrict__ M32) {
+  __shared__ float D[32][33], T[32][33];
+  __shared__ int64_t si[32], sj[32];
+  __shared__ int pi[32], pj[32], need;
+  const int64_t I0 = (int64_t)blockIdx.x * 32, J0 = (int64_t)blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  if (ty == 0) {
+    const int64_t i = min(I0 + tx, n - 1), j = min(J0 + tx, n - 1);
+    si[tx] = perm_src(N, i);
+    sj[tx] = perm_src(N, j);
+    pi[tx] = grand_pid(N, (int)si[tx]);
+    pj[tx] = grand_pid(N, (int)sj[tx]);
+    // need: bit 0 = some entry stored directly, bit 1 = some entry transposed
+    const int imin = __reduce_min_sync(0xffffffffu, pi[tx]), imax = __reduce_max_sync(0xffffffffu, pi[tx]);
+    const int jmin = __reduce_min_sync(0xffffffffu, pj[tx]), jmax = __reduce_max_sync(0xffffffffu, pj[tx]);
+    if (tx == 0) need = (imin <= jmax ? 1 : 0) | (imax > jmin ? 2 : 0);
+  }
+  __syncthreads();
+  const int t = ty * 32 + tx;
+  const bool full = I0 + 32 <= n && J0 + 32 <= n && si[31] - si[0] == 31;  // rows contiguous in the source
+  if (need == 1 && full && (ld & 3) == 0 && (n & 3) == 0 && (si[0] & 3) == 0) {
+    // all in place: one 16-byte move per thread (4 rows of one column)
+    const int r4 = 4 * (t & 7), k = t >> 3;
+    *reinterpret_cast<float4*>(M32 + I0 + r4 + (J0 + k) * n) =
+        *reinterpret_cast<const float4*>(Mh + si[0] + r4 + sj[k] * ld);
+    return;
+  }
+  for (int k = ty; k < 32; k += blockDim.y) {
+    if (need & 1) D[k][tx] = Mh[si[tx] + sj[k] * ld];  // (I0 + tx, J0 + k) in place
+    if (need & 2) T[k][tx] = Mh[sj[tx] + si[k] * ld];  // (I0 + k, J0 + tx) at the mirrored position
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += blockDim.y) {
+    const int64_t i = I0 + tx, j = J0 + k;
+    if (i < n && j < n) M32[i + j * n] = pi[tx] <= pj[k] ? D[k][tx] : T[tx][k];
+  }
 }
 
 // x (FP64) as float pairs
@@ -105,11 +137,6 @@ __global__ void gemv_planes_part(int m, int k, const float* __restrict__ Mh, con
   }
 #pragma unroll
   for (int r = 0; r < R; r++) part[((size_t)c * R + r) * m + i] = dsf_to(acc[r]);
-}
-
-// particle of grand-matrix index x
-__device__ __forceinline__ int grand_pid(int N, int x) {
-  return x < 3 * N ? x / 3 : (x < 6 * N ? (x - 3 * N) / 3 : (x - 6 * N) / 5);
 }
 
 // Symmetric M f over the stored half of M's planes: the entries whose row's
@@ -388,6 +415,7 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   const float* Ml = Mh + (size_t)ld * n;
   const unsigned gchunks = (unsigned)((n + GEMV_PL_CHUNK - 1) / GEMV_PL_CHUNK);
   const bool symv = n % 4 == 0 && ld % 4 == 0;
+  bool mirrored = false;
   const int nbt = (int)((n + SYMV_T - 1) / SYMV_T);
   float2* fs = (float2*)rsd_scratch(ctx, "mixed_fs", sizeof(float2) * (size_t)nr * n);
   double* gpart = symv ? (double*)rsd_scratch(ctx, "mixed_symv_part", sizeof(double) * 2 * (size_t)nbt * nbt * SYMV_T)
@@ -408,10 +436,9 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   info->n_contact = nc;
   cudaEventRecord(ctx->ev[6], s);
   // FP32 factor of M' (stresslets first)
-  if (nn % 4 == 0 && ld % 4 == 0 && ((uintptr_t)Mh & 15) == 0) {
-    convert_perm4<<<(unsigned)((n * n / 4 + 255) / 256), 256, 0, s>>>(nn, n, Mh, ld, M32); RSD_LAUNCH_NOTE();
-  } else {
-    convert_perm<<<(unsigned)((n * n + 255) / 256), 256, 0, s>>>(nn, n, Mh, ld, M32); RSD_LAUNCH_NOTE();
+  {
+    const dim3 tg((unsigned)((n + 31) / 32), (unsigned)((n + 31) / 32));
+    convert_perm_half<<<tg, dim3(32, 8), 0, s>>>(nn, n, Mh, ld, M32); RSD_LAUNCH_NOTE();
   }
   int inf = 0;
   // Tensor-core precision per factor.  The refinement contracts by about the
@@ -469,6 +496,11 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
         symv_planes_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>((int)n, 1, nbt, gpart, pcol, -1.0, r1 + (size_t)c * n, n); RSD_LAUNCH_NOTE();
       }
     } else {
+      // full product: the mirrored entries are filled in first
+      if (!mirrored) {
+        RSD_TRY(rsd_mirror_planes(ctx, nn, M, ld));
+        mirrored = true;
+      }
       if (nr == 1) {
         gemv_planes_part<1><<<dim3((unsigned)((n + 255) / 256), gchunks), 256, 0, s>>>((int)n, (int)n, Mh, Ml, ld, fs, gpart); RSD_LAUNCH_NOTE();
       } else {

@@ -110,9 +110,12 @@ __host__ __device__ inline void rsd_skew_correction(const double* LR, const doub
 // ------------------------------------------------------------ kernels
 // Ewald (ewald.cu).  RSD_PREC_FP64: d_M is the FP64 grand mobility (ld
 // ldm).  RSD_PREC_MIXED: the same buffer holds it as two FP32 planes, hi at
-// (float*)d_M and lo at (float*)d_M + ldm * 11 nn, both with ld ldm.
+// (float*)d_M and lo at (float*)d_M + ldm * 11 nn, both with ld ldm, and
+// only the entries whose row's particle is at most the column's are written
+// (M is symmetric); rsd_mirror_planes fills the others.
 int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
                        double mu_f, int precision, double* d_M, int64_t ldm);
+int rsd_mirror_planes(rsd_ctx* ctx, int nn, double* d_M, int64_t ldm);
 int rsd_count_overlaps(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
                        int* count);
 // Lubrication (lub.cu)

@@ -28,7 +28,8 @@ __global__ void fill_ein(int nn, const double* __restrict__ ei5, double* __restr
 
 // averageU (src/matrices.f90:230-253): U_ave = sum_i (APP F)(3i) / N with
 // F(3j) = 6 pi mu_f radii_test; out[0] accumulates sum_ij APP(3i,3j)
-// Mh, Ml: the mixed form's M as FP32 planes (hi + lo); null for FP64 M
+// Mh, Ml: the mixed form's M as FP32 planes (hi + lo, the half with row
+// particle <= column particle stored); null for FP64 M
 __global__ void sum_app_xx(int nn, const double* __restrict__ M, const float* __restrict__ Mh,
                            const float* __restrict__ Ml, int64_t ld, double* __restrict__ out) {
   __shared__ double red[256];
@@ -37,7 +38,8 @@ __global__ void sum_app_xx(int nn, const double* __restrict__ M, const float* __
        t += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(t % nn), j = (int)(t / nn);
     const int64_t o = 3 * i + (int64_t)(3 * j) * ld;
-    s += Mh ? (double)Mh[o] + (double)Ml[o] : M[o];
+    const int64_t os = 3 * min(i, j) + (int64_t)(3 * max(i, j)) * ld;  // the stored half of the planes
+    s += Mh ? (double)Mh[os] + (double)Ml[os] : M[o];
   }
   red[threadIdx.x] = s;
   __syncthreads();
