@@ -1456,6 +1456,7 @@ struct TriArgs {
   int* ready;       // per block: parts published
   int* ticket;
   int* err;
+  int b0;           // forward: blocks before b0 are zero on entry (and stay zero)
 };
 
 // waits until all parts of block blk are published (thread 0 of the CTA)
@@ -1483,7 +1484,7 @@ __global__ void __launch_bounds__(TRI_THREADS) tri_forward(TriArgs A) {
   __shared__ int task_s;
   __shared__ volatile int abort_s;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const int nb = A.nb, total = TRI_Q * (nb - 1);
+  const int nb = A.nb, b0 = A.b0, total = TRI_Q * (nb - 1 - b0);
   if (t == 0) abort_s = 0;
   for (;;) {
     __syncthreads();
@@ -1491,7 +1492,7 @@ __global__ void __launch_bounds__(TRI_THREADS) tri_forward(TriArgs A) {
     __syncthreads();
     const int task = task_s;
     if (task >= total || abort_s) break;
-    const int j = 1 + task / TRI_Q, q = task % TRI_Q;
+    const int j = b0 + 1 + task / TRI_Q, q = task % TRI_Q;
     // columns col0 + cc of block j (TRI_QS / 8 per warp); each lane sums 16
     // rows of each source tile per column.  A tile is loaded into registers
     // before its source block is awaited (it does not depend on it).
@@ -1502,7 +1503,7 @@ __global__ void __launch_bounds__(TRI_THREADS) tri_forward(TriArgs A) {
     for (int cc = 0; cc < CPW; cc++)
 #pragma unroll
       for (int r = 0; r < NR; r++) acc[cc][r] = 0.f;
-    for (int c = 0; c < j; c++) {
+    for (int c = b0; c < j; c++) {  // the zero blocks before b0 add nothing
       const int c0 = c * NB2;  // a full block: c < nb - 1
       float4 v[CPW][NB2 / 128];
 #pragma unroll
@@ -1512,7 +1513,7 @@ __global__ void __launch_bounds__(TRI_THREADS) tri_forward(TriArgs A) {
 #pragma unroll
         for (int i = 0; i < NB2 / 128; i++) v[cc][i] = __ldcs(reinterpret_cast<const float4*>(u + 4 * lane + 128 * i));
       }
-      if (t == 0 && c > 0) tri_wait(A, c, &abort_s);
+      if (t == 0 && c > b0) tri_wait(A, c, &abort_s);
       __syncthreads();
       if (abort_s) break;
       for (int e = t; e < NB2; e += TRI_THREADS)
@@ -1714,7 +1715,7 @@ int rsd_uhat_build(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const float
 
 // X (n x nrhs, ld ldx) <- (U^T U)^-1 X with the block-scaled factor; Y is
 // n x nrhs scratch (ld ldx).
-int rsd_uhat_solve(rsd_ctx* ctx, const rsd_uhat* h, float* X, int64_t ldx, int nrhs, float* Y) {
+int rsd_uhat_solve(rsd_ctx* ctx, const rsd_uhat* h, float* X, int64_t ldx, int nrhs, float* Y, int zero_lead) {
   if (nrhs < 1 || nrhs > 2) return rsd_fail(ctx, RSD_EARG, "uhat solve: 1 or 2 right-hand sides");
   const int n = h->n, nblk2 = (n + NB2 - 1) / NB2;
   cudaStream_t s = ctx->stream;
@@ -1722,15 +1723,20 @@ int rsd_uhat_solve(rsd_ctx* ctx, const rsd_uhat* h, float* X, int64_t ldx, int n
   if (nblk2 > TRI_MAX_BLOCKS) return rsd_fail(ctx, RSD_EUNSUP, "uhat solve: order %d above %d", n, TRI_MAX_BLOCKS * NB2);
   int* sync = rsd_uhat_error_flag(ctx);  // [0] error (cumulative), [1] ticket, ready counts
   if (!sync) return RSD_ENOMEM;
-  TriArgs A{h->Uh, h->ld, n, nblk2, X, ldx, sync + 2, sync + 1, sync};
+  // leading zero blocks of the right-hand side: the forward sweep starts at
+  // the first block that can be nonzero (z is zero before it)
+  const int b0 = zero_lead > 0 ? min(zero_lead / NB2, nblk2 - 1) : 0;
+  TriArgs A{h->Uh, h->ld, n, nblk2, X, ldx, sync + 2, sync + 1, sync, b0};
   const int tasks = TRI_Q * (nblk2 - 1);
   const int grid = max(1, min(tasks, 4 * gsm));
-  if (tasks > 0) {  // forward, in place on X
+  const int ftasks = TRI_Q * (nblk2 - 1 - b0);
+  if (ftasks > 0) {  // forward, in place on X
     RSD_CUDA(ctx, cudaMemsetAsync(sync + 1, 0, sizeof(int) * (size_t)(1 + nblk2), s));
+    const int fgrid = max(1, min(ftasks, 4 * gsm));
     if (nrhs == 1)
-      tri_forward<1><<<grid, TRI_THREADS, 0, s>>>(A);
+      tri_forward<1><<<fgrid, TRI_THREADS, 0, s>>>(A);
     else
-      tri_forward<2><<<grid, TRI_THREADS, 0, s>>>(A);
+      tri_forward<2><<<fgrid, TRI_THREADS, 0, s>>>(A);
     RSD_LAUNCH_NOTE();
   }
   if (nrhs == 1)
@@ -1740,6 +1746,7 @@ int rsd_uhat_solve(rsd_ctx* ctx, const rsd_uhat* h, float* X, int64_t ldx, int n
   RSD_LAUNCH_NOTE();
   if (tasks > 0) {  // backward, in place on Y
     A.V = Y;
+    A.b0 = 0;
     RSD_CUDA(ctx, cudaMemsetAsync(sync + 1, 0, sizeof(int) * (size_t)(1 + nblk2), s));
     if (nrhs == 1)
       tri_backward<1><<<grid, TRI_THREADS, 0, s>>>(A);

@@ -543,7 +543,7 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
     du_vec<<<nblk(n * nr), 256, 0, s>>>(P, n, nr, u32, dv); RSD_LAUNCH_NOTE();
     to32_perm<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, dv, n, 1, t32); RSD_LAUNCH_NOTE();
     if (use_uh)
-      RSD_TRY(rsd_uhat_solve(ctx, &uh_m, t32, n, nr, ywork));
+      RSD_TRY(rsd_uhat_solve(ctx, &uh_m, t32, n, nr, ywork, (int)Q));
     else
       RSD_TRY(rsd_potrs_wide_s(ctx, (int)n, M32, n, W_m, t32, n, nr, ywork));
     from32_perm<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, t32, y, 1); RSD_LAUNCH_NOTE();

@@ -182,7 +182,9 @@ struct rsd_uhat {
   const float* G = nullptr;
 };
 int rsd_uhat_build(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const float* W2, const char* tag, rsd_uhat* out);
-int rsd_uhat_solve(rsd_ctx* ctx, const rsd_uhat* h, float* X, int64_t ldx, int nrhs, float* Y);
+// zero_lead: the number of leading entries of X known to be zero (the
+// forward sweep skips the whole zero blocks)
+int rsd_uhat_solve(rsd_ctx* ctx, const rsd_uhat* h, float* X, int64_t ldx, int nrhs, float* Y, int zero_lead = 0);
 // device word that turns nonzero when a wait of the solves' dataflow sweeps
 // timed out (zero it before the solves, read it after synchronising)
 int* rsd_uhat_error_flag(rsd_ctx* ctx);
