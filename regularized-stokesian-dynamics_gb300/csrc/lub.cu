@@ -334,36 +334,40 @@ __global__ void lub_self(int N, const int* __restrict__ off, const int* __restri
     self[t] = v * scale;
 }
 
-// y = L w for the sparse operator, one thread per (row, right-hand side):
-// the particle's self block, then its pairs as first and as second particle.
-__global__ void lub_spmv_k(int N, const int* __restrict__ off, const int* __restrict__ off2,
+// y = L w for the sparse operator: the particle's self block, then its pairs
+// as first and as second particle.  One warp per (particle, right-hand
+// side): lane r + 11 g (r < 11, g < 2) takes row r and every other
+// neighbour block starting at g; the two halves are added by a shuffle
+// (fixed order)
+__global__ void lub_spmv_w(int N, const int* __restrict__ off, const int* __restrict__ off2,
                            const int* __restrict__ list2, const int2* __restrict__ pairs,
                            const double* __restrict__ blk, const double* __restrict__ self, double scale, int nr,
                            const double* __restrict__ w, int64_t ldw, double* __restrict__ y, int64_t ldy) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t rows = 11LL * N;
-  if (t >= rows * nr) return;
-  const int i = (int)(t % rows), col = (int)(t / rows);
-  const int u = i / 11, r = i % 11;
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wid >= (int64_t)N * nr) return;
+  const int u = (int)(wid % N), col = (int)(wid / N);
+  const int r = lane % 11, g = lane / 11;
   const double* wc = w + col * ldw;
   double vs = 0.0, vp = 0.0;
-  const double* S = self + (size_t)u * 121;
+  if (g < 2) {
+    if (g == 0) {
+      const double* S = self + (size_t)u * 121;
 #pragma unroll
-  for (int c = 0; c < 11; c++) vs += S[r + 11 * c] * wc[gidx(N, u, c)];
-  for (int p = off[u]; p < off[u + 1]; p++) {
-    const double* B = blk + (size_t)p * PB;
-    const int b = pairs[p].y;
+      for (int c = 0; c < 11; c++) vs += S[r + 11 * c] * wc[gidx(N, u, c)];
+    }
+    const int p1 = off[u], n1 = off[u + 1] - p1, q2 = off2[u], n2 = off2[u + 1] - q2;
+    for (int k = g; k < n1 + n2; k += 2) {
+      const bool first = k < n1;
+      const int p = first ? p1 + k : list2[q2 + k - n1];
+      const double* B = blk + (size_t)p * PB;
+      const int o = first ? pairs[p].y : pairs[p].x;
 #pragma unroll
-    for (int c = 0; c < 11; c++) vp += pair_entry(B, r, c, true) * wc[gidx(N, b, c)];
+      for (int c = 0; c < 11; c++) vp += pair_entry(B, r, c, first) * wc[gidx(N, o, c)];
+    }
   }
-  for (int q = off2[u]; q < off2[u + 1]; q++) {
-    const int p = list2[q];
-    const double* B = blk + (size_t)p * PB;
-    const int a = pairs[p].x;
-#pragma unroll
-    for (int c = 0; c < 11; c++) vp += pair_entry(B, r, c, false) * wc[gidx(N, a, c)];
-  }
-  y[gidx(N, u, r) + col * ldy] = vs + vp * scale;
+  vp += __shfl_down_sync(0xffffffffu, vp, 11);
+  if (lane < 11) y[gidx(N, u, r) + col * ldy] = vs + vp * scale;
 }
 
 // A (FP32, ld lda) += the force/torque-velocity part L_PP of the sparse
@@ -532,8 +536,8 @@ int rsd_lub_build_sparse(rsd_ctx* ctx, const rsd_lubtab* tab, int nn, int nb, in
 // y (11N x nr, grand layout, ld ldy) = L w
 int rsd_lub_spmv(rsd_ctx* ctx, const rsd_lub_sparse* sp, int nr, const double* w, int64_t ldw, double* y,
                  int64_t ldy) {
-  const int64_t tot = 11LL * sp->nn * nr;
-  lub_spmv_k<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(sp->nn, sp->off, sp->off2, sp->list2, sp->pairs,
+  const int64_t tot = 32LL * sp->nn * nr;  // one warp per particle and right-hand side
+  lub_spmv_w<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(sp->nn, sp->off, sp->off2, sp->list2, sp->pairs,
                                                                       sp->blk, sp->self, sp->scale, nr, w, ldw, y,
                                                                       ldy); RSD_LAUNCH_NOTE();
   RSD_CUDA(ctx, cudaGetLastError());
