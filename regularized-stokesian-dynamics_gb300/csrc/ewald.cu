@@ -965,18 +965,25 @@ __global__ void __launch_bounds__(REAL_THREADS, MINB) ewald_pair_real_eq(int nn,
   __syncthreads();
   int a, b;
   if (!pair_of(nn, &a, &b)) return;
-  double R[3] = {pos[3 * a] - pos[3 * b], pos[3 * a + 1] - pos[3 * b + 1], pos[3 * a + 2] - pos[3 * b + 2]};
-  double dmin;
-  rsd_skew_correction(L.LR, L.LI, R, &dmin);
-  const dsf Rs[3] = {dsf_from(R[0]), dsf_from(R[1]), dsf_from(R[2])};
-  const float Rf[3] = {Rs[0].hi, Rs[1].hi, Rs[2].hi};
-  float A[9];
+  float A[9], LIf[9];
   dsf As[9];
 #pragma unroll
   for (int k = 0; k < 9; k++) {
     As[k] = dsf_from(L.LR[k]);
     A[k] = As[k].hi;
+    LIf[k] = (float)L.LI[k];
   }
+  // minimum image: the lattice shift found in FP32, applied in double-single
+  const double R[3] = {pos[3 * a] - pos[3 * b], pos[3 * a + 1] - pos[3 * b + 1], pos[3 * a + 2] - pos[3 * b + 2]};
+  dsf Rs[3];
+  {
+    const float R0[3] = {(float)R[0], (float)R[1], (float)R[2]};
+    int k[3];
+    rsd_skew_shift_f32(A, LIf, R0, k);
+#pragma unroll
+    for (int i = 0; i < 3; i++) Rs[i] = dsf_from(R[i]) - (k[0] * As[i] + k[1] * As[3 + i] + k[2] * As[6 + i]);
+  }
+  const float Rf[3] = {Rs[0].hi, Rs[1].hi, Rs[2].hi};
   const int NR = L.NR;
   const float lamf = (float)L.lam, lam2f = lamf * lamf, cdf = (float)(2.0 * RSD_PIP5 * L.lam);
   // far images, FP32

@@ -90,6 +90,27 @@ __device__ inline double eps3(int i, int j, int k) {
 __device__ inline bool near_pair(const rsd_lat_dev& L, int is_period, const double* pos, const double* radii, int a,
                                  int b) {
   double R[3] = {pos[3 * a] - pos[3 * b], pos[3 * a + 1] - pos[3 * b + 1], pos[3 * a + 2] - pos[3 * b + 2]};
+  {  // FP32 screen: pairs clearly beyond the cut-off need no FP64 test
+    float LRf[9], LIf[9], Rf[3] = {(float)R[0], (float)R[1], (float)R[2]};
+    for (int k = 0; k < 9; k++) {
+      LRf[k] = (float)L.LR[k];
+      LIf[k] = (float)L.LI[k];
+    }
+    float d2;
+    if (is_period) {
+      int k[3];
+      rsd_skew_shift_f32(LRf, LIf, Rf, k);
+      d2 = 0.f;
+      for (int i = 0; i < 3; i++) {
+        const float e = Rf[i] - (LRf[i] * k[0] + LRf[i + 3] * k[1] + LRf[i + 6] * k[2]);
+        d2 += e * e;
+      }
+    } else {
+      d2 = Rf[0] * Rf[0] + Rf[1] * Rf[1] + Rf[2] * Rf[2];
+    }
+    const float lim = 2.0f * (float)(radii[a] + radii[b]) * 1.001f + 1e-3f;  // s = 4 with a margin
+    if (d2 > lim * lim) return false;
+  }
   double r = sqrt(R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
   if (is_period) rsd_skew_correction(L.LR, L.LI, R, &r);
   const double s = r / (0.5 * (radii[a] + radii[b]));

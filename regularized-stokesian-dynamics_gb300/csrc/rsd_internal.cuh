@@ -107,6 +107,38 @@ __host__ __device__ inline void rsd_skew_correction(const double* LR, const doub
   *dmin = sqrt(D0);
 }
 
+// The lattice shift of rsd_skew_correction, found in FP32: the integer
+// multiples k of the lattice vectors (columns of LR) with R - LR k the
+// minimum image among the 8 corner shifts of the cell R falls in.  Where two
+// images are within FP32 rounding of each other either may be chosen; both
+// are minimum images to that accuracy.  For screening and for kernels that
+// apply the shift in their own precision (no FP64 operations).
+__host__ __device__ inline void rsd_skew_shift_f32(const float* LR, const float* LI, const float R[3], int k[3]) {
+  float X[3], RC[3];
+  for (int i = 0; i < 3; i++) {
+    X[i] = floorf(LI[i] * R[0] + LI[i + 3] * R[1] + LI[i + 6] * R[2]);
+    k[i] = (int)X[i];
+  }
+  for (int i = 0; i < 3; i++) RC[i] = R[i] - (LR[i] * X[0] + LR[i + 3] * X[1] + LR[i + 6] * X[2]);
+  float D0 = RC[0] * RC[0] + RC[1] * RC[1] + RC[2] * RC[2];
+  int best = 0;
+  for (int m = 1; m < 8; m++) {
+    const float M0 = (float)((m >> 2) & 1), M1 = (float)((m >> 1) & 1), M2 = (float)(m & 1);
+    float d = 0.f;
+    for (int i = 0; i < 3; i++) {
+      const float e = RC[i] - (LR[i] * M0 + LR[i + 3] * M1 + LR[i + 6] * M2);
+      d += e * e;
+    }
+    if (d < D0) {
+      D0 = d;
+      best = m;
+    }
+  }
+  k[0] += (best >> 2) & 1;
+  k[1] += (best >> 1) & 1;
+  k[2] += best & 1;
+}
+
 // ------------------------------------------------------------ kernels
 // Ewald (ewald.cu).  RSD_PREC_FP64: d_M is the FP64 grand mobility (ld
 // ldm).  RSD_PREC_MIXED: the same buffer holds it as two FP32 planes, hi at
