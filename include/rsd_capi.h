@@ -97,7 +97,7 @@ int rsd_ctx_set_mixed_truncation(rsd_ctx* ctx, double lam_r_max, double k2_over_
  * it; a larger value moves work from the real-space images to the cheaper
  * reciprocal vectors, and the image cubes are widened to hold the
  * truncation spheres.  1 keeps the reference's lammda, NR and NI; the
- * default is 1.5.  The FP64 form always uses the reference's values. */
+ * default is 1.75.  The FP64 form always uses the reference's values. */
 int rsd_ctx_set_mixed_lambda_scale(rsd_ctx* ctx, double scale);
 /* Equal radii, mixed-precision assembly: the double-single near images are
  * summed in `passes` passes (1 to 4), each over one part of the moments

@@ -157,7 +157,7 @@ class Context:
         """Truncation of the mixed-precision Ewald sums."""
         self.check(_lib.rsd_ctx_set_mixed_truncation(self.h, float(lam_r_max), float(k2_over_4lam2_max)))
 
-    def set_mixed_lambda_scale(self, scale=1.5):
+    def set_mixed_lambda_scale(self, scale=1.75):
         """Ewald splitting parameter of the mixed assembly relative to the
         reference's."""
         self.check(_lib.rsd_ctx_set_mixed_lambda_scale(self.h, float(scale)))

@@ -603,8 +603,26 @@ __global__ void ewald_kblock_list(rsd_lat_dev L, int count, const int* __restric
   for (int i = 60; i < KBW; i++) put_weight<T>(e + i, 0.0);
 }
 
-__device__ __forceinline__ void acc_norm(float&) {}
 __device__ __forceinline__ void acc_norm(dsacc& a) { dsacc_norm(a); }
+
+// FP32 sum of the vectors of one chunk (f), folded at the end of every chunk
+// into a double-single total (hi + lo, Knuth's two-sum).  A plain FP32 sum
+// over all K32 vectors has a rounding error ~ sqrt(K32) times that of its
+// terms, which grows with the number of FP32 vectors (with lambda^3).
+struct fchunk {
+  float f, hi, lo;
+};
+__device__ __forceinline__ fchunk fma(float e, float c, fchunk a) {
+  a.f = __fmaf_rn(e, c, a.f);
+  return a;
+}
+__device__ __forceinline__ void acc_norm(fchunk& a) {
+  const float s = __fadd_rn(a.hi, a.f);
+  const float bb = __fsub_rn(s, a.hi);
+  a.lo = __fadd_rn(a.lo, __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(a.f, bb)));
+  a.hi = s;
+  a.f = 0.f;
+}
 
 __device__ __forceinline__ float trig_c(float2 v) { return v.x; }
 __device__ __forceinline__ float trig_s(float2 v) { return v.y; }
@@ -666,13 +684,13 @@ __global__ void __launch_bounds__(128) ewald_pair_kblock(int nn, int K32, const 
   const bool valid = pair_of(nn, &a, &b);
   dsacc acc[60];
   {
-    float f[60];
+    fchunk f[60];
 #pragma unroll
-    for (int q = 0; q < 60; q++) f[q] = 0.f;
+    for (int q = 0; q < 60; q++) f[q] = fchunk{0.f, 0.f, 0.f};
     kblock_accumulate<float, float2>(nn, K32, W32, c32, reinterpret_cast<float*>(sw),
                                      reinterpret_cast<float2*>(sca), reinterpret_cast<float2*>(scb), valid, f);
 #pragma unroll
-    for (int q = 0; q < 60; q++) acc[q] = dsacc(f[q], 0.f);
+    for (int q = 0; q < 60; q++) acc[q] = dsacc(f[q].hi, f[q].lo);
   }
   kblock_accumulate<dsf, float4>(nn, K64, W64, c64, sw, sca, scb, valid, acc);
   if (!valid) return;
@@ -1307,8 +1325,8 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
       // Double-single: real images with lambda r < mixed_rcut (default 4.5)
       // and reciprocal vectors with k^2/(4 lambda^2) <= 3 pi mixed_kshell^2
       // (default 1); FP32 for the rest.  The FP32 error of a block follows
-      // the largest FP32 term: at the defaults (with lambda x 1.5) a step's
-      // velocities move by ~3e-11 and its stresslets by ~3e-10 relative.
+      // the largest FP32 term: at the defaults (with lambda x 1.75) a step's
+      // velocities move by ~3e-11 and its stresslets by ~2e-10 relative.
       // Truncation: real images with lambda r >= mixed_rmax and reciprocal
       // vectors with k^2 / (4 lambda^2) >= mixed_kexp are dropped (each
       // changes a block by less than ~1e-12 of its largest entry at the

@@ -37,7 +37,7 @@ struct rsd_ctx {
   double mixed_rmax = 6.0;  // mixed assembly: real images with lambda r beyond this dropped
   double mixed_kexp = 10.0 * 3.141592653589793;  // and reciprocal vectors with k^2/(4 lambda^2) beyond this
   int mixed_real_passes = 1;  // mixed assembly, equal radii: passes over the near images (moment parts)
-  double mixed_lambda_scale = 1.5;  // mixed assembly: Ewald splitting parameter relative to the reference's
+  double mixed_lambda_scale = 1.75;  // mixed assembly: Ewald splitting parameter relative to the reference's
   cudaStream_t side = nullptr;  // higher-priority stream for look-ahead panels
   cudaEvent_t ev_panel = nullptr, ev_next = nullptr;
   int* d_info = nullptr;  // device-side status words

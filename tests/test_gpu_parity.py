@@ -261,7 +261,7 @@ def test_mixed_step_meets_velocity_tolerance(rsd, ctx, tabs, N, phi, gmin, have_
     assert np.allclose(g["yeta_mu"], r["yeta_mu"], rtol=1e-8, atol=0)
 
 
-@pytest.mark.parametrize("scale,split", [(1.0, (4.0, 1)), (2.0, (4.5, 2))])
+@pytest.mark.parametrize("scale,split", [(1.0, (4.0, 1)), (1.5, (4.5, 1)), (2.0, (4.5, 2))])
 def test_mixed_step_other_splits(rsd, ctx, tabs, scale, split):
     """The mixed form under another Ewald splitting parameter and near/far
     split (the Ewald sum does not depend on them): same 1e-8 bound."""
