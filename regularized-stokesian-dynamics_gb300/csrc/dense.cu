@@ -418,22 +418,25 @@ __global__ void __launch_bounds__(256) potf2_upper(T* __restrict__ A, int64_t ld
 }
 
 // FP32 diagonal block (jb <= 128): upper Cholesky factor U and its inverse
-// W = U^-1 in one CTA of 8 warps, in padded shared memory (ld 129, so that
-// row and column walks hit distinct banks).  Right-looking over 32-wide
-// sub-blocks D:
+// W = U^-1 in one CTA of 8 warps.  Right-looking over 32-wide sub-blocks D:
 //   - warp 0 factors D in registers (lane = column) and inverts the factor
 //     by back substitution, also in registers; D^-1 is the sub-block's
-//     diagonal block of W;
-//   - the row panel R next to D becomes D^-T R (a 32-deep product, one warp
-//     per column, lane = row), kept also transposed for the update;
-//   - the trailing block loses R^T R: lane = row, 8 columns per warp task,
-//     so each 32-row x 8-column task reads 9 values per 8 FMAs.
-// The off-diagonal W blocks follow level by level,
-// W_ij = -W_ii (sum_{p=i+1..j} U_ip W_pj), one warp per (block, 4 columns).
-// U goes back to A; W goes to Wout (NB x NB, lower part and rows/columns
-// past jb zero).  info as DPOTRF.
-constexpr int PLD = NB + 1;
-constexpr int RTLD = 33;
+//     diagonal block of W, kept row- and column-major for the steps below;
+//   - the row panel R next to D becomes D^-T R: lane = row, column `lane` of
+//     D^-1 in registers, each column of R read as 16-byte broadcasts;
+//   - the trailing block loses R^T R: lane = row i, column i of R in
+//     registers, each other column read as 16-byte broadcasts (from the
+//     transposed copy RT that the panel step writes).
+// W's off-diagonal blocks come one column block at a time,
+// W(0:c, c) = -W(0:c, 0:c) (U(0:c, c) D_c^-1): warps 1-7 form column block
+// c while warp 0 factors sub-block c + 1, and all warps form the last one.
+// Every shared load is a 16-byte broadcast or a walk with lanes on distinct
+// banks (columns PV = 132 floats apart, so 16-byte column reads of 8 lanes
+// fall on distinct bank groups).  U goes back to A; W goes to Wout (NB x NB,
+// lower part and rows/columns past jb zero).  info as DPOTRF.
+constexpr int PV = NB + 4;      // ld of U and W (16-byte aligned columns)
+constexpr int DV = 36;          // ld of the D^-1 copies and of RT
+constexpr int TV = 3 * 32 + 4;  // ld of T = U(0:c, c) D_c^-1, c <= 3
 // Loads of an FP32 tile into shared memory with many loads in flight: a
 // loop of one load per iteration serialises the DRAM round trips of a
 // single CTA (~0.7 us each), so each thread first issues a batch of 16
@@ -506,20 +509,27 @@ __device__ __forceinline__ void chol32_step(float (&r)[32], float (&dinv)[32], i
 
 // A full 32 x 32 diagonal sub-block (warp-wide, no branches): the factor in
 // registers (written to S), then D^-1 column `lane` by back substitution in
-// axpy form, U's rows read from shared memory at the same address for every
-// lane (written to Wm and Dinv, (p, i) at Dinv[p * 33 + i]).  Returns the
-// 1-based index of the first pivot that is not positive and finite, 0 if
-// none.
-__device__ __forceinline__ int diag32_factor_inv(float* S, float* Wm, float* Dinv, int k0, int lane) {
+// axpy form, U's columns read from shared memory as 16-byte broadcasts.
+// D^-1 goes to Wm, to Dn (row-major) and to Dt (column-major), ld DV.
+// Returns the 1-based index of the first pivot that is not positive and
+// finite, 0 if none (the same for every lane).
+__device__ __forceinline__ int diag32_factor_inv(float* S, float* Wm, float* Dn, float* Dt, int k0, int lane) {
   float r[32], dinv[32];
+  float4* sc = reinterpret_cast<float4*>(S + k0 + (k0 + lane) * PV);
 #pragma unroll
-  for (int i = 0; i < 32; i++) r[i] = S[(k0 + i) + (k0 + lane) * PLD];
+  for (int g = 0; g < 8; g++) {
+    const float4 v = sc[g];
+    r[4 * g] = v.x;
+    r[4 * g + 1] = v.y;
+    r[4 * g + 2] = v.z;
+    r[4 * g + 3] = v.w;
+  }
   int bad = 0;
   chol32_step<0>(r, dinv, lane, bad);
   if (bad) return bad;
+  // entries below the diagonal stay as loaded (zero)
 #pragma unroll
-  for (int i = 0; i < 32; i++)
-    if (i <= lane) S[(k0 + i) + (k0 + lane) * PLD] = r[i];
+  for (int g = 0; g < 8; g++) sc[g] = make_float4(r[4 * g], r[4 * g + 1], r[4 * g + 2], r[4 * g + 3]);
   __syncwarp();
   float x[32], acc[32];
 #pragma unroll
@@ -529,23 +539,37 @@ __device__ __forceinline__ int diag32_factor_inv(float* S, float* Wm, float* Din
     const int p = 31 - q;
     const float v = ((p == lane ? 1.f : 0.f) - acc[p]) * dinv[p];
     x[p] = p <= lane ? v : 0.f;
+    // acc(i) += U(i, p) x(p); the terms added to acc(i >= p) are never read
+    const float4* up = reinterpret_cast<const float4*>(S + k0 + (k0 + p) * PV);
 #pragma unroll
-    for (int i = 0; i < p; i++) acc[i] = fmaf(S[(k0 + i) + (k0 + p) * PLD], x[p], acc[i]);
+    for (int g = 0; g < (p + 3) / 4; g++) {
+      const float4 u = up[g];
+      acc[4 * g] = fmaf(u.x, x[p], acc[4 * g]);
+      acc[4 * g + 1] = fmaf(u.y, x[p], acc[4 * g + 1]);
+      acc[4 * g + 2] = fmaf(u.z, x[p], acc[4 * g + 2]);
+      acc[4 * g + 3] = fmaf(u.w, x[p], acc[4 * g + 3]);
+    }
+  }
+  float4* wc = reinterpret_cast<float4*>(Wm + k0 + (k0 + lane) * PV);
+  float4* dt = reinterpret_cast<float4*>(Dt + lane * DV);
+#pragma unroll
+  for (int g = 0; g < 8; g++) {
+    const float4 v = make_float4(x[4 * g], x[4 * g + 1], x[4 * g + 2], x[4 * g + 3]);
+    wc[g] = v;
+    dt[g] = v;
   }
 #pragma unroll
-  for (int i = 0; i < 32; i++) {
-    Wm[(k0 + i) + (k0 + lane) * PLD] = x[i];
-    Dinv[i * 33 + lane] = x[i];
-  }
+  for (int i = 0; i < 32; i++) Dn[i * DV + lane] = x[i];
   return 0;
 }
 
 // The trailing sub-block of kw < 32 columns (zero-padded to 32), as
 // diag32_factor_inv with IEEE square roots and divisions.
-__device__ __forceinline__ int diag_partial_factor_inv(float* S, float* Wm, float* Dinv, int k0, int kw, int lane) {
+__device__ __forceinline__ int diag_partial_factor_inv(float* S, float* Wm, float* Dn, float* Dt, int k0, int kw,
+                                                       int lane) {
   float r[32];
 #pragma unroll
-  for (int i = 0; i < 32; i++) r[i] = S[(k0 + i) + (k0 + lane) * PLD];
+  for (int i = 0; i < 32; i++) r[i] = S[(k0 + i) + (k0 + lane) * PV];
   int bad = 0;
 #pragma unroll
   for (int k = 0; k < 32; k++) {
@@ -580,128 +604,186 @@ __device__ __forceinline__ int diag_partial_factor_inv(float* S, float* Wm, floa
   if (lane < kw) {
 #pragma unroll
     for (int i = 0; i < 32; i++) {
-      if (i <= lane) S[(k0 + i) + (k0 + lane) * PLD] = r[i];
-      Wm[(k0 + i) + (k0 + lane) * PLD] = x[i];
+      if (i <= lane) S[(k0 + i) + (k0 + lane) * PV] = r[i];
+      Wm[(k0 + i) + (k0 + lane) * PV] = x[i];
     }
   }
 #pragma unroll
-  for (int i = 0; i < 32; i++) Dinv[i * 33 + lane] = x[i];
+  for (int i = 0; i < 32; i++) {
+    Dn[i * DV + lane] = x[i];
+    Dt[lane * DV + i] = x[i];
+  }
   return 0;
 }
 
-// FP32 diagonal block (jb <= 128) of the blocked Cholesky: its upper factor
-// U in place and W = U^-1 into Wout (NB x NB, zero below the diagonal).  In
-// 32-wide sub-blocks: warp 0 factors and inverts the diagonal sub-block D,
-// all warps form the row panel D^-T R and the trailing update; at the end
-// W's off-diagonal blocks are filled level by level from the D^-1.
-constexpr int SMEM_POTF2_INV = (2 * NB * PLD + NB * RTLD + 32 * 33 + 3 * 32 * 33) * (int)sizeof(float);
+// 32-term dot product of a register column with a 16-byte aligned shared
+// column read as broadcasts, in four partial sums.
+__device__ __forceinline__ float dot32_bcast(const float (&a)[32], const float* __restrict__ col) {
+  const float4* c4 = reinterpret_cast<const float4*>(col);
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll
+  for (int g = 0; g < 8; g++) {
+    const float4 v = c4[g];
+    s0 = fmaf(a[4 * g], v.x, s0);
+    s1 = fmaf(a[4 * g + 1], v.y, s1);
+    s2 = fmaf(a[4 * g + 2], v.z, s2);
+    s3 = fmaf(a[4 * g + 3], v.w, s3);
+  }
+  return (s0 + s1) + (s2 + s3);
+}
+
+// Column block c >= 1 of W = U^-1 (rows 0..32c-1) by warps tw = 0..nw-1 of
+// a team: T = U(0:c, c) D_c^-1 into Tt, then W(0:c, c) = -W(0:c, 0:c) T
+// (W upper triangular).  Tasks are (32-row block, 8 columns), lane = row;
+// `sync` (a barrier of the team) separates the two products.
+template <typename Sync>
+__device__ __forceinline__ void w_column_block(const float* __restrict__ S, float* __restrict__ Wm,
+                                               const float* __restrict__ Dt, float* __restrict__ Tt, int c, int tw,
+                                               int nw, int lane, Sync sync) {
+  const int ntask = 4 * c;
+  for (int task = tw; task < ntask; task += nw) {
+    const int rb = task >> 2, j0 = (task & 3) * 8, p = 32 * rb + lane;
+    float u[32];
+#pragma unroll
+    for (int q = 0; q < 32; q++) u[q] = S[p + (32 * c + q) * PV];
+#pragma unroll 4  // a full unroll hoists all 64 broadcasts and spills
+    for (int jj = 0; jj < 8; jj++) Tt[(j0 + jj) * TV + p] = dot32_bcast(u, Dt + (j0 + jj) * DV);
+  }
+  sync();
+  for (int task = tw; task < ntask; task += nw) {
+    const int rb = task >> 2, j0 = (task & 3) * 8, p = 32 * rb + lane;
+    float acc[8];
+#pragma unroll
+    for (int jj = 0; jj < 8; jj++) acc[jj] = 0.f;
+    for (int pb = rb; pb < c; pb++) {
+      float w[32];
+#pragma unroll
+      for (int q = 0; q < 32; q++) w[q] = Wm[p + (32 * pb + q) * PV];
+#pragma unroll
+      for (int jj = 0; jj < 8; jj++) acc[jj] += dot32_bcast(w, Tt + (j0 + jj) * TV + 32 * pb);
+    }
+#pragma unroll
+    for (int jj = 0; jj < 8; jj++) Wm[p + (32 * c + j0 + jj) * PV] = -acc[jj];
+  }
+}
+
+constexpr int SMEM_POTF2_INV = (2 * NB * PV + NB * DV + 4 * 32 * DV + 32 * TV) * (int)sizeof(float);
 __global__ void __launch_bounds__(256) potf2_inv_f32(float* __restrict__ A, int64_t lda, int jb,
                                                      int* __restrict__ info, int j0, float* __restrict__ Wout) {
-  extern __shared__ unsigned char smraw[];
-  float* S = (float*)smraw;       // U, NB x NB, ld PLD
-  float* Wm = S + NB * PLD;       // W, NB x NB, ld PLD
-  float* RT = Wm + NB * PLD;      // D^-T R transposed: trailing column c, row p at RT[c * RTLD + p]
-  float* Dinv = RT + NB * RTLD;   // D^-1 (32 x 32): (p, i) at Dinv[p * 33 + i]
-  float* Tt = Dinv + 32 * 33;     // 3 temporaries of 32 x 32: (r, c) at r * 33 + c
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float* S = (float*)smraw;      // U, NB x NB, ld PV
+  float* Wm = S + NB * PV;       // W, NB x NB, ld PV
+  float* RT = Wm + NB * PV;      // R = D^-T (row panel) transposed: column c of R at RT[c * DV]
+  float* Dd = RT + NB * DV;      // two buffers of D^-1: row-major (Dn), then column-major (Dt), ld DV
+  float* Tt = Dd + 4 * 32 * DV;  // T = U(0:c, c) D_c^-1: column j at Tt[j * TV]
   __shared__ int failed;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  load_tile_f32(A, lda, jb, jb, NB, S, PLD, 1);
-  for (int e = t; e < NB * NB; e += 256) Wm[(e % NB) + (e / NB) * PLD] = 0.f;
+  load_tile_f32(A, lda, jb, jb, NB, S, PV, 1);
+  {
+    float4* w4 = reinterpret_cast<float4*>(Wm);
+    for (int e = t; e < NB * PV / 4; e += 256) w4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
   if (t == 0) failed = 0;
   __syncthreads();
   const int nsub = (jb + 31) / 32;
   for (int kb = 0; kb < nsub; kb++) {
     const int k0 = kb * 32, kw = min(32, jb - k0);
+    float* Dn = Dd + (kb & 1) * 2 * 32 * DV;
+    float* Dt = Dn + 32 * DV;
     if (warp == 0) {
-      const int bad = kw == 32 ? diag32_factor_inv(S, Wm, Dinv, k0, lane)
-                               : diag_partial_factor_inv(S, Wm, Dinv, k0, kw, lane);
+      const int bad = kw == 32 ? diag32_factor_inv(S, Wm, Dn, Dt, k0, lane)
+                               : diag_partial_factor_inv(S, Wm, Dn, Dt, k0, kw, lane);
       if (bad && lane == 0) {
         failed = 1;
         atomicCAS(info, 0, j0 + k0 + bad);
       }
+    } else if (kb >= 2) {
+      // column block kb - 1 of W, beside the factor of sub-block kb
+      w_column_block(S, Wm, Dd + ((kb - 1) & 1) * 2 * 32 * DV + 32 * DV, Tt, kb - 1, warp - 1, 7, lane,
+                     [] { asm volatile("bar.sync 1, 224;" ::: "memory"); });
     }
     __syncthreads();
     if (failed) return;
     const int m0 = k0 + kw, mw = jb - m0;
-    // row panel: R <- D^-T R, four columns per warp, lane = row
-    for (int c0 = 4 * warp; c0 < mw; c0 += 32) {
-      float v[4] = {0.f, 0.f, 0.f, 0.f};
-      int col[4];
+    if (mw <= 0) continue;
+    // row panel: R <- D^-T R, lane = row, four columns per warp
+    {
+      float dl[32];
 #pragma unroll
-      for (int q = 0; q < 4; q++) col[q] = m0 + min(c0 + q, mw - 1);
-#pragma unroll 8
-      for (int p = 0; p < 32; p++) {
-        const float d = Dinv[p * 33 + lane];
+      for (int q = 0; q < 32; q++) dl[q] = Dn[q * DV + lane];  // D^-1(q, lane)
+      for (int c0 = 4 * warp; c0 < mw; c0 += 32) {
+        float v[4];
 #pragma unroll
-        for (int q = 0; q < 4; q++) v[q] = fmaf(d, S[(k0 + p) + col[q] * PLD], v[q]);
+        for (int cc = 0; cc < 4; cc++) v[cc] = dot32_bcast(dl, S + k0 + (m0 + min(c0 + cc, mw - 1)) * PV);
+        __syncwarp();
+#pragma unroll
+        for (int cc = 0; cc < 4; cc++)
+          if (c0 + cc < mw) {
+            if (lane < kw) S[(k0 + lane) + (m0 + c0 + cc) * PV] = v[cc];
+            RT[(c0 + cc) * DV + lane] = lane < kw ? v[cc] : 0.f;
+          }
       }
-      __syncwarp();
-#pragma unroll
-      for (int q = 0; q < 4; q++)
-        if (c0 + q < mw) {
-          if (lane < kw) S[(k0 + lane) + col[q] * PLD] = v[q];
-          RT[(c0 + q) * RTLD + lane] = (lane < kw) ? v[q] : 0.f;
-        }
     }
     __syncthreads();
     // trailing update of the upper part: lane = row i of a 32-row block,
-    // 8 columns per task
-    const int nrb = (mw + 31) / 32, ncg = (mw + 7) / 8;
-    for (int task = warp; task < nrb * ncg; task += 8) {
-      const int rb = task % nrb, cg = task / nrb;
-      const int i = rb * 32 + lane, c0 = cg * 8;
-      if (rb * 32 > c0 + 7) continue;  // entirely below the diagonal
-      float acc[8];
+    // column i of R in registers, 8 columns per task (columns >= the block)
+    {
+      const int nrb = (mw + 31) / 32;
+      int ntask = 0;
+      for (int rb = 0; rb < nrb; rb++) ntask += (mw - 32 * rb + 7) / 8;
+      for (int task = warp; task < ntask; task += 8) {
+        int rb = 0, rem = task;
+        while (rem >= (mw - 32 * rb + 7) / 8) {
+          rem -= (mw - 32 * rb + 7) / 8;
+          rb++;
+        }
+        const int c0 = 32 * rb + 8 * rem, i = 32 * rb + lane;
+        float a[32];
+        const float4* ri = reinterpret_cast<const float4*>(RT + i * DV);
 #pragma unroll
-      for (int q = 0; q < 8; q++) acc[q] = 0.f;
-      const int ir = min(i, NB - 1);
-#pragma unroll 4
-      for (int p = 0; p < 32; p++) {
-        const float a = RT[ir * RTLD + p];
+        for (int g = 0; g < 8; g++) {
+          const float4 v = ri[g];
+          a[4 * g] = v.x;
+          a[4 * g + 1] = v.y;
+          a[4 * g + 2] = v.z;
+          a[4 * g + 3] = v.w;
+        }
+        float o[8];
 #pragma unroll
-        for (int q = 0; q < 8; q++) acc[q] += a * RT[min(c0 + q, NB - 1) * RTLD + p];
-      }
-      if (i < mw) {
+        for (int jj = 0; jj < 8; jj++) o[jj] = dot32_bcast(a, RT + min(c0 + jj, mw - 1) * DV);
 #pragma unroll
-        for (int q = 0; q < 8; q++)
-          if (c0 + q < mw && i <= c0 + q) S[(m0 + i) + (m0 + c0 + q) * PLD] -= acc[q];
+        for (int jj = 0; jj < 8; jj++) {
+          const int c = c0 + jj;
+          if (c < mw && i <= c) S[(m0 + i) + (m0 + c) * PV] -= o[jj];
+        }
       }
     }
     __syncthreads();
   }
-  // off-diagonal W blocks, level by level: warp per (block, 4 columns)
-  for (int d = 1; d < nsub; d++) {
-    const int nb = nsub - d;
-    for (int task = warp; task < nb * 8; task += 8) {  // T_b = sum_p U_{bi,p} W_{p,bj}
-      const int b = task / 8, c0 = (task % 8) * 4, bi = b, bj = b + d;
-      float acc[4] = {0.f, 0.f, 0.f, 0.f};
-      for (int q = 32 * (bi + 1); q < 32 * (bj + 1); q++) {
-        const float u = S[(32 * bi + lane) + q * PLD];
-#pragma unroll
-        for (int cc = 0; cc < 4; cc++) acc[cc] += u * Wm[q + (32 * bj + c0 + cc) * PLD];
-      }
-#pragma unroll
-      for (int cc = 0; cc < 4; cc++) Tt[b * 32 * 33 + lane * 33 + c0 + cc] = acc[cc];
-    }
-    __syncthreads();
-    for (int task = warp; task < nb * 8; task += 8) {  // W_{bi,bj} = -W_{bi,bi} T_b
-      const int b = task / 8, c0 = (task % 8) * 4, bi = b, bj = b + d;
-      float acc[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 8
-      for (int q = 0; q < 32; q++) {
-        const float w = Wm[(32 * bi + lane) + (32 * bi + q) * PLD];
-#pragma unroll
-        for (int cc = 0; cc < 4; cc++) acc[cc] += w * Tt[b * 32 * 33 + q * 33 + c0 + cc];
-      }
-#pragma unroll
-      for (int cc = 0; cc < 4; cc++) Wm[(32 * bi + lane) + (32 * bj + c0 + cc) * PLD] = -acc[cc];
-    }
+  if (nsub >= 2) {
+    w_column_block(S, Wm, Dd + ((nsub - 1) & 1) * 2 * 32 * DV + 32 * DV, Tt, nsub - 1, warp, 8, lane,
+                   [] { __syncthreads(); });
     __syncthreads();
   }
-  for (int e = t; e < NB * NB; e += 256) {
-    const int i = e % NB, j = e / NB;
-    if (i < jb && j < jb && i <= j) A[i + (int64_t)j * lda] = S[i + j * PLD];
-    Wout[e] = (i < jb && j < jb && i <= j) ? Wm[i + j * PLD] : 0.f;
+  const bool avec = ((lda & 3) == 0) && (((uintptr_t)A & 15) == 0);
+  for (int e = t; e < NB * NB / 4; e += 256) {
+    const int j = e / (NB / 4), i = (e % (NB / 4)) * 4;
+    const float4 w = *reinterpret_cast<const float4*>(Wm + i + j * PV);
+    const float4 u = *reinterpret_cast<const float4*>(S + i + j * PV);
+    const bool cj = j < jb;
+    const float wv[4] = {w.x, w.y, w.z, w.w}, uv[4] = {u.x, u.y, u.z, u.w};
+    float wo[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) wo[q] = (cj && i + q <= j && i + q < jb) ? wv[q] : 0.f;
+    *reinterpret_cast<float4*>(Wout + i + j * NB) = make_float4(wo[0], wo[1], wo[2], wo[3]);
+    if (!cj) continue;
+    if (avec && i + 3 <= j && i + 3 < jb) {
+      *reinterpret_cast<float4*>(A + i + (int64_t)j * lda) = u;
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (i + q <= j && i + q < jb) A[i + q + (int64_t)j * lda] = uv[q];
+    }
   }
 }
 
