@@ -1161,48 +1161,46 @@ int rsd_potrf_upper_t(rsd_ctx* ctx, int n, T* d_A, int64_t lda, int* info, const
   bool two_level = false;
   if constexpr (F32) two_level = tc && ctx->use_tc && rsd_tc_syrk_ok(d_A, lda, d_A, lda, NB);
   if constexpr (F32) {
-    if (two_level) {
-      RSD_TRY(potrf_two_level_f32(ctx, n, d_A, lda, tc, W));
-      goto done;
+    if (two_level) RSD_TRY(potrf_two_level_f32(ctx, n, d_A, lda, tc, W));
+  }
+  if (!two_level) {
+    RSD_CUDA(ctx, cudaEventRecord(ctx->ev_next, s));
+    for (int j0 = 0, b = 0; j0 < n; j0 += NB, b++) {
+      const int jb = n - j0 < NB ? n - j0 : NB;
+      T* Ajj = d_A + j0 + (int64_t)j0 * lda;
+      const int rest = n - j0 - jb;
+      T* Apan = d_A + j0 + (int64_t)(j0 + jb) * lda;
+      // panel j on the side stream, after the first tile row of step j-1's update
+      RSD_CUDA(ctx, cudaStreamWaitEvent(s2, ctx->ev_next, 0));
+      if constexpr (F32) {
+        // factor + inverse of the diagonal block, then the panel as W_jj^T B
+        T* Wb = W + (size_t)b * NB * NB;
+        potf2_inv_f32<<<1, 256, SMEM_POTF2_INV, s2>>>(Ajj, lda, jb, ctx->d_info, j0, Wb); RSD_LAUNCH_NOTE();
+        if (rest > 0) {
+          launch_gemm<T>(s2, gp(jb, rest, jb, 1.0, Wb, NB, 1, Apan, lda, 0, 0.0, T1, NB));
+          RSD_CUDA(ctx, cudaMemcpy2DAsync(Apan, lda * sizeof(T), T1, NB * sizeof(T), jb * sizeof(T), rest,
+                                          cudaMemcpyDeviceToDevice, s2));
+        }
+      } else {
+        potf2_upper<T><<<1, 256, smem_potf2<T>(jb), s2>>>(Ajj, lda, jb, ctx->d_info, j0); RSD_LAUNCH_NOTE();
+        if (rest > 0) {
+          trsm_panel<T><<<(rest + TRSM_COLS - 1) / TRSM_COLS, TRSM_COLS, smem_trsm<T>(), s2>>>(Ajj, lda, jb, rest, Apan); RSD_LAUNCH_NOTE();
+        }
+      }
+      RSD_CUDA(ctx, cudaEventRecord(ctx->ev_panel, s2));
+      RSD_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_panel, 0));
+      if (rest > 0) {
+        // trailing A22 -= Apan^T Apan: first tile row (the next panel's input), then the rest
+        T* A22 = d_A + (j0 + jb) + (int64_t)(j0 + jb) * lda;
+        const int m1 = rest < NB ? rest : NB;
+        RSD_TRY(trailing_update<T>(ctx, tc, Apan, lda, jb, m1, rest, A22, lda, 0));
+        RSD_CUDA(ctx, cudaEventRecord(ctx->ev_next, s));
+        if (rest > NB)
+          RSD_TRY(trailing_update<T>(ctx, tc, Apan + (int64_t)NB * lda, lda, jb, rest - NB, rest - NB,
+                                     A22 + NB + (int64_t)NB * lda, lda, 1));
+      }
     }
   }
-  RSD_CUDA(ctx, cudaEventRecord(ctx->ev_next, s));
-  for (int j0 = 0, b = 0; j0 < n; j0 += NB, b++) {
-    const int jb = n - j0 < NB ? n - j0 : NB;
-    T* Ajj = d_A + j0 + (int64_t)j0 * lda;
-    const int rest = n - j0 - jb;
-    T* Apan = d_A + j0 + (int64_t)(j0 + jb) * lda;
-    // panel j on the side stream, after the first tile row of step j-1's update
-    RSD_CUDA(ctx, cudaStreamWaitEvent(s2, ctx->ev_next, 0));
-    if constexpr (F32) {
-      // factor + inverse of the diagonal block, then the panel as W_jj^T B
-      T* Wb = W + (size_t)b * NB * NB;
-      potf2_inv_f32<<<1, 256, SMEM_POTF2_INV, s2>>>(Ajj, lda, jb, ctx->d_info, j0, Wb); RSD_LAUNCH_NOTE();
-      if (rest > 0) {
-        launch_gemm<T>(s2, gp(jb, rest, jb, 1.0, Wb, NB, 1, Apan, lda, 0, 0.0, T1, NB));
-        RSD_CUDA(ctx, cudaMemcpy2DAsync(Apan, lda * sizeof(T), T1, NB * sizeof(T), jb * sizeof(T), rest,
-                                        cudaMemcpyDeviceToDevice, s2));
-      }
-    } else {
-      potf2_upper<T><<<1, 256, smem_potf2<T>(jb), s2>>>(Ajj, lda, jb, ctx->d_info, j0); RSD_LAUNCH_NOTE();
-      if (rest > 0) {
-        trsm_panel<T><<<(rest + TRSM_COLS - 1) / TRSM_COLS, TRSM_COLS, smem_trsm<T>(), s2>>>(Ajj, lda, jb, rest, Apan); RSD_LAUNCH_NOTE();
-      }
-    }
-    RSD_CUDA(ctx, cudaEventRecord(ctx->ev_panel, s2));
-    RSD_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_panel, 0));
-    if (rest > 0) {
-      // trailing A22 -= Apan^T Apan: first tile row (the next panel's input), then the rest
-      T* A22 = d_A + (j0 + jb) + (int64_t)(j0 + jb) * lda;
-      const int m1 = rest < NB ? rest : NB;
-      RSD_TRY(trailing_update<T>(ctx, tc, Apan, lda, jb, m1, rest, A22, lda, 0));
-      RSD_CUDA(ctx, cudaEventRecord(ctx->ev_next, s));
-      if (rest > NB)
-        RSD_TRY(trailing_update<T>(ctx, tc, Apan + (int64_t)NB * lda, lda, jb, rest - NB, rest - NB,
-                                   A22 + NB + (int64_t)NB * lda, lda, 1));
-    }
-  }
-done:
   // diagonal-block inverses for the solves; the FP32 paths made them with
   // their diagonal blocks, the FP64 one takes them here
   if (!F32) {
@@ -1435,9 +1433,9 @@ int rsd_wide_inverses_s(rsd_ctx* ctx, int n, const float* U, int64_t ldu, const 
 //   forward   z_b = r_b - sum_{c<b} Uh_cb^T z_c        (unit diagonal blocks)
 //   middle    w_b = G_b z_b,  G_b = W_b W_b^T = (U_bb^T U_bb)^-1
 //   backward  x_b = w_b - sum_{c>b} Uh_bc x_c
-// Each direction is one streaming launch per block (the strip of Uh next to
-// the block), with no diagonal solve in between.  Uh and G are formed once
-// per factor on tensor cores (3xTF32).
+// Each direction is one dataflow launch over all blocks (tri_forward,
+// tri_backward), the middle one block-diagonal product (blockdiag_gemv).
+// Uh and G are formed once per factor on tensor cores (3xTF32).
 namespace {
 
 __global__ void transpose_block(int nb2, const float* __restrict__ W, float* __restrict__ WT) {
@@ -1451,71 +1449,10 @@ __global__ void transpose_block(int nb2, const float* __restrict__ W, float* __r
   for (int k = threadIdx.y; k < 32; k += blockDim.y) Tb[(j0 + threadIdx.x) + (size_t)(i0 + k) * nb2] = t[threadIdx.x][k];
 }
 
-// forward strip: z_rest[c] -= sum_k S(k, c) z_b[k], one warp per column c
-template <int NR>
-__global__ void __launch_bounds__(256) strip_t_update(int kb, int rest, const float* __restrict__ S, int64_t lds,
-                                                      const float* __restrict__ zb, float* __restrict__ zr,
-                                                      int64_t ldx) {
-  __shared__ __align__(16) float sz[NR][NB2];
-  for (int k = threadIdx.x; k < kb; k += blockDim.x)
-    for (int r = 0; r < NR; r++) sz[r][k] = zb[k + r * ldx];
-  __syncthreads();
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int c = warp; c < rest; c += nwarps) {
-    const float* col = S + (int64_t)c * lds;
-    float acc[NR];
-    for (int r = 0; r < NR; r++) acc[r] = 0.f;
-#pragma unroll 4
-    for (int k = lane * 4; k < kb; k += 128) {  // kb is a multiple of 4
-      const float4 v = *reinterpret_cast<const float4*>(col + k);
-      for (int r = 0; r < NR; r++) {
-        const float4 zz = *reinterpret_cast<const float4*>(&sz[r][k]);
-        acc[r] += v.x * zz.x + v.y * zz.y + v.z * zz.z + v.w * zz.w;
-      }
-    }
-    for (int r = 0; r < NR; r++) {
-      float a = acc[r];
-      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-      if (lane == 0) zr[c + r * ldx] -= a;
-    }
-  }
-}
-
-// backward strip: w[i] -= sum_k S(i, k) x_b[k], i < rows; a CTA takes 64
-// rows and splits the k range over four warp pairs, reduced in shared memory
-template <int NR>
-__global__ void __launch_bounds__(256) strip_n_update(int rows, int kb, const float* __restrict__ S, int64_t lds,
-                                                      const float* __restrict__ xb, float* __restrict__ w,
-                                                      int64_t ldx) {
-  __shared__ float sx[NR][NB2];
-  __shared__ float part[NR][4][64];
-  for (int k = threadIdx.x; k < kb; k += blockDim.x)
-    for (int r = 0; r < NR; r++) sx[r][k] = xb[k + r * ldx];
-  __syncthreads();
-  const int il = threadIdx.x & 63, g = threadIdx.x >> 6;
-  const int i = blockIdx.x * 64 + il;
-  const int kq = (kb + 3) / 4, k0 = g * kq, k1 = min(kb, k0 + kq);
-  float acc[NR];
-  for (int r = 0; r < NR; r++) acc[r] = 0.f;
-  if (i < rows) {
-#pragma unroll 8
-    for (int k = k0; k < k1; k++) {
-      const float v = S[i + (int64_t)k * lds];
-      for (int r = 0; r < NR; r++) acc[r] += v * sx[r][k];
-    }
-  }
-  for (int r = 0; r < NR; r++) part[r][g][il] = acc[r];
-  __syncthreads();
-  if (g == 0 && i < rows)
-    for (int r = 0; r < NR; r++)
-      w[i + r * ldx] -= (part[r][0][il] + part[r][1][il]) + (part[r][2][il] + part[r][3][il]);
-}
-
 // ------------------------------------------- dataflow block sweeps
 // One persistent launch per direction of the block-scaled solve instead of
-// one launch per 512-block.  A task is one 64-wide quarter-of-a-quarter
-// ("part") of a target block: its CTA walks the source blocks in order,
+// one launch per 512-block.  A task is one 32-wide part (of TRI_Q) of a
+// target block: its CTA walks the source blocks in order,
 // waits until each source block is published, and accumulates that tile's
 // product in registers, so every sum has a fixed order (deterministic) and
 // nothing is reduced across CTAs.  Tasks are taken from a ticket counter in

@@ -100,7 +100,6 @@ __global__ void ewald_ktable_list(rsd_lat_dev L, int count, const int* __restric
   for (int m = 0; m < RSD_NMOM_KSIN; m++) e[3 + RSD_NMOM_KCOS + m] = (T)ws[m];
 }
 
-__device__ __forceinline__ void put_trig(double2* p, double c, double sn) { *p = make_double2(c, sn); }
 __device__ __forceinline__ void put_trig(float2* p, double c, double sn) { *p = make_float2((float)c, (float)sn); }
 __device__ __forceinline__ void put_trig(float4* p, double c, double sn) {
   const dsf dc = dsf_from(c), ds = dsf_from(sn);
@@ -1300,8 +1299,14 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
   const int w = 2 * L.NI + 1;
   const int Kh = (w * w * w - 1) / 2;
   double* tab = (double*)rsd_scratch(ctx, "ewald_ktab", sizeof(double) * (size_t)Kh * KW);
-  double2* cs = (double2*)rsd_scratch(ctx, "ewald_trig", sizeof(double2) * (size_t)Kh * nn);
-  if (!tab || !cs) return RSD_ENOMEM;
+  if (!tab) return RSD_ENOMEM;
+  // FP64 cos/sin per (vector, particle): the FP64 form only (the mixed form
+  // keeps its own FP32 and float-pair lists)
+  double2* cs = nullptr;
+  if (precision != RSD_PREC_MIXED) {
+    cs = (double2*)rsd_scratch(ctx, "ewald_trig", sizeof(double2) * (size_t)Kh * nn);
+    if (!cs) return RSD_ENOMEM;
+  }
   const double inv_pimu = 1.0 / (RSD_PI * mu_f);
   cudaStream_t s = ctx->stream;
   ewald_ktable<<<(Kh + 127) / 128, 128, 0, s>>>(L, Kh, tab); RSD_LAUNCH_NOTE();
