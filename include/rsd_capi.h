@@ -119,9 +119,13 @@ int rsd_calc_lattice_inverse(rsd_lattice* lat, double ews_err, int32_t nn, const
 /* PER_GRPERY_INV_FRI (src/per_GRPY_YZD.f90:13-200): Ewald-summed periodic
  * grand mobility, scaled by 1/(pi mu_f), split into APP (6nn x 6nn),
  * APQ (6nn x 5nn), AQQ (5nn x 5nn).  Calls CALC_LATTICE_INVERSE first and
- * leaves its results in *lat.  correction_method != 0 (overlap corrections
- * of GRPY_YZD.f90:768-836) is not built: with an overlapping pair it returns
- * RSD_EUNSUP, without one it is ignored, like the reference. */
+ * leaves its results in *lat.  correction_method (per_GRPY_YZD.f90:98-116)
+ * acts on pairs whose minimum image overlaps or touches (r <= a_i + a_j):
+ * 0 none; 1 adds Yamakawa's overlapping-sphere blocks minus the free-space
+ * pair (overlap_Yamakawa_CORRECTION_IJ, GRPY_YZD.f90:789-811); 2 (the
+ * regularized correction, GRPY_YZD.f90:813-836) is not built and returns
+ * RSD_EUNSUP when a pair overlaps (ignored without one, like the
+ * reference); other values return RSD_EARG. */
 int rsd_per_grpery_inv_fri(rsd_ctx* ctx, int32_t nn, const double* p_pos, const double* radii, rsd_lattice* lat,
                            double ews_err, double mu_f, int32_t correction_method, double* APP, double* APQ,
                            double* AQQ);

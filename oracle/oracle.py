@@ -62,6 +62,7 @@ def lib():
         L = ctypes.CDLL(LIB)
         dp = ctypes.POINTER(ctypes.c_double)
         L.rsdo_per_grpery_inv_fri.restype = ctypes.c_int
+        L.rsdo_overlap_correction_ij.restype = ctypes.c_int
         L.rsdo_lubmxcalc.restype = ctypes.c_int
         L.rsdo_lubtab_load.restype = ctypes.c_int
         L.rsdo_lubtab_sizeof.restype = ctypes.c_int
@@ -143,9 +144,41 @@ def per_rotne_prager_ij(lat: Lattice, R, aI: float, aJ: float, include_k: bool =
     return f(TT, (3, 3)), f(RR, (3, 3)), f(TR, (3, 3)), f(QQ, (5, 5)), f(G, (3, 5)), f(H, (3, 5))
 
 
+def _pair_blocks(fn, *args):
+    TT, RR, TR, QQ, G, H = (np.zeros(9), np.zeros(9), np.zeros(9), np.zeros(25), np.zeros(15), np.zeros(15))
+    rc = fn(*args, _p(TT), _p(RR), _p(TR), _p(QQ), _p(G), _p(H))
+    f = lambda x, s: x.reshape(s, order="F")
+    return rc, (f(TT, (3, 3)), f(RR, (3, 3)), f(TR, (3, 3)), f(QQ, (5, 5)), f(G, (3, 5)), f(H, (3, 5)))
+
+
+def yamakawa_ij(R, aI: float, aJ: float):
+    """YAMAKAWA_IJ (src/GRPY_YZD.f90:768-786): the overlapping-sphere pair
+    blocks TT, RR, TR (3,3), QQ_TR (5,5), GPQ_TR, HPQ_TR (3,5)."""
+    R = np.ascontiguousarray(R, dtype=np.float64)
+    return _pair_blocks(lib().rsdo_yamakawa_ij, _p(R), ctypes.c_double(aI), ctypes.c_double(aJ))[1]
+
+
+def rotne_prager_ij_fts(R, aI: float, aJ: float):
+    """ROTNE_PRAGER_IJ_FTS (src/stokesian_Green.f90:11-109): the free-space
+    pair with that file's derivative chain."""
+    R = np.ascontiguousarray(R, dtype=np.float64)
+    return _pair_blocks(lib().rsdo_rotne_prager_ij_fts, _p(R), ctypes.c_double(aI), ctypes.c_double(aJ))[1]
+
+
+def overlap_correction_ij(method: int, R, aI: float, aJ: float):
+    """overlap_*_CORRECTION_IJ (src/GRPY_YZD.f90:789-836); None for a method
+    the oracle does not restate."""
+    R = np.ascontiguousarray(R, dtype=np.float64)
+    rc, blocks = _pair_blocks(lib().rsdo_overlap_correction_ij, ctypes.c_int(method), _p(R), ctypes.c_double(aI),
+                              ctypes.c_double(aJ))
+    return blocks if rc == 0 else None
+
+
 def per_grpery_inv_fri(pos, radii, lat: Lattice, ews_err: float, mu_f: float, correction_method: int = 0):
     """PER_GRPERY_INV_FRI: returns (grmobmx (11N,11N) Fortran-ordered,
-    n_overlap).  APP/APQ/AQQ are grmobmx[:6N,:6N], [:6N,6N:], [6N:,6N:]."""
+    n_overlap).  APP/APQ/AQQ are grmobmx[:6N,:6N], [:6N,6N:], [6N:,6N:].
+    correction_method 1 adds the Yamakawa correction to overlapping pairs;
+    n_overlap counts the overlapping pairs of a method not restated."""
     pos = np.ascontiguousarray(pos, dtype=np.float64)
     radii = np.ascontiguousarray(radii, dtype=np.float64)
     N = len(radii)

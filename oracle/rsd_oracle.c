@@ -15,6 +15,10 @@
  *   src/Ewald_summation.f90 PER_ROTNE_PRAGER_SELF 19-191,
  *                           PER_ROTNE_PRAGER_IJ 196-423, helpers 427-1257
  *   src/per_GRPY_YZD.f90    PER_GRPERY_INV_FRI 13-200
+ *   src/GRPY_YZD.f90        YAMAKAWA_*_IJ 326-786, overlap_Yamakawa_
+ *                           CORRECTION_IJ 789-811 (correction method 1)
+ *   src/stokesian_Green.f90 ROTNE_PRAGER_IJ_FTS 11-109
+ *   src/tensors.f90         CALC_RR ... CALC_t4D2 182-440 (Yamakawa tensors)
  *   src/hydro_lub.f90       lubmxcalc 22-308, lubcalc 310-398,
  *                           lubtabcalc 400-525
  * Arrays are column-major like Fortran; indices are 0-based here.
@@ -594,9 +598,19 @@ int rsdo_farfield_table_variant = 0;
  * QQP_TR (5,5), GPQ_TR, HPQ_TR (3,5).  R is the minimum-image separation.
  * With include_k = 0 and NR = 0 and lam = 0 this is the free-space pair
  * (the n = 0 image of the unscreened sum). */
+static void per_rotne_prager_ij_v(const rsdo_lattice *lat, const double R[3], double aaI, double aaJ,
+                                  int include_k, int table_variant, double TTP[9], double RRP[9], double TRP[9],
+                                  double QQP_TR[25], double GPQ_TR[15], double HPQ_TR[15]);
 void rsdo_per_rotne_prager_ij(const rsdo_lattice *lat, const double R[3], double aaI, double aaJ, int include_k,
                               double TTP[9], double RRP[9], double TRP[9], double QQP_TR[25], double GPQ_TR[15],
                               double HPQ_TR[15]) {
+  per_rotne_prager_ij_v(lat, R, aaI, aaJ, include_k, rsdo_farfield_table_variant, TTP, RRP, TRP, QQP_TR, GPQ_TR,
+                        HPQ_TR);
+}
+
+static void per_rotne_prager_ij_v(const rsdo_lattice *lat, const double R[3], double aaI, double aaJ,
+                                  int include_k, int table_variant, double TTP[9], double RRP[9], double TRP[9],
+                                  double QQP_TR[25], double GPQ_TR[15], double HPQ_TR[15]) {
   init_tensors();
   const double lam = lat->lammda, phix = 1 - 0.2 * lat->phi;
   const double nondim_a = 1.0 / (6.0 * aaI), nondim_a3 = 1.0 / (6.0 * aaI * aaI * aaI);
@@ -617,7 +631,7 @@ void rsdo_per_rotne_prager_ij(const rsdo_lattice *lat, const double R[3], double
         erfc_chain(lam, dist, e);
         rerfc_tensors(lam, RN, dist, e, 1, &t);
         j_chain(&t, 1, &c);
-        if (rsdo_farfield_table_variant) {
+        if (table_variant) {
           /* The generator of the reference's tablefar.txt (FarfieldForce/
            * tools.f90 Init_DDD2_Jg) writes the delta_ij x_k x_l / r^7 term
            * of the free-space fourth derivative with the opposite sign
@@ -738,6 +752,234 @@ void rsdo_per_rotne_prager_ij(const rsdo_lattice *lat, const double R[3], double
   qq_tr(QQP_TR, QQP);
 }
 
+/* ------------------------------------------------ overlap corrections */
+/* Unit-vector tensors of the Yamakawa forms, src/tensors.f90:182-440:
+ * CALC_RR (RR_ij = r_i r_j), CALC_EPSR (EPSR_ij = eps_ijk r_k), CALC_UR
+ * (UR_ijk = delta_ij r_k), CALC_RRR, CALC_EPSRR (EPSR_ij r_k), and the
+ * rank-4 CALC_t4D0 = 3/2 (RR - I/3)(RR - I/3),
+ * CALC_t4D1 = 1/2 (d_jl r_i r_k + d_ik r_j r_l + d_jk r_i r_l + d_il r_j r_k
+ *                  - 4 r_i r_j r_k r_l),
+ * CALC_t4D2 = 1/2 (d_ik d_jl + d_jk d_il - d_ij d_kl + d_kl r_i r_j
+ *                  + d_ij r_k r_l - 3 r_i r_j r_k r_l)
+ * (the index pairs as t2at2b_t4 + t4trans build them, 443-560). */
+typedef struct {
+  double RR[9], EPSR[9], UR[27], RRR[27], EPSRR[27], D0[81], D1[81], D2[81];
+} yk_tensors_t;
+
+static void yk_tensors(const double R[3], double *dist, yk_tensors_t *t) {
+  init_tensors();
+  const double d = sqrt(R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
+  const double rw[3] = {R[0] / d, R[1] / d, R[2] / d};
+  *dist = d;
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) t->RR[I2(i, j)] = rw[i] * rw[j];
+  memset(t->EPSR, 0, sizeof t->EPSR);
+  t->EPSR[I2(0, 1)] = rw[2];
+  t->EPSR[I2(1, 2)] = rw[0];
+  t->EPSR[I2(2, 0)] = rw[1];
+  t->EPSR[I2(1, 0)] = -rw[2];
+  t->EPSR[I2(2, 1)] = -rw[0];
+  t->EPSR[I2(0, 2)] = -rw[1];
+  for (int k = 0; k < 3; k++)
+    for (int j = 0; j < 3; j++)
+      for (int i = 0; i < 3; i++) {
+        t->UR[I3(i, j, k)] = KD[I2(i, j)] * rw[k];
+        t->RRR[I3(i, j, k)] = rw[i] * rw[j] * rw[k];
+        t->EPSRR[I3(i, j, k)] = t->EPSR[I2(i, j)] * rw[k];
+      }
+  for (int l = 0; l < 3; l++)
+    for (int k = 0; k < 3; k++)
+      for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 3; i++) {
+          const double rrrr = rw[i] * rw[j] * rw[k] * rw[l];
+          const int q = I4(i, j, k, l);
+          t->D0[q] = 1.5 * (t->RR[I2(i, j)] - KD[I2(i, j)] / 3.0) * (t->RR[I2(k, l)] - KD[I2(k, l)] / 3.0);
+          t->D1[q] = 0.5 * (KD[I2(j, l)] * rw[i] * rw[k] + KD[I2(i, k)] * rw[j] * rw[l] +
+                            KD[I2(j, k)] * rw[i] * rw[l] + KD[I2(i, l)] * rw[j] * rw[k] - 4.0 * rrrr);
+          t->D2[q] = 0.5 * (KD[I2(i, k)] * KD[I2(j, l)] + KD[I2(j, k)] * KD[I2(i, l)] -
+                            KD[I2(i, j)] * KD[I2(k, l)] + KD[I2(k, l)] * rw[i] * rw[j] +
+                            KD[I2(i, j)] * rw[k] * rw[l] - 3.0 * rrrr);
+        }
+}
+
+/* YAMAKAWA_TT_IJ, src/GRPY_YZD.f90:326-368: both radius orders use the same
+ * form outside; inside the larger sphere the larger sphere's mobility. */
+static void yamakawa_tt(const double R[3], double aaI, double aaJ, double A1[9]) {
+  yk_tensors_t t;
+  double dist;
+  yk_tensors(R, &dist, &t);
+  const double abig = aaI <= aaJ ? aaJ : aaI, adiff = aaI <= aaJ ? aaJ - aaI : aaI - aaJ;
+  if (dist <= adiff) {
+    for (int q = 0; q < 9; q++) A1[q] = 1.0 / 6.0 / abig * KD[q];
+    return;
+  }
+  const double dist2 = dist * dist, dist3 = dist2 * dist, d = aaI - aaJ;
+  const double pre = 1.0 / (6 * 32 * aaI * aaJ);
+  const double pu = 16 * (aaI + aaJ) - (d * d + 3 * dist2) * (d * d + 3 * dist2) / dist3;
+  const double prr = 3 * (d * d - dist2) * (d * d - dist2) / dist3;
+  for (int q = 0; q < 9; q++) A1[q] = pre * (pu * KD[q] + prr * t.RR[q]);
+}
+
+/* YAMAKAWA_RR_IJ, src/GRPY_YZD.f90:373-439 */
+static void yamakawa_rr(const double R[3], double aaI, double aaJ, double A1[9]) {
+  yk_tensors_t t;
+  double dist;
+  yk_tensors(R, &dist, &t);
+  const double abig = aaI <= aaJ ? aaJ : aaI, adiff = aaI <= aaJ ? aaJ - aaI : aaI - aaJ;
+  if (dist <= adiff) {
+    for (int q = 0; q < 9; q++) A1[q] = 1.0 / 8.0 / (abig * abig * abig) * KD[q];
+    return;
+  }
+  const double dist2 = dist * dist, dist3 = dist2 * dist, d = aaI - aaJ;
+  const double aI2 = aaI * aaI, aJ2 = aaJ * aaJ, aI3 = aI2 * aaI, aJ3 = aJ2 * aaJ;
+  const double pre = 1.0 / (8 * 64 * aI3 * aJ3);
+  const double pu = 5 * dist3 - 27 * dist * (aI2 + aJ2) + 32 * (aI3 + aJ3) - 9 * (aI2 - aJ2) * (aI2 - aJ2) / dist -
+                    d * d * d * d * (aI2 + 4 * aaI * aaJ + aJ2) / dist3;
+  const double prr = 3 * (d * d - dist2) * (d * d - dist2) * ((aI2 + 4 * aaI * aaJ + aJ2) - dist2) / dist3;
+  for (int q = 0; q < 9; q++) A1[q] = pre * (pu * KD[q] + prr * t.RR[q]);
+}
+
+/* YAMAKAWA_RT_IJ, src/GRPY_YZD.f90:467-500 */
+static void yamakawa_rt(const double R[3], double aaI, double aaJ, double A1[9]) {
+  yk_tensors_t t;
+  double dist;
+  yk_tensors(R, &dist, &t);
+  double f;
+  if (aaI <= aaJ && dist <= aaJ - aaI) {
+    f = 0.0;
+  } else if (aaI > aaJ && dist <= aaI - aaJ) {
+    f = dist / (8 * aaI * aaI * aaI);
+  } else {
+    const double pre = 1.0 / (16 * 8 * aaI * aaI * aaI * aaJ);
+    const double s = (aaI - aaJ) + dist;
+    f = pre * s * s * (aaJ * aaJ + 2 * aaJ * (aaI + dist) - 3 * (aaI - dist) * (aaI - dist)) / (dist * dist);
+  }
+  for (int q = 0; q < 9; q++) A1[q] = f * t.EPSR[q];
+}
+
+/* YAMAKAWA_RD_IJ, src/GRPY_YZD.f90:512-553 */
+static void yamakawa_rd(const double R[3], double aaI, double aaJ, double C1[27]) {
+  yk_tensors_t t;
+  double dist;
+  yk_tensors(R, &dist, &t);
+  const double adiff = aaI <= aaJ ? aaJ - aaI : aaI - aaJ;
+  if (dist <= adiff) {
+    memset(C1, 0, sizeof(double) * 27);
+    return;
+  }
+  const double dist2 = dist * dist, d = aaI - aaJ;
+  const double f = -3.0 / (256.0 * aaI * aaI * aaI * aaJ * aaJ * aaJ * dist2 * dist) * (d * d - dist2) *
+                   (d * d - dist2) * ((aaI * aaI + 4 * aaI * aaJ + aaJ * aaJ) - dist2);
+  for (int q = 0; q < 27; q++) C1[q] = f * t.EPSRR[q];
+}
+
+/* YAMAKAWA_TD_IJ, src/GRPY_YZD.f90:582-640 */
+static void yamakawa_td(const double R[3], double aaI, double aaJ, double C1[27]) {
+  yk_tensors_t t;
+  double dist;
+  yk_tensors(R, &dist, &t);
+  if (aaI <= aaJ && dist <= aaJ - aaI) {
+    for (int q = 0; q < 27; q++) C1[q] = -3.0 * dist / (20.0 * aaJ * aaJ * aaJ) * t.UR[q];
+    return;
+  }
+  if (aaI > aaJ && dist <= aaI - aaJ) {
+    memset(C1, 0, sizeof(double) * 27);
+    return;
+  }
+  const double dist2 = dist * dist, dist4 = dist2 * dist2, d = aaI - aaJ;
+  const double pre = 1.0 / (aaI * aaJ * aaJ * aaJ);
+  const double pur = (10.0 * dist2 - 24.0 * aaI * dist + 15.0 * (aaI * aaI - aaJ * aaJ) -
+                      d * d * d * d * d * (aaI + 5.0 * aaJ) / dist4) / 320.0;
+  const double prrr = (d * d - dist2) * (d * d - dist2) * (d * (aaI + 5 * aaJ) - dist2) / (128.0 * dist4);
+  for (int q = 0; q < 27; q++) C1[q] = pre * (pur * t.UR[q] + prrr * t.RRR[q]);
+}
+
+/* YAMAKAWA_DD_IJ, src/GRPY_YZD.f90:665-766 (t4D2 is replaced by
+ * t4D2 - t4D1 before either branch, 693) */
+static void yamakawa_dd(const double R[3], double aaI, double aaJ, double B1[81]) {
+  yk_tensors_t t;
+  double dist;
+  yk_tensors(R, &dist, &t);
+  for (int q = 0; q < 81; q++) t.D2[q] = t.D2[q] - t.D1[q];
+  const double abig = aaI <= aaJ ? aaJ : aaI, adiff = aaI <= aaJ ? aaJ - aaI : aaI - aaJ;
+  if (dist <= adiff) {
+    for (int q = 0; q < 81; q++) B1[q] = 3.0 / (abig * abig * abig * 20.0) * (t.D0[q] + t.D1[q] + t.D2[q]);
+    return;
+  }
+  const double dist3 = dist * dist * dist, dist5 = dist3 * dist * dist, d = aaI - aaJ;
+  const double aI2 = aaI * aaI, aJ2 = aaJ * aaJ, aI3 = aI2 * aaI, aJ3 = aJ2 * aaJ;
+  const double d4 = d * d * d * d, d6 = d4 * d * d;
+  const double c0 = 3.0 / (1280.0 * aI3 * aJ3) *
+                    (+3.0 * d6 * (aI2 + 6.0 * aaI * aaJ + aJ2) / dist5 - 10.0 * d4 * (aI2 + 4.0 * aaI * aaJ + aJ2) / dist3 +
+                     32.0 * (aI3 + aJ3) - 30.0 * (aI2 + aJ2) * dist + 5.0 * dist3);
+  const double c1 = 3.0 / (1280.0 * aI3 * aJ3) *
+                    (-2.0 * d6 * (aI2 + 6.0 * aaI * aaJ + aJ2) / dist5 + 5.0 * d4 * (aI2 + 4.0 * aaI * aaJ + aJ2) / dist3 -
+                     15.0 * (aI2 - aJ2) * (aI2 - aJ2) / dist + 32.0 * (aI3 + aJ3) - 25.0 * (aI2 + aJ2) * dist +
+                     5.0 * dist3);
+  const double c2 = 3.0 / (2560.0 * aI3 * aJ3) *
+                    (+d6 * (aI2 + 6.0 * aaI * aaJ + aJ2) / dist5 - 30.0 * (aI2 - aJ2) * (aI2 - aJ2) / dist +
+                     64.0 * (aI3 + aJ3) - 40.0 * (aI2 + aJ2) * dist + 5.0 * dist3);
+  for (int q = 0; q < 81; q++) B1[q] = c0 * t.D0[q] + c1 * t.D1[q] + c2 * t.D2[q];
+}
+
+/* YAMAKAWA_IJ, src/GRPY_YZD.f90:768-786: the overlapping-sphere pair
+ * blocks (TR from the RT block of the swapped pair, transposed). */
+void rsdo_yamakawa_ij(const double R[3], double aaI, double aaJ, double TTPY[9], double RRPY[9], double TRPY[9],
+                      double QQPY_TR[25], double GPQY_TR[15], double HPQY_TR[15]) {
+  init_tensors();
+  yamakawa_tt(R, aaI, aaJ, TTPY);
+  yamakawa_rr(R, aaI, aaJ, RRPY);
+  const double mR[3] = {-R[0], -R[1], -R[2]};
+  double RT0[9], G[27], H[27], Q[81];
+  yamakawa_rt(mR, aaJ, aaI, RT0);
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) TRPY[I2(i, j)] = RT0[I2(j, i)];
+  yamakawa_td(R, aaI, aaJ, G);
+  yamakawa_rd(R, aaI, aaJ, H);
+  yamakawa_dd(R, aaI, aaJ, Q);
+  gh_tr(GPQY_TR, G);
+  gh_tr(HPQY_TR, H);
+  qq_tr(QQPY_TR, Q);
+}
+
+/* ROTNE_PRAGER_IJ_FTS, src/stokesian_Green.f90:11-109: the free-space
+ * pair.  Its chain (Init_*_Jg, 215-433) is the unscreened one of
+ * PER_ROTNE_PRAGER_IJ, except that Init_DDD2_Jg (295-312) writes the
+ * delta_ij x_k x_l / r^7 term with the sign of the tablefar.txt generator:
+ * the n = 0 image at lammda = 0 with that variant. */
+void rsdo_rotne_prager_ij_fts(const double R[3], double aaI, double aaJ, double TTP[9], double RRP[9], double TRP[9],
+                              double QQP_TR[25], double GPQ_TR[15], double HPQ_TR[15]) {
+  rsdo_lattice fl;
+  memset(&fl, 0, sizeof fl);
+  fl.LV = 1.0;
+  per_rotne_prager_ij_v(&fl, R, aaI, aaJ, 0, 1, TTP, RRP, TRP, QQP_TR, GPQ_TR, HPQ_TR);
+}
+
+/* overlap_Yamakawa_CORRECTION_IJ (method 1), src/GRPY_YZD.f90:789-811:
+ * Yamakawa's overlapping-sphere blocks minus the free-space pair.  Method 2
+ * (overlap_Regular_CORRECTION_IJ, 813-836, Regularization.f90) is not
+ * restated: returns -1 for it, 0 otherwise. */
+int rsdo_overlap_correction_ij(int method, const double R[3], double aaI, double aaJ, double TTPC[9],
+                               double RRPC[9], double TRPC[9], double QQPC_TR[25], double GPQC_TR[15],
+                               double HPQC_TR[15]) {
+  if (method != 1) return -1;
+  double TTY[9], RRY[9], TRY[9], QQY[25], GY[15], HY[15];
+  double TT[9], RR[9], TR[9], QQ[25], G[15], H[15];
+  rsdo_yamakawa_ij(R, aaI, aaJ, TTY, RRY, TRY, QQY, GY, HY);
+  rsdo_rotne_prager_ij_fts(R, aaI, aaJ, TT, RR, TR, QQ, G, H);
+  for (int q = 0; q < 9; q++) {
+    TTPC[q] = TTY[q] - TT[q];
+    RRPC[q] = RRY[q] - RR[q];
+    TRPC[q] = TRY[q] - TR[q];
+  }
+  for (int q = 0; q < 25; q++) QQPC_TR[q] = QQY[q] - QQ[q];
+  for (int q = 0; q < 15; q++) {
+    GPQC_TR[q] = GY[q] - G[q];
+    HPQC_TR[q] = HY[q] - H[q];
+  }
+  return 0;
+}
+
 /* Scatter of one (alpha,beta) block and its mirror into grmobmx(11N,11N),
  * src/per_GRPY_YZD.f90:123-151,160-188 */
 static void scatter_pair(double *G, long n11, int NN, int al, int be, const double *a, const double *b,
@@ -766,8 +1008,9 @@ static void scatter_pair(double *G, long n11, int NN, int al, int be, const doub
  * grand mobility grmobmx (11N x 11N, column-major) already divided by
  * (pi mu_f); APP/APQ/AQQ are its blocks.  lat must hold LR, LI, LV; the
  * routine fills lammda, NR, NI, phi exactly as CALC_LATTICE_INVERSE does.
- * correction_method != 0 with an overlapping pair returns the count of
- * overlapping pairs (positive) without applying a correction. */
+ * correction_method = 1 adds the Yamakawa correction to overlapping pairs;
+ * another nonzero method with an overlapping pair returns the count of
+ * such pairs (positive) without applying a correction. */
 int rsdo_per_grpery_inv_fri(int NN, const double *p_pos, const double *radii, rsdo_lattice *lat, double ews_err,
                             double mu_f, int correction_method, double *grmobmx) {
   init_tensors();
@@ -789,7 +1032,25 @@ int rsdo_per_grpery_inv_fri(int NN, const double *p_pos, const double *radii, rs
       rsdo_per_skew_correction(lat->LR, lat->LI, R, &dmin);
       double TTP[9], RRP[9], TRP[9], QQP[25], GPQ[15], HPQ[15];
       rsdo_per_rotne_prager_ij(lat, R, radii[al], radii[be], 1, TTP, RRP, TRP, QQP, GPQ, HPQ);
-      if (correction_method != 0 && dmin <= radii[al] + radii[be]) overl++;
+      /* per_GRPY_YZD.f90:98-116: the correction for pairs whose minimum
+       * image overlaps (or touches), evaluated at the minimum image */
+      if (correction_method != 0 && dmin <= radii[al] + radii[be]) {
+        double TTC[9], RRC[9], TRC[9], QQC[25], GC[15], HC[15];
+        if (rsdo_overlap_correction_ij(correction_method, R, radii[al], radii[be], TTC, RRC, TRC, QQC, GC, HC) == 0) {
+          for (int q = 0; q < 9; q++) {
+            TTP[q] += TTC[q];
+            RRP[q] += RRC[q];
+            TRP[q] += TRC[q];
+          }
+          for (int q = 0; q < 25; q++) QQP[q] += QQC[q];
+          for (int q = 0; q < 15; q++) {
+            GPQ[q] += GC[q];
+            HPQ[q] += HC[q];
+          }
+        } else {
+          overl++;
+        }
+      }
       double TRPm[9], GPQm[15];
       for (int q = 0; q < 9; q++) TRPm[q] = -TRP[q];
       for (int q = 0; q < 15; q++) GPQm[q] = -GPQ[q];

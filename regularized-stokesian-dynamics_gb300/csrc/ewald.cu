@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "ewald_gen.cuh"
+#include "overlap.cuh"
 #include "dsf.cuh"
 #include "rsd_internal.cuh"
 
@@ -1210,7 +1211,60 @@ __global__ void overlap_count(int nn, rsd_lat_dev L, const double* __restrict__ 
   if (d <= radii[a] + radii[b]) atomicAdd(count, 1);
 }
 
+// Overlapping pairs (minimum image with r <= a_i + a_j, the test of
+// per_GRPY_YZD.f90:98) into a list of at most cap pairs; count ends at the
+// number found.
+__global__ void overlap_list(int nn, rsd_lat_dev L, const double* __restrict__ pos, const double* __restrict__ radii,
+                             int cap, int2* __restrict__ list, int* __restrict__ count) {
+  int a, b;
+  if (!pair_of(nn, &a, &b)) return;
+  double R[3] = {pos[3 * a] - pos[3 * b], pos[3 * a + 1] - pos[3 * b + 1], pos[3 * a + 2] - pos[3 * b + 2]};
+  double d;
+  rsd_skew_correction(L.LR, L.LI, R, &d);
+  if (d <= radii[a] + radii[b]) {
+    const int k = atomicAdd(count, 1);
+    if (k < cap) list[k] = make_int2(a, b);
+  }
+}
+
+// Overlap correction (correction_method 1) of the listed pairs, one thread
+// per pair, added to the assembled blocks at the minimum image: the blocks
+// of different pairs are disjoint, so the sum does not depend on the order
+// of the list.
+template <typename S>
+__global__ void __launch_bounds__(64) overlap_correct(int npair, const int2* __restrict__ list, int nn, rsd_lat_dev L,
+                                                       const double* __restrict__ pos,
+                                                       const double* __restrict__ radii, double inv_pimu, S sk) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= npair) return;
+  const int a = list[q].x, b = list[q].y;
+  double R[3] = {pos[3 * a] - pos[3 * b], pos[3 * a + 1] - pos[3 * b + 1], pos[3 * a + 2] - pos[3 * b + 2]};
+  double d;
+  rsd_skew_correction(L.LR, L.LI, R, &d);
+  double v[60];
+  rsd_overlap_correction60(R, radii[a], radii[b], v);
+  for (int k = 0; k < 60; k++) v[k] *= inv_pimu;
+  store_pair_d(sk, nn, a, b, v, 1);
+}
+
 }  // namespace
+
+int rsd_overlap_correct(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
+                        double mu_f, int npair, double* d_M, int64_t ldm) {
+  if (npair <= 0) return RSD_OK;
+  const rsd_lat_dev L = rsd_lat_pack(lat);
+  int* cnt = (int*)rsd_scratch(ctx, "overlap_count", sizeof(int));
+  int2* list = (int2*)rsd_scratch(ctx, "overlap_list", sizeof(int2) * (size_t)npair);
+  if (!cnt || !list) return RSD_ENOMEM;
+  RSD_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int), ctx->stream));
+  dim3 blk(32, 4), grd((nn + 31) / 32, (nn + 3) / 4);
+  overlap_list<<<grd, blk, 0, ctx->stream>>>(nn, L, d_pos, d_radii, npair, list, cnt); RSD_LAUNCH_NOTE();
+  const DenseSink dsk{d_M, ldm};
+  overlap_correct<DenseSink><<<(npair + 63) / 64, 64, 0, ctx->stream>>>(npair, list, nn, L, d_pos, d_radii,
+                                                                       1.0 / (RSD_PI * mu_f), dsk); RSD_LAUNCH_NOTE();
+  RSD_CUDA(ctx, cudaGetLastError());
+  return RSD_OK;
+}
 
 int rsd_count_overlaps(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
                        int* count) {

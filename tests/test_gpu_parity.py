@@ -95,6 +95,34 @@ def test_grand_mobility_unequal_radii(rsd, ctx):
         assert np.abs(a - b).max() <= 1e-12 * np.abs(G).max()
 
 
+@pytest.mark.parametrize("T", [0.0, 0.37])
+def test_overlap_correction_matches_oracle(rsd, ctx, T):
+    """correction_method 1 (Yamakawa, per_GRPY_YZD.f90:98-116) on pairs whose
+    minimum image overlaps: a partial overlap of unequal spheres, a small
+    sphere inside a larger one, and a pair that overlaps only across the
+    periodic boundary; against the oracle to 1e-12 of the largest entry."""
+    N, L = 10, 9.0
+    rng = np.random.default_rng(20261210)
+    pos = rsd.configs.packing(N, 0.05, 0.5, seed=20260211)[0] * (L / rsd.configs.box_edge(N, 0.05))
+    radii = np.where(rng.random(N) < 0.5, 1.0, 0.6)
+    radii[:6] = [1.0, 0.8, 1.0, 0.5, 1.0, 1.0]
+    pos[1] = pos[0] + np.array([1.1, 0.4, -0.3])
+    pos[3] = pos[2] + np.array([0.2, -0.1, 0.15])
+    pos[4] = np.array([0.3, 4.0, 4.0])
+    pos[5] = np.array([L - 0.9, 4.2, 4.1])
+    pos = np.mod(pos, L)
+    lat_g = rsd.SET_LATTICE_SKEW(T, [L, L, L], 1.0)
+    APP, APQ, AQQ = rsd.PER_GRPERY_INV_FRI(ctx, pos, radii, lat_g, 1e-10, MU, correction_method=1)
+    G, nov = o.per_grpery_inv_fri(pos, radii, o.set_lattice_skew(T, [L, L, L], 1.0), 1e-10, MU, correction_method=1)
+    G0, _ = o.per_grpery_inv_fri(pos, radii, o.set_lattice_skew(T, [L, L, L], 1.0), 1e-10, MU)
+    assert nov == 0
+    scale = np.abs(G).max()
+    assert np.abs(G - G0).max() > 1e-6 * scale  # the corrections are applied
+    oPP, oPQ, oQQ = o.split_mobility(G, N)
+    for a, b in ((APP, oPP), (APQ, oPQ), (AQQ, oQQ)):
+        assert np.abs(a - b).max() <= 1e-12 * scale
+
+
 def test_grand_mobility_device_variant(rsd, ctx):
     import torch
     pos, radii, L = rsd.configs.packing(27, 0.2, 0.01, seed=20260300)
@@ -239,8 +267,11 @@ def test_errors_are_reported_not_faulted(rsd, ctx):
     over = pos.copy()
     over[1] = over[0] + np.array([1.5, 0, 0])
     with pytest.raises(rsd.RSDError) as e:
-        rsd.PER_GRPERY_INV_FRI(ctx, over, radii, lat, 1e-10, MU, correction_method=1)
+        rsd.PER_GRPERY_INV_FRI(ctx, over, radii, lat, 1e-10, MU, correction_method=2)
     assert e.value.code == rsd.RSD_EUNSUP
+    with pytest.raises(rsd.RSDError) as e:
+        rsd.PER_GRPERY_INV_FRI(ctx, over, radii, lat, 1e-10, MU, correction_method=3)
+    assert e.value.code == rsd.RSD_EARG
     with pytest.raises(rsd.RSDError) as e:
         rsd.PER_GRPERY_INV_FRI(ctx, pos, radii, lat, 1e-10, -1.0)
     assert e.value.code == rsd.RSD_EARG
