@@ -165,6 +165,13 @@ def rotne_prager_ij_fts(R, aI: float, aJ: float):
     return _pair_blocks(lib().rsdo_rotne_prager_ij_fts, _p(R), ctypes.c_double(aI), ctypes.c_double(aJ))[1]
 
 
+def regular_rotne_prager_ij(R, aI: float, aJ: float):
+    """Regular_ROTNE_PRAGER_IJ (src/Regularization.f90:18-162): the
+    regularized pair blocks."""
+    R = np.ascontiguousarray(R, dtype=np.float64)
+    return _pair_blocks(lib().rsdo_regular_rotne_prager_ij, _p(R), ctypes.c_double(aI), ctypes.c_double(aJ))[1]
+
+
 def overlap_correction_ij(method: int, R, aI: float, aJ: float):
     """overlap_*_CORRECTION_IJ (src/GRPY_YZD.f90:789-836); None for a method
     the oracle does not restate."""
@@ -177,8 +184,9 @@ def overlap_correction_ij(method: int, R, aI: float, aJ: float):
 def per_grpery_inv_fri(pos, radii, lat: Lattice, ews_err: float, mu_f: float, correction_method: int = 0):
     """PER_GRPERY_INV_FRI: returns (grmobmx (11N,11N) Fortran-ordered,
     n_overlap).  APP/APQ/AQQ are grmobmx[:6N,:6N], [:6N,6N:], [6N:,6N:].
-    correction_method 1 adds the Yamakawa correction to overlapping pairs;
-    n_overlap counts the overlapping pairs of a method not restated."""
+    correction_method 1 (Yamakawa) or 2 (regularized) adds its correction to
+    overlapping pairs; n_overlap counts the overlapping pairs of another
+    nonzero method."""
     pos = np.ascontiguousarray(pos, dtype=np.float64)
     radii = np.ascontiguousarray(radii, dtype=np.float64)
     N = len(radii)

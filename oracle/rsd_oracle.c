@@ -15,8 +15,9 @@
  *   src/Ewald_summation.f90 PER_ROTNE_PRAGER_SELF 19-191,
  *                           PER_ROTNE_PRAGER_IJ 196-423, helpers 427-1257
  *   src/per_GRPY_YZD.f90    PER_GRPERY_INV_FRI 13-200
- *   src/GRPY_YZD.f90        YAMAKAWA_*_IJ 326-786, overlap_Yamakawa_
- *                           CORRECTION_IJ 789-811 (correction method 1)
+ *   src/GRPY_YZD.f90        YAMAKAWA_*_IJ 326-786, overlap_*_CORRECTION_IJ
+ *                           789-836 (correction methods 1 and 2)
+ *   src/Regularization.f90  Regular_ROTNE_PRAGER_IJ 18-162, helpers 169-778
  *   src/stokesian_Green.f90 ROTNE_PRAGER_IJ_FTS 11-109
  *   src/tensors.f90         CALC_RR ... CALC_t4D2 182-440 (Yamakawa tensors)
  *   src/hydro_lub.f90       lubmxcalc 22-308, lubcalc 310-398,
@@ -955,17 +956,120 @@ void rsdo_rotne_prager_ij_fts(const double R[3], double aaI, double aaJ, double 
   per_rotne_prager_ij_v(&fl, R, aaI, aaJ, 0, 1, TTP, RRP, TRP, QQP_TR, GPQ_TR, HPQ_TR);
 }
 
-/* overlap_Yamakawa_CORRECTION_IJ (method 1), src/GRPY_YZD.f90:789-811:
- * Yamakawa's overlapping-sphere blocks minus the free-space pair.  Method 2
- * (overlap_Regular_CORRECTION_IJ, 813-836, Regularization.f90) is not
- * restated: returns -1 for it, 0 otherwise. */
+/* The regularized potential of src/Regularization.f90, Phi'(r) = erf(kapa r):
+ * Init_E_def / Init_erf1..5 (400-472, erf1..erf5 the derivatives of
+ * erf(kapa r)), Init_DD_phir ... Init_DDD4_phir (552-778), into the
+ * derivative tensors that the J chain (Init_Jr ... Init_DD2_Kr, 169-392,
+ * the same steps as Ewald_summation.f90's) takes. */
+static void rphi_tensors(double kapa, const double *rn, double r, rerfc_t *o) {
+  const double rlam2 = r * r * kapa * kapa, rlam4 = rlam2 * rlam2;
+  const double E_def = 2.0 * PIP5 * kapa * exp(-rlam2);
+  const double f0 = erf(kapa * r), erf1 = E_def, erf2 = -2.0 * kapa * kapa * r * E_def;
+  const double erf3 = 2.0 * kapa * kapa * E_def * (2.0 * rlam2 - 1.0);
+  const double erf4 = -4.0 * kapa * kapa * kapa * kapa * r * E_def * (2.0 * rlam2 - 3.0);
+  const double erf5 = 4.0 * kapa * kapa * kapa * kapa * E_def * (4.0 * rlam4 - 12.0 * rlam2 + 3.0);
+  const double r2 = r * r, r3 = r2 * r, r4 = r2 * r2, r5 = r3 * r2, r6 = r5 * r, r7 = r6 * r, r8 = r7 * r,
+               r9 = r8 * r;
+  double kl[27], rl[27], klm[81], rlm[81];
+  init_kijl(rn, kl);
+  init_rijl(rn, rl);
+  init_kijlm(rn, klm);
+  init_rijlm(rn, rlm);
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++)
+      o->DD[I2(i, j)] = (KD[I2(i, j)] / r - rn[i] * rn[j] / r3) * f0 + rn[i] * rn[j] / r2 * erf1;
+  o->D2 = 2.0 / r * f0 + erf1;
+  o->D4 = 4.0 / r * erf2 + erf3;
+  for (int l = 0; l < 3; l++) {
+    o->DD2[l] = -2.0 * rn[l] / r3 * f0 + 2.0 * rn[l] / r2 * erf1 + rn[l] / r * erf2;
+    o->DD4[l] = -4.0 * rn[l] / r3 * erf2 + 4.0 * rn[l] / r2 * erf3 + rn[l] / r * erf4;
+  }
+  for (int m = 0; m < 3; m++)
+    for (int l = 0; l < 3; l++) {
+      const double kd = KD[I2(l, m)], rr = rn[l] * rn[m];
+      o->DDD2[I2(l, m)] = (-2.0 * kd / r3 + 6.0 * rr / r5) * f0 + (2.0 * kd / r2 - 6.0 * rr / r4) * erf1 +
+                          (kd / r + rr / r3) * erf2 + rr / r2 * erf3;
+      o->DDD4[I2(l, m)] = (-4.0 * kd / r3 + 12.0 * rr / r5) * erf2 + (4.0 * kd / r2 - 12.0 * rr / r4) * erf3 +
+                          (kd / r + 3.0 * rr / r3) * erf4 + rr / r2 * erf5;
+    }
+  for (int q = 0; q < 27; q++) {
+    const double k = kl[q], rr = rl[q];
+    o->DDD[q] = (-k / r3 + 3.0 * rr / r5) * f0 + (k / r2 - 3.0 * rr / r4) * erf1 + rr / r3 * erf2;
+    o->DDDD2[q] = (6.0 * k / r5 - 30.0 * rr / r7) * f0 + (-6.0 * k / r4 + 30.0 * rr / r6) * erf1 +
+                  (k / r3 - 9.0 * rr / r5) * erf2 + (k / r2 - rr / r4) * erf3 + rr / r3 * erf4;
+  }
+  for (int q = 0; q < 81; q++) {
+    const double ii = IIISO[q], k = klm[q], rr = rlm[q];
+    o->DDDD[q] = (-ii / r3 + 3.0 * k / r5 - 15.0 * rr / r7) * f0 + (ii / r2 - 3.0 * k / r4 + 15.0 * rr / r6) * erf1 +
+                 (k / r3 - 6.0 * rr / r5) * erf2 + rr / r4 * erf3;
+    o->DDDDD2[q] = (6.0 * ii / r5 - 30.0 * k / r7 + 210.0 * rr / r9) * f0 +
+                   (-6.0 * ii / r4 + 30.0 * k / r6 - 210.0 * rr / r8) * erf1 +
+                   (ii / r3 - 9.0 * k / r5 + 75.0 * rr / r7) * erf2 + (ii / r2 - k / r4 - 5.0 * rr / r6) * erf3 +
+                   (k / r3 - 4.0 * rr / r5) * erf4 + rr / r4 * erf5;
+  }
+}
+
+/* Regular_ROTNE_PRAGER_IJ, src/Regularization.f90:18-162: the pair blocks
+ * of the regularized Green's function with kapa = sqrt(pi)/3/|a_I + a_J -
+ * r| (78), one image, the block formulas of PER_ROTNE_PRAGER_IJ's real sum
+ * without the volume-fraction factor. */
+void rsdo_regular_rotne_prager_ij(const double R[3], double aaI, double aaJ, double TTP[9], double RRP[9],
+                                  double TRP[9], double QQP_TR[25], double GPQ_TR[15], double HPQ_TR[15]) {
+  init_tensors();
+  const double nondim_a = 1.0 / (6.0 * aaI), nondim_a3 = 1.0 / (6.0 * aaI * aaI * aaI);
+  const double dist = sqrt(R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
+  const double kapa = sqrt(PAI) / 3.0 / fabs((aaI + aaJ) - dist);
+  rerfc_t t;
+  jchain_t c;
+  rphi_tensors(kapa, R, dist, &t);
+  j_chain(&t, 1, &c);
+  double QQP[81], GPQ[27], HPQ[27], RRPAA[9] = {0}, HPQAA[27] = {0};
+  for (int q = 0; q < 9; q++)
+    TTP[q] = (0.75 * aaI * c.Jr[q] + 0.75 * aaI * (aaI * aaI + aaJ * aaJ) / 6.0 * c.D2_Jr[q]) * nondim_a;
+  for (int k = 0; k < 3; k++)
+    for (int l = 0; l < 3; l++)
+      for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 3; i++) RRPAA[I2(i, j)] = RRPAA[I2(i, j)] + EPS[I3(i, k, l)] * c.D_Ror[I3(l, j, k)];
+  for (int q = 0; q < 9; q++) RRP[q] = 3.0 * aaI * aaI * aaI / 8.0 * RRPAA[q] * nondim_a3;
+  for (int l = 0; l < 3; l++)
+    for (int k = 0; k < 3; k++)
+      for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 3; i++) {
+          const double QQPAA = 0.5 * (c.D_Kr[I4(i, k, l, j)] + c.D_Kr[I4(j, k, l, i)]);
+          const double QQPAB = 0.5 * (c.DD2_Kr[I4(i, k, l, j)] + c.DD2_Kr[I4(j, k, l, i)]);
+          QQP[I4(i, j, k, l)] = (-3.0 / 4.0 * aaI * aaI * aaI * QQPAA -
+                                 3.0 / 40.0 * aaI * aaI * aaI * (aaI * aaI + aaJ * aaJ) * QQPAB) * nondim_a3;
+        }
+  for (int q = 0; q < 27; q++)
+    GPQ[q] = -0.75 * aaI * (c.Kr[q] + (aaI * aaI / 6.0 + 0.1 * aaJ * aaJ) * c.D2_Kr[q]) * nondim_a;
+  for (int l = 0; l < 3; l++)
+    for (int m = 0; m < 3; m++)
+      for (int k = 0; k < 3; k++)
+        for (int j = 0; j < 3; j++)
+          for (int i = 0; i < 3; i++)
+            HPQAA[I3(i, j, k)] = HPQAA[I3(i, j, k)] +
+                                 EPS[I3(i, l, m)] * (c.D_Kr[I4(m, j, k, l)] + 0.1 * aaJ * aaJ * c.DD2_Kr[I4(m, j, k, l)]);
+  for (int q = 0; q < 27; q++) HPQ[q] = -3.0 / 8.0 * aaI * aaI * aaI * HPQAA[q] * nondim_a3;
+  for (int q = 0; q < 9; q++) TRP[q] = (aaI * (3.0 / 4.0) * c.Ror[q] + aaI * aaI * aaI / 8.0 * c.D2_Ror[q]) * nondim_a;
+  gh_tr(GPQ_TR, GPQ);
+  gh_tr(HPQ_TR, HPQ);
+  qq_tr(QQP_TR, QQP);
+}
+
+/* overlap_Yamakawa_CORRECTION_IJ (method 1), src/GRPY_YZD.f90:789-811,
+ * and overlap_Regular_CORRECTION_IJ (method 2), 813-836: Yamakawa's
+ * overlapping-sphere blocks, or the regularized ones, minus the free-space
+ * pair.  Returns -1 for another method, 0 otherwise. */
 int rsdo_overlap_correction_ij(int method, const double R[3], double aaI, double aaJ, double TTPC[9],
                                double RRPC[9], double TRPC[9], double QQPC_TR[25], double GPQC_TR[15],
                                double HPQC_TR[15]) {
-  if (method != 1) return -1;
+  if (method != 1 && method != 2) return -1;
   double TTY[9], RRY[9], TRY[9], QQY[25], GY[15], HY[15];
   double TT[9], RR[9], TR[9], QQ[25], G[15], H[15];
-  rsdo_yamakawa_ij(R, aaI, aaJ, TTY, RRY, TRY, QQY, GY, HY);
+  if (method == 1)
+    rsdo_yamakawa_ij(R, aaI, aaJ, TTY, RRY, TRY, QQY, GY, HY);
+  else
+    rsdo_regular_rotne_prager_ij(R, aaI, aaJ, TTY, RRY, TRY, QQY, GY, HY);
   rsdo_rotne_prager_ij_fts(R, aaI, aaJ, TT, RR, TR, QQ, G, H);
   for (int q = 0; q < 9; q++) {
     TTPC[q] = TTY[q] - TT[q];
@@ -1008,9 +1112,9 @@ static void scatter_pair(double *G, long n11, int NN, int al, int be, const doub
  * grand mobility grmobmx (11N x 11N, column-major) already divided by
  * (pi mu_f); APP/APQ/AQQ are its blocks.  lat must hold LR, LI, LV; the
  * routine fills lammda, NR, NI, phi exactly as CALC_LATTICE_INVERSE does.
- * correction_method = 1 adds the Yamakawa correction to overlapping pairs;
- * another nonzero method with an overlapping pair returns the count of
- * such pairs (positive) without applying a correction. */
+ * correction_method 1 (Yamakawa) or 2 (regularized) adds its correction to
+ * overlapping pairs; another nonzero method with an overlapping pair
+ * returns the count of such pairs (positive) without applying one. */
 int rsdo_per_grpery_inv_fri(int NN, const double *p_pos, const double *radii, rsdo_lattice *lat, double ews_err,
                             double mu_f, int correction_method, double *grmobmx) {
   init_tensors();

@@ -3,9 +3,10 @@
     python regularized-stokesian-dynamics_gb300/build.py [--force]
 
 Each translation unit in csrc/ is compiled by its own nvcc process (in
-parallel), then linked with -shared.  The generated header ewald_gen.cuh is
-committed; it is regenerated from gen_ewald.py only when sympy is importable
-and the generator is newer than the header.
+parallel), then linked with -shared.  The generated headers ewald_gen.cuh and
+overlap_gen.cuh are committed; each is regenerated from its generator
+(gen_ewald.py, gen_overlap.py) only when sympy is importable and the
+generator is newer than the header.
 """
 import os
 import subprocess
@@ -28,18 +29,23 @@ def nvcc():
     return "nvcc"
 
 
+GENERATED = [("gen_ewald.py", "ewald_gen.cuh"), ("gen_overlap.py", "overlap_gen.cuh")]
+
+
 def _maybe_regenerate():
-    gen = os.path.join(CSRC, "gen_ewald.py")
-    hdr = os.path.join(CSRC, "ewald_gen.cuh")
-    if os.path.exists(hdr) and os.path.getmtime(hdr) >= os.path.getmtime(gen):
-        return
-    try:
-        import sympy  # noqa: F401
-    except ImportError:
-        if not os.path.exists(hdr):
-            raise RuntimeError("ewald_gen.cuh is missing and sympy is not available to generate it")
-        return
-    subprocess.check_call([sys.executable, gen])
+    for gen_name, hdr_name in GENERATED:
+        gen = os.path.join(CSRC, gen_name)
+        hdr = os.path.join(CSRC, hdr_name)
+        deps = [gen] + ([os.path.join(CSRC, "gen_ewald.py")] if gen_name != "gen_ewald.py" else [])
+        if os.path.exists(hdr) and os.path.getmtime(hdr) >= max(os.path.getmtime(d) for d in deps):
+            continue
+        try:
+            import sympy  # noqa: F401
+        except ImportError:
+            if not os.path.exists(hdr):
+                raise RuntimeError("%s is missing and sympy is not available to generate it" % hdr_name)
+            continue
+        subprocess.check_call([sys.executable, gen])
 
 
 def _deps_mtime():

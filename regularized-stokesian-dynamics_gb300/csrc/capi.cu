@@ -363,18 +363,12 @@ extern "C" int rsd_per_grpery_inv_fri_dev(rsd_ctx* ctx, int32_t nn, const double
   if (correction_method < 0 || correction_method > 2)
     return rsd_fail(ctx, RSD_EARG, "correction_method=%d: 0 (none), 1 (Yamakawa) or 2 (regularized)", correction_method);
   RSD_TRY(rsd_calc_lattice_inverse(lat, ews_err, nn, radii.data()));
-  // overlap corrections, per_GRPY_YZD.f90:98-116: method 1 (Yamakawa) is
-  // added after the Ewald sums; method 2 (regularized Green's function) is
-  // not built
+  // overlap corrections, per_GRPY_YZD.f90:98-116: method 1 (Yamakawa) or 2
+  // (regularized Green's function), added after the Ewald sums
   int nov = 0;
-  if (correction_method != 0) {
-    RSD_TRY(rsd_count_overlaps(ctx, nn, d_pos, d_radii, lat, &nov));
-    if (nov > 0 && correction_method == 2)
-      return rsd_fail(ctx, RSD_EUNSUP, "%d overlapping pairs and correction_method=2: the regularized correction is "
-                      "not built", nov);
-  }
+  if (correction_method != 0) RSD_TRY(rsd_count_overlaps(ctx, nn, d_pos, d_radii, lat, &nov));
   RSD_TRY(rsd_ewald_assemble(ctx, nn, d_pos, d_radii, lat, mu_f, RSD_PREC_FP64, d_M, ldm));
-  return rsd_overlap_correct(ctx, nn, d_pos, d_radii, lat, mu_f, nov, d_M, ldm);
+  return rsd_overlap_correct(ctx, correction_method, nn, d_pos, d_radii, lat, mu_f, nov, d_M, ldm);
 }
 
 extern "C" int rsd_per_grpery_inv_fri(rsd_ctx* ctx, int32_t nn, const double* p_pos, const double* radii,

@@ -1227,13 +1227,13 @@ __global__ void overlap_list(int nn, rsd_lat_dev L, const double* __restrict__ p
   }
 }
 
-// Overlap correction (correction_method 1) of the listed pairs, one thread
+// Overlap correction (correction_method 1 or 2) of the listed pairs, one thread
 // per pair, added to the assembled blocks at the minimum image: the blocks
 // of different pairs are disjoint, so the sum does not depend on the order
 // of the list.
 template <typename S>
-__global__ void __launch_bounds__(64) overlap_correct(int npair, const int2* __restrict__ list, int nn, rsd_lat_dev L,
-                                                       const double* __restrict__ pos,
+__global__ void __launch_bounds__(64) overlap_correct(int method, int npair, const int2* __restrict__ list, int nn,
+                                                       rsd_lat_dev L, const double* __restrict__ pos,
                                                        const double* __restrict__ radii, double inv_pimu, S sk) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= npair) return;
@@ -1242,15 +1242,15 @@ __global__ void __launch_bounds__(64) overlap_correct(int npair, const int2* __r
   double d;
   rsd_skew_correction(L.LR, L.LI, R, &d);
   double v[60];
-  rsd_overlap_correction60(R, radii[a], radii[b], v);
+  rsd_overlap_correction60(method, R, radii[a], radii[b], v);
   for (int k = 0; k < 60; k++) v[k] *= inv_pimu;
   store_pair_d(sk, nn, a, b, v, 1);
 }
 
 }  // namespace
 
-int rsd_overlap_correct(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
-                        double mu_f, int npair, double* d_M, int64_t ldm) {
+int rsd_overlap_correct(rsd_ctx* ctx, int method, int nn, const double* d_pos, const double* d_radii,
+                        const rsd_lattice* lat, double mu_f, int npair, double* d_M, int64_t ldm) {
   if (npair <= 0) return RSD_OK;
   const rsd_lat_dev L = rsd_lat_pack(lat);
   int* cnt = (int*)rsd_scratch(ctx, "overlap_count", sizeof(int));
@@ -1260,7 +1260,7 @@ int rsd_overlap_correct(rsd_ctx* ctx, int nn, const double* d_pos, const double*
   dim3 blk(32, 4), grd((nn + 31) / 32, (nn + 3) / 4);
   overlap_list<<<grd, blk, 0, ctx->stream>>>(nn, L, d_pos, d_radii, npair, list, cnt); RSD_LAUNCH_NOTE();
   const DenseSink dsk{d_M, ldm};
-  overlap_correct<DenseSink><<<(npair + 63) / 64, 64, 0, ctx->stream>>>(npair, list, nn, L, d_pos, d_radii,
+  overlap_correct<DenseSink><<<(npair + 63) / 64, 64, 0, ctx->stream>>>(method, npair, list, nn, L, d_pos, d_radii,
                                                                        1.0 / (RSD_PI * mu_f), dsk); RSD_LAUNCH_NOTE();
   RSD_CUDA(ctx, cudaGetLastError());
   return RSD_OK;

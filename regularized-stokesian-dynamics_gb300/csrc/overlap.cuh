@@ -1,9 +1,10 @@
-// Overlap correction of the grand mobility, correction_method 1 of
-// per_GRPY_YZD.f90:98-116: for a pair whose minimum image overlaps or
-// touches (r <= a_i + a_j), Yamakawa's overlapping-sphere pair blocks
-// (GRPY_YZD.f90:326-786) minus the free-space pair (stokesian_Green.f90:
-// 11-109) are added to the Ewald-summed blocks (overlap_Yamakawa_
-// CORRECTION_IJ, GRPY_YZD.f90:789-811).
+// Overlap corrections of the grand mobility, per_GRPY_YZD.f90:98-116: for a
+// pair whose minimum image overlaps or touches (r <= a_i + a_j), method 1
+// adds Yamakawa's overlapping-sphere pair blocks (GRPY_YZD.f90:326-786) and
+// method 2 the regularized pair blocks (Regularization.f90:18-162, generated
+// in overlap_gen.cuh), each minus the free-space pair (stokesian_Green.f90:
+// 11-109) (overlap_Yamakawa_CORRECTION_IJ and overlap_Regular_CORRECTION_IJ,
+// GRPY_YZD.f90:789-836).
 //
 // rsd_overlap_correction60 returns the correction as the 60 values of a
 // pair in the order of the pair kernels (TT 0-5 and RR 6-11 as the upper
@@ -24,6 +25,7 @@
 // also compiles for the host, where the unit test defines __device__ away.
 #pragma once
 #include "ewald_gen.cuh"
+#include "overlap_gen.cuh"
 
 namespace rsd_overlap {
 
@@ -197,14 +199,35 @@ __device__ inline void free_space60(const double R[3], double ai, double aj, con
   add_gh(Y, [&](int c, int i, int j) { return eps_x(c, i, R) * R[j]; }, wh, v + 45);
 }
 
+// The regularized pair blocks of Regular_ROTNE_PRAGER_IJ as 60 values, with
+// kap = sqrt(pi) / 3 / |a_i + a_j - r| (Regularization.f90:78); at exact
+// contact kap is infinite and the blocks are NaN, as in the reference.
+__device__ inline void regular60(const double R[3], double ai, double aj, double* v) {
+  const double r = sqrt(R[0] * R[0] + R[1] * R[1] + R[2] * R[2]), ir = 1.0 / r;
+  const double kap = 1.77245385090551602730 / 3.0 / fabs((ai + aj) - r);
+  const double Ed = 2.0 * 0.56418958354775628695 * kap * exp(-kap * kap * r * r);
+  double acc[RSD_NMOM_REG];
+  rsd_reg_image<double>(R[0], R[1], R[2], r, ir, erf(kap * r), Ed, kap, acc);
+  rsd_reg_epilogue<double>(acc, ai, aj, v);
+  const double na = 1.0 / (6.0 * ai), na3 = 1.0 / (6.0 * ai * ai * ai);
+  for (int q = 0; q < 60; q++) {
+    const bool a3 = (q >= 6 && q < 12) || (q >= 15 && q < 30) || q >= 45;
+    v[q] *= a3 ? na3 : na;
+  }
+}
+
 }  // namespace rsd_overlap
 
-// The correction of overlap_Yamakawa_CORRECTION_IJ as 60 values; R is the
+// The correction of overlap_Yamakawa_CORRECTION_IJ (method 1) or
+// overlap_Regular_CORRECTION_IJ (method 2) as 60 values; R is the
 // minimum-image separation x_i - x_j with 0 < |R| <= a_i + a_j.
-__device__ inline void rsd_overlap_correction60(const double R[3], double ai, double aj, double v[60]) {
+__device__ inline void rsd_overlap_correction60(int method, const double R[3], double ai, double aj, double v[60]) {
   double Y[45], f[60];
   rsd_overlap::y2_basis(Y);
-  rsd_overlap::yamakawa60(R, ai, aj, Y, v);
+  if (method == 1)
+    rsd_overlap::yamakawa60(R, ai, aj, Y, v);
+  else
+    rsd_overlap::regular60(R, ai, aj, v);
   rsd_overlap::free_space60(R, ai, aj, Y, f);
   for (int q = 0; q < 60; q++) v[q] -= f[q];
 }

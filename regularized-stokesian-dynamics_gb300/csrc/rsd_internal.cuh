@@ -150,11 +150,11 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
 int rsd_mirror_planes(rsd_ctx* ctx, int nn, double* d_M, int64_t ldm);
 int rsd_count_overlaps(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
                        int* count);
-// Adds the overlap correction of correction_method 1 (GRPY_YZD.f90:789-811)
-// to the FP64 grand mobility for the npair overlapping pairs that
+// Adds the overlap correction of correction_method 1 or 2 (GRPY_YZD.f90:
+// 789-836) to the FP64 grand mobility for the npair overlapping pairs that
 // rsd_count_overlaps counted.
-int rsd_overlap_correct(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
-                        double mu_f, int npair, double* d_M, int64_t ldm);
+int rsd_overlap_correct(rsd_ctx* ctx, int method, int nn, const double* d_pos, const double* d_radii,
+                        const rsd_lattice* lat, double mu_f, int npair, double* d_M, int64_t ldm);
 // Lubrication (lub.cu)
 int rsd_lub_assemble(rsd_ctx* ctx, const rsd_lubtab* tab, int nn, int nb, int is_period, const double* d_pos,
                      const double* d_radii, const rsd_lattice* lat, double mu_f, double* d_L, int64_t ldl,

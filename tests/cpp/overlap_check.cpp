@@ -1,16 +1,24 @@
-// Host build of the overlap correction of the grand mobility (overlap.cuh,
-// the device code of correction_method 1) for tests/test_overlap.py, which
-// compares it with the oracle's restatement of GRPY_YZD.f90.
+// Host build of the overlap corrections of the grand mobility (overlap.cuh,
+// the device code of correction_method 1 and 2) for tests/test_overlap.py,
+// which compares it with the oracle's restatement of GRPY_YZD.f90 and
+// Regularization.f90.
 #include <cmath>
 #define __device__
 #define __host__
 #define __forceinline__ inline
+using std::erf;
+using std::exp;
+using std::fabs;
 using std::fma;
 using std::sqrt;
 #include "overlap.cuh"
 
-extern "C" void ovl_correction60(const double R[3], double ai, double aj, double out[60]) {
-  rsd_overlap_correction60(R, ai, aj, out);
+extern "C" void ovl_correction60(int method, const double R[3], double ai, double aj, double out[60]) {
+  rsd_overlap_correction60(method, R, ai, aj, out);
+}
+
+extern "C" void ovl_regular60(const double R[3], double ai, double aj, double out[60]) {
+  rsd_overlap::regular60(R, ai, aj, out);
 }
 
 extern "C" void ovl_yamakawa60(const double R[3], double ai, double aj, double out[60]) {

@@ -95,12 +95,13 @@ def test_grand_mobility_unequal_radii(rsd, ctx):
         assert np.abs(a - b).max() <= 1e-12 * np.abs(G).max()
 
 
-@pytest.mark.parametrize("T", [0.0, 0.37])
-def test_overlap_correction_matches_oracle(rsd, ctx, T):
-    """correction_method 1 (Yamakawa, per_GRPY_YZD.f90:98-116) on pairs whose
-    minimum image overlaps: a partial overlap of unequal spheres, a small
-    sphere inside a larger one, and a pair that overlaps only across the
-    periodic boundary; against the oracle to 1e-12 of the largest entry."""
+@pytest.mark.parametrize("method,T", [(1, 0.0), (1, 0.37), (2, 0.0), (2, 0.37)])
+def test_overlap_correction_matches_oracle(rsd, ctx, method, T):
+    """correction_method 1 (Yamakawa) and 2 (regularized), per_GRPY_YZD.f90:
+    98-116, on pairs whose minimum image overlaps: a partial overlap of
+    unequal spheres, a small sphere inside a larger one, and a pair that
+    overlaps only across the periodic boundary; against the oracle to 1e-12
+    of the largest entry."""
     N, L = 10, 9.0
     rng = np.random.default_rng(20261210)
     pos = rsd.configs.packing(N, 0.05, 0.5, seed=20260211)[0] * (L / rsd.configs.box_edge(N, 0.05))
@@ -112,8 +113,9 @@ def test_overlap_correction_matches_oracle(rsd, ctx, T):
     pos[5] = np.array([L - 0.9, 4.2, 4.1])
     pos = np.mod(pos, L)
     lat_g = rsd.SET_LATTICE_SKEW(T, [L, L, L], 1.0)
-    APP, APQ, AQQ = rsd.PER_GRPERY_INV_FRI(ctx, pos, radii, lat_g, 1e-10, MU, correction_method=1)
-    G, nov = o.per_grpery_inv_fri(pos, radii, o.set_lattice_skew(T, [L, L, L], 1.0), 1e-10, MU, correction_method=1)
+    APP, APQ, AQQ = rsd.PER_GRPERY_INV_FRI(ctx, pos, radii, lat_g, 1e-10, MU, correction_method=method)
+    G, nov = o.per_grpery_inv_fri(pos, radii, o.set_lattice_skew(T, [L, L, L], 1.0), 1e-10, MU,
+                                  correction_method=method)
     G0, _ = o.per_grpery_inv_fri(pos, radii, o.set_lattice_skew(T, [L, L, L], 1.0), 1e-10, MU)
     assert nov == 0
     scale = np.abs(G).max()
@@ -266,9 +268,6 @@ def test_errors_are_reported_not_faulted(rsd, ctx):
     assert e.value.code == rsd.RSD_ENAN
     over = pos.copy()
     over[1] = over[0] + np.array([1.5, 0, 0])
-    with pytest.raises(rsd.RSDError) as e:
-        rsd.PER_GRPERY_INV_FRI(ctx, over, radii, lat, 1e-10, MU, correction_method=2)
-    assert e.value.code == rsd.RSD_EUNSUP
     with pytest.raises(rsd.RSDError) as e:
         rsd.PER_GRPERY_INV_FRI(ctx, over, radii, lat, 1e-10, MU, correction_method=3)
     assert e.value.code == rsd.RSD_EARG

@@ -1,8 +1,11 @@
-"""Overlap correction of the grand mobility, correction_method 1
-(per_GRPY_YZD.f90:98-116, overlap_Yamakawa_CORRECTION_IJ GRPY_YZD.f90:
-789-811): the oracle's restatement checked by limits of the formulas, and
-the device code (csrc/overlap.cuh, built for the host with g++) checked
-against the oracle.  No GPU needed.
+"""Overlap corrections of the grand mobility (per_GRPY_YZD.f90:98-116):
+method 1, overlap_Yamakawa_CORRECTION_IJ (GRPY_YZD.f90:789-811), and method
+2, overlap_Regular_CORRECTION_IJ (813-836, Regularization.f90).  The
+oracle's restatements are checked by limits of the formulas, and the device
+code (csrc/overlap.cuh with the generated csrc/overlap_gen.cuh, built for
+the host with g++) against the oracle.  No GPU needed.  (gen_overlap.py
+itself checks the regularized potential's derivative tensors against
+sympy's derivatives when it generates the header.)
 
 Two properties of the reference's formulas, asserted here as they are:
   - stokesian_Green.f90's free-space pair (ROTNE_PRAGER_IJ_FTS) differs
@@ -47,9 +50,12 @@ def d(a):
     return np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
-def call60(fn, R, ai, aj):
+def call60(fn, R, ai, aj, method=None):
     out = np.zeros(60)
-    fn(d(R), ctypes.c_double(ai), ctypes.c_double(aj), d(out))
+    if method is None:
+        fn(d(R), ctypes.c_double(ai), ctypes.c_double(aj), d(out))
+    else:
+        fn(ctypes.c_int(method), d(R), ctypes.c_double(ai), ctypes.c_double(aj), d(out))
     return unpack(out)
 
 
@@ -104,7 +110,39 @@ def test_free_space_pair_of_the_green_chain():
 
 
 @pytest.mark.parametrize("ai,aj", RADII)
-def test_device_correction_matches_oracle(ovl, ai, aj):
+def test_regular_pair_tends_to_free_space_at_contact(ai, aj):
+    """kapa = sqrt(pi)/3/|a_I + a_J - r| grows without bound at contact,
+    where the regularized pair becomes the unscreened (Ewald-chain) one."""
+    rng = np.random.default_rng(14)
+    lat = free_space_lattice()
+    for f in (1 - 1e-3, 1 - 1e-6):
+        R = unit(rng) * (ai + aj) * f
+        Rg = o.regular_rotne_prager_ij(R, ai, aj)
+        F = o.per_rotne_prager_ij(lat, R, ai, aj, include_k=False)
+        for name, g, fr in zip(NAMES, Rg, F):
+            assert np.abs(g - fr).max() <= 1e-13 * np.abs(fr).max(), name
+
+
+@pytest.mark.parametrize("ai,aj", RADII)
+def test_device_regular_pair_matches_oracle(ovl, ai, aj):
+    """The generated regularized pair (overlap_gen.cuh) against the oracle's
+    restatement of Regular_ROTNE_PRAGER_IJ, where erf(kapa r) and its
+    derivatives matter (kapa r of order 1).  The blocks come out of
+    cancelling terms of the size of the unscreened pair at the same
+    separation, so the bound, 1e-12, is relative to that pair."""
+    rng = np.random.default_rng(int(100 * ai + 10 * aj) + 1)
+    for sep in list(rng.uniform(0.05, 0.95, 30) * (ai + aj)):
+        R = unit(rng) * sep
+        ref = o.regular_rotne_prager_ij(R, ai, aj)
+        got = call60(ovl.ovl_regular60, R, ai, aj)
+        fs = o.rotne_prager_ij_fts(R, ai, aj)
+        for name, a, b, f in zip(NAMES, ref, got, fs):
+            assert np.abs(a - b).max() <= 1e-12 * max(np.abs(a).max(), np.abs(f).max()), (name, sep)
+
+
+@pytest.mark.parametrize("method", [1, 2])
+@pytest.mark.parametrize("ai,aj", RADII)
+def test_device_correction_matches_oracle(ovl, ai, aj, method):
     """overlap.cuh (Yamakawa forms, the generated image at lambda = 0 plus
     the closed-form sign term) against the oracle's Fortran-order
     restatement, over overlapping and fully-inside separations.  The
@@ -114,12 +152,14 @@ def test_device_correction_matches_oracle(ovl, ai, aj):
     ~7e-13 of that scale on its diagonal, which the 60-value form holds as
     exact zeros)."""
     rng = np.random.default_rng(int(100 * ai + 10 * aj))
-    seps = list(rng.uniform(0.02, 1.0, 40) * (ai + aj)) + [ai + aj, abs(ai - aj) * 0.5 + 0.01]
+    seps = list(rng.uniform(0.02, 0.999, 40) * (ai + aj)) + [abs(ai - aj) * 0.5 + 0.01]
+    if method == 1:
+        seps.append(ai + aj)  # (method 2 is NaN at exact contact, as in the reference)
     for sep in seps:
         R = unit(rng) * sep
-        ref = o.overlap_correction_ij(1, R, ai, aj)
-        got = call60(ovl.ovl_correction60, R, ai, aj)
-        yam = o.yamakawa_ij(R, ai, aj)
+        ref = o.overlap_correction_ij(method, R, ai, aj)
+        got = call60(ovl.ovl_correction60, R, ai, aj, method)
+        yam = o.yamakawa_ij(R, ai, aj) if method == 1 else o.regular_rotne_prager_ij(R, ai, aj)
         fs = o.rotne_prager_ij_fts(R, ai, aj)
         for name, a, b, y, f in zip(NAMES, ref, got, yam, fs):
             scale = max(np.abs(y).max(), np.abs(f).max(), 1e-300)
@@ -137,18 +177,19 @@ def test_device_free_space_matches_green_chain(ovl):
                 assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max(), name
 
 
-def test_oracle_assembly_applies_method_1():
-    """PER_GRPERY_INV_FRI with correction_method 1: the overlapping pair's
-    blocks move by the correction / (pi mu_f), the others stay; method 2 is
-    not restated and only counts the overlapping pairs."""
+@pytest.mark.parametrize("method", [1, 2])
+def test_oracle_assembly_applies_the_correction(method):
+    """PER_GRPERY_INV_FRI with correction_method 1 or 2: the overlapping
+    pair's blocks move by the correction / (pi mu_f), the others stay; an
+    unknown method only counts the overlapping pairs."""
     L, mu = 10.0, o.mu_f_dimensionless(1.0)
     pos = np.array([[1.0, 1.0, 1.0], [2.2, 1.5, 0.6], [6.0, 6.5, 5.0]])
     radii = np.array([1.0, 0.8, 1.0])
     out = {}
-    for cm in (0, 1, 2):
+    for cm in (0, method, 3):
         lat = o.set_lattice_skew(0.0, [L, L, L], 1.0)
         out[cm] = o.per_grpery_inv_fri(pos, radii, lat, 1e-10, mu, correction_method=cm)
-    (G0, n0), (G1, n1), (G2, n2) = out[0], out[1], out[2]
+    (G0, n0), (G1, n1), (G2, n2) = out[0], out[method], out[3]
     assert n0 == 0 and n1 == 0 and n2 == 1
     assert np.array_equal(G0, G2)
     N = 3
@@ -161,7 +202,7 @@ def test_oracle_assembly_applies_method_1():
         mask[np.ix_(rows(a), rows(b))] = True
     assert np.all(diff[~mask] == 0)
     R = pos[0] - pos[1]
-    TT, RR, TR, QQ, Gb, Hb = o.overlap_correction_ij(1, R, radii[0], radii[1])
+    TT, RR, TR, QQ, Gb, Hb = o.overlap_correction_ij(method, R, radii[0], radii[1])
     s = np.pi * mu
     assert np.allclose(diff[np.ix_(rows(0)[:3], rows(1)[:3])], TT / s, rtol=0, atol=1e-14)
     assert np.allclose(diff[np.ix_(rows(0)[6:], rows(1)[6:])], QQ / s, rtol=0, atol=1e-14)
