@@ -122,10 +122,10 @@ int rsd_calc_lattice_inverse(rsd_lattice* lat, double ews_err, int32_t nn, const
  * leaves its results in *lat.  correction_method (per_GRPY_YZD.f90:98-116)
  * acts on pairs whose minimum image overlaps or touches (r <= a_i + a_j):
  * 0 none; 1 adds Yamakawa's overlapping-sphere blocks minus the free-space
- * pair (overlap_Yamakawa_CORRECTION_IJ, GRPY_YZD.f90:789-811); 2 (the
- * regularized correction, GRPY_YZD.f90:813-836) is not built and returns
- * RSD_EUNSUP when a pair overlaps (ignored without one, like the
- * reference); other values return RSD_EARG. */
+ * pair (overlap_Yamakawa_CORRECTION_IJ, GRPY_YZD.f90:789-811); 2 adds the
+ * regularized pair blocks of Regularization.f90 minus the free-space pair
+ * (overlap_Regular_CORRECTION_IJ, 813-836; NaN for a pair at exact contact,
+ * as in the reference); other values return RSD_EARG. */
 int rsd_per_grpery_inv_fri(rsd_ctx* ctx, int32_t nn, const double* p_pos, const double* radii, rsd_lattice* lat,
                            double ews_err, double mu_f, int32_t correction_method, double* APP, double* APQ,
                            double* AQQ);
