@@ -206,6 +206,20 @@ int rsd_stepper_nogmres(rsd_ctx* ctx, int32_t nn, const double* APP, const doubl
                         const double* Fe_inter, const double* conf, const double* u_brown, double* U_par,
                         double* SijN_hyd, double* SijN_FP, double* SijN_B, double* RPP, int32_t* info);
 
+/* hydro_SD_FTS (src/stepper.f90:476-546), the FTS solve of the GMRES
+ * variant (useGMRESmethod).  The reference alternates two GMRES(2) solves,
+ * a mobility one and a lubrication one, until the FTS residual is below
+ * LINERR 1e-2; its inner tolerance (1e-12 relative) can hold the residual
+ * above that, after which it returns the last velocity iterate and leaves
+ * SijN unassigned.  This returns the solution that the iteration
+ * approaches, solved directly: U_par = RPP^-1 (Fe + RPQ EIN) and
+ * SijN = RPQ^T U_par - RQQ EIN (R = MobToResist_FTS(A) + [rfu rfe; . rse]).
+ * info as MATREV's (mobility, then RPP); on info != 0 the outputs are not
+ * written. */
+int rsd_hydro_sd_fts(rsd_ctx* ctx, int32_t nn, const double* APP, const double* APQ, const double* AQQ,
+                     const double* rfu, const double* rfe, const double* rse, const double* Fe, const double* EIN,
+                     double* U_par, double* SijN, int32_t* info);
+
 /* ------------------------------------------------------------ fused step */
 #define RSD_PREC_FP64 0  /* plain: every kernel in FP64 */
 #define RSD_PREC_MIXED 1 /* FP32 bulk + FP64 near terms and refinement */

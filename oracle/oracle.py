@@ -330,6 +330,148 @@ def stepper_nogmres(G, rfu, rfe, rse, Fe, EIN, Fe_inter, conf, u_brown=None):
                 info_m=info_m, info_r=info_r, RPQ=RPQ, RQQ=RQQ)
 
 
+def _grotmat(a, b, real_tol=1e-14):
+    """grotmat (src/tools/gmres_mod.f90:178-201): Givens rotation."""
+    if abs(b) < real_tol:
+        return 1.0, 0.0
+    if abs(b) > abs(a):
+        t = a / b
+        sn = 1.0 / np.sqrt(1.0 + t * t)
+        return t * sn, sn
+    t = b / a
+    cs = 1.0 / np.sqrt(1.0 + t * t)
+    return cs, t * cs
+
+
+def _invtrisup(M, vec):
+    """invtrisup (src/tools/algebra_lin.f90:72-100): upper triangular solve."""
+    n = len(vec)
+    res = np.zeros(n)
+    res[n - 1] = vec[n - 1] / M[n - 1, n - 1]
+    for ii in range(n - 2, -1, -1):
+        res[ii] = vec[ii]
+        for ji in range(ii + 1, n):
+            res[ii] = res[ii] - M[ii, ji] * res[ji]
+        res[ii] = res[ii] / M[ii, ii]
+    return res
+
+
+def gmres(x, b, A, tol, itmax, rst):
+    """gmres (src/tools/gmres_mod.f90:48-175): restarted GMRES(rst) with
+    Givens rotations, relative residual tol; returns (x, iter, res) with
+    iter = -1 when not converged.  A is a dense matrix (matVecProd)."""
+    x = np.array(x, dtype=np.float64)
+    n = len(x)
+    nb2 = np.sqrt(b @ b)
+    if nb2 / n < 1e-8:
+        nb2 = np.sqrt(n)
+    nb2 = 1.0 / nb2
+    r = b - A @ x
+    nr2 = np.sqrt(r @ r)
+    res = nr2 * nb2
+    if res < tol:
+        return x, 0, res
+    V = np.zeros((rst + 1, n))
+    H = np.zeros((rst + 1, rst))
+    cs, sn = np.zeros(rst), np.zeros(rst)
+    for it in range(1, itmax + 1):
+        s = np.zeros(rst + 1)
+        s[0] = nr2
+        V[0] = r / nr2
+        for ii in range(rst):
+            w = A @ V[ii]
+            for kk in range(ii + 1):
+                H[kk, ii] = w @ V[kk]
+                w = w - H[kk, ii] * V[kk]
+            H[ii + 1, ii] = np.sqrt(w @ w)
+            with np.errstate(divide="ignore", invalid="ignore"):  # as the Fortran: no breakdown test
+                V[ii + 1] = w / H[ii + 1, ii]
+            for kk in range(ii):
+                t = cs[kk] * H[kk, ii] + sn[kk] * H[kk + 1, ii]
+                H[kk + 1, ii] = -sn[kk] * H[kk, ii] + cs[kk] * H[kk + 1, ii]
+                H[kk, ii] = t
+            cs[ii], sn[ii] = _grotmat(H[ii, ii], H[ii + 1, ii])
+            t = cs[ii] * s[ii]
+            s[ii + 1] = -sn[ii] * s[ii]
+            s[ii] = t
+            H[ii, ii] = cs[ii] * H[ii, ii] + sn[ii] * H[ii + 1, ii]
+            H[ii + 1, ii] = 0.0
+            res = abs(s[ii + 1]) * nb2
+            if res < tol:
+                y = _invtrisup(H[:ii + 1, :ii + 1], s[:ii + 1])
+                for kk in range(ii + 1):
+                    x = x + V[kk] * y[kk]
+                return x, it, res
+        y = _invtrisup(H[:rst, :rst], s[:rst])
+        for kk in range(rst):
+            x = x + V[kk] * y[kk]
+        r = b - A @ x
+        nr2 = np.sqrt(r @ r)
+        res = nr2 * nb2
+        if res < tol:
+            return x, it, res
+    return x, -1, res
+
+
+def _m_tr_front(APP, APQ, AQQ):
+    """M_Tr_front (src/matrices.f90:166-190): (A_Tr_front, A_Tr_back)."""
+    n6, n5 = APP.shape[0], AQQ.shape[0]
+    F = np.zeros((n6 + n5, n6 + n5))
+    B = np.zeros((n6 + n5, n6 + n5))
+    F[:n6, :n6] = np.eye(n6)
+    F[:n6, n6:] = -APQ
+    F[n6:, n6:] = -AQQ
+    B[n6:, n6:] = -np.eye(n5)
+    B[:n6, :n6] = APP
+    B[n6:, :n6] = APQ.T
+    return F, B
+
+
+def _part_to_whole(APP, APQ, AQQ):
+    """Part_to_Whole (src/matrices.f90:193-203)."""
+    return np.block([[APP, APQ], [APQ.T, AQQ]])
+
+
+def hydro_sd_fts(APP, APQ, AQQ, rfu, rfe, rse, Fe, EIN, linerr=1e-10, trace=None):
+    """hydro_SD_FTS (src/stepper.f90:476-546) with simplegmres
+    (src/tools/gmres_mod_gmres.f90:23-61: GMRES(2), tol = 100 REAL_TOL =
+    1e-12, 200 cycles): up to 50 alternations of a mobility solve and a
+    lubrication solve until the FTS residual norm is below linerr 1e-2.
+    Returns U_Par and SijN as the reference leaves them (SijN None when the
+    loop ends unconverged: the reference does not assign it), the outer
+    iteration count (-1 unconverged) and the last residual norm; trace, if
+    a list, receives every residual norm."""
+    n6 = APP.shape[0]
+    n = n6 + AQQ.shape[0]
+    A = _part_to_whole(APP, APQ, AQQ)
+    gL, gR = _m_tr_front(APP, APQ, AQQ)
+    RlubM = _part_to_whole(rfu, rfe, rse) @ A + np.eye(n)
+    # Whole_to_Part keeps the upper-right block; M_Tr_front uses its transpose
+    RL, RR = _m_tr_front(RlubM[:n6, :n6], RlubM[:n6, n6:], RlubM[n6:, n6:])
+    Fff = np.array(Fe, dtype=np.float64)
+    F1 = np.zeros(n)
+    F2 = np.zeros(n)
+    F1[n6:] = -EIN
+    F2[:n6] = Fe
+    err = np.inf
+    U_Par = None
+    for i in range(1, 51):
+        F1[:n6] = Fff
+        U1, _, _ = gmres(np.zeros(n), gR @ F1, gL, 1e-12, 200, 2)
+        F2[n6:] = U1[n6:]
+        U2, _, _ = gmres(U1.copy(), RL @ F2, RR, 1e-12, 200, 2)
+        Fff = U2[:n6]
+        U_Par = U1[:n6]
+        Sff = U1[n6:]
+        ev = np.concatenate([Fff + rfu @ U_Par + rfe @ (-EIN), APQ.T @ Fff + AQQ @ Sff])
+        err = np.linalg.norm(np.concatenate([Fe, -EIN]) - ev)
+        if trace is not None:
+            trace.append(err)
+        if err < linerr * 1e-2:
+            return dict(U_Par=APP @ Fff + APQ @ (-EIN), SijN=U2[n6:], iters=i, err=err)
+    return dict(U_Par=U_Par, SijN=None, iters=-1, err=err)
+
+
 def average_u(APP, N, mu_f, radii_test=1.0):
     """averageU (src/matrices.f90:230-253)."""
     F = np.zeros(6 * N)

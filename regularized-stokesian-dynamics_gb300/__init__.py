@@ -88,6 +88,7 @@ _sig("rsd_cholesky", _i, [_vp, _i32, _dp, _ip])
 _sig("rsd_mob_to_resist_fts", _i, [_vp, _i32, _dp, _dp, _dp, _dp, _dp, _dp, _ip])
 _sig("rsd_arrangement", _i, [_vp, _i32, _dp, _dp, _dp, _dp, _ip])
 _sig("rsd_stepper_nogmres", _i, [_vp, _i32] + [_dp] * 11 + [_dp] * 5 + [_ip])
+_sig("rsd_hydro_sd_fts", _i, [_vp, _i32] + [_dp] * 8 + [_dp] * 2 + [_ip])
 _sig("rsd_stepper_stokesian", _i, [_vp, _vp, ctypes.POINTER(StepParams), _dp, _dp, _dp, _dp, _dp, _dp,
                                    ctypes.POINTER(StepInfo)])
 _sig("rsd_stepper_stokesian_dev", _i, [_vp, _vp, ctypes.POINTER(StepParams), _vp, _vp, _vp, _vp, _vp, _dp,
@@ -368,6 +369,20 @@ def STEPPER_NOGmres(ctx: Context, APP, APQ, AQQ, rfu, rfe, rse, Fe, EIN, Fe_inte
                                        _p(ub) if ub is not None else None, _p(U_par), _p(Sh), _p(Sfp), _p(Sb),
                                        _p(RPP), ctypes.byref(info)))
     return dict(U_par=U_par, SijN_hyd=Sh, SijN_FP=Sfp, SijN_B=Sb, RPP=RPP, info=info.value)
+
+
+def hydro_SD_FTS(ctx: Context, APP, APQ, AQQ, rfu, rfe, rse, Fe, EIN):
+    """hydro_SD_FTS (src/stepper.f90:476-546), the FTS solve of the GMRES
+    variant (useGMRESmethod): U_par and SijN of the resistance problem that
+    its splitting iteration approaches, solved directly."""
+    N = APP.shape[0] // 6
+    mats = [np.asfortranarray(x, dtype=np.float64) for x in (APP, APQ, AQQ, rfu, rfe, rse)]
+    Fe, EIN = _f64(Fe), _f64(EIN)
+    U_par, SijN = np.empty(6 * N), np.empty(5 * N)
+    info = ctypes.c_int32(0)
+    ctx.check(_lib.rsd_hydro_sd_fts(ctx.h, N, *[_p(m) for m in mats], _p(Fe), _p(EIN), _p(U_par), _p(SijN),
+                                    ctypes.byref(info)))
+    return dict(U_par=U_par, SijN=SijN, info=info.value)
 
 
 # ------------------------------------------------------------------ fused step

@@ -530,14 +530,13 @@ static void ei_trans_y2(const double E[9], double out[5]) {
   }
 }
 
-extern "C" int rsd_stepper_nogmres(rsd_ctx* ctx, int32_t nn, const double* APP, const double* APQ, const double* AQQ,
-                                   const double* rfu, const double* rfe, const double* rse, const double* Fe,
-                                   const double* EIN, const double* Fe_inter, const double* conf,
-                                   const double* u_brown, double* U_par, double* SijN_hyd, double* SijN_FP,
-                                   double* SijN_B, double* RPP, int32_t* info) {
-  if (!ctx || nn < 1 || !APP || !APQ || !AQQ || !rfu || !rfe || !rse || !Fe || !EIN || !Fe_inter || !conf ||
-      !U_par || !SijN_hyd || !SijN_FP || !SijN_B || !RPP || !info)
-    return rsd_fail(ctx, RSD_EARG, "rsd_stepper_nogmres: bad arguments");
+// The resistance solve of STEPPER_NOGmres; RPP (the inverse left by
+// Rheology) is written only when non-null, and the stresslet dipole of the
+// interparticle forces is added only when conf is non-null.
+static int nogmres_impl(rsd_ctx* ctx, int32_t nn, const double* APP, const double* APQ, const double* AQQ,
+                        const double* rfu, const double* rfe, const double* rse, const double* Fe, const double* EIN,
+                        const double* Fe_inter, const double* conf, const double* u_brown, double* U_par,
+                        double* SijN_hyd, double* SijN_FP, double* SijN_B, double* RPP, int32_t* info) {
   RSD_TRY(rsd_set_device(ctx));
   cudaStream_t s = ctx->stream;
   const int64_t n = 11LL * nn, p = 6LL * nn, q = 5LL * nn;
@@ -605,12 +604,14 @@ extern "C" int rsd_stepper_nogmres(rsd_ctx* ctx, int32_t nn, const double* APP, 
   RSD_CUDA(ctx, cudaMemcpyAsync(SijN_FP, S + q, sizeof(double) * q, cudaMemcpyDeviceToHost, s));
   RSD_CUDA(ctx, cudaMemcpyAsync(SijN_B, S + 2 * q, sizeof(double) * q, cudaMemcpyDeviceToHost, s));
   // Rheology leaves RPP inverted
-  RSD_TRY(rsd_potri_upper_tag(ctx, (int)p, P, p, "rpp"));
-  RSD_TRY(rsd_mirror_upper(ctx, (int)p, P, p));
-  RSD_CUDA(ctx, cudaMemcpyAsync(RPP, P, sizeof(double) * p * p, cudaMemcpyDeviceToHost, s));
+  if (RPP) {
+    RSD_TRY(rsd_potri_upper_tag(ctx, (int)p, P, p, "rpp"));
+    RSD_TRY(rsd_mirror_upper(ctx, (int)p, P, p));
+    RSD_CUDA(ctx, cudaMemcpyAsync(RPP, P, sizeof(double) * p * p, cudaMemcpyDeviceToHost, s));
+  }
   RSD_TRY(sync(ctx));
   // stresslet dipole of the interparticle forces (Rheology 425-444)
-  for (int kk = 0; kk < nn; kk++) {
+  for (int kk = 0; conf && kk < nn; kk++) {
     double Sij[9];
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++)
@@ -620,5 +621,33 @@ extern "C" int rsd_stepper_nogmres(rsd_ctx* ctx, int32_t nn, const double* APP, 
     for (int m = 0; m < 5; m++) SijN_FP[5 * kk + m] += part[m];
   }
   *info = 0;
+  return RSD_OK;
+}
+
+extern "C" int rsd_stepper_nogmres(rsd_ctx* ctx, int32_t nn, const double* APP, const double* APQ, const double* AQQ,
+                                   const double* rfu, const double* rfe, const double* rse, const double* Fe,
+                                   const double* EIN, const double* Fe_inter, const double* conf,
+                                   const double* u_brown, double* U_par, double* SijN_hyd, double* SijN_FP,
+                                   double* SijN_B, double* RPP, int32_t* info) {
+  if (!ctx || nn < 1 || !APP || !APQ || !AQQ || !rfu || !rfe || !rse || !Fe || !EIN || !Fe_inter || !conf ||
+      !U_par || !SijN_hyd || !SijN_FP || !SijN_B || !RPP || !info)
+    return rsd_fail(ctx, RSD_EARG, "rsd_stepper_nogmres: bad arguments");
+  return nogmres_impl(ctx, nn, APP, APQ, AQQ, rfu, rfe, rse, Fe, EIN, Fe_inter, conf, u_brown, U_par, SijN_hyd,
+                      SijN_FP, SijN_B, RPP, info);
+}
+
+// hydro_SD_FTS: the solution of the FTS resistance problem that the
+// reference's splitting iteration approaches, U = RPP^-1 (Fe + RPQ EIN) and
+// S = RPQ^T U - RQQ EIN (= mu EIN + RPQ^T RPP^-1 Fe), solved directly.
+extern "C" int rsd_hydro_sd_fts(rsd_ctx* ctx, int32_t nn, const double* APP, const double* APQ, const double* AQQ,
+                                const double* rfu, const double* rfe, const double* rse, const double* Fe,
+                                const double* EIN, double* U_par, double* SijN, int32_t* info) {
+  if (!ctx || nn < 1 || !APP || !APQ || !AQQ || !rfu || !rfe || !rse || !Fe || !EIN || !U_par || !SijN || !info)
+    return rsd_fail(ctx, RSD_EARG, "rsd_hydro_sd_fts: bad arguments");
+  std::vector<double> s_fe(5 * (size_t)nn), s_b(5 * (size_t)nn);
+  RSD_TRY(nogmres_impl(ctx, nn, APP, APQ, AQQ, rfu, rfe, rse, Fe, EIN, Fe, nullptr, nullptr, U_par, SijN,
+                       s_fe.data(), s_b.data(), nullptr, info));
+  if (*info == 0)
+    for (size_t k = 0; k < s_fe.size(); k++) SijN[k] += s_fe[k];
   return RSD_OK;
 }
