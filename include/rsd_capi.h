@@ -206,6 +206,23 @@ int rsd_stepper_nogmres(rsd_ctx* ctx, int32_t nn, const double* APP, const doubl
                         const double* Fe_inter, const double* conf, const double* u_brown, double* U_par,
                         double* SijN_hyd, double* SijN_FP, double* SijN_B, double* RPP, int32_t* info);
 
+/* DMDX_CAL (src/stepper.f90:664-688): the Brownian drift term
+ * DMDX = (A1 - A2) Z / deta, A1 and A2 the translational blocks
+ * APP(1:3nn, 1:3nn) of the grand mobility (PER_GRPERY_INV_FRI with lat,
+ * ews_err = LINERR, mu_f, correction_method) at conf +- deta Z / 2, with
+ * deta the REAL*8 value of the default-real literal 0.001 (1.0000000474974513e-3).
+ * conf and Z as the reference's CONF(3, nn) and Z(3 nn). */
+int rsd_dmdx_cal(rsd_ctx* ctx, int32_t nn, const double* conf, const double* radii, rsd_lattice* lat, double ews_err,
+                 double mu_f, int32_t correction_method, const double* Z, double* DMDX);
+/* The Brownian velocity of STEPPER_Stokesian with BROWN (src/stepper.f90:
+ * 72-86): CHOLESKY of A = APP(1:3nn, 1:3nn) (APP the caller's 6nn x 6nn
+ * mobility block at conf), VB = sqrt(2 kBT) L Z / dt, and
+ * u_brown = VB + kBT DMDX_CAL(Z).  Z (3nn) are the standard normal numbers
+ * that the reference draws with GAUSS (the caller draws them).  info is
+ * CHOLESKY's (positive: A not SPD, nothing written; the reference stops). */
+int rsd_brownian_velocity(rsd_ctx* ctx, int32_t nn, const double* APP, const double* conf, const double* radii,
+                          rsd_lattice* lat, double ews_err, double mu_f, int32_t correction_method, const double* Z,
+                          double kBT, double dt, double* u_brown, int32_t* info);
 /* hydro_SD_FTS (src/stepper.f90:476-546), the FTS solve of the GMRES
  * variant (useGMRESmethod).  The reference alternates two GMRES(2) solves,
  * a mobility one and a lubrication one, until the FTS residual is below

@@ -330,6 +330,40 @@ def stepper_nogmres(G, rfu, rfe, rse, Fe, EIN, Fe_inter, conf, u_brown=None):
                 info_m=info_m, info_r=info_r, RPQ=RPQ, RQQ=RQQ)
 
 
+# deta of DMDX_CAL: PARAMETER(deta=0.001) gives the REAL*8 the value of the
+# default-real (single precision) literal
+DMDX_DETA = float(np.float32(0.001))
+
+
+def dmdx_cal(conf, radii, lattice_fn, ews_err, mu_f, Z, correction_method=0):
+    """DMDX_CAL (src/stepper.f90:664-688): DMDX = (A1 - A2) Z / deta with A1,
+    A2 the translational blocks APP(1:3N,1:3N) of PER_GRPERY_INV_FRI at
+    CONF +- deta Z / 2.  lattice_fn() returns a fresh lattice (the routine
+    fills it)."""
+    conf = np.asarray(conf, dtype=np.float64)
+    Z = np.asarray(Z, dtype=np.float64)
+    N = conf.shape[0]
+    Zc = Z.reshape(N, 3)
+    G1, _ = per_grpery_inv_fri(conf + 0.5 * DMDX_DETA * Zc, radii, lattice_fn(), ews_err, mu_f, correction_method)
+    G2, _ = per_grpery_inv_fri(conf - 0.5 * DMDX_DETA * Zc, radii, lattice_fn(), ews_err, mu_f, correction_method)
+    A1, A2 = G1[:3 * N, :3 * N], G2[:3 * N, :3 * N]
+    return ((A1 - A2) @ Z) / DMDX_DETA
+
+
+def brownian_velocity(APP, conf, radii, lattice_fn, ews_err, mu_f, Z, kBT, dt, correction_method=0):
+    """u_brown of STEPPER_Stokesian with BROWN (src/stepper.f90:72-86):
+    CHOLESKY (DPOTRF 'L', src/matrices.f90:126-157) of APP(1:3N,1:3N),
+    VB = sqrt(2 kBT) L Z / DT, u_brown = VB + kBT DMDX_CAL."""
+    from scipy.linalg import lapack
+    N = np.asarray(conf).shape[0]
+    A = np.asfortranarray(APP[:3 * N, :3 * N], dtype=np.float64).copy(order="F")
+    L, info = lapack.dpotrf(A, lower=1, clean=1)
+    if info:
+        return None, int(info)
+    VB = np.sqrt(2.0 * kBT) * (L @ Z) / dt
+    return VB + kBT * dmdx_cal(conf, radii, lattice_fn, ews_err, mu_f, Z, correction_method), 0
+
+
 def _grotmat(a, b, real_tol=1e-14):
     """grotmat (src/tools/gmres_mod.f90:178-201): Givens rotation."""
     if abs(b) < real_tol:

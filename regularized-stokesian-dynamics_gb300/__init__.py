@@ -89,6 +89,8 @@ _sig("rsd_mob_to_resist_fts", _i, [_vp, _i32, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
 _sig("rsd_arrangement", _i, [_vp, _i32, _dp, _dp, _dp, _dp, _ip])
 _sig("rsd_stepper_nogmres", _i, [_vp, _i32] + [_dp] * 11 + [_dp] * 5 + [_ip])
 _sig("rsd_hydro_sd_fts", _i, [_vp, _i32] + [_dp] * 8 + [_dp] * 2 + [_ip])
+_sig("rsd_dmdx_cal", _i, [_vp, _i32, _dp, _dp, _vp, _d, _d, _i32, _dp, _dp])
+_sig("rsd_brownian_velocity", _i, [_vp, _i32, _dp, _dp, _dp, _vp, _d, _d, _i32, _dp, _d, _d, _dp, _ip])
 _sig("rsd_stepper_stokesian", _i, [_vp, _vp, ctypes.POINTER(StepParams), _dp, _dp, _dp, _dp, _dp, _dp,
                                    ctypes.POINTER(StepInfo)])
 _sig("rsd_stepper_stokesian_dev", _i, [_vp, _vp, ctypes.POINTER(StepParams), _vp, _vp, _vp, _vp, _vp, _dp,
@@ -383,6 +385,29 @@ def hydro_SD_FTS(ctx: Context, APP, APQ, AQQ, rfu, rfe, rse, Fe, EIN):
     ctx.check(_lib.rsd_hydro_sd_fts(ctx.h, N, *[_p(m) for m in mats], _p(Fe), _p(EIN), _p(U_par), _p(SijN),
                                     ctypes.byref(info)))
     return dict(U_par=U_par, SijN=SijN, info=info.value)
+
+
+def DMDX_CAL(ctx: Context, conf, radii, lattice: Lattice, ews_err, mu_f, Z, correction_method=0):
+    """DMDX_CAL (src/stepper.f90:664-688): (A1 - A2) Z / deta from the
+    translational mobility blocks at conf +- deta Z / 2."""
+    conf, r, Z = _f64(conf), _f64(radii), _f64(Z)
+    out = np.empty(3 * len(r))
+    ctx.check(_lib.rsd_dmdx_cal(ctx.h, len(r), _p(conf), _p(r), ctypes.byref(lattice), ews_err, mu_f,
+                                correction_method, _p(Z), _p(out)))
+    return out
+
+
+def brownian_velocity(ctx: Context, APP, conf, radii, lattice: Lattice, ews_err, mu_f, Z, kBT, dt,
+                      correction_method=0):
+    """u_brown of STEPPER_Stokesian with BROWN (src/stepper.f90:72-86) for
+    the caller's standard normal numbers Z (3N)."""
+    APP = np.asfortranarray(APP, dtype=np.float64)
+    conf, r, Z = _f64(conf), _f64(radii), _f64(Z)
+    out = np.empty(3 * len(r))
+    info = ctypes.c_int32(0)
+    ctx.check(_lib.rsd_brownian_velocity(ctx.h, len(r), _p(APP), _p(conf), _p(r), ctypes.byref(lattice), ews_err,
+                                         mu_f, correction_method, _p(Z), kBT, dt, _p(out), ctypes.byref(info)))
+    return out
 
 
 # ------------------------------------------------------------------ fused step

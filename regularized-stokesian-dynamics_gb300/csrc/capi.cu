@@ -471,6 +471,94 @@ extern "C" int rsd_cholesky(rsd_ctx* ctx, int32_t n, double* B, int32_t* info) {
   return inf > 0 ? inf : RSD_OK;
 }
 
+// ------------------------------------------------------------- Brownian
+namespace {
+__global__ void zero_strict_lower(int n, double* __restrict__ A, int64_t lda) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i < n && i > j) A[i + (int64_t)j * lda] = 0.0;
+}
+
+// deta of DMDX_CAL: PARAMETER(deta=0.001) gives a REAL*8 the value of the
+// default-real (single precision) literal
+constexpr double DMDX_DETA = (double)0.001f;
+
+// d_out = (A1 - A2) Z / deta with A1, A2 the translational blocks of the
+// grand mobility at conf +- deta Z / 2 (DMDX_CAL, stepper.f90:664-688).
+int dmdx_dev(rsd_ctx* ctx, int32_t nn, const double* conf, const double* radii, rsd_lattice* lat, double ews_err,
+             double mu_f, int32_t correction_method, const double* Z, double* d_out) {
+  const int64_t n = 11LL * nn, t = 3LL * nn;
+  std::vector<double> c1(3 * (size_t)nn), c2(3 * (size_t)nn);
+  for (size_t k = 0; k < c1.size(); k++) {
+    c1[k] = conf[k] + 0.5 * DMDX_DETA * Z[k];
+    c2[k] = conf[k] - 0.5 * DMDX_DETA * Z[k];
+  }
+  double *d1, *d2, *dr, *dz;
+  RSD_TRY(upload(ctx, "dmdx_conf1", c1.data(), c1.size(), &d1));
+  RSD_TRY(upload(ctx, "dmdx_conf2", c2.data(), c2.size(), &d2));
+  RSD_TRY(upload(ctx, "dmdx_radii", radii, nn, &dr));
+  RSD_TRY(upload(ctx, "dmdx_z", Z, (size_t)t, &dz));
+  double* M1 = (double*)rsd_scratch(ctx, "dmdx_M1", sizeof(double) * n * n);
+  double* M2 = (double*)rsd_scratch(ctx, "dmdx_M2", sizeof(double) * n * n);
+  if (!M1 || !M2) return RSD_ENOMEM;
+  RSD_TRY(rsd_per_grpery_inv_fri_dev(ctx, nn, d1, dr, lat, ews_err, mu_f, correction_method, M1, n));
+  RSD_TRY(rsd_per_grpery_inv_fri_dev(ctx, nn, d2, dr, lat, ews_err, mu_f, correction_method, M2, n));
+  rsd_gemm_f64(ctx->stream, (int)t, 1, (int)t, 1.0 / DMDX_DETA, M1, n, 0, dz, t, 0, 0.0, d_out, t);
+  rsd_gemm_f64(ctx->stream, (int)t, 1, (int)t, -1.0 / DMDX_DETA, M2, n, 0, dz, t, 0, 1.0, d_out, t);
+  RSD_CUDA(ctx, cudaGetLastError());
+  return RSD_OK;
+}
+}  // namespace
+
+extern "C" int rsd_dmdx_cal(rsd_ctx* ctx, int32_t nn, const double* conf, const double* radii, rsd_lattice* lat,
+                            double ews_err, double mu_f, int32_t correction_method, const double* Z, double* DMDX) {
+  if (!ctx || nn < 1 || !conf || !radii || !lat || !Z || !DMDX)
+    return rsd_fail(ctx, RSD_EARG, "rsd_dmdx_cal: bad arguments");
+  if (!finite_all(conf, 3 * (size_t)nn) || !finite_all(radii, nn) || !finite_all(Z, 3 * (size_t)nn))
+    return rsd_fail(ctx, RSD_ENAN, "non-finite positions, radii or Z");
+  RSD_TRY(rsd_set_device(ctx));
+  double* d = (double*)rsd_scratch(ctx, "dmdx_out", sizeof(double) * 3 * (size_t)nn);
+  if (!d) return RSD_ENOMEM;
+  RSD_TRY(dmdx_dev(ctx, nn, conf, radii, lat, ews_err, mu_f, correction_method, Z, d));
+  RSD_CUDA(ctx, cudaMemcpyAsync(DMDX, d, sizeof(double) * 3 * (size_t)nn, cudaMemcpyDeviceToHost, ctx->stream));
+  return sync(ctx);
+}
+
+extern "C" int rsd_brownian_velocity(rsd_ctx* ctx, int32_t nn, const double* APP, const double* conf,
+                                     const double* radii, rsd_lattice* lat, double ews_err, double mu_f,
+                                     int32_t correction_method, const double* Z, double kBT, double dt,
+                                     double* u_brown, int32_t* info) {
+  if (!ctx || nn < 1 || !APP || !conf || !radii || !lat || !Z || !u_brown || !info || !(dt != 0.0))
+    return rsd_fail(ctx, RSD_EARG, "rsd_brownian_velocity: bad arguments");
+  if (!finite_all(Z, 3 * (size_t)nn)) return rsd_fail(ctx, RSD_ENAN, "non-finite Z");
+  RSD_TRY(rsd_set_device(ctx));
+  const int64_t t = 3LL * nn, p = 6LL * nn;
+  // CHOLESKY of the translational block A = APP(1:3N, 1:3N): U = L^T from
+  // the upper factorisation, the strict lower part cleared
+  std::vector<double> As((size_t)(t * t));
+  for (int64_t j = 0; j < t; j++)
+    for (int64_t i = 0; i < t; i++) As[i + j * t] = (i <= j) ? APP[j + i * p] : 0.0;
+  double *dA, *dz;
+  RSD_TRY(upload(ctx, "brown_A", As.data(), As.size(), &dA));
+  RSD_TRY(upload(ctx, "brown_z", Z, (size_t)t, &dz));
+  int inf = 0;
+  RSD_TRY(rsd_potrf_upper_tag(ctx, (int)t, dA, t, &inf, "brown"));
+  *info = inf;
+  if (inf) return inf;
+  zero_strict_lower<<<dim3((unsigned)((t + 255) / 256), (unsigned)t), 256, 0, ctx->stream>>>((int)t, dA, t);
+  double* vb = (double*)rsd_scratch(ctx, "brown_vb", sizeof(double) * 2 * (size_t)t);
+  if (!vb) return RSD_ENOMEM;
+  // VB = sqrt(2 kBT) L Z / DT (stepper.f90:79)
+  rsd_gemm_f64(ctx->stream, (int)t, 1, (int)t, std::sqrt(2.0 * kBT) / dt, dA, t, 1, dz, t, 0, 0.0, vb, t);
+  RSD_CUDA(ctx, cudaGetLastError());
+  RSD_TRY(dmdx_dev(ctx, nn, conf, radii, lat, ews_err, mu_f, correction_method, Z, vb + t));
+  std::vector<double> h(2 * (size_t)t);
+  RSD_CUDA(ctx, cudaMemcpyAsync(h.data(), vb, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->stream));
+  RSD_TRY(sync(ctx));
+  // u_brown = VB + kBT DMDX (stepper.f90:81-83)
+  for (int64_t k = 0; k < t; k++) u_brown[k] = h[k] + kBT * h[t + k];
+  return RSD_OK;
+}
+
 extern "C" int rsd_mob_to_resist_fts(rsd_ctx* ctx, int32_t nn, const double* APP, const double* APQ,
                                      const double* AQQ, double* RPP, double* RPQ, double* RQQ, int32_t* info) {
   if (!ctx || nn < 1 || !APP || !APQ || !AQQ || !RPP || !RPQ || !RQQ || !info)

@@ -266,6 +266,28 @@ def test_hydro_sd_fts_matches_oracle(rsd, ctx, tabs, case):
         assert rel(got["U_par"], it["U_Par"]) <= 1e-9
 
 
+def test_brownian_terms_match_oracle(rsd, ctx):
+    """DMDX_CAL and the Brownian velocity of STEPPER_Stokesian (stepper.f90:
+    72-86, 664-688) for given normal numbers Z.  DMDX divides the difference
+    of two assemblies by deta ~ 1e-3, which scales their entry-level
+    rounding by 1e3: bound 1e-7 for it, 1e-9 for the velocity (dominated by
+    the Cholesky term)."""
+    from tests.test_brownian import dilute
+    pos, radii, L, lat_fn = dilute()
+    N = len(radii)
+    Z = np.random.default_rng(21).normal(size=3 * N)
+    lat_g = rsd.SET_LATTICE_SKEW(0.0, [L, L, L], 1.0)
+    d_g = rsd.DMDX_CAL(ctx, pos, radii, lat_g, 1e-10, MU, Z)
+    d_o = o.dmdx_cal(pos, radii, lat_fn, 1e-10, MU, Z)
+    assert rel(d_g, d_o) <= 1e-7
+    G, _ = o.per_grpery_inv_fri(pos, radii, lat_fn(), 1e-10, MU)
+    APP = G[:6 * N, :6 * N]
+    u_g = rsd.brownian_velocity(ctx, APP, pos, radii, rsd.SET_LATTICE_SKEW(0.0, [L, L, L], 1.0), 1e-10, MU, Z,
+                                0.7, 1e-3)
+    u_o, info = o.brownian_velocity(APP, pos, radii, lat_fn, 1e-10, MU, Z, 0.7, 1e-3)
+    assert info == 0 and rel(u_g, u_o) <= 1e-9
+
+
 @pytest.mark.parametrize("workload", ["small", "config1"])
 def test_fused_step_matches_oracle(rsd, ctx, tabs, workload):
     if workload == "small":
