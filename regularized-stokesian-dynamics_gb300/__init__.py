@@ -467,3 +467,4 @@ def lubdat_dir():
 
 
 from . import configs  # noqa: E402,F401
+from . import driver_files  # noqa: E402,F401

@@ -15,6 +15,11 @@ Writes
       reference reads at run time (examples/lubdat), byte for byte; they
       are inputs of lubmxcalc, kept in the reference's own file format so
       the C-ABI loader reads the same files a Fortran run reads.
+  tests/golden/io/{control_file.dat,initial_config.dat}  the reference's
+      example driver inputs (examples/), byte for byte, and
+  tests/golden/io/output_head.VTF  the first 40 records of its example
+      trajectory output (examples/gmmres_output.VTF), for the readers and
+      writers of the driver's file formats.
 """
 import os
 import shutil
@@ -39,7 +44,14 @@ def main(ref):
     os.makedirs(os.path.join(HERE, "lubdat"), exist_ok=True)
     for name in ("r2babc.dat", "r2bgh.dat", "r2bm.dat"):
         shutil.copyfile(os.path.join(ref, "examples", "lubdat", name), os.path.join(HERE, "lubdat", name))
-    print("wrote %d tablefar rows and 3 lubrication tables" % len(rows))
+    os.makedirs(os.path.join(HERE, "io"), exist_ok=True)
+    for name in ("control_file.dat", "initial_config.dat"):
+        shutil.copyfile(os.path.join(ref, "examples", name), os.path.join(HERE, "io", name))
+    with open(os.path.join(ref, "examples", "gmmres_output.VTF")) as fp:
+        head = [fp.readline() for _ in range(40)]
+    with open(os.path.join(HERE, "io", "output_head.VTF"), "w") as fp:
+        fp.write("".join(head))
+    print("wrote %d tablefar rows, 3 lubrication tables and the driver file fixtures" % len(rows))
 
 
 if __name__ == "__main__":
