@@ -9,8 +9,8 @@ lattices -- the second must not see the first one's table -- and compares
 each with the allocating entry point rsd_per_grpery_inv_fri_dev, to the
 1e-12 relative tolerance of the mobility parity tests.  It also checks that
 a request beyond the array's limit is refused with RSD_ELIMIT.  Kept in a
-file collected last so that a first-failure stop has run every other test;
-it passes alone in a fresh process as well.
+file collected after the parity files so that a first-failure stop has run
+them; it passes alone in a fresh process as well.
 """
 import ctypes
 
