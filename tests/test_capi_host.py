@@ -2,6 +2,7 @@
 every entry point include/rsd_capi.h declares; the lattice routines (host
 code) match the oracle; inputs are validated; seeded configurations are
 deterministic and respect their minimum gap."""
+import ctypes
 import os
 import re
 
@@ -85,3 +86,18 @@ def test_box_edges_match_the_workloads(rsd):
     assert abs(rsd.configs.box_edge(512, 0.45) - 16.8286) < 1e-4
     assert abs(rsd.configs.box_edge(1000, 0.50) - 20.3098) < 1e-4
     assert abs(rsd.configs.box_edge(2048, 0.50) - 25.7919) < 1e-4
+
+
+def test_new_entry_points_check_their_arguments_without_a_device(rsd):
+    """hydro_SD_FTS, DMDX_CAL and the Brownian velocity reject a missing
+    context or array with RSD_EARG before any device work."""
+    lib = rsd.library()
+    z = np.zeros(64)
+    p = z.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    info = ctypes.c_int32(0)
+    lat = rsd.Lattice()
+    assert lib.rsd_hydro_sd_fts(None, 1, p, p, p, p, p, p, p, p, p, p, ctypes.byref(info)) == rsd.RSD_EARG
+    assert lib.rsd_hydro_sd_fts(None, 1, p, p, p, p, p, p, p, p, None, p, ctypes.byref(info)) == rsd.RSD_EARG
+    assert lib.rsd_dmdx_cal(None, 1, p, p, ctypes.byref(lat), 1e-10, 0.3, 0, p, p) == rsd.RSD_EARG
+    assert lib.rsd_brownian_velocity(None, 1, p, p, p, ctypes.byref(lat), 1e-10, 0.3, 0, p, 1.0, 1e-3, p,
+                                     ctypes.byref(info)) == rsd.RSD_EARG
