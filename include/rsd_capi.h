@@ -104,6 +104,11 @@ int rsd_ctx_set_mixed_lambda_scale(rsd_ctx* ctx, double scale);
  * (fewer live accumulators and a shorter loop per pass; r, erfc and exp are
  * evaluated once per pass).  A performance setting; the sums are the same. */
 int rsd_ctx_set_mixed_real_passes(rsd_ctx* ctx, int32_t passes);
+/* Overlap corrections in the fused step (rsd_stepper_stokesian): the
+ * correction_method of per_GRPY_YZD.f90:98-116 (0 none, the default; 1
+ * Yamakawa; 2 regularized), added to the grand mobility of either precision
+ * form for the pairs whose minimum image overlaps. */
+int rsd_ctx_set_correction_method(rsd_ctx* ctx, int32_t method);
 
 /* ---------------------------------------------------------------- lattice */
 /* SET_LATTICE_SKEW (src/csd_post.f90:105-136) with MAT_INV3

@@ -526,17 +526,19 @@ def yetamu_solve(APP, SijN_hyd, SijN_FP, SijN_B, EIN, LV, mu_f, phi, N):
     return y
 
 
-def stepper_stokesian(conf, radii, LB, T, dt, gamma, mu_f, ews_err, tab: LubTab, Fe=None, Fe_inter=None):
+def stepper_stokesian(conf, radii, LB, T, dt, gamma, mu_f, ews_err, tab: LubTab, Fe=None, Fe_inter=None,
+                      correction_method=0):
     """One STEPPER_Stokesian step (src/stepper.f90:33-156) on the plain
     LAPACK FTS periodic path with lubrication (no Brownian motion, no DEM
-    sub-stepping, no rigid bodies).  Returns the updated configuration and
+    sub-stepping, no rigid bodies), with the module's correction_method
+    passed to PER_GRPERY_INV_FRI.  Returns the updated configuration and
     everything the reference computes on the way."""
     conf = np.array(conf, dtype=np.float64)
     N = conf.shape[0]
     Eij, omega_bg, omegaT = init_u_bg(gamma)
     EIN = ein_trans_y2(Eij, N)
     lat = set_lattice_skew(T, LB, gamma)
-    G, _ = per_grpery_inv_fri(conf, radii, lat, ews_err, mu_f, 0)
+    G, _ = per_grpery_inv_fri(conf, radii, lat, ews_err, mu_f, correction_method)
     Fe = np.zeros(6 * N) if Fe is None else np.asarray(Fe, dtype=np.float64)
     Fe_inter = np.zeros(6 * N) if Fe_inter is None else np.asarray(Fe_inter, dtype=np.float64)
     rfu, rfe, rse, ncontact = lubmxcalc(conf, radii, lat, mu_f, tab)

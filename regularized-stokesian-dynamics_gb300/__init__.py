@@ -100,6 +100,7 @@ _sig("rsd_ctx_set_mixed_split", _i, [_vp, _d, _i32])
 _sig("rsd_ctx_set_mixed_truncation", _i, [_vp, _d, _d])
 _sig("rsd_ctx_set_mixed_lambda_scale", _i, [_vp, _d])
 _sig("rsd_ctx_set_mixed_real_passes", _i, [_vp, _i32])
+_sig("rsd_ctx_set_correction_method", _i, [_vp, _i32])
 _sig("rsd_syrk_f32_dev", _i, [_vp, _i32, _i32, _vp, _i64, _vp, _i64, _i32])
 _sig("rsd_potrf_f32_dev", _i, [_vp, _i32, _vp, _i64, _i32, _ip])
 _sig("rsd_potri_f32_dev", _i, [_vp, _i32, _vp, _i64, _i32])
@@ -168,6 +169,11 @@ class Context:
     def set_mixed_real_passes(self, passes=1):
         """Passes over the near images of the equal-radius mixed assembly."""
         self.check(_lib.rsd_ctx_set_mixed_real_passes(self.h, int(passes)))
+
+    def set_correction_method(self, method=0):
+        """Overlap corrections in the fused step (correction_method of
+        per_GRPY_YZD.f90:98-116: 0 none, 1 Yamakawa, 2 regularized)."""
+        self.check(_lib.rsd_ctx_set_correction_method(self.h, int(method)))
 
     def set_tensor_cores(self, mode=1):
         """FP32 factorisations of the mixed form: 1 (or True, the default)

@@ -151,6 +151,13 @@ extern "C" int rsd_ctx_set_mixed_lambda_scale(rsd_ctx* c, double scale) {
   return RSD_OK;
 }
 
+extern "C" int rsd_ctx_set_correction_method(rsd_ctx* c, int method) {
+  if (!c) return RSD_EARG;
+  if (method < 0 || method > 2) return rsd_fail(c, RSD_EARG, "correction_method must be 0, 1 or 2");
+  c->correction_method = method;
+  return RSD_OK;
+}
+
 extern "C" int rsd_ctx_set_mixed_real_passes(rsd_ctx* c, int passes) {
   if (!c) return RSD_EARG;
   if (passes < 1 || passes > 4) return rsd_fail(c, RSD_EARG, "mixed real-space passes must be 1 to 4");
@@ -368,7 +375,7 @@ extern "C" int rsd_per_grpery_inv_fri_dev(rsd_ctx* ctx, int32_t nn, const double
   int nov = 0;
   if (correction_method != 0) RSD_TRY(rsd_count_overlaps(ctx, nn, d_pos, d_radii, lat, &nov));
   RSD_TRY(rsd_ewald_assemble(ctx, nn, d_pos, d_radii, lat, mu_f, RSD_PREC_FP64, d_M, ldm));
-  return rsd_overlap_correct(ctx, correction_method, nn, d_pos, d_radii, lat, mu_f, nov, d_M, ldm);
+  return rsd_overlap_correct(ctx, correction_method, RSD_PREC_FP64, nn, d_pos, d_radii, lat, mu_f, nov, d_M, ldm);
 }
 
 extern "C" int rsd_per_grpery_inv_fri(rsd_ctx* ctx, int32_t nn, const double* p_pos, const double* radii,

@@ -1249,7 +1249,7 @@ __global__ void __launch_bounds__(64) overlap_correct(int method, int npair, con
 
 }  // namespace
 
-int rsd_overlap_correct(rsd_ctx* ctx, int method, int nn, const double* d_pos, const double* d_radii,
+int rsd_overlap_correct(rsd_ctx* ctx, int method, int precision, int nn, const double* d_pos, const double* d_radii,
                         const rsd_lattice* lat, double mu_f, int npair, double* d_M, int64_t ldm) {
   if (npair <= 0) return RSD_OK;
   const rsd_lat_dev L = rsd_lat_pack(lat);
@@ -1259,9 +1259,18 @@ int rsd_overlap_correct(rsd_ctx* ctx, int method, int nn, const double* d_pos, c
   RSD_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int), ctx->stream));
   dim3 blk(32, 4), grd((nn + 31) / 32, (nn + 3) / 4);
   overlap_list<<<grd, blk, 0, ctx->stream>>>(nn, L, d_pos, d_radii, npair, list, cnt); RSD_LAUNCH_NOTE();
-  const DenseSink dsk{d_M, ldm};
-  overlap_correct<DenseSink><<<(npair + 63) / 64, 64, 0, ctx->stream>>>(method, npair, list, nn, L, d_pos, d_radii,
-                                                                       1.0 / (RSD_PI * mu_f), dsk); RSD_LAUNCH_NOTE();
+  const double inv_pimu = 1.0 / (RSD_PI * mu_f);
+  const unsigned nblk = (unsigned)((npair + 63) / 64);
+  if (precision == RSD_PREC_MIXED) {
+    float* hi = reinterpret_cast<float*>(d_M);
+    const PlaneSink psk{hi, hi + (size_t)ldm * (11LL * nn), ldm};
+    overlap_correct<PlaneSink><<<nblk, 64, 0, ctx->stream>>>(method, npair, list, nn, L, d_pos, d_radii, inv_pimu,
+                                                             psk); RSD_LAUNCH_NOTE();
+  } else {
+    const DenseSink dsk{d_M, ldm};
+    overlap_correct<DenseSink><<<nblk, 64, 0, ctx->stream>>>(method, npair, list, nn, L, d_pos, d_radii, inv_pimu,
+                                                             dsk); RSD_LAUNCH_NOTE();
+  }
   RSD_CUDA(ctx, cudaGetLastError());
   return RSD_OK;
 }

@@ -38,6 +38,7 @@ struct rsd_ctx {
   double mixed_kexp = 10.0 * 3.141592653589793;  // and reciprocal vectors with k^2/(4 lambda^2) beyond this
   int mixed_real_passes = 1;  // mixed assembly, equal radii: passes over the near images (moment parts)
   double mixed_lambda_scale = 1.75;  // mixed assembly: Ewald splitting parameter relative to the reference's
+  int correction_method = 0;  // fused step: overlap corrections of the grand mobility (0, 1 or 2)
   cudaStream_t side = nullptr;  // higher-priority stream for look-ahead panels
   cudaEvent_t ev_panel = nullptr, ev_next = nullptr;
   int* d_info = nullptr;  // device-side status words
@@ -151,9 +152,10 @@ int rsd_mirror_planes(rsd_ctx* ctx, int nn, double* d_M, int64_t ldm);
 int rsd_count_overlaps(rsd_ctx* ctx, int nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
                        int* count);
 // Adds the overlap correction of correction_method 1 or 2 (GRPY_YZD.f90:
-// 789-836) to the FP64 grand mobility for the npair overlapping pairs that
-// rsd_count_overlaps counted.
-int rsd_overlap_correct(rsd_ctx* ctx, int method, int nn, const double* d_pos, const double* d_radii,
+// 789-836) for the npair overlapping pairs that rsd_count_overlaps counted,
+// to the grand mobility in the layout of `precision` (FP64, or the mixed
+// form's FP32 planes over the stored half).
+int rsd_overlap_correct(rsd_ctx* ctx, int method, int precision, int nn, const double* d_pos, const double* d_radii,
                         const rsd_lattice* lat, double mu_f, int npair, double* d_M, int64_t ldm);
 // Lubrication (lub.cu)
 int rsd_lub_assemble(rsd_ctx* ctx, const rsd_lubtab* tab, int nn, int nb, int is_period, const double* d_pos,

@@ -230,6 +230,12 @@ extern "C" int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, co
   cudaEventRecord(ctx->ev[0], s);
   // grand mobility
   RSD_TRY(rsd_ewald_assemble(ctx, nn, d_conf, d_radii, &lat, p->mu_f, p->precision, M, n));
+  if (ctx->correction_method) {  // overlap corrections (per_GRPY_YZD.f90:98-116)
+    int nov = 0;
+    RSD_TRY(rsd_count_overlaps(ctx, nn, d_conf, d_radii, &lat, &nov));
+    RSD_TRY(rsd_overlap_correct(ctx, ctx->correction_method, p->precision, nn, d_conf, d_radii, &lat, p->mu_f, nov,
+                                M, n));
+  }
   cudaEventRecord(ctx->ev[1], s);
   // averageU on APP before it is overwritten
   const bool planes = p->precision == RSD_PREC_MIXED;

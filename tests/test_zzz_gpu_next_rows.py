@@ -1,5 +1,6 @@
 """GPU tests of the rows widened last (overlap correction method 2, the
-GMRES variant's FTS solve, the Brownian terms), through the C-ABI against
+GMRES variant's FTS solve, the Brownian terms, overlap corrections in the
+fused step), through the C-ABI against
 the oracle; tolerances as in test_gpu_parity.py, stated per test.  Kept in a
 file collected after the others so that a first-failure stop has run every
 other GPU test."""
@@ -85,3 +86,27 @@ def test_brownian_terms_match_oracle(rsd, ctx):
                                 0.7, 1e-3)
     u_o, info = o.brownian_velocity(APP, pos, radii, lat_fn, 1e-10, MU, Z, 0.7, 1e-3)
     assert info == 0 and rel(u_g, u_o) <= 1e-9
+
+
+def test_fused_step_with_overlap_correction(rsd, tabs):
+    """The fused step with Context.set_correction_method(2): one particle
+    moved to r = 1.9a of another (it also touches a third); the FP64 form
+    against the oracle's STEPPER_Stokesian with the same correction (1e-9),
+    the mixed form against the FP64 form (1e-8).  (Method 1 makes this
+    mobility indefinite, as the reference's own formulas do.)"""
+    N = 27
+    pos, radii, L = rsd.configs.packing(N, 0.2, 0.01, seed=20260500)
+    pos[1] = np.mod(pos[0] + np.array([1.9, 0.0, 0.0]), L)
+    c = rsd.Context(0)
+    c.set_correction_method(2)
+    g = rsd.STEPPER_Stokesian(c, tabs[0], pos, radii, 0.0, 1e-3, [L, L, L], 1.0, MU, 1e-10)
+    r = o.stepper_stokesian(pos, radii, [L, L, L], 0.0, 1e-3, 1.0, MU, 1e-10, tabs[1], correction_method=2)
+    assert g["info"].info == 0 and r["info_m"] == 0
+    assert rel(g["U_pos"], r["U_pos"]) <= 1e-9
+    assert rel(g["SijN"], r["SijN_hyd"]) <= 1e-9
+    assert np.abs(g["conf"] - r["conf"]).max() <= 1e-12 * L
+    m = rsd.STEPPER_Stokesian(c, tabs[0], pos, radii, 0.0, 1e-3, [L, L, L], 1.0, MU, 1e-10,
+                              precision=rsd.PREC_MIXED)
+    assert rel(m["U_pos"], g["U_pos"]) <= 1e-8 and rel(m["SijN"], g["SijN"]) <= 1e-8
+    r0 = o.stepper_stokesian(pos, radii, [L, L, L], 0.0, 1e-3, 1.0, MU, 1e-10, tabs[1])
+    assert rel(g["U_pos"], r0["U_pos"]) > 1e-6  # the correction changed the step
