@@ -480,9 +480,11 @@ extern "C" int rsd_cholesky(rsd_ctx* ctx, int32_t n, double* B, int32_t* info) {
 
 // ------------------------------------------------------------- Brownian
 namespace {
+// columns j = blockIdx.y, blockIdx.y + gridDim.y, ...
 __global__ void zero_strict_lower(int n, double* __restrict__ A, int64_t lda) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-  if (i < n && i > j) A[i + (int64_t)j * lda] = 0.0;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int j = blockIdx.y; j < n; j += gridDim.y)
+    if (i < n && i > j) A[i + (int64_t)j * lda] = 0.0;
 }
 
 // deta of DMDX_CAL: PARAMETER(deta=0.001) gives a REAL*8 the value of the
@@ -551,7 +553,8 @@ extern "C" int rsd_brownian_velocity(rsd_ctx* ctx, int32_t nn, const double* APP
   RSD_TRY(rsd_potrf_upper_tag(ctx, (int)t, dA, t, &inf, "brown"));
   *info = inf;
   if (inf) return inf;
-  zero_strict_lower<<<dim3((unsigned)((t + 255) / 256), (unsigned)t), 256, 0, ctx->stream>>>((int)t, dA, t);
+  zero_strict_lower<<<dim3((unsigned)((t + 255) / 256), (unsigned)(t < 65535 ? t : 65535)), 256, 0, ctx->stream>>>(
+      (int)t, dA, t);
   double* vb = (double*)rsd_scratch(ctx, "brown_vb", sizeof(double) * 2 * (size_t)t);
   if (!vb) return RSD_ENOMEM;
   // VB = sqrt(2 kBT) L Z / DT (stepper.f90:79)
