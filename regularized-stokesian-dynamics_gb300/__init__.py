@@ -473,4 +473,12 @@ def lubdat_dir():
 
 
 from . import configs  # noqa: E402,F401
+from . import driver  # noqa: E402,F401
 from . import driver_files  # noqa: E402,F401
+
+
+def driver_step(ctx: Context, tab: LubTab, precision=PREC_MIXED):
+    """The fused step as the step callable of driver.run."""
+    def step(conf, radii, T, dt, LB, gamma, mu_f, ews_err):
+        return STEPPER_Stokesian(ctx, tab, conf, radii, T, dt, LB, gamma, mu_f, ews_err, precision=precision)
+    return step

@@ -1,0 +1,87 @@
+"""The driver's time loop (driver.py) on the CPU with the oracle's step: a
+small periodic FTS suspension written as initial_config.dat, the example
+control_file.dat switched to that case.  The loop exits once T exceeds
+END_TIME (strictly, main.f90:211), so END_TIME = 3 DT gives four steps; its
+files must hold one frame and one viscosity record per step, and its last
+configuration must equal four oracle steps taken directly."""
+import importlib.util
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from oracle import oracle as o
+from tests.test_gmres_variant import configs
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+IO = os.path.join(ROOT, "tests", "golden", "io")
+LUBDAT = os.path.join(ROOT, "tests", "golden", "lubdat")
+
+
+@pytest.fixture(scope="module")
+def drv():
+    """driver.py and driver_files.py loaded as a package of their own: host
+    code, no CUDA library needed."""
+    import types
+    pkg = os.path.join(ROOT, "regularized-stokesian-dynamics_gb300")
+    host = types.ModuleType("rsd_host")
+    host.__path__ = [pkg]
+    sys.modules["rsd_host"] = host
+    for name in ("driver_files", "driver"):
+        spec = importlib.util.spec_from_file_location("rsd_host." + name, os.path.join(pkg, name + ".py"))
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules["rsd_host." + name] = mod
+        spec.loader.exec_module(mod)
+    return sys.modules["rsd_host.driver"], sys.modules["rsd_host.driver_files"]
+
+
+def control_for_periodic_fts(tmp_path):
+    src = open(os.path.join(IO, "control_file.dat")).read().split("\n")
+    set_line = {1: ".true.", 3: ".true.", 7: ".false.", 9: ".true.", 10: ".true.", 18: "1.0", 19: "1.0",
+                27: "0.5", 37: "0.003", 38: "1e-3", 39: "1"}  # 0-based records
+    for i, v in set_line.items():
+        src[i] = v + "    ! set by the test"
+    p = tmp_path / "control_file.dat"
+    p.write_text("\n".join(src))
+    return str(p)
+
+
+def test_loop_matches_direct_oracle_steps(drv, tmp_path):
+    driver, files = drv
+    control = control_for_periodic_fts(tmp_path)
+    c = files.read_control(control)
+    assert c["FTS_method"] and c["uselub"] and c["IsPeriod"] and c["simplePeriod"]
+    assert (c["radii_test"], c["radii_true"], c["Gamma_alpha"], c["END_TIME"], c["BASE_DT"], c["K_WRITE"]) == \
+        (1.0, 1.0, 0.5, 0.003, 1e-3, 1)
+    pos, radii, L = configs().packing(8, 0.2, 0.05, seed=20261100)
+    init = str(tmp_path / "initial_config.dat")
+    files.write_initial_config(init, pos, radii, [L, L, L])
+    tab = o.LubTab(LUBDAT)
+    mu = 1.0 / np.pi
+
+    def step(conf, r, T, dt, LB, gamma, mu_f, ews):
+        return o.stepper_stokesian(conf, r, LB, T, dt, gamma, mu_f, ews, tab)
+
+    vtf, yeta = str(tmp_path / "output.VTF"), str(tmp_path / "yeta_mu.txt")
+    res = driver.run(control, init, step, vtf, yeta)
+    assert res["steps"] == 4  # T = 0, 1e-3, 2e-3, 3e-3 (T == END_TIME does not exit)
+    rows = files.read_vtf(vtf)
+    assert len(rows) == 4 * 8 and [r[0] for r in rows[::8]] == pytest.approx([0.0, 1e-3, 2e-3, 3e-3], abs=1e-15)
+    yl = [line for line in open(yeta) if line.strip()]
+    assert len(yl) == 4 and all(len(line.rstrip("\n")) == 10 * 24 for line in yl)
+    d = files.read_initial_config(init)  # positions and box as the file holds them (15 digits)
+    conf, radii, LB, T = np.array(d["conf"]), np.array(d["radii"]), d["LB"], 0.0
+    for _ in range(4):
+        out = o.stepper_stokesian(conf, radii, LB, T, 1e-3, 0.5, mu, c["LINERR"], tab)
+        conf, T = out["conf"], T + 1e-3
+    assert np.abs(res["conf"] - conf).max() == 0.0
+
+
+def test_unsupported_settings_are_refused(drv, tmp_path):
+    driver, files = drv
+    c = files.read_control(os.path.join(IO, "control_file.dat"))  # the example: not periodic, no FTS
+    d = files.read_initial_config(os.path.join(IO, "initial_config.dat"))  # a conglomerate
+    with pytest.raises(ValueError) as e:
+        driver.check_supported(c, d)
+    assert "IsPeriod" in str(e.value) and "conglomerates" in str(e.value)
