@@ -110,3 +110,23 @@ def test_fused_step_with_overlap_correction(rsd, tabs):
     assert rel(m["U_pos"], g["U_pos"]) <= 1e-8 and rel(m["SijN"], g["SijN"]) <= 1e-8
     r0 = o.stepper_stokesian(pos, radii, [L, L, L], 0.0, 1e-3, 1.0, MU, 1e-10, tabs[1])
     assert rel(g["U_pos"], r0["U_pos"]) > 1e-6  # the correction changed the step
+
+
+def test_driver_loop_on_the_fused_step(rsd, tabs, tmp_path):
+    """The driver's time loop (driver.py) over the reference's file formats
+    with the fused FP64 step, against the same loop with the oracle's step:
+    four steps, positions to 1e-12 of the box."""
+    from tests.test_driver_loop import control_for_periodic_fts
+    control = control_for_periodic_fts(tmp_path)
+    pos, radii, L = rsd.configs.packing(8, 0.2, 0.05, seed=20261100)
+    init = str(tmp_path / "initial_config.dat")
+    rsd.driver_files.write_initial_config(init, pos, radii, [L, L, L])
+    g = rsd.driver.run(control, init, rsd.driver_step(rsd.Context(0), tabs[0], precision=rsd.PREC_FP64),
+                       str(tmp_path / "g.VTF"), str(tmp_path / "g_yeta.txt"))
+
+    def ostep(conf, r, T, dt, LB, gamma, mu_f, ews):
+        return o.stepper_stokesian(conf, r, LB, T, dt, gamma, mu_f, ews, tabs[1])
+
+    r = rsd.driver.run(control, init, ostep, str(tmp_path / "o.VTF"), str(tmp_path / "o_yeta.txt"))
+    assert g["steps"] == r["steps"] == 4
+    assert np.abs(g["conf"] - r["conf"]).max() <= 1e-12 * L
