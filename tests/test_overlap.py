@@ -207,3 +207,22 @@ def test_oracle_assembly_applies_the_correction(method):
     assert np.allclose(diff[np.ix_(rows(0)[:3], rows(1)[:3])], TT / s, rtol=0, atol=1e-14)
     assert np.allclose(diff[np.ix_(rows(0)[6:], rows(1)[6:])], QQ / s, rtol=0, atol=1e-14)
     assert np.abs(G1 - G1.T).max() <= 1e-14 * np.abs(G1).max()
+
+
+@pytest.mark.parametrize("a", [1.0, 0.7])
+def test_yamakawa_equal_spheres_are_the_published_forms(a):
+    """Equal spheres of radius a overlapping at r < 2a: the Rotne-Prager-
+    Yamakawa translational and rotational mobilities (in the units of the
+    pair kernels, before 1/(pi mu_f)):
+      TT = 1/(6a) [(1 - 9r/(32a)) I + 3r/(32a) rr],
+      RR = 1/(8a^3) [(1 - 27r/(32a) + 5r^3/(64a^3)) I + (9r/(32a) - 3r^3/(64a^3)) rr]."""
+    rng = np.random.default_rng(15)
+    for r in (0.1 * a, 0.9 * a, 1.7 * a, 1.999 * a):
+        u = unit(rng)
+        TT, RR, _, _, _, _ = o.yamakawa_ij(u * r, a, a)
+        rr = np.outer(u, u)
+        tt = ((1 - 9 * r / (32 * a)) * np.eye(3) + 3 * r / (32 * a) * rr) / (6 * a)
+        rot = ((1 - 27 * r / (32 * a) + 5 * r ** 3 / (64 * a ** 3)) * np.eye(3)
+               + (9 * r / (32 * a) - 3 * r ** 3 / (64 * a ** 3)) * rr) / (8 * a ** 3)
+        assert np.abs(TT - tt).max() <= 1e-15 * np.abs(tt).max()
+        assert np.abs(RR - rot).max() <= 1e-14 * np.abs(rot).max()
