@@ -9,18 +9,25 @@ them (through scipy's bundled LAPACK).
 Reference routines restated here (paths inside the reference project):
   src/matrices.f90      MATREV 4-34, arrangResist 218-228, averageU 230-253,
                         MobToResist_FTS 393-416, arrangement 432-445
-  src/stepper.f90       STEPPER_Stokesian 33-156, STEPPER_conf 160-227,
-                        STEPPER_NOGmres 348-410, Rheology 412-447
+  src/stepper.f90       STEPPER_Stokesian 33-156 (with its BROWN block
+                        72-86), STEPPER_conf 160-227, STEPPER_NOGmres
+                        348-410, Rheology 412-447, hydro_SD_FTS 476-546,
+                        DMDX_CAL 664-688
+  src/tools/gmres_mod.f90, gmres_mod_gmres.f90, algebra_lin.f90
+                        gmres 48-201, simplegmres 23-61, invtrisup 72-100
+  src/matrices.f90      M_Tr_front 166-190, Part_to_Whole 193-203
   src/csd_post.f90      yetamu_solve 313-367, INIT_u_bg 442-479,
                         calc_uo_bg 497-522
   src/tensors.f90       EI_transY2 / EIN_transY2 890-919
   src/mymodules.f90     dimensionless viscosity mu_f 816,846
+(the overlap corrections are restated in rsd_oracle.c).
 
 Parity status: the free-space pair tensors, the Y2 projection and MATREV are
 pinned against the reference's tablefar.txt (see tests/test_oracle_pins.py);
-the periodic Ewald sum, the lubrication assembly and the solve chain are
-restated from source with no reference outputs to pin them (parity unpinned
-for those parts).
+the overlap blocks for equal spheres against the published
+Rotne-Prager-Yamakawa forms (tests/test_overlap.py); the periodic Ewald sum,
+the lubrication assembly and the solve chain are restated from source with
+no reference outputs to pin them (parity unpinned for those parts).
 """
 from __future__ import annotations
 
