@@ -17,6 +17,9 @@ Fortran driver (host-side Python, no GPU).
   yeta_mu.txt         main.f90:197-201: T yeta_mu(1:5) LB(1) frequency GAMMA
                       GAMMAangle, format (12ES24.15)
 
+A run resumes from the last output.VTF frame written as a hot start
+(hot_start_from_vtf), the reference's own checkpoint.
+
 List-directed input follows Fortran's rules for what these files hold:
 values separated by blanks or commas, repeat counts r*c, logicals written
 T/F/.true./.false./true/false (the first letter after an optional period),
@@ -197,6 +200,26 @@ def read_vtf(path):
             if line.strip():
                 rows.append(read_values(line, "r" * 8, "%s:%d" % (path, i + 1)))
     return rows
+
+
+def hot_start_from_vtf(vtf_path, LB, init_path):
+    """Checkpoint / resume as the reference does it: the last frame of an
+    output.VTF (its trailing records with one time value) written as a
+    hot-start initial_config.dat.  A frame holds the state at the start of
+    its step, so the resumed run repeats that step."""
+    rows = read_vtf(vtf_path)
+    if not rows:
+        raise FormatError("%s: no records" % vtf_path)
+    T = rows[-1][0]
+    k = len(rows)
+    while k > 0 and rows[k - 1][0] == T:
+        k -= 1
+    frame = rows[k:]
+    conf = [r[1:4] for r in frame]
+    radii = [r[4] for r in frame]
+    U = [u for r in frame for u in r[5:8]]
+    write_initial_config(init_path, conf, radii, LB, T=T, U_pos=U)
+    return len(frame), T
 
 
 def yeta_record(T, yeta_mu, L, frequency, gamma, gamma_angle):

@@ -85,3 +85,31 @@ def test_unsupported_settings_are_refused(drv, tmp_path):
     with pytest.raises(ValueError) as e:
         driver.check_supported(c, d)
     assert "IsPeriod" in str(e.value) and "conglomerates" in str(e.value)
+
+
+def test_resume_from_the_last_frame(drv, tmp_path):
+    """Checkpoint / resume: the last output.VTF frame of a four-step run as a
+    hot start; one more step from it lands exactly on the four-step run's
+    final configuration (the frame is the state before the last step)."""
+    driver, files = drv
+    control = control_for_periodic_fts(tmp_path)
+    pos, radii, L = configs().packing(8, 0.2, 0.05, seed=20261100)
+    init = str(tmp_path / "initial_config.dat")
+    files.write_initial_config(init, pos, radii, [L, L, L])
+    tab = o.LubTab(LUBDAT)
+
+    def step(conf, r, T, dt, LB, gamma, mu_f, ews):
+        return o.stepper_stokesian(conf, r, LB, T, dt, gamma, mu_f, ews, tab)
+
+    vtf = str(tmp_path / "output.VTF")
+    first = driver.run(control, init, step, vtf, str(tmp_path / "yeta_mu.txt"))
+    LB = files.read_initial_config(init)["LB"]
+    hot = str(tmp_path / "initial_config_hot.dat")
+    n, T = files.hot_start_from_vtf(vtf, LB, hot)
+    assert n == 8 and T == pytest.approx(3e-3, abs=1e-15)
+    d = files.read_initial_config(hot)
+    assert d["hot_start"] and len(d["U_pos"]) == 24
+    second = driver.run(control, hot, step, str(tmp_path / "o2.VTF"), str(tmp_path / "y2.txt"), max_steps=1)
+    assert second["steps"] == 1
+    # the frame's positions went through 15-digit records
+    assert np.abs(second["conf"] - first["conf"]).max() <= 1e-13 * L
