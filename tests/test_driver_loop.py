@@ -113,3 +113,17 @@ def test_resume_from_the_last_frame(drv, tmp_path):
     assert second["steps"] == 1
     # the frame's positions went through 15-digit records
     assert np.abs(second["conf"] - first["conf"]).max() <= 1e-13 * L
+
+
+@pytest.mark.parametrize("key,value", [("useDEM", True), ("useDEMstepper", True), ("Boundary", True),
+                                       ("wall_method", True), ("BROWN", True), ("Oscillation_shear", True),
+                                       ("IsPeriod", False), ("FTS_method", False), ("IsCaseLattice", 2)])
+def test_each_unsupported_setting_is_named(drv, tmp_path, key, value):
+    driver, files = drv
+    c = files.read_control(control_for_periodic_fts(tmp_path))
+    d = {"K_rb": 0, "F_rb": 0}
+    driver.check_supported(c, d)  # the periodic FTS case passes
+    c[key] = value
+    with pytest.raises(ValueError) as e:
+        driver.check_supported(c, d)
+    assert key in str(e.value)
