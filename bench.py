@@ -90,12 +90,16 @@ def measured_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons during the timed region."""
+    """nvidia-smi clocks and throttle reasons during the timed region; the
+    raw samples go to RSD_CLOCKS_DIR (default: the system's temporary
+    directory), their summary into the JSON line."""
 
     def __init__(self, index):
+        import tempfile
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
+        folder = os.environ.get("RSD_CLOCKS_DIR", tempfile.gettempdir())
+        self.path = os.path.join(folder, "clocks_%d.csv" % os.getpid())
 
     def start(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
