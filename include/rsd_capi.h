@@ -142,21 +142,21 @@ int rsd_per_grpery_inv_fri_dev(rsd_ctx* ctx, int32_t nn, const double* d_pos, co
 
 /* Allocation-free variant of rsd_per_grpery_inv_fri_dev.  No counterpart in
  * the reference: it serves callers that cannot call cudaMalloc -- programs
- * that give all device memory to their own fixed pool at start, code that
- * runs while a CUDA graph is being captured, and time-step loops that cannot
- * afford the device-wide synchronisation cudaMalloc/cudaFree imply.  It
- * takes no context, allocates nothing and runs on `stream` (a cudaStream_t,
- * NULL for the default stream) on the current device; the caller passes the
- * inputs and the output, as in the _dev entry point.  Its one scratch
- * buffer, the reciprocal-vector weight table, is a static device array of
- * about 1.6 MB that every GPU loading the library holds until exit; it fits
- * at most 2456 reciprocal vectors in the half space (NI <= 8), and a larger
- * request returns RSD_ELIMIT before any kernel that writes the output runs.
- * All calls on a device share that array and it keeps the last call's
- * contents: calls that overlap on the GPU race and must be serialised by the
- * caller.  The first call on each device looks the array's address up; make
- * it before any stream capture.  Returns once the work is enqueued (after one
- * small synchronous read of the radii's cube sum). */
+ * that give all device memory to their own fixed pool at start, and
+ * time-step loops that cannot afford the device-wide synchronisation
+ * cudaMalloc/cudaFree imply.  It takes no context, allocates nothing and runs
+ * on `stream` (a cudaStream_t, NULL for the default stream) on the current
+ * device; the caller passes the inputs and the output, as in the _dev entry
+ * point.  Its one scratch buffer, the reciprocal-vector weight table, is a
+ * static device array of about 1.6 MB that every GPU loading the library
+ * holds until exit; it fits at most 2456 reciprocal vectors in the half space
+ * (NI <= 8: EWS_ERR above about 5e-88 in a cubic box), and a larger request
+ * returns RSD_ELIMIT before any kernel that writes the output runs.  All
+ * calls on a device share that array and it keeps the last call's contents:
+ * calls that overlap on the GPU race and must be serialised by the caller.
+ * The first call on each device looks the array's address up with that
+ * device current.  The call synchronises `stream` once, to read the radii's
+ * cube sum back for NR, NI and phi, and returns once the rest is enqueued. */
 int rsd_per_grpery_inv_fri_static(int32_t nn, const double* d_pos, const double* d_radii, rsd_lattice* lat,
                                   double ews_err, double mu_f, double* d_grmobmx, int64_t ldm, void* stream);
 

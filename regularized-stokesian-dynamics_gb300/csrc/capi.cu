@@ -244,8 +244,12 @@ static void eig3(const double Ain[9], double ev[3]) {
   for (int i = 0; i < 3; i++) ev[i] = a[i][i];
 }
 
-extern "C" int rsd_calc_lattice_inverse(rsd_lattice* lat, double ews_err, int32_t nn, const double* radii) {
-  if (!lat || !radii || nn < 1 || !(ews_err > 0.0) || !(lat->LV > 0.0)) return RSD_EARG;
+// CALC_LATTICE_INVERSE (src/csd_post.f90:158-183) for a given cube sum of
+// the radii: the one place that derives lammda, NR, NI and phi, shared by
+// rsd_calc_lattice_inverse and the allocation-free assembly (which reduces
+// the cube sum on the device).
+int rsd_lattice_params(rsd_lattice* lat, double ews_err, double sum_a3) {
+  if (!lat || !(ews_err > 0.0) || !(lat->LV > 0.0)) return RSD_EARG;
   lat->sig = pow(lat->LV, 1.0 / 3.0) / sqrt(2.0 * RSD_PI);
   lat->lammda = sqrt(RSD_PI) / pow(lat->LV, 1.0 / 3.0);
   lat->logerr = -log(ews_err);
@@ -261,11 +265,16 @@ extern "C" int rsd_calc_lattice_inverse(rsd_lattice* lat, double ews_err, int32_
   const double lmin = fmin(le[0], fmin(le[1], le[2])), lmax = fmax(le[0], fmax(le[1], le[2]));
   lat->NR = (int)(sqrt(2.0 * lat->logerr * (lat->sig * lat->sig) / lmin) + 1);
   lat->NI = (int)(sqrt(lat->logerr / (2.0 * (RSD_PI * RSD_PI) * (lat->sig * lat->sig) * (1.0 / lmax))) + 1);
-  double s3 = 0.0;
-  for (int i = 0; i < nn; i++) s3 += radii[i] * radii[i] * radii[i];
-  lat->phi = s3 * 4.0 / 3.0 * RSD_PI / lat->LV;
+  lat->phi = sum_a3 * 4.0 / 3.0 * RSD_PI / lat->LV;
   if (lat->NR > 40 || lat->NI > 40) return RSD_EARG;  // absurd lattice
   return RSD_OK;
+}
+
+extern "C" int rsd_calc_lattice_inverse(rsd_lattice* lat, double ews_err, int32_t nn, const double* radii) {
+  if (!lat || !radii || nn < 1) return RSD_EARG;
+  double s3 = 0.0;
+  for (int i = 0; i < nn; i++) s3 += radii[i] * radii[i] * radii[i];
+  return rsd_lattice_params(lat, ews_err, s3);
 }
 
 // ------------------------------------------------------------ lub tables

@@ -2,26 +2,31 @@
 // rsd_per_grpery_inv_fri_dev), for callers that cannot call cudaMalloc:
 // applications that hand all device memory to their own fixed pool at start
 // (a Fortran driver with a static memory budget, a framework with a caching
-// allocator), code running while a CUDA graph is being captured, and loops
-// that must not pay the device-wide synchronisation cudaMalloc and cudaFree
-// imply.  The caller still passes inputs and outputs; the only scratch, the
-// table of reciprocal-vector weights, lives in the file-scope array below.
+// allocator), and loops that must not pay the device-wide synchronisation
+// cudaMalloc and cudaFree imply.  The caller still passes inputs and outputs;
+// the only scratch, the table of reciprocal-vector weights, lives in the
+// file-scope array below.
 //
 // Limits and sharing:
 //   - at most RSD_NOALLOC_MAX_KVEC reciprocal vectors in the half space, i.e.
-//     NI <= 8 (EWS_ERR >= ~1e-25 in a cubic box); larger requests return
-//     RSD_ELIMIT before anything is launched;
+//     NI <= 8.  In a cubic box NI = int(sqrt(-ln(EWS_ERR)/pi)) + 1, so that
+//     holds for EWS_ERR above about 5e-88; a sheared lattice has a larger NI
+//     for the same EWS_ERR, so there EWS_ERR must stay above a larger value.  Larger requests return
+//     RSD_ELIMIT before any kernel that writes the output runs;
 //   - every GPU that loads the library holds the array (~1.6 MB) until the
 //     process exits;
 //   - every call on a device uses the same array and it keeps the last
 //     call's contents; calls that overlap on the GPU (other streams, other
 //     host threads) race on it and must be serialised by the caller;
 //   - the first call on a device looks the array's address up with
-//     cudaGetSymbolAddress; make that first call before any stream capture.
+//     cudaGetSymbolAddress, with that device current;
+//   - the call reads the radii's cube sum back to the host (one small
+//     synchronous copy on `stream`) to derive NR, NI and phi.
 // The pair kernel evaluates sincos(k.R) per pair instead of reading the
 // per-particle trig table the allocating path keeps.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstring>
 
@@ -37,7 +42,9 @@ static __device__ __align__(256) double rsd_noalloc_scratch[RSD_NOALLOC_DOUBLES]
 namespace {
 
 constexpr int NA_MAXDEV = 64;
-double* g_scratch[NA_MAXDEV] = {};  // device address of rsd_noalloc_scratch, per device
+// device address of rsd_noalloc_scratch, per device; host threads making
+// their first calls at the same time each look it up and store the same value
+std::atomic<double*> g_scratch[NA_MAXDEV] = {};
 
 __device__ inline void na_half_space_index(int h, int NI, int* nx, int* ny, int* nz) {
   const int w = 2 * NI + 1;
@@ -249,48 +256,6 @@ __global__ void __launch_bounds__(64) na_self(int nn, rsd_lat_dev L, int Kh, con
     for (int y = 0; y < 5; y++) M[(6 * N + 5 * a + x) + (int64_t)(6 * N + 5 * a + y) * ldm] = qq[x][y];
 }
 
-// CALC_LATTICE_INVERSE (src/csd_post.f90:158-183) with the radii's cube sum
-// already reduced on the device
-int na_lattice(rsd_lattice* lat, double ews_err, double sum_a3) {
-  if (!(ews_err > 0.0) || !(lat->LV > 0.0)) return RSD_EARG;
-  lat->sig = pow(lat->LV, 1.0 / 3.0) / sqrt(2.0 * RSD_PI);
-  lat->lammda = sqrt(RSD_PI) / pow(lat->LV, 1.0 / 3.0);
-  lat->logerr = -log(ews_err);
-  double a[3][3];
-  for (int i = 0; i < 3; i++)
-    for (int j = 0; j < 3; j++) {
-      double s = 0.0;
-      for (int k = 0; k < 3; k++) s += lat->LR[k + 3 * i] * lat->LR[k + 3 * j];
-      a[i][j] = s;
-    }
-  for (int sweep = 0; sweep < 60; sweep++) {  // eigenvalues by cyclic Jacobi
-    if (a[0][1] == 0.0 && a[0][2] == 0.0 && a[1][2] == 0.0) break;
-    for (int p = 0; p < 2; p++)
-      for (int q = p + 1; q < 3; q++) {
-        if (a[p][q] == 0.0) continue;
-        const double th = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
-        const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-        for (int k = 0; k < 3; k++) {
-          const double x = a[k][p], y = a[k][q];
-          a[k][p] = c * x - s * y;
-          a[k][q] = s * x + c * y;
-        }
-        for (int k = 0; k < 3; k++) {
-          const double x = a[p][k], y = a[q][k];
-          a[p][k] = c * x - s * y;
-          a[q][k] = s * x + c * y;
-        }
-      }
-  }
-  const double lmin = fmin(a[0][0], fmin(a[1][1], a[2][2])), lmax = fmax(a[0][0], fmax(a[1][1], a[2][2]));
-  lat->NR = (int)(sqrt(2.0 * lat->logerr * (lat->sig * lat->sig) / lmin) + 1);
-  lat->NI = (int)(sqrt(lat->logerr / (2.0 * (RSD_PI * RSD_PI) * (lat->sig * lat->sig) * (1.0 / lmax))) + 1);
-  lat->phi = sum_a3 * 4.0 / 3.0 * RSD_PI / lat->LV;
-  if (lat->NR > 40 || lat->NI > 40) return RSD_EARG;
-  return RSD_OK;
-}
-
 }  // namespace
 
 extern "C" int rsd_per_grpery_inv_fri_static(int32_t nn, const double* d_pos, const double* d_radii,
@@ -299,16 +264,17 @@ extern "C" int rsd_per_grpery_inv_fri_static(int32_t nn, const double* d_pos, co
   if (nn < 1 || !d_pos || !d_radii || !lat || !d_grmobmx || ldm < 11LL * nn || !(mu_f > 0)) return RSD_EARG;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAXDEV) return RSD_ECUDA;
-  if (!g_scratch[dev]) {
+  double* scratch = g_scratch[dev].load(std::memory_order_acquire);
+  if (!scratch) {
     // set-up, once per device, with that device current
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, rsd_noalloc_scratch) != cudaSuccess || !p) {
       cudaGetLastError();
       return RSD_ECUDA;
     }
-    g_scratch[dev] = (double*)p;
+    scratch = (double*)p;
+    g_scratch[dev].store(scratch, std::memory_order_release);
   }
-  double* scratch = g_scratch[dev];
   cudaStream_t s = (cudaStream_t)stream;
   // the cube sum of the radii is the only value that starts the call at
   // zero; it is written whole by one block, so nothing needs clearing
@@ -318,7 +284,7 @@ extern "C" int rsd_per_grpery_inv_fri_static(int32_t nn, const double* d_pos, co
   if (cudaMemcpyAsync(&sum_a3, d_sum, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return RSD_ECUDA;
-  int rc = na_lattice(lat, ews_err, sum_a3);
+  int rc = rsd_lattice_params(lat, ews_err, sum_a3);
   if (rc != RSD_OK) return rc;
   const int w = 2 * lat->NI + 1;
   const int Kh = (w * w * w - 1) / 2;

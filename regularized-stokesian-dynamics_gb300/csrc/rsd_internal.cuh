@@ -81,6 +81,9 @@ struct rsd_lat_dev {
   int NR, NI;
 };
 rsd_lat_dev rsd_lat_pack(const rsd_lattice* lat);
+// CALC_LATTICE_INVERSE's derived values (lammda, sig, logerr, NR, NI, phi)
+// from lat->LR, lat->LV, EWS_ERR and the cube sum of the radii (capi.cu)
+int rsd_lattice_params(rsd_lattice* lat, double ews_err, double sum_a3);
 
 // PER_SKEW_CORRECTION (src/csd_post.f90:24-63): minimum image in the
 // skewed lattice, testing the 8 corner shifts like the reference.

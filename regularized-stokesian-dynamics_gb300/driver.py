@@ -12,8 +12,13 @@ viscosity mu_f -> 1/pi, BASE_DT, T0 and END_TIME times lambda_time; the
 shear rate GAMMA = Gamma_alpha / lambda_time (main.f90:147-151); times are
 written divided by lambda_time.  The start time is the first column of
 initial_config.dat's last particle record (INITIAL_CONF reads T from every
-record).  The step itself is a callable, so that the same loop runs the GPU
-step or, in tests, the oracle's:
+record).  Those times were written divided by lambda_time and INITIAL_CONF
+reads them back unscaled, so with lambda_time != 1 the reference resumes a
+hot start at T / lambda_time in internal units (the wrong time and shear
+strain); run() does the same by default, and hot_start_time_scaled=True
+multiplies the start time by lambda_time, which makes a resume exact.  The
+step itself is a callable, so that the same loop runs the GPU step or, in
+tests, the oracle's:
 
     step(conf (N x 3), radii, T, dt, LB, gamma, mu_f, ews_err)
         -> dict(conf=..., U_pos=... (6N), yeta_mu=... (5))
@@ -39,9 +44,11 @@ def check_supported(control, init):
         raise ValueError("not covered by this driver: " + ", ".join(bad))
 
 
-def run(control_path, init_path, step, vtf_path, yeta_path, max_steps=None):
+def run(control_path, init_path, step, vtf_path, yeta_path, max_steps=None, hot_start_time_scaled=False):
     """Runs the loop; returns the last configuration, U_pos, T (in the
-    file's time unit) and the number of steps."""
+    file's time unit) and the number of steps.  hot_start_time_scaled: take
+    initial_config.dat's time as written in the file's unit (T / lambda_time)
+    and scale it back; the default reads it unscaled, as the reference does."""
     c = files.read_control(control_path)
     d = files.read_initial_config(init_path)
     check_supported(c, d)
@@ -58,7 +65,10 @@ def run(control_path, init_path, step, vtf_path, yeta_path, max_steps=None):
     U_pos = np.zeros(6 * N)
     if d["U_pos"] is not None:
         U_pos[:3 * N] = d["U_pos"]
-    T = d["T"][-1] if d["T"] else c["T0"] * lam_time
+    if d["T"]:
+        T = d["T"][-1] * (lam_time if hot_start_time_scaled else 1.0)
+    else:
+        T = c["T0"] * lam_time
     k = 0
     with open(vtf_path, "w") as vtf, open(yeta_path, "w") as yeta:
         while True:

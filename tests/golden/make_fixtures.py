@@ -5,6 +5,8 @@ on the GPU machines, so the outputs are committed):
 
     python tests/golden/make_fixtures.py /path/to/reference
 
+(or with the checkout's path in the environment variable RSD_REFERENCE).
+
 Writes
   tests/golden/tablefar_equal.txt  the equal-sphere rows (lambda = 1) of the
       reference's own output table src/lubrication tabel/FarfieldForce/
@@ -55,4 +57,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("RSD_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_fixtures.py <reference checkout> (or set RSD_REFERENCE)")
+    main(ref)

@@ -115,6 +115,40 @@ def test_resume_from_the_last_frame(drv, tmp_path):
     assert np.abs(second["conf"] - first["conf"]).max() <= 1e-13 * L
 
 
+def test_resume_with_a_time_unit_other_than_one(drv, tmp_path):
+    """radii_test / radii_true = 2, so lambda_time = 2 and output.VTF holds
+    T / 2.  Read back unscaled, as the reference's INITIAL_CONF does, the
+    resume starts at half the time (another shear strain, so another
+    configuration); with hot_start_time_scaled it continues exactly."""
+    driver, files = drv
+    control = control_for_periodic_fts(tmp_path)
+    lines = open(control).read().split("\n")
+    lines[18] = "2.0    ! set by the test"  # radii_test
+    open(control, "w").write("\n".join(lines))
+    c = files.read_control(control)
+    assert c["radii_test"] / c["radii_true"] == 2.0
+    pos, radii, L = configs().packing(8, 0.2, 0.05, seed=20261101)
+    init = str(tmp_path / "initial_config.dat")
+    files.write_initial_config(init, pos, radii, [L, L, L])
+    tab = o.LubTab(LUBDAT)
+
+    def step(conf, r, T, dt, LB, gamma, mu_f, ews):
+        return o.stepper_stokesian(conf, r, LB, T, dt, gamma, mu_f, ews, tab)
+
+    first = driver.run(control, init, step, str(tmp_path / "output.VTF"), str(tmp_path / "yeta_mu.txt"))
+    assert first["steps"] == 4
+    hot = str(tmp_path / "initial_config_hot.dat")
+    n, T = files.hot_start_from_vtf(str(tmp_path / "output.VTF"), files.read_initial_config(init)["LB"], hot)
+    assert T == pytest.approx(3e-3, abs=1e-15)  # file unit: internal 6e-3 / 2
+    exact = driver.run(control, hot, step, str(tmp_path / "o2.VTF"), str(tmp_path / "y2.txt"), max_steps=1,
+                       hot_start_time_scaled=True)
+    assert exact["T"] == pytest.approx(4e-3, abs=1e-15)
+    assert np.abs(exact["conf"] - first["conf"]).max() <= 1e-13 * L
+    as_ref = driver.run(control, hot, step, str(tmp_path / "o3.VTF"), str(tmp_path / "y3.txt"), max_steps=1)
+    assert as_ref["T"] == pytest.approx(2.5e-3, abs=1e-15)
+    assert np.abs(as_ref["conf"] - first["conf"]).max() > 1e-9 * L
+
+
 @pytest.mark.parametrize("key,value", [("useDEM", True), ("useDEMstepper", True), ("Boundary", True),
                                        ("wall_method", True), ("BROWN", True), ("Oscillation_shear", True),
                                        ("IsPeriod", False), ("FTS_method", False), ("IsCaseLattice", 2)])

@@ -1,10 +1,10 @@
 """The allocation-free grand-mobility entry point, through the C-ABI.
 
 rsd_per_grpery_inv_fri_static is for callers that cannot call cudaMalloc
-(a host program whose device memory is all in its own pool, work issued
-while a CUDA graph is captured, loops that cannot take cudaMalloc's device
-synchronisation).  Its only scratch is a static device array shared by all
-calls, so this test makes two calls in a row with different sizes and
+(a host program whose device memory is all in its own pool, loops that
+cannot take cudaMalloc's device synchronisation).  Its only scratch is a
+static device array shared by all calls, so this test makes two calls in a
+row with different sizes and
 lattices -- the second must not see the first one's table -- and compares
 each with the allocating entry point rsd_per_grpery_inv_fri_dev, to the
 1e-12 relative tolerance of the mobility parity tests.  It also checks that
