@@ -110,6 +110,17 @@ int rsd_ctx_set_mixed_real_passes(rsd_ctx* ctx, int32_t passes);
  * form for the pairs whose minimum image overlaps. */
 int rsd_ctx_set_correction_method(rsd_ctx* ctx, int32_t method);
 
+/* Bounds of the device-side waits of the mixed form's FP32 kernels (no
+ * counterpart in the reference): every mbarrier wait of the tensor-core
+ * GEMMs gives up after tc_wait_ns nanoseconds (0: the default, 0.5 s), and
+ * every wait of the refinement's dataflow triangular sweeps after
+ * tri_spin_polls polls of at least 64 ns (0: the default, 2^21).  A wait
+ * that gives up ends its kernel without a fault: the kernel drains the
+ * copies and MMAs it issued, frees its tensor memory, skips its stores and
+ * raises an error word; the call returns RSD_ETIMEOUT and the context stays
+ * usable.  Values far below the defaults only serve to exercise that path. */
+int rsd_ctx_set_wait_limits(rsd_ctx* ctx, int64_t tc_wait_ns, int64_t tri_spin_polls);
+
 /* ---------------------------------------------------------------- lattice */
 /* SET_LATTICE_SKEW (src/csd_post.f90:105-136) with MAT_INV3
  * (src/tensors.f90:704-726): fills lat->LR, LI, LV for strain time T. */

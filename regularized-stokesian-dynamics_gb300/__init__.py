@@ -101,6 +101,7 @@ _sig("rsd_ctx_set_mixed_truncation", _i, [_vp, _d, _d])
 _sig("rsd_ctx_set_mixed_lambda_scale", _i, [_vp, _d])
 _sig("rsd_ctx_set_mixed_real_passes", _i, [_vp, _i32])
 _sig("rsd_ctx_set_correction_method", _i, [_vp, _i32])
+_sig("rsd_ctx_set_wait_limits", _i, [_vp, _i64, _i64])
 _sig("rsd_syrk_f32_dev", _i, [_vp, _i32, _i32, _vp, _i64, _vp, _i64, _i32])
 _sig("rsd_potrf_f32_dev", _i, [_vp, _i32, _vp, _i64, _i32, _ip])
 _sig("rsd_potri_f32_dev", _i, [_vp, _i32, _vp, _i64, _i32])
@@ -174,6 +175,12 @@ class Context:
         """Overlap corrections in the fused step (correction_method of
         per_GRPY_YZD.f90:98-116: 0 none, 1 Yamakawa, 2 regularized)."""
         self.check(_lib.rsd_ctx_set_correction_method(self.h, int(method)))
+
+    def set_wait_limits(self, tc_wait_ns=0, tri_spin_polls=0):
+        """Bounds of the mixed form's device-side waits (0: the defaults,
+        0.5 s and 2^21 polls); a wait that gives up makes the call return
+        RSD_ETIMEOUT."""
+        self.check(_lib.rsd_ctx_set_wait_limits(self.h, int(tc_wait_ns), int(tri_spin_polls)))
 
     def set_tensor_cores(self, mode=1):
         """FP32 factorisations of the mixed form: 1 (or True, the default)

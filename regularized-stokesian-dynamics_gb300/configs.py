@@ -16,6 +16,14 @@ stays >= 1e-4 a.
 Gaps are measured with the minimum image of the unsheared cubic lattice; a
 step at strain gamma T shifts images by L gamma T along x, so runs start at
 T = 0 like the reference's shear start-up.
+
+sheared_packing() gives a configuration for a run that is already at strain
+s (the Lees-Edwards lattice with LR(1,3) = s L, csd_post.f90:105-136): the
+packing above is sheared affinely, x += ds z, in increments of the lattice's
+skew (the images follow the same affine map, so every pair, across the
+boundary too, moves continuously), and after each increment overlapping
+pairs (gap below g_min in the sheared minimum image) are pushed apart along
+their centre line until none is left.
 """
 from __future__ import annotations
 
@@ -151,6 +159,94 @@ def min_gap(pos, L, a=1.0):
         d = _min_image(pos[i + 1:] - pos[i], L)
         best = min(best, float(np.sqrt(np.min(np.einsum("ij,ij->i", d, d)))) - 2 * a)
     return best
+
+
+def _sheared_lattice(L, skew):
+    LR = np.diag([L, L, L]).astype(float)
+    LR[0, 2] = skew * L
+    return LR, np.linalg.inv(LR)
+
+
+_SHIFTS = np.array([[i, j, k] for i in (-1, 0, 1) for j in (-1, 0, 1) for k in (-1, 0, 1)], dtype=float)
+
+
+def sheared_min_image(d, LR, LI):
+    """Minimum images of separations d (..., 3) in the lattice LR (skew in
+    [0, 1]): the nearest of the 27 cells around the rounded fractional
+    coordinates."""
+    u = d @ LI.T
+    u -= np.round(u)
+    c = (u[..., None, :] + _SHIFTS) @ LR.T
+    k = np.argmin(np.einsum("...ij,...ij->...i", c, c), axis=-1)
+    return np.take_along_axis(c, k[..., None, None], axis=-2)[..., 0, :]
+
+
+def _pairs_within(pos, L, skew, cut, chunk=512):
+    """Pairs i < j whose minimum image is closer than cut (< L/2), with the
+    integer lattice shift n of that image: d_ij = pos[j] - pos[i] + LR n.
+    For such a pair the shift along z (and y) is the one that brings that
+    coordinate within L/2, and then the one along x the same for x
+    (LR = [[L, 0, skew L], [0, L, 0], [0, 0, L]])."""
+    N = len(pos)
+    ii, jj, nn = [], [], []
+    for a in range(0, N, chunk):
+        d = pos[None, :, :] - pos[a:a + chunk, None, :]
+        n3 = -np.round(d[..., 2] / L)
+        n2 = -np.round(d[..., 1] / L)
+        x = d[..., 0] + skew * L * n3
+        n1 = -np.round(x / L)
+        r2 = (x + L * n1) ** 2 + (d[..., 1] + L * n2) ** 2 + (d[..., 2] + L * n3) ** 2
+        i, j = np.nonzero(r2 < cut * cut)
+        keep = j > i + a
+        i, j = i[keep], j[keep]
+        ii.append(i + a)
+        jj.append(j)
+        nn.append(np.stack([n1[i, j], n2[i, j], n3[i, j]], -1))
+    return np.concatenate(ii), np.concatenate(jj), np.concatenate(nn)
+
+
+def sheared_min_gap(pos, L, skew, a=1.0):
+    """Smallest surface gap in the lattice of skew `skew` (0 <= skew <= 1)."""
+    LR, LI = _sheared_lattice(L, skew)
+    i, j, n = _pairs_within(pos, L, skew, 2 * a + 1.0)
+    if len(i) == 0:
+        return np.inf
+    d = pos[j] - pos[i] + n @ LR.T
+    return float(np.sqrt(np.einsum("ij,ij->i", d, d)).min()) - 2 * a
+
+
+def sheared_packing(N, phi, g_min, seed, strain, sweeps=200, near_contact=False, a=1.0, dskew=0.005):
+    """A packing valid at Lees-Edwards skew mod(strain, 1): every surface gap
+    in the sheared minimum image is at least g_min (near_contact pairs keep
+    at least 1e-4 a).  Positions are wrapped into the sheared cell."""
+    pos, radii, L = packing(N, phi, g_min, seed, sweeps=sweeps, near_contact=near_contact, a=a)
+    target = float(strain) % 1.0
+    hard = 2 * a + (1e-4 * a if near_contact else g_min * a)
+    push = hard + 0.01 * a
+    skew, nlist_at = 0.0, -1.0
+    while skew < target:
+        ds = min(dskew, target - skew)
+        pos[:, 0] += ds * pos[:, 2]  # affine shear of the positions with the lattice
+        skew += ds
+        LR, LI = _sheared_lattice(L, skew)
+        if skew - nlist_at > 0.05:
+            i, j, n = _pairs_within(pos, L, skew, 2 * a + 1.0)
+            nlist_at = skew
+        for _ in range(2000):
+            d = pos[j] - pos[i] + n @ LR.T
+            r = np.sqrt(np.einsum("ij,ij->i", d, d))
+            bad = r < hard
+            if not bad.any():
+                break
+            u = d[bad] / r[bad, None] * (0.5 * (push - r[bad]))[:, None]
+            np.add.at(pos, i[bad], -u)
+            np.add.at(pos, j[bad], u)
+        else:
+            raise RuntimeError("sheared packing: overlaps remain at skew %.3f" % skew)
+    LR, LI = _sheared_lattice(L, target)
+    u = pos @ LI.T
+    pos = (u - np.floor(u)) @ LR.T
+    return pos, radii, L
 
 
 # Workloads by number: the configurations the step is measured and checked on.

@@ -158,6 +158,14 @@ extern "C" int rsd_ctx_set_correction_method(rsd_ctx* c, int method) {
   return RSD_OK;
 }
 
+extern "C" int rsd_ctx_set_wait_limits(rsd_ctx* c, int64_t tc_wait_ns, int64_t tri_spin_polls) {
+  if (!c) return RSD_EARG;
+  if (tc_wait_ns < 0 || tri_spin_polls < 0) return rsd_fail(c, RSD_EARG, "wait limits must be >= 0");
+  c->tc_wait_ns = tc_wait_ns;
+  c->tri_spin_polls = tri_spin_polls;
+  return RSD_OK;
+}
+
 extern "C" int rsd_ctx_set_mixed_real_passes(rsd_ctx* c, int passes) {
   if (!c) return RSD_EARG;
   if (passes < 1 || passes > 4) return rsd_fail(c, RSD_EARG, "mixed real-space passes must be 1 to 4");

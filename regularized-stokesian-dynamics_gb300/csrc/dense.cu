@@ -1460,7 +1460,8 @@ __global__ void transpose_block(int nb2, const float* __restrict__ W, float* __r
 // task a CTA waits for was taken earlier by a running CTA (no deadlock).  A
 // finished part is published by data, fence and a per-block counter; a
 // block is usable once all TRI_Q of its parts are in.  Waits are bounded
-// (TRI_SPIN_LIMIT polls); a timeout sets *err and every CTA leaves its loop.
+// (the context's poll limit, TRI_SPIN_LIMIT by default); a timeout sets *err
+// and every CTA leaves its loop.
 constexpr int TRI_Q = 16, TRI_QS = NB2 / TRI_Q;  // parts per block, columns/rows per part
 constexpr int TRI_THREADS = 256;
 constexpr long long TRI_SPIN_LIMIT = 1LL << 21;  // polls of >= 64 ns: a fraction of a second
@@ -1476,6 +1477,7 @@ struct TriArgs {
   int* ticket;
   int* err;
   int b0;           // forward: blocks before b0 are zero on entry (and stay zero)
+  long long spin;   // polls before a wait gives up
 };
 
 // waits until all parts of block blk are published (thread 0 of the CTA)
@@ -1486,7 +1488,7 @@ __device__ __forceinline__ void tri_wait(const TriArgs& A, int blk, volatile int
       *abort_s = 1;
       return;
     }
-    if (++it > TRI_SPIN_LIMIT) {
+    if (++it > A.spin) {
       atomicExch(A.err, 1);
       *abort_s = 1;
       return;
@@ -1745,7 +1747,8 @@ int rsd_uhat_solve(rsd_ctx* ctx, const rsd_uhat* h, float* X, int64_t ldx, int n
   // leading zero blocks of the right-hand side: the forward sweep starts at
   // the first block that can be nonzero (z is zero before it)
   const int b0 = zero_lead > 0 ? min(zero_lead / NB2, nblk2 - 1) : 0;
-  TriArgs A{h->Uh, h->ld, n, nblk2, X, ldx, sync + 2, sync + 1, sync, b0};
+  TriArgs A{h->Uh, h->ld, n, nblk2, X, ldx, sync + 2, sync + 1, sync, b0,
+            ctx->tri_spin_polls > 0 ? ctx->tri_spin_polls : TRI_SPIN_LIMIT};
   const int tasks = TRI_Q * (nblk2 - 1);
   const int grid = max(1, min(tasks, 4 * gsm));
   const int ftasks = TRI_Q * (nblk2 - 1 - b0);

@@ -39,6 +39,8 @@ struct rsd_ctx {
   int mixed_real_passes = 1;  // mixed assembly, equal radii: passes over the near images (moment parts)
   double mixed_lambda_scale = 1.75;  // mixed assembly: Ewald splitting parameter relative to the reference's
   int correction_method = 0;  // fused step: overlap corrections of the grand mobility (0, 1 or 2)
+  long long tc_wait_ns = 0;      // bound of the tensor-core kernels' mbarrier waits (0: 0.5 s)
+  long long tri_spin_polls = 0;  // bound of the dataflow sweeps' waits in polls (0: 2^21)
   cudaStream_t side = nullptr;  // higher-priority stream for look-ahead panels
   cudaEvent_t ev_panel = nullptr, ev_next = nullptr;
   int* d_info = nullptr;  // device-side status words

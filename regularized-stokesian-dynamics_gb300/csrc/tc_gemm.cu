@@ -21,10 +21,11 @@
 // the K range of a tile at its first column (for triangular operands whose
 // rows below that are zero).
 //
-// Every mbarrier wait is bounded by the global timer; a timeout sets an abort
-// flag that ends every role's loop, records a code in *err, waits (bounded)
-// for the copies already issued, frees the tensor memory and skips the store.
-// The host turns the code into RSD_ETIMEOUT.
+// Every mbarrier wait is bounded by the global timer (the context's wait
+// limit, 0.5 s by default); a timeout sets an abort flag that ends every
+// role's loop, records a code in *err, waits (bounded by 0.5 s) for the TMA
+// copies and the MMAs already issued, frees the tensor memory and skips the
+// store.  The host turns the code into RSD_ETIMEOUT.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
@@ -62,6 +63,7 @@ struct TcArgs {
   int ksplit;    // > 0: CTA z sums K in [z ksplit, (z + 1) ksplit) (a multiple of TC_KC; reduce = 1)
   float alpha;
   int* err;
+  unsigned long long wait_ns;  // bound of each mbarrier wait
   // batches (ksplit = 0): CTA z adds z times these to the coordinates of A
   // (k, m), B (k, n) and C (m, n); the batch's n extent is n - z * ndec
   int zak, zam, zbk, zbn, zcm, zcn, ncols, ndec;
@@ -90,11 +92,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 // Bounded wait; false on a timeout (which raises the abort flag) or when
 // another role has aborted.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, int* err,
-                                          int code) {
+                                          int code, unsigned long long limit_ns) {
   const uint64_t t0 = global_ns();
   while (!mbar_try_wait(bar, parity)) {
     if (*abort_flag) return false;
-    if (global_ns() - t0 > TC_WAIT_NS) {
+    if (global_ns() - t0 > limit_ns) {
       *abort_flag = 1;
       atomicExch(err, code);
       return false;
@@ -207,7 +209,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcCfg<PREC>::MIN_CTAS)
       for (int s = 0; s < ST; s++) last[s] = -1;
       for (int c = 0; c < nch; c++) {
         const int s = c % ST;
-        if (c >= ST && !mbar_wait(TC_EMPTY(s), ((c / ST) - 1) & 1, &abort_flag, a.err, 1)) break;
+        if (c >= ST && !mbar_wait(TC_EMPTY(s), ((c / ST) - 1) & 1, &abort_flag, a.err, 1, a.wait_ns)) break;
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(TC_FULL(s)), "r"(2 * TC_CHUNK)
                      : "memory");
         const uint32_t st = sbase + s * SB;
@@ -227,10 +229,12 @@ __global__ void __launch_bounds__(TC_THREADS, TcCfg<PREC>::MIN_CTAS)
   } else if (warp == 1) {
     if (lane == 0) {  // MMA issuer
       bool ok = true;
+      int issued = 0;
       for (int c = 0; c < nch; c++) {
         const int s = c % ST;
-        ok = mbar_wait(PREC == 3 ? TC_CONV(s) : TC_FULL(s), (c / ST) & 1, &abort_flag, a.err, 2);
+        ok = mbar_wait(PREC == 3 ? TC_CONV(s) : TC_FULL(s), (c / ST) & 1, &abort_flag, a.err, 2, a.wait_ns);
         if (!ok) break;
+        issued = c + 1;
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t st = sbase + s * SB;
 #pragma unroll
@@ -245,7 +249,9 @@ __global__ void __launch_bounds__(TC_THREADS, TcCfg<PREC>::MIN_CTAS)
         }
         mma_commit(TC_EMPTY(s));
       }
-      if (ok && nch > 0) {
+      // `done` completes once every MMA issued here has finished (after an
+      // abort too, so that the tensor memory is not freed under them)
+      if (issued > 0) {
         mma_commit(done);
       } else {
         asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(done) : "memory");
@@ -256,7 +262,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcCfg<PREC>::MIN_CTAS)
     if (PREC == 3) {  // split each landed stage into TF32 head and tail
       for (int c = 0; c < nch; c++) {
         const int s = c % ST;
-        if (!mbar_wait(TC_FULL(s), (c / ST) & 1, &abort_flag, a.err, 3)) break;
+        if (!mbar_wait(TC_FULL(s), (c / ST) & 1, &abort_flag, a.err, 3, a.wait_ns)) break;
         unsigned char* st = base + s * SB;
 #pragma unroll
         for (int op = 0; op < 2; op++) {
@@ -285,7 +291,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcCfg<PREC>::MIN_CTAS)
     }
     // epilogue
     // warp-uniform: tcgen05.ld is a warp-collective instruction
-    const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0, &abort_flag, a.err, 4) ? 1 : 0) != 0;
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0, &abort_flag, a.err, 4, a.wait_ns) ? 1 : 0) != 0;
     if (ok) {
       asm volatile("tcgen05.fence::after_thread_sync;");
       float* sOut = reinterpret_cast<float*>(base);
@@ -332,7 +338,18 @@ __global__ void __launch_bounds__(TC_THREADS, TcCfg<PREC>::MIN_CTAS)
 #undef TC_EMPTY
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(TC_TILE));
+  if (warp == 0) {
+    if (abort_flag) {  // MMAs issued before an abort may still run: wait (bounded) for `done`
+      if (lane == 0) {
+        const uint64_t t0 = global_ns();
+        while (!mbar_try_wait(done, 0) && global_ns() - t0 < TC_WAIT_NS) {
+        }
+      }
+      __syncwarp();
+      asm volatile("tcgen05.fence::after_thread_sync;");
+    }
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(TC_TILE));
+  }
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
@@ -368,6 +385,10 @@ int encode_2d(rsd_ctx* ctx, CUtensorMap* tm, const float* ptr, uint64_t inner, u
 
 bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
+unsigned long long wait_limit(const rsd_ctx* ctx) {
+  return ctx->tc_wait_ns > 0 ? (unsigned long long)ctx->tc_wait_ns : TC_WAIT_NS;
+}
+
 }  // namespace
 
 // Nonzero when the tensor-core trailing update applies: 16-byte aligned
@@ -400,7 +421,7 @@ int rsd_tc_gemm(rsd_ctx* ctx, int prec, int m, int n, int K, float alpha, const 
   RSD_TRY(encode_2d(ctx, &tmA, A, K, m, lda, TC_KC, TC_TILE, CU_TENSOR_MAP_SWIZZLE_128B));
   RSD_TRY(encode_2d(ctx, &tmB, B, K, n, ldb, TC_KC, TC_TILE, CU_TENSOR_MAP_SWIZZLE_128B));
   RSD_TRY(encode_2d(ctx, &tmC, C, m, n, ldc, TC_TILE, TC_TILE, CU_TENSOR_MAP_SWIZZLE_NONE));
-  TcArgs a{K, tri, klo_col, reduce, ksplit, alpha, d_err, 0, 0, 0, 0, 0, 0, 0, 0};
+  TcArgs a{K, tri, klo_col, reduce, ksplit, alpha, d_err, wait_limit(ctx), 0, 0, 0, 0, 0, 0, 0, 0};
   const dim3 grid((m + TC_TILE - 1) / TC_TILE, (n + TC_TILE - 1) / TC_TILE, ksplit > 0 ? (K + ksplit - 1) / ksplit : 1);
   cudaStream_t st = stream ? stream : ctx->stream;
   if (prec == 1) {
@@ -429,7 +450,7 @@ int rsd_tc_gemm_zbatch(rsd_ctx* ctx, int prec, int m, int n, int K, float alpha,
   RSD_TRY(encode_2d(ctx, &tmA, A, a_rows, a_cols, lda, TC_KC, TC_TILE, CU_TENSOR_MAP_SWIZZLE_128B));
   RSD_TRY(encode_2d(ctx, &tmB, B, b_rows, b_cols, ldb, TC_KC, TC_TILE, CU_TENSOR_MAP_SWIZZLE_128B));
   RSD_TRY(encode_2d(ctx, &tmC, C, c_rows, c_cols, ldc, TC_TILE, TC_TILE, CU_TENSOR_MAP_SWIZZLE_NONE));
-  TcArgs a{K, 0, 0, 0, 0, alpha, d_err, zak, zam, zbk, zbn, zcm, zcn, n, ndec};
+  TcArgs a{K, 0, 0, 0, 0, alpha, d_err, wait_limit(ctx), zak, zam, zbk, zbn, zcm, zcn, n, ndec};
   const dim3 grid((m + TC_TILE - 1) / TC_TILE, (n + TC_TILE - 1) / TC_TILE, nbatch);
   if (prec == 1) {
     tc_gemm_kernel<1><<<grid, TC_THREADS, TcCfg<1>::SMEM, ctx->stream>>>(tmA, tmB, tmC, a);

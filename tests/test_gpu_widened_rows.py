@@ -1,9 +1,7 @@
 """GPU tests of the rows widened last (overlap correction method 2, the
 GMRES variant's FTS solve, the Brownian terms, overlap corrections in the
-fused step), through the C-ABI against
-the oracle; tolerances as in test_gpu_parity.py, stated per test.  Kept in a
-file collected after the others so that a first-failure stop has run every
-other GPU test."""
+fused step), through the C-ABI against the oracle; tolerances as in
+test_gpu_parity.py, stated per test."""
 import numpy as np
 import pytest
 
