@@ -3,17 +3,29 @@
 
 Workload: N = 2048 monodisperse spheres, volume fraction 0.5, seeded minimum
 gap 1e-4 a, Lees-Edwards shear rate 1, dt = 5e-4, Ewald tolerance 1e-10,
-lubrication on -- one STEPPER_Stokesian step per timed iteration, all
-inputs resident in HBM.  The grand mobility alone (4.06 GB FP64) is larger
-than L2, so no flush is needed between iterations.
+lubrication on -- one STEPPER_Stokesian step per timed iteration, all inputs
+resident in HBM.  The grand mobility alone (4.06 GB FP64) is larger than L2,
+so no flush is needed between iterations.
+
+The step's cost follows the Lees-Edwards strain: CALC_LATTICE_INVERSE
+(csd_post.f90:158-183) gives NR = NI = 3 at zero skew and up to 5 near skew
+1, i.e. 685 to 2661 Ewald images per pair (1538 on average over a strain
+cycle).  The headline therefore runs the step at a stratified set of
+strains covering one cycle -- skew (k + 1/2)/S, k = 0..S-1 (S = 5: 0.1, 0.3,
+0.5, 0.7, 0.9; NR = NI = 3, 4, 4, 4, 5; 1543 images per pair on average) --
+each from a configuration valid at that strain (configs.sheared_series: the
+seeded packing sheared affinely with the lattice and its overlaps relaxed),
+the timed steps spread round-robin over the strata, and `value` is the
+strain-averaged steps/s.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--precision mixed|fp64] [--N 2048] [--phi 0.5]
+                    [--precision mixed|fp64] [--strata 5] [--N 2048] [--phi 0.5]
 
 Prints one JSON line (rank 0).  With --gpus N > 1 under torchrun every rank
 steps its own independent replica (the step does not shard; replicas only).
 --impl reference times the CPU restatement of the reference's routines on the
-host cores instead (bounded samples, see cpu_step_sample()).
+host cores instead (bounded samples per step, extrapolated; see
+cpu_step_sample()).
 """
 import argparse
 import json
@@ -21,7 +33,6 @@ import math
 import os
 import subprocess
 import sys
-import threading
 import time
 
 import numpy as np
@@ -36,10 +47,11 @@ SEED_BASE = 20260000
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--strata", type=int, default=5, help="strains of the Lees-Edwards cycle the steps run at")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--N", type=int, default=2048)
     ap.add_argument("--phi", type=float, default=0.5)
@@ -51,6 +63,8 @@ def parse():
     ap.add_argument("--no-peaks", action="store_true")
     ap.add_argument("--tensor-cores", type=int, default=1, choices=[0, 1, 3],
                     help="FP32 factorisations of the mixed form: 1 TF32/3xTF32 per factor, 3 all 3xTF32, 0 SIMT")
+    ap.add_argument("--validate-cpu-model", action="store_true",
+                    help="(reference arm) time one whole CPU step at N=512 and compare it with the sample model")
     return ap.parse_args()
 
 
@@ -64,6 +78,11 @@ def dist_env():
 def replica_seed(rank):
     """Seed of rank `rank`'s packing: every replica steps its own system."""
     return SEED_BASE + 5000 + rank
+
+
+def strata_skews(S):
+    """Skews (k + 1/2)/S of the strain cycle, k = 0..S-1."""
+    return [(k + 0.5) / S for k in range(S)]
 
 
 def max_over_ranks(x, ws, dist, torch, device):
@@ -84,9 +103,11 @@ def replica_throughput(ws, steps, seconds):
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fp:
-            return json.load(fp)
+            d = json.load(fp)
+            d["source"] = "measured"
+            return d
     except OSError:
-        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
 class ClockSampler:
@@ -143,35 +164,16 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def fp64_gemm_peak(torch, dev):
-    """cuBLAS DGEMM rate on this GPU (TFLOP/s): the denominator for the FP64
-    kernels, since the measured-peaks file carries BF16 and HBM only."""
-    n = 8192
-    a = torch.randn(n, n, dtype=torch.float64, device=dev)
-    b = torch.randn(n, n, dtype=torch.float64, device=dev)
-    c = a @ b
-    torch.cuda.synchronize(dev)
-    best = 0.0
-    for _ in range(2):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        c = a @ b
-        e1.record()
-        torch.cuda.synchronize(dev)
-        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
-    del a, b, c
-    return best
-
-
-def fp32_gemm_peak(torch, dev):
-    """cuBLAS FP32 GEMM with TF32 tensor cores, TFLOP/s: the denominator for
-    the FP32 factorisations of the mixed form, whose GEMMs run on tcgen05 in
-    TF32 and 3xTF32 (the measured-peaks file carries BF16 and HBM only)."""
+def gemm_peak(torch, dev, dtype, tf32=False):
+    """cuBLAS GEMM rate on this GPU (TFLOP/s), 8192^3, best of a few: the
+    builder-measured denominators for the FP64 form (DGEMM) and for the
+    mixed form's TF32 factorisations (FP32 GEMM with TF32 tensor cores),
+    beside the measured BF16 peak."""
     prev = torch.backends.cuda.matmul.allow_tf32
-    torch.backends.cuda.matmul.allow_tf32 = True
+    torch.backends.cuda.matmul.allow_tf32 = tf32
     n = 8192
-    a = torch.randn(n, n, dtype=torch.float32, device=dev)
-    b = torch.randn(n, n, dtype=torch.float32, device=dev)
+    a = torch.randn(n, n, dtype=dtype, device=dev)
+    b = torch.randn(n, n, dtype=dtype, device=dev)
     c = a @ b
     torch.cuda.synchronize(dev)
     best = 0.0
@@ -187,104 +189,149 @@ def fp32_gemm_peak(torch, dev):
     return best
 
 
+def images(NR, NI):
+    return (2 * NR + 1) ** 3, (2 * NI + 1) ** 3 - 1
+
+
 def ewald_flops(N, NR, NI):
     """Algorithmic FLOP of one grand-mobility assembly: 500 per real image and
-    150 per reciprocal vector, over the unordered pairs (all images) and the
-    self terms (n != 0 and k != 0)."""
-    nr = (2 * NR + 1) ** 3
-    nk = (2 * NI + 1) ** 3 - 1
+    150 per reciprocal vector of the reference's cubes, over the unordered
+    pairs (all images) and the self terms (n != 0 and k != 0)."""
+    nr, nk = images(NR, NI)
     pairs = N * (N - 1) // 2
     return pairs * (nr * 500.0 + nk * 150.0) + N * ((nr - 1) * 500.0 + nk * 150.0)
 
 
-def solve_flops(N, precision):
-    """Plain FP64: Cholesky + SPD inverse of M (n^3, n = 11N) and Cholesky of
-    RPP ((6N)^3/3): 1403 N^3.  Mixed: FP32 Cholesky of M' (n^3/3), inverse of
-    its 6N Schur factor (2 (6N)^3/3) and Cholesky of RPP ((6N)^3/3): 660 N^3."""
-    if precision == "fp64":
-        return 1403.0 * N ** 3
-    return (1331.0 / 3.0 + 216.0) * N ** 3
+SOLVE_FLOP_PER_N3 = 1403.0  # Cholesky + SPD inverse of M (n = 11N) and Cholesky of RPP (6N)
 
 
-def cpu_step_sample(pos, radii, L, N, dt, threads):
-    """Seconds per step of the CPU restatement of the reference's routines at
-    the full workload, from bounded samples:
-      assembly  PER_GRPERY_INV_FRI on the first 96 particles in the full box
-                (4560 pairs, same images per pair), scaled to N(N-1)/2 pairs
-                plus N self terms;
-      lub       lubmxcalc at N = 512 at the same volume fraction, scaled by
-                (N/512)^2 (pair sweep and dense outputs are O(N^2));
-      solve     LAPACK DPOTRF + DPOTRI of the 11*512 grand mobility plus DPOTRF
-                of the 6*512 RPP block (scipy's OpenBLAS), scaled by (N/512)^3.
-    Returns (seconds, description)."""
+def lattice_of(skew, L, radii, ews=1e-10):
+    """NR, NI of CALC_LATTICE_INVERSE at skew `skew` (the oracle's lattice
+    routines, host only)."""
     from oracle import oracle as o
-    from scipy.linalg import lapack
+    lat = o.set_lattice_skew(skew, [L, L, L], 1.0)
+    o.calc_lattice_inverse(lat, ews, radii)
+    return lat.NR, lat.NI
 
-    mu = o.mu_f_dimensionless(1.0)
-    lat = o.set_lattice_skew(0.0, [L, L, L], 1.0)
-    ns = min(96, N)
-    t0 = time.perf_counter()
-    G, _ = o.per_grpery_inv_fri(pos[:ns], radii[:ns], lat, 1e-10, mu)
-    t_asm = time.perf_counter() - t0
-    pairs_s = ns * (ns - 1) / 2 + ns
-    pairs = N * (N - 1) / 2 + N
-    t_asm_full = t_asm * pairs / pairs_s
-    n_l = min(512, N)
-    lat2 = o.set_lattice_skew(0.0, [L, L, L], 1.0)
+
+# ---------------------------------------------------------------- CPU arm
+class CpuModel:
+    """Seconds per step of the CPU restatement of the reference's routines
+    (the oracle: C + scipy's OpenBLAS LAPACK) at the full workload, from
+    bounded samples timed each step and scaled by unit counts:
+      assembly  PER_GRPERY_INV_FRI on the first 96 particles of the stratum's
+                configuration in the full box at its strain (the same images
+                per pair), scaled to N(N-1)/2 pairs plus N self terms;
+      lub       lubmxcalc on a 512-particle box at the same volume fraction,
+                scaled by (N/512)^2 (pair sweep and dense outputs are O(N^2));
+      solve     LAPACK DPOTRF + DPOTRI of an assembled 512-particle grand
+                mobility (n = 5632, the oracle's own matrix at phi) plus
+                DPOTRF of its 6N RPP block, scaled by (N/512)^3."""
+
+    def __init__(self, N, phi, gmin, strata, L, radii, sweeps, threads):
+        from oracle import oracle as o
+        self.o = o
+        self.N, self.strata, self.L, self.radii, self.threads = N, strata, L, radii, threads
+        self.mu = o.mu_f_dimensionless(1.0)
+        self.tab = o.LubTab(os.path.join(ROOT, "tests", "golden", "lubdat"))
+        cfg = _configs()
+        self.ns = min(512, N)
+        self.pos_s, _, self.Ls = cfg.packing(self.ns, phi, gmin, SEED_BASE + 5900, sweeps=min(sweeps, 50))
+        self.radii_s = np.ones(self.ns)
+        lat = o.set_lattice_skew(0.0, [self.Ls] * 3, 1.0)
+        t0 = time.perf_counter()
+        G, _ = o.per_grpery_inv_fri(self.pos_s, self.radii_s, lat, 1e-10, self.mu)
+        self.setup_assembly_s = time.perf_counter() - t0
+        self.Ms = np.asfortranarray(G)
+        self.Rs = np.asfortranarray(np.linalg.inv(G)[:6 * self.ns, :6 * self.ns] + np.eye(6 * self.ns))
+
+    def sample(self, k):
+        """One bounded sample at stratum k; returns (seconds per full step,
+        dict of measured sample seconds and scale factors)."""
+        from scipy.linalg import lapack
+        o, N = self.o, self.N
+        pos, skew = self.strata[k]
+        lat = o.set_lattice_skew(skew, [self.L] * 3, 1.0)
+        na = min(96, N)
+        t0 = time.perf_counter()
+        o.per_grpery_inv_fri(pos[:na], self.radii[:na], lat, 1e-10, self.mu)
+        t_asm = time.perf_counter() - t0
+        s_asm = (N * (N - 1) / 2 + N) / (na * (na - 1) / 2 + na)
+        lat2 = o.set_lattice_skew(0.0, [self.Ls] * 3, 1.0)
+        t0 = time.perf_counter()
+        o.lubmxcalc(self.pos_s, self.radii_s, lat2, self.mu, self.tab)
+        t_lub = time.perf_counter() - t0
+        s_lub = (N / self.ns) ** 2
+        A = self.Ms.copy(order="F")
+        B = self.Rs.copy(order="F")
+        t0 = time.perf_counter()
+        c, _ = lapack.dpotrf(A, lower=0, clean=0, overwrite_a=1)
+        lapack.dpotri(c, lower=0, overwrite_c=1)
+        lapack.dpotrf(B, lower=0, clean=0, overwrite_a=1)
+        t_sol = time.perf_counter() - t0
+        s_sol = (N / self.ns) ** 3
+        NR, NI = lat.NR, lat.NI
+        total = t_asm * s_asm + t_lub * s_lub + t_sol * s_sol
+        return total, {"skew": skew, "NR": NR, "NI": NI, "assembly_sample_s": t_asm, "assembly_scale": s_asm,
+                       "lub_sample_s": t_lub, "lub_scale": s_lub, "solve_sample_s": t_sol, "solve_scale": s_sol}
+
+    def describe(self, k):
+        return ("port (C restatement + OpenBLAS LAPACK), %d threads; per step, at the step's stratum of the strain "
+                "cycle: assembly of %d particles' pairs at that strain scaled to %d pairs, lub at N=%d scaled by "
+                "N^2, DPOTRF+DPOTRI of an assembled n=%d grand mobility + DPOTRF of its RPP scaled by n^3 "
+                "(extrapolated from samples timed every step)" % (self.threads, min(96, self.N),
+                                                                  self.N * (self.N - 1) // 2, self.ns, 11 * self.ns))
+
+
+def validate_cpu_model(args, threads):
+    """One whole oracle step at N = 512 (phi, gap and strain 0 as the model's
+    samples) against the model's prediction for N = 512."""
+    from oracle import oracle as o
+    cfg = _configs()
+    N = 512
+    pos, radii, L = cfg.packing(N, args.phi, args.gmin, SEED_BASE + 5901, sweeps=50)
+    model = CpuModel(N, args.phi, args.gmin, [(pos, 0.0)], L, radii, 50, threads)
+    pred, parts = model.sample(0)
     tab = o.LubTab(os.path.join(ROOT, "tests", "golden", "lubdat"))
-    # a 512-particle box at the same volume fraction
-    L2 = L * (n_l / N) ** (1.0 / 3.0)
-    sel = pos[np.all(pos < L2, axis=1)][:n_l] if N > n_l else pos
-    lat2 = o.set_lattice_skew(0.0, [L2, L2, L2], 1.0)
     t0 = time.perf_counter()
-    o.lubmxcalc(sel, np.ones(len(sel)), lat2, mu, tab)
-    t_lub = (time.perf_counter() - t0) * (N / max(len(sel), 1)) ** 2
-    n_s = 11 * n_l
-    rng = np.random.default_rng(0)
-    X = rng.standard_normal((n_s, n_s))
-    A = np.asfortranarray(X @ X.T / n_s + np.eye(n_s))
-    B = np.asfortranarray(A[:6 * n_l, :6 * n_l].copy())
-    t0 = time.perf_counter()
-    c, _ = lapack.dpotrf(A, lower=0, clean=0, overwrite_a=1)
-    lapack.dpotri(c, lower=0, overwrite_c=1)
-    lapack.dpotrf(B, lower=0, clean=0, overwrite_a=1)
-    t_solve = (time.perf_counter() - t0) * (N / n_l) ** 3
-    total = t_asm_full + t_lub + t_solve
-    desc = ("port (C restatement + OpenBLAS LAPACK), %d threads; per step = assembly of %d particles' %d pairs "
-            "scaled to %d, lub at N=%d scaled by N^2, DPOTRF+DPOTRI at n=%d scaled by n^3 "
-            "(assembly %.1f s, lub %.2f s, solve %.1f s)" % (threads, ns, int(pairs_s), int(pairs), len(sel), n_s,
-                                                           t_asm_full, t_lub, t_solve))
-    return total, desc
+    o.stepper_stokesian(pos, radii, [L, L, L], 0.0, args.dt, 1.0, o.mu_f_dimensionless(1.0), 1e-10, tab)
+    full = time.perf_counter() - t0
+    return {"N": N, "full_step_s": full, "model_s": pred, "model_over_full": pred / full, "parts": parts}
 
 
 def reference_arm(args):
     ws, rank, local = dist_env()
     if rank != 0:
         return
-    import __graft_entry__ as ge
     from oracle import oracle as o
     o.build()
-    rsd_cfg = _configs()
-    pos, radii, L = rsd_cfg.packing(args.N, args.phi, args.gmin, replica_seed(0), sweeps=args.sweeps)
     threads = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    for _ in range(args.warmup):
-        cpu_step_sample(pos, radii, L, args.N, args.dt, threads)
-    ts = []
-    desc = ""
-    for _ in range(args.steps):
-        t, desc = cpu_step_sample(pos, radii, L, args.N, args.dt, threads)
+    cfg = _configs()
+    skews = strata_skews(max(1, args.strata))
+    series, radii, L = cfg.sheared_series(args.N, args.phi, args.gmin, replica_seed(0), skews, sweeps=args.sweeps)
+    strata = list(zip(series, skews))
+    model = CpuModel(args.N, args.phi, args.gmin, strata, L, radii, args.sweeps, threads)
+    S = len(strata)
+    for w in range(args.warmup):
+        model.sample((S - 1 - w) % S)
+    ts, parts = [], []
+    for k in range(args.steps):
+        t, p = model.sample(k % S)
         ts.append(t)
+        parts.append(p)
     sec = float(np.mean(ts))
     v = 1.0 / sec
     line = {"metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded sphere packing)",
-            "config": {"workload": "STEPPER_Stokesian step, N=%d phi=%.2f gap>=%g, shear 1, dt %g, Ewald 1e-10, lub on"
-                                   % (args.N, args.phi, args.gmin, args.dt), "l2": "inputs larger than L2"},
+            "data": "synthetic (seeded sphere packing sheared to each stratum)",
+            "config": {"workload": workload_name(args), "strata_skew": skews, "l2": "inputs larger than L2"},
             "impl": "reference",
-            "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port", "sample": desc},
+            "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+                             "sample": model.describe(0), "extrapolated": True, "samples": parts},
             "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if args.validate_cpu_model:
+        line["cpu_model_check"] = validate_cpu_model(args, threads)
     print(json.dumps(line), flush=True)
 
 
@@ -297,6 +344,25 @@ def _configs():
     return mod
 
 
+def workload_name(args):
+    return ("STEPPER_Stokesian step, N=%d phi=%.2f gap>=%g, shear 1, dt %g, Ewald 1e-10, lub on; strain-averaged "
+            "over %d strata of the Lees-Edwards cycle" % (args.N, args.phi, args.gmin, args.dt, args.strata))
+
+
+def read_traffic(key):
+    tfile = os.path.join(ROOT, "profiles", "traffic.txt")
+    if os.path.exists(tfile):
+        for line in open(tfile):
+            k, _, v = line.partition("=")
+            if k.strip() == key:
+                try:
+                    return float(v.split()[0])
+                except (ValueError, IndexError):
+                    return None
+    return None
+
+
+# ---------------------------------------------------------------- GPU arm
 def main():
     args = parse()
     if args.impl == "reference":
@@ -314,147 +380,168 @@ def main():
     torch.cuda.set_device(dev)
     rsd = ge.load_package()
     prec = rsd.PREC_MIXED if args.precision == "mixed" else rsd.PREC_FP64
-    pos, radii, L = rsd.configs.packing(args.N, args.phi, args.gmin, replica_seed(rank), sweeps=args.sweeps)
     N = args.N
+    S = max(1, args.strata)
+    skews = strata_skews(S)
+    series, radii, L = rsd.configs.sheared_series(N, args.phi, args.gmin, replica_seed(rank), skews,
+                                                  sweeps=args.sweeps)
     mu = rsd.mu_f_dimensionless(1.0)
     ctx = rsd.Context(local)
     ctx.set_tensor_cores(args.tensor_cores)
     tab = rsd.LubTab(rsd.lubdat_dir())
-    conf_t = torch.tensor(pos, dtype=torch.float64, device=dev)
     radii_t = torch.tensor(radii, dtype=torch.float64, device=dev)
+    conf = [torch.tensor(p, dtype=torch.float64, device=dev) for p in series]
+    Ts = list(skews)  # shear rate 1: strain = T
     U_t = torch.empty(6 * N, dtype=torch.float64, device=dev)
     S_t = torch.empty(5 * N, dtype=torch.float64, device=dev)
     torch.cuda.synchronize(dev)
-    T = 0.0
     stream = torch.cuda.ExternalStream(ctx.stream)
     lib = rsd.library()
 
-    def step():
-        nonlocal T
-        y, info = rsd.stepper_stokesian_dev(ctx, tab, conf_t, radii_t, T, args.dt, [L, L, L], 1.0, mu, 1e-10, U_t, S_t,
-                                            precision=prec)
-        T += args.dt
+    def step(k, precision=prec):
+        y, info = rsd.stepper_stokesian_dev(ctx, tab, conf[k], radii_t, Ts[k], args.dt, [L, L, L], 1.0, mu, 1e-10,
+                                            U_t, S_t, precision=precision)
+        Ts[k] += args.dt
         return y, info
 
-    for _ in range(args.warmup):
-        step()
+    # warm-up from the largest images down, so that every grow-only buffer
+    # has its final size before the timed region
+    for w in range(args.warmup):
+        step((S - 1 - w) % S)
     sampler = ClockSampler(local) if rank == 0 else None
     if ws > 1:
         dist.barrier()
     torch.cuda.synchronize(dev)
     if sampler:
         sampler.start()
-    n0 = lib.rsd_launch_count() if hasattr(lib, "rsd_launch_count") else 0
+    n0 = lib.rsd_launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     phases = np.zeros(4)
-    infos = []
-    for _ in range(args.steps):
-        y, info = step()
-        phases += ctx.phase_ms()
-        infos.append((info.NR, info.NI, info.iterations, info.residual))
+    infos, per_stratum = [], [[] for _ in range(S)]
+    for i in range(args.steps):
+        k = i % S
+        y, info = step(k)
+        ph = ctx.phase_ms()
+        phases += ph
+        infos.append((k, info.NR, info.NI, info.iterations, info.residual, float(y[0])))
+        per_stratum[k].append(float(ph[:3].sum()))
     e1.record(stream)
     torch.cuda.synchronize(dev)
-    launches = (lib.rsd_launch_count() - n0) if hasattr(lib, "rsd_launch_count") else None
+    launches = lib.rsd_launch_count() - n0
     ms = e0.elapsed_time(e1)
     clocks = sampler.stop() if sampler else None
     ms = max_over_ranks(ms, ws, dist, torch, dev)
     ms_per_step = ms / args.steps
     value = replica_throughput(ws, args.steps, ms * 1e-3)
-    # end to end through the host C-ABI call (H2D of the inputs, D2H of the results)
+    # end to end through the host C-ABI call (H2D of the inputs, D2H of the
+    # results every step), round-robin over the same strata
     e2e = None
     if not args.no_e2e:
-        conf_h = conf_t.cpu().numpy().copy()
+        conf_h = [c.cpu().numpy().copy() for c in conf]
+        Te = list(Ts)
         t0 = time.perf_counter()
-        Te = T
-        for _ in range(args.steps):
-            out = rsd.STEPPER_Stokesian(ctx, tab, conf_h, radii, Te, args.dt, [L, L, L], 1.0, mu, 1e-10,
+        for i in range(args.steps):
+            k = i % S
+            out = rsd.STEPPER_Stokesian(ctx, tab, conf_h[k], radii, Te[k], args.dt, [L, L, L], 1.0, mu, 1e-10,
                                         precision=prec)
-            conf_h = out["conf"]
-            Te += args.dt
+            conf_h[k] = out["conf"]
+            Te[k] += args.dt
         te = max_over_ranks(time.perf_counter() - t0, ws, dist, torch, dev)
-        e2e = {"value": replica_throughput(ws, args.steps, te), "unit": "steps/s", "h2d_bytes_per_step": 8 * (3 * N + N),
-               "d2h_bytes_per_step": 8 * (3 * N + 6 * N + 5 * N)}
-    # the plain FP64 form on the same start configuration: its steps/s and the
-    # mixed form's velocity / stresslet error against it
+        e2e = {"value": replica_throughput(ws, args.steps, te), "unit": "steps/s",
+               "h2d_bytes_per_step": 8 * (3 * N + N), "d2h_bytes_per_step": 8 * (3 * N + 6 * N + 5 * N)}
+    # the plain FP64 form at every stratum (its own step from the same
+    # configuration): steps/s and the mixed form's errors against it
     plain = None
     if not args.no_plain and args.precision == "mixed":
-        c0 = torch.tensor(pos, dtype=torch.float64, device=dev)
-        Um, Sm = torch.empty_like(U_t), torch.empty_like(S_t)
-        rsd.stepper_stokesian_dev(ctx, tab, c0.clone(), radii_t, 0.0, args.dt, [L, L, L], 1.0, mu, 1e-10, Um, Sm,
-                                  precision=rsd.PREC_MIXED)
-        Up, Sp = torch.empty_like(U_t), torch.empty_like(S_t)
-        rsd.stepper_stokesian_dev(ctx, tab, c0.clone(), radii_t, 0.0, args.dt, [L, L, L], 1.0, mu, 1e-10, Up, Sp,
-                                  precision=rsd.PREC_FP64)  # warm-up of the plain path's buffers
-        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        p0.record(stream)
-        rsd.stepper_stokesian_dev(ctx, tab, c0.clone(), radii_t, 0.0, args.dt, [L, L, L], 1.0, mu, 1e-10, Up, Sp,
-                                  precision=rsd.PREC_FP64)
-        p1.record(stream)
-        torch.cuda.synchronize(dev)
-        pms = p0.elapsed_time(p1)
-        pph = ctx.phase_ms()
-        verr = float((Um - Up).abs().max() / Up.abs().max())
-        serr = float((Sm - Sp).abs().max() / Sp.abs().max())
-        plain = {"steps_per_s": 1000.0 / pms, "ms_per_step": pms,
+        pms_all, verr, serr, yerr, pph_all = [], 0.0, 0.0, 0.0, np.zeros(4)
+        for k in range(S):
+            c0 = conf[k].clone()
+            Um, Sm = torch.empty_like(U_t), torch.empty_like(S_t)
+            ym, _ = rsd.stepper_stokesian_dev(ctx, tab, c0.clone(), radii_t, Ts[k], args.dt, [L, L, L], 1.0, mu,
+                                              1e-10, Um, Sm, precision=rsd.PREC_MIXED)
+            Up, Sp = torch.empty_like(U_t), torch.empty_like(S_t)
+            if k == 0:  # the plain path's buffers, once
+                rsd.stepper_stokesian_dev(ctx, tab, c0.clone(), radii_t, Ts[k], args.dt, [L, L, L], 1.0, mu, 1e-10,
+                                          Up, Sp, precision=rsd.PREC_FP64)
+            p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            p0.record(stream)
+            yp, _ = rsd.stepper_stokesian_dev(ctx, tab, c0.clone(), radii_t, Ts[k], args.dt, [L, L, L], 1.0, mu,
+                                              1e-10, Up, Sp, precision=rsd.PREC_FP64)
+            p1.record(stream)
+            torch.cuda.synchronize(dev)
+            pms_all.append(p0.elapsed_time(p1))
+            pph_all += ctx.phase_ms()
+            verr = max(verr, float((Um - Up).abs().max() / Up.abs().max()))
+            serr = max(serr, float((Sm - Sp).abs().max() / Sp.abs().max()))
+            yerr = max(yerr, abs(ym[0] - yp[0]) / abs(yp[0]))
+        pms = float(np.mean(pms_all))
+        pph = pph_all / S
+        plain = {"steps_per_s": 1000.0 / pms, "ms_per_step": pms, "ms_per_stratum": pms_all,
                  "phases_ms": {"assembly": pph[0], "lub": pph[1], "solve": pph[2]},
-                 "solve_tflops_fp64": solve_flops(N, "fp64") / (pph[2] * 1e-3) / 1e12,
-                 "mixed_over_plain": (1000.0 / pms and value / ws / (1000.0 / pms)),
-                 "vel_err_mixed_vs_fp64": verr, "stresslet_err_mixed_vs_fp64": serr}
+                 "solve_tflops_fp64": SOLVE_FLOP_PER_N3 * N ** 3 / (pph[2] * 1e-3) / 1e12,
+                 "mixed_over_plain": (value / ws) / (1000.0 / pms),
+                 "vel_err_mixed_vs_fp64": verr, "stresslet_err_mixed_vs_fp64": serr,
+                 "viscosity_err_mixed_vs_fp64": yerr}
     if rank != 0:
         if ws > 1:
             dist.barrier()
         return
     peaks = measured_peaks()
-    fp64_peak = None if args.no_peaks else fp64_gemm_peak(torch, dev)
-    fp32_peak = None if args.no_peaks else fp32_gemm_peak(torch, dev)
-    NR, NI = infos[0][0], infos[0][1]
+    fp64_peak = None if args.no_peaks else gemm_peak(torch, dev, torch.float64)
+    tf32_peak = None if args.no_peaks else gemm_peak(torch, dev, torch.float32, tf32=True)
     ph = phases / args.steps
-    asm_flop = ewald_flops(N, NR, NI)
+    asm_flop = float(np.mean([ewald_flops(N, i[1], i[2]) for i in infos]))
     asm_rate = asm_flop / (ph[0] * 1e-3) / 1e12
-    factor_ms = ph[2] - ph[3]
-    solve_rate = solve_flops(N, args.precision) / (factor_ms * 1e-3) / 1e12
-    dominant = "solve" if ph[2] >= ph[0] else "assembly"
-    if dominant == "solve":
-        rate, pk = solve_rate, (fp64_peak if args.precision == "fp64" else fp32_peak)
-        pipe = "FP64" if args.precision == "fp64" else "FP32"
-        pipe = "FP64" if args.precision == "fp64" else "TF32 tensor"
-        src = ("cuBLAS %s 8192^3 measured in this run (the measured-peaks file has BF16 and HBM only)"
-               % ("DGEMM" if args.precision == "fp64" else "FP32 GEMM with TF32 tensor cores"))
-    else:
-        rate, pk, pipe = asm_rate, fp64_peak, "FP64"
-        src = "cuBLAS DGEMM 8192^3 measured in this run (the measured-peaks file has BF16 and HBM only)"
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic.txt")
-    if os.path.exists(tfile):
-        for line in open(tfile):
-            k, _, v = line.partition("=")
-            if k.strip() == "%s_%s_bytes_per_launch" % (dominant, args.precision):
-                traffic = float(v)
-    kname = {"solve": "factorisations of the solve (%s): Cholesky, SPD inverse, Cholesky of RPP" % args.precision,
-             "assembly": "grand-mobility assembly (%s)" % args.precision}[dominant]
-    roofline = {"bound": "tensor", "pipe": pipe, "kernel": kname, "achieved": rate,
-                "peak": pk, "unit": "TFLOP/s", "frac": (rate / pk) if pk else None, "traffic": traffic,
-                "peak_source": src}
+    solve_flop = SOLVE_FLOP_PER_N3 * N ** 3
+    solve_rate = solve_flop / (ph[2] * 1e-3) / 1e12
+    bf16 = peaks.get("bf16_tflops")
+    traffic = read_traffic("solve_%s_bytes_per_step" % args.precision)
+    roofline = {"bound": "tensor", "kernel": "the step's solve phase (%s): the factorisations on tcgen05 and the FP64 "
+                                             "refinement, %g N^3 FLOP per step" % (args.precision, SOLVE_FLOP_PER_N3),
+                "achieved": solve_rate, "peak": bf16, "unit": "TFLOP/s",
+                "frac": solve_rate / bf16 if bf16 else None, "traffic": traffic,
+                "peak_source": "dense BF16 tensor rate, %s (MEASURED_PEAKS.json)" % peaks.get("source"),
+                "tf32_peak_builder_measured": tf32_peak,
+                "frac_of_tf32_builder_measured": solve_rate / tf32_peak if tf32_peak else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over the solve phase's launches "
+                                  "of one step (profiles/traffic.txt)"}
+    by_stratum = []
+    for k in range(S):
+        its = [i for i in infos if i[0] == k]
+        if not its:
+            continue
+        by_stratum.append({"skew": skews[k], "NR": its[0][1], "NI": its[0][2],
+                           "images_per_pair": sum(images(its[0][1], its[0][2])),
+                           "ms_per_step": float(np.mean(per_stratum[k])),
+                           "iterations": [i[3] for i in its], "residual": [i[4] for i in its],
+                           "yeta_mu": [i[5] for i in its]})
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
-        sec, desc = cpu_step_sample(pos, radii, L, N, args.dt, threads)
-        cpu = {"value": 1.0 / sec, "unit": "steps/s", "cores": threads, "kind": "port", "sample": desc}
+        model = CpuModel(N, args.phi, args.gmin, list(zip(series, skews)), L, radii, args.sweeps, threads)
+        secs, parts = [], []
+        for k in range(S):
+            t, p = model.sample(k)
+            secs.append(t)
+            parts.append(p)
+        cpu = {"value": 1.0 / float(np.mean(secs)), "unit": "steps/s", "cores": threads, "kind": "port",
+               "sample": model.describe(0), "extrapolated": True, "samples": parts}
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-            "data": "synthetic (seeded sphere packing, no dataset)",
-            "config": {"workload": "STEPPER_Stokesian step, N=%d phi=%.2f gap>=%g, shear 1, dt %g, Ewald 1e-10, lub on"
-                                   % (N, args.phi, args.gmin, args.dt),
-                       "precision": args.precision, "tensor_cores": args.tensor_cores, "NR": NR, "NI": NI,
+            "data": "synthetic (seeded sphere packing sheared to each stratum, no dataset)",
+            "config": {"workload": workload_name(args), "precision": args.precision,
+                       "tensor_cores": args.tensor_cores, "strata_skew": skews,
+                       "mean_images_per_pair": float(np.mean([sum(images(i[1], i[2])) for i in infos])),
                        "l2": "inputs larger than L2 (grand mobility %.2f GB)" % (8 * (11 * N) ** 2 / 1e9),
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "phases_ms": {"assembly": ph[0], "lub": ph[1], "solve": ph[2], "refinement": ph[3]},
+            "strata": by_stratum,
             "plain_fp64": plain,
-            "refinement": {"iterations": [i[2] for i in infos], "residual": [i[3] for i in infos]},
-            "kernels": {"assembly_tflops": asm_rate, "solve_tflops": solve_rate,
-                        "assembly_algorithmic_flop": asm_flop, "solve_algorithmic_flop": solve_flops(N, args.precision)},
+            "kernels": {"assembly_tflops_algorithmic": asm_rate, "assembly_algorithmic_flop": asm_flop,
+                        "solve_tflops_algorithmic": solve_rate, "solve_algorithmic_flop": solve_flop,
+                        "fp64_dgemm_peak_builder_measured": fp64_peak},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
     print(json.dumps(line), flush=True)
     if ws > 1:

@@ -280,6 +280,8 @@ typedef struct rsd_step_info {
   double residual;    /* mixed: final relative residual */
   double phi;         /* volume fraction */
   double LV;          /* cell volume */
+  int32_t rpp_iterations; /* FP64 form with a PCG RPP solver: its iterations
+                             (negative: not converged, factorised instead) */
 } rsd_step_info;
 
 /* One STEPPER_Stokesian step (src/stepper.f90:33-156) on the periodic FTS
@@ -296,6 +298,82 @@ int rsd_stepper_stokesian(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_step_pa
 int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_step_params* p, double* d_conf,
                               const double* d_radii, const double* d_Fe, double* d_U_pos, double* d_SijN,
                               double yeta_mu[5], rsd_step_info* info);
+
+/* --------------------------------- learned preconditioner of the RPP solve */
+/* The resistance solve of STEPPER_NOGmres (src/stepper.f90:370-393,
+ * MATREV(RPP)) by preconditioned conjugate gradients in FP64 instead of a
+ * dense Cholesky factorisation.  The reference has no counterpart: it always
+ * factors RPP (LAPACK DPOTRF/DPOTRI).  The preconditioner is a block-sparse
+ * approximate inverse G = D^-1/2 Z^T Z D^-1/2 of RPP (D its diagonal, Z
+ * block lower triangular with 6 x 6 blocks on each particle and on each pair
+ * of particles closer than 3 a_avg, b < a), either exact (the factorised
+ * sparse approximate inverse, from one local dense solve per particle) or
+ * emitted by a 3-layer message-passing network (hidden width 64, BF16
+ * weights and activations, FP32 accumulation) over those pairs, whose inputs
+ * are the Jacobi-scaled blocks of RPP and the pair gaps. */
+#define RSD_PC_NONE 0
+#define RSD_PC_JACOBI 1
+#define RSD_PC_BLOCK_JACOBI 2
+#define RSD_PC_FSAI 3
+#define RSD_PC_LEARNED 4
+typedef struct rsd_lp rsd_lp;
+/* Number of network parameters (FP32). */
+int64_t rsd_lp_param_count(void);
+/* A network on CUDA device `device`: from `params` (rsd_lp_param_count()
+ * FP32 values, e.g. trained weights) or, when NULL, initialised from `seed`. */
+int rsd_lp_create(rsd_lp** net, int device, const float* params, uint64_t seed);
+int rsd_lp_destroy(rsd_lp* net);
+/* Current parameters and/or last gradient to host arrays (either may be NULL). */
+int rsd_lp_get_params(rsd_lp* net, float* params, float* grad);
+/* The near-neighbour graph of a configuration: edges (a <- b), b != a, with
+ * minimum-image centre distance below 3 (a_a + a_b)/2, in CSR by a (h_off,
+ * nn + 1), sources ascending (h_src), surface gaps (h_gap); any of the host
+ * arrays may be NULL (n_edges alone sizes them). */
+int rsd_lp_graph_dev(rsd_ctx* ctx, int32_t nn, const double* d_pos, const double* d_radii, const rsd_lattice* lat,
+                     int32_t* n_edges, int32_t* h_off, int32_t* h_src, float* h_gap);
+/* The network alone on a given graph (CSR d_off, edges d_src -> d_dst) and
+ * FP32 inputs d_xn (nn x 36) and d_xe (ne x 40): outputs the blocks d_zd
+ * (nn x 36) and d_ze (ne x 36); when d_dzd and d_dze are given, also the
+ * gradient of the parameters for those output gradients (read it with
+ * rsd_lp_get_params). */
+int rsd_lp_forward_dev(rsd_ctx* ctx, rsd_lp* net, int32_t nn, int32_t ne, const int32_t* d_off, const int32_t* d_src,
+                       const int32_t* d_dst, const float* d_xn, const float* d_xe, const float* d_dzd,
+                       const float* d_dze, float* d_zd, float* d_ze);
+/* One Adam step (beta 0.9, 0.999, eps 1e-8) on the stored gradient. */
+int rsd_lp_adam_step(rsd_lp* net, float lr);
+/* One training step on one resistance matrix: d_rpp (6nn x 6nn, grand
+ * layout, ld, FP32 if fp32 != 0 else FP64, full symmetric storage) of the
+ * configuration d_pos/d_radii on lattice lat; the targets are its exact FSAI
+ * blocks; loss returns the mean squared block error before the step. */
+int rsd_lp_train_step(rsd_ctx* ctx, rsd_lp* net, int32_t nn, const double* d_pos, const double* d_radii,
+                      const rsd_lattice* lat, int32_t fp32, const void* d_rpp, int64_t ld, float lr, double* loss);
+/* The blocks of Z for mode RSD_PC_BLOCK_JACOBI, RSD_PC_FSAI or
+ * RSD_PC_LEARNED to host arrays (h_zd nn x 36, h_ze n_edges x 36 in the
+ * graph's edge order; entries of edges (a <- b) with b >= a are not used). */
+int rsd_lp_blocks_dev(rsd_ctx* ctx, rsd_lp* net, int32_t mode, int32_t nn, const double* d_pos, const double* d_radii,
+                      const rsd_lattice* lat, int32_t fp32, const void* d_rpp, int64_t ld, float* h_zd, float* h_ze,
+                      int32_t* n_edges);
+/* RPP x = b by PCG in FP64 (d_rpp FP64, full symmetric storage in the grand
+ * layout, ld; d_b, d_x: nrhs columns of 6nn) with preconditioner `mode`
+ * (net only for RSD_PC_LEARNED), to relative residual tol or maxit
+ * iterations; iters and resid return the largest over the columns. */
+int rsd_lp_pcg_dev(rsd_ctx* ctx, rsd_lp* net, int32_t mode, int32_t nn, const double* d_pos, const double* d_radii,
+                   const rsd_lattice* lat, const double* d_rpp, int64_t ld, int32_t nrhs, const double* d_b,
+                   double* d_x, double tol, int32_t maxit, int32_t* iters, double* resid);
+/* RPP = (M^-1)_PP + rfu of one configuration (the matrix STEPPER_NOGmres
+ * factors), into d_rpp (6nn x 6nn, ld): FP64 through the plain FP64 path
+ * (precision RSD_PREC_FP64) or FP32 through the mixed form's factors
+ * (RSD_PREC_MIXED, about 1e-4 relative).  p->T sets the strain; lat returns
+ * the lattice. */
+int rsd_resistance_pp_dev(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_step_params* p, const double* d_conf,
+                          const double* d_radii, void* d_rpp, int64_t ld, rsd_lattice* lat);
+/* The RPP solve of the plain FP64 fused step: mode RSD_PC_NONE keeps the
+ * Cholesky factorisation (the default); RSD_PC_JACOBI, RSD_PC_BLOCK_JACOBI,
+ * RSD_PC_FSAI or RSD_PC_LEARNED (with `net`) use PCG to relative residual
+ * tol (0: 1e-12) within maxit iterations (0: 1000), falling back to the
+ * Cholesky factorisation when it does not converge.  rsd_step_info reports
+ * the iterations. */
+int rsd_ctx_set_rpp_solver(rsd_ctx* ctx, int32_t mode, rsd_lp* net, double tol, int32_t maxit);
 
 /* ------------------------------------------ FP32 blocks of the mixed form */
 /* The reference solves in FP64 only (LAPACK DPOTRF/DPOTRI); these are the

@@ -22,6 +22,7 @@ LIBPATH = os.path.join(HERE, "librsd_gb300.so")
 RSD_OK, RSD_EARG, RSD_ECUDA, RSD_ENAN, RSD_ETIMEOUT, RSD_ENOMEM, RSD_EIO, RSD_EUNSUP = 0, -1, -2, -3, -4, -5, -6, -7
 RSD_ELIMIT = -8
 PREC_FP64, PREC_MIXED = 0, 1
+PC_NONE, PC_JACOBI, PC_BLOCK_JACOBI, PC_FSAI, PC_LEARNED = 0, 1, 2, 3, 4
 PAI = 3.141592653589793238462643383279502884
 
 if not os.path.exists(LIBPATH):
@@ -51,7 +52,7 @@ class StepParams(ctypes.Structure):
 class StepInfo(ctypes.Structure):
     _fields_ = [("info", ctypes.c_int32), ("n_contact", ctypes.c_int32), ("NR", ctypes.c_int32),
                 ("NI", ctypes.c_int32), ("iterations", ctypes.c_int32), ("residual", ctypes.c_double),
-                ("phi", ctypes.c_double), ("LV", ctypes.c_double)]
+                ("phi", ctypes.c_double), ("LV", ctypes.c_double), ("rpp_iterations", ctypes.c_int32)]
 
 
 def _sig(name, res, args):
@@ -102,6 +103,20 @@ _sig("rsd_ctx_set_mixed_lambda_scale", _i, [_vp, _d])
 _sig("rsd_ctx_set_mixed_real_passes", _i, [_vp, _i32])
 _sig("rsd_ctx_set_correction_method", _i, [_vp, _i32])
 _sig("rsd_ctx_set_wait_limits", _i, [_vp, _i64, _i64])
+_sig("rsd_ctx_set_rpp_solver", _i, [_vp, _i32, _vp, _d, _i32])
+_sig("rsd_lp_param_count", ctypes.c_int64, [])
+_sig("rsd_lp_create", _i, [ctypes.POINTER(_vp), _i, _vp, ctypes.c_uint64])
+_sig("rsd_lp_destroy", _i, [_vp])
+_sig("rsd_lp_get_params", _i, [_vp, _vp, _vp])
+_sig("rsd_lp_graph_dev", _i, [_vp, _i32, _vp, _vp, _LP, ctypes.POINTER(_i32), _vp, _vp, _vp])
+_sig("rsd_lp_forward_dev", _i, [_vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp])
+_sig("rsd_lp_adam_step", _i, [_vp, ctypes.c_float])
+_sig("rsd_lp_train_step", _i, [_vp, _vp, _i32, _vp, _vp, _LP, _i32, _vp, _i64, ctypes.c_float, _dp])
+_sig("rsd_lp_blocks_dev", _i, [_vp, _vp, _i32, _i32, _vp, _vp, _LP, _i32, _vp, _i64, _vp, _vp,
+                               ctypes.POINTER(_i32)])
+_sig("rsd_lp_pcg_dev", _i, [_vp, _vp, _i32, _i32, _vp, _vp, _LP, _vp, _i64, _i32, _vp, _vp, _d, _i32,
+                            ctypes.POINTER(_i32), _dp])
+_sig("rsd_resistance_pp_dev", _i, [_vp, _vp, ctypes.POINTER(StepParams), _vp, _vp, _vp, _i64, _LP])
 _sig("rsd_syrk_f32_dev", _i, [_vp, _i32, _i32, _vp, _i64, _vp, _i64, _i32])
 _sig("rsd_potrf_f32_dev", _i, [_vp, _i32, _vp, _i64, _i32, _ip])
 _sig("rsd_potri_f32_dev", _i, [_vp, _i32, _vp, _i64, _i32])
@@ -181,6 +196,15 @@ class Context:
         0.5 s and 2^21 polls); a wait that gives up makes the call return
         RSD_ETIMEOUT."""
         self.check(_lib.rsd_ctx_set_wait_limits(self.h, int(tc_wait_ns), int(tri_spin_polls)))
+
+    def set_rpp_solver(self, mode=0, net=None, tol=0.0, maxit=0):
+        """RPP solve of the plain FP64 step: PC_NONE keeps the Cholesky
+        factorisation; PC_JACOBI, PC_BLOCK_JACOBI, PC_FSAI or PC_LEARNED
+        (with a LearnedPreconditioner) use PCG, the factorisation its
+        fallback."""
+        self._rpp_net = net  # keep the network alive while the context uses it
+        self.check(_lib.rsd_ctx_set_rpp_solver(self.h, int(mode), net.h if net is not None else None, float(tol),
+                                               int(maxit)))
 
     def set_tensor_cores(self, mode=1):
         """FP32 factorisations of the mixed form: 1 (or True, the default)
@@ -467,6 +491,156 @@ def stepper_stokesian_dev(ctx: Context, tab: LubTab, conf_t, radii_t, T, dt, LB,
                                         S_t.data_ptr(), _p(y), ctypes.byref(info))
     ctx.check(rc)
     return y, info
+
+
+# ------------------------------------------------------- learned preconditioner
+LP_PARAMS_FILE = os.path.join(HERE, "lp_params.npy")
+
+
+class LearnedPreconditioner:
+    """The message-passing network that emits the block-sparse approximate
+    inverse of RPP (include/rsd_capi.h, rsd_lp_*).  params: FP32 array of
+    rsd_lp_param_count() values, or None for a seeded initialisation."""
+
+    def __init__(self, device=0, params=None, seed=20260400):
+        self.h = _vp()
+        self.n = int(_lib.rsd_lp_param_count())
+        buf = None
+        if params is not None:
+            buf = np.ascontiguousarray(params, dtype=np.float32)
+            if buf.size != self.n:
+                raise ValueError("expected %d parameters, got %d" % (self.n, buf.size))
+        rc = _lib.rsd_lp_create(ctypes.byref(self.h), device, buf.ctypes.data if buf is not None else None,
+                                ctypes.c_uint64(seed))
+        if rc != 0:
+            raise RSDError(rc, "cannot create the learned preconditioner on CUDA device %d" % device)
+
+    @classmethod
+    def trained(cls, device=0, path=None):
+        """The network with the committed trained parameters."""
+        return cls(device, np.load(path or LP_PARAMS_FILE))
+
+    def params(self):
+        out = np.empty(self.n, dtype=np.float32)
+        rc = _lib.rsd_lp_get_params(self.h, out.ctypes.data, None)
+        if rc:
+            raise RSDError(rc, "rsd_lp_get_params")
+        return out
+
+    def grad(self):
+        out = np.empty(self.n, dtype=np.float32)
+        rc = _lib.rsd_lp_get_params(self.h, None, out.ctypes.data)
+        if rc:
+            raise RSDError(rc, "rsd_lp_get_params")
+        return out
+
+    def forward(self, ctx, off, src, dst, xn, xe, dzd=None, dze=None):
+        """The network on a given graph and FP32 inputs (torch CUDA tensors);
+        returns (zd, ze); with dzd and dze also the parameter gradient."""
+        import torch
+        nn, ne = xn.shape[0], xe.shape[0]
+        zd = torch.empty((nn, 36), dtype=torch.float32, device=xn.device)
+        ze = torch.empty((max(ne, 1), 36), dtype=torch.float32, device=xn.device)
+        torch.cuda.synchronize(xn.device)
+        ctx.check(_lib.rsd_lp_forward_dev(ctx.h, self.h, nn, ne, off.data_ptr(), src.data_ptr(), dst.data_ptr(),
+                                          xn.data_ptr(), xe.data_ptr(),
+                                          dzd.data_ptr() if dzd is not None else None,
+                                          dze.data_ptr() if dze is not None else None, zd.data_ptr(), ze.data_ptr()))
+        return zd, ze[:ne]
+
+    def adam_step(self, lr):
+        rc = _lib.rsd_lp_adam_step(self.h, ctypes.c_float(lr))
+        if rc:
+            raise RSDError(rc, "rsd_lp_adam_step")
+
+    def train_step(self, ctx, pos_t, radii_t, lattice, rpp_t, lr):
+        """One supervised step on one resistance matrix (torch CUDA tensor,
+        FP32 or FP64, the transpose view of a column-major 6N x 6N array, as
+        resistance_pp_dev returns it); returns the loss."""
+        import torch
+        loss = ctypes.c_double(0.0)
+        torch.cuda.synchronize(pos_t.device)
+        ctx.check(_lib.rsd_lp_train_step(ctx.h, self.h, radii_t.shape[0], pos_t.data_ptr(), radii_t.data_ptr(),
+                                         ctypes.byref(lattice), int(rpp_t.dtype == torch.float32),
+                                         rpp_t.data_ptr(), rpp_t.stride(1), ctypes.c_float(lr), ctypes.byref(loss)))
+        return loss.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.rsd_lp_destroy(self.h)
+            self.h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def resistance_pp_dev(ctx, tab, conf_t, radii_t, T, LB, gamma, mu_f, ews_err, precision=PREC_FP64, use_lub=True):
+    """RPP = (M^-1)_PP + rfu of a configuration on the GPU (FP64 from the
+    plain path, FP32 from the mixed form's factors), as a (6N, 6N) tensor
+    whose memory is column-major (returned as a transpose view), and the
+    lattice."""
+    import torch
+    N = radii_t.shape[0]
+    P = 6 * N
+    dt = torch.float64 if precision == PREC_FP64 else torch.float32
+    buf = torch.empty((P, P), dtype=dt, device=conf_t.device)
+    p = step_params(N, LB, T, 0.0, gamma, mu_f, ews_err, use_lub=use_lub, precision=precision)
+    lat = Lattice()
+    torch.cuda.synchronize(conf_t.device)
+    ctx.check(_lib.rsd_resistance_pp_dev(ctx.h, tab.h if tab is not None else None, ctypes.byref(p),
+                                         conf_t.data_ptr(), radii_t.data_ptr(), buf.data_ptr(), P,
+                                         ctypes.byref(lat)))
+    return buf.t(), lat
+
+
+def lp_graph_dev(ctx, pos_t, radii_t, lattice):
+    """The preconditioner's near-neighbour graph: (off, src, gap) arrays."""
+    N = radii_t.shape[0]
+    ne = ctypes.c_int32(0)
+    ctx.check(_lib.rsd_lp_graph_dev(ctx.h, N, pos_t.data_ptr(), radii_t.data_ptr(), ctypes.byref(lattice),
+                                    ctypes.byref(ne), None, None, None))
+    off = np.empty(N + 1, dtype=np.int32)
+    src = np.empty(max(ne.value, 1), dtype=np.int32)
+    gap = np.empty(max(ne.value, 1), dtype=np.float32)
+    ctx.check(_lib.rsd_lp_graph_dev(ctx.h, N, pos_t.data_ptr(), radii_t.data_ptr(), ctypes.byref(lattice),
+                                    ctypes.byref(ne), off.ctypes.data, src.ctypes.data, gap.ctypes.data))
+    return off, src[:ne.value], gap[:ne.value]
+
+
+def lp_blocks_dev(ctx, net, mode, pos_t, radii_t, lattice, rpp_t):
+    """The blocks of Z (zd: N x 6 x 6, ze: edges x 6 x 6) for a mode."""
+    import torch
+    N = radii_t.shape[0]
+    ne = ctypes.c_int32(0)
+    off, src, gap = lp_graph_dev(ctx, pos_t, radii_t, lattice)
+    zd = np.empty((N, 36), dtype=np.float32)
+    ze = np.empty((max(len(src), 1), 36), dtype=np.float32)
+    torch.cuda.synchronize(pos_t.device)
+    ctx.check(_lib.rsd_lp_blocks_dev(ctx.h, net.h if net is not None else None, int(mode), N, pos_t.data_ptr(),
+                                     radii_t.data_ptr(), ctypes.byref(lattice), int(rpp_t.dtype == torch.float32),
+                                     rpp_t.data_ptr(), rpp_t.stride(1), zd.ctypes.data, ze.ctypes.data,
+                                     ctypes.byref(ne)))
+    return zd.reshape(N, 6, 6), ze[:ne.value].reshape(-1, 6, 6), off, src
+
+
+def pcg_dev(ctx, net, mode, pos_t, radii_t, lattice, rpp_t, b_t, tol=1e-12, maxit=2000):
+    """RPP x = b (columns of b_t, a (6N,) or (nrhs, 6N) FP64 tensor in the
+    grand layout) by PCG in FP64 with preconditioner `mode`; returns x,
+    iterations and the relative residual."""
+    import torch
+    N = radii_t.shape[0]
+    b = b_t.reshape(-1, 6 * N).contiguous()
+    x = torch.empty_like(b)
+    it, res = ctypes.c_int32(0), ctypes.c_double(0.0)
+    torch.cuda.synchronize(pos_t.device)
+    ctx.check(_lib.rsd_lp_pcg_dev(ctx.h, net.h if net is not None else None, int(mode), N, pos_t.data_ptr(),
+                                  radii_t.data_ptr(), ctypes.byref(lattice), rpp_t.data_ptr(), rpp_t.stride(1),
+                                  b.shape[0], b.data_ptr(), x.data_ptr(), float(tol), int(maxit), ctypes.byref(it),
+                                  ctypes.byref(res)))
+    return x.reshape(b_t.shape), it.value, res.value
 
 
 def mu_f_dimensionless(mu_f_in=1.0):

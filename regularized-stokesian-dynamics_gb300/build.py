@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librsd_gb300.so")
-SOURCES = ["ewald.cu", "lub.cu", "dense.cu", "capi.cu", "step.cu", "mixed.cu", "noalloc.cu", "tc_gemm.cu"]
+SOURCES = ["ewald.cu", "lub.cu", "dense.cu", "capi.cu", "step.cu", "mixed.cu", "noalloc.cu", "tc_gemm.cu", "learned.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -215,38 +215,51 @@ def sheared_min_gap(pos, L, skew, a=1.0):
     return float(np.sqrt(np.einsum("ij,ij->i", d, d)).min()) - 2 * a
 
 
+def sheared_series(N, phi, g_min, seed, strains, sweeps=200, near_contact=False, a=1.0, dskew=0.005):
+    """Configurations valid at each Lees-Edwards skew mod(strain, 1) of
+    `strains` (each in [0, 1), ascending), from one packing sheared
+    incrementally: every surface gap in the sheared minimum image is at least
+    g_min (near_contact pairs keep at least 1e-4 a).  Returns the list of
+    positions (wrapped into each sheared cell), the radii and the box edge."""
+    pos, radii, L = packing(N, phi, g_min, seed, sweeps=sweeps, near_contact=near_contact, a=a)
+    hard = 2 * a + (1e-4 * a if near_contact else g_min * a)
+    push = hard + 0.01 * a
+    skew, nlist_at = 0.0, -1.0
+    out = []
+    for target in [float(x) % 1.0 for x in strains]:
+        if target < skew:
+            raise ValueError("strains must be ascending within [0, 1)")
+        while skew < target:
+            ds = min(dskew, target - skew)
+            pos[:, 0] += ds * pos[:, 2]  # affine shear of the positions with the lattice
+            skew += ds
+            LR, LI = _sheared_lattice(L, skew)
+            if skew - nlist_at > 0.05:
+                i, j, n = _pairs_within(pos, L, skew, 2 * a + 1.0)
+                nlist_at = skew
+            for _ in range(2000):
+                d = pos[j] - pos[i] + n @ LR.T
+                r = np.sqrt(np.einsum("ij,ij->i", d, d))
+                bad = r < hard
+                if not bad.any():
+                    break
+                u = d[bad] / r[bad, None] * (0.5 * (push - r[bad]))[:, None]
+                np.add.at(pos, i[bad], -u)
+                np.add.at(pos, j[bad], u)
+            else:
+                raise RuntimeError("sheared packing: overlaps remain at skew %.3f" % skew)
+        LR, LI = _sheared_lattice(L, target)
+        u = pos @ LI.T
+        out.append((u - np.floor(u)) @ LR.T)
+    return out, radii, L
+
+
 def sheared_packing(N, phi, g_min, seed, strain, sweeps=200, near_contact=False, a=1.0, dskew=0.005):
     """A packing valid at Lees-Edwards skew mod(strain, 1): every surface gap
     in the sheared minimum image is at least g_min (near_contact pairs keep
     at least 1e-4 a).  Positions are wrapped into the sheared cell."""
-    pos, radii, L = packing(N, phi, g_min, seed, sweeps=sweeps, near_contact=near_contact, a=a)
-    target = float(strain) % 1.0
-    hard = 2 * a + (1e-4 * a if near_contact else g_min * a)
-    push = hard + 0.01 * a
-    skew, nlist_at = 0.0, -1.0
-    while skew < target:
-        ds = min(dskew, target - skew)
-        pos[:, 0] += ds * pos[:, 2]  # affine shear of the positions with the lattice
-        skew += ds
-        LR, LI = _sheared_lattice(L, skew)
-        if skew - nlist_at > 0.05:
-            i, j, n = _pairs_within(pos, L, skew, 2 * a + 1.0)
-            nlist_at = skew
-        for _ in range(2000):
-            d = pos[j] - pos[i] + n @ LR.T
-            r = np.sqrt(np.einsum("ij,ij->i", d, d))
-            bad = r < hard
-            if not bad.any():
-                break
-            u = d[bad] / r[bad, None] * (0.5 * (push - r[bad]))[:, None]
-            np.add.at(pos, i[bad], -u)
-            np.add.at(pos, j[bad], u)
-        else:
-            raise RuntimeError("sheared packing: overlaps remain at skew %.3f" % skew)
-    LR, LI = _sheared_lattice(L, target)
-    u = pos @ LI.T
-    pos = (u - np.floor(u)) @ LR.T
-    return pos, radii, L
+    out, radii, L = sheared_series(N, phi, g_min, seed, [strain], sweeps, near_contact, a, dskew)
+    return out[0], radii, L
 
 
 # Workloads by number: the configurations the step is measured and checked on.

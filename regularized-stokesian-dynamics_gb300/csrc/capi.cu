@@ -166,6 +166,17 @@ extern "C" int rsd_ctx_set_wait_limits(rsd_ctx* c, int64_t tc_wait_ns, int64_t t
   return RSD_OK;
 }
 
+extern "C" int rsd_ctx_set_rpp_solver(rsd_ctx* c, int32_t mode, rsd_lp* net, double tol, int32_t maxit) {
+  if (!c) return RSD_EARG;
+  if (mode < RSD_PC_NONE || mode > RSD_PC_LEARNED || (mode == RSD_PC_LEARNED && !net) || tol < 0 || maxit < 0)
+    return rsd_fail(c, RSD_EARG, "rpp solver: mode 0-4 (4 needs a network), tol >= 0, maxit >= 0");
+  c->rpp_mode = mode;
+  c->rpp_net = net;
+  c->rpp_tol = tol;
+  c->rpp_maxit = maxit;
+  return RSD_OK;
+}
+
 extern "C" int rsd_ctx_set_mixed_real_passes(rsd_ctx* c, int passes) {
   if (!c) return RSD_EARG;
   if (passes < 1 || passes > 4) return rsd_fail(c, RSD_EARG, "mixed real-space passes must be 1 to 4");

@@ -401,9 +401,12 @@ inline unsigned nblk(int64_t n) { return (unsigned)((n + 255) / 256); }
 
 }  // namespace
 
+// rpp_out (optional): stop once RPP32 = A^-1 + rfu is formed and copy it
+// there (6nn x 6nn, ld rpp_ld, full symmetric storage, FP32).
 int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d_pos, const double* d_radii,
                     const rsd_lattice* lat, const rsd_lubtab* tab, const rsd_step_params* p, const double* ein,
-                    const double* Fe, double* U_par, double* S_hyd, rsd_step_info* info) {
+                    const double* Fe, double* U_par, double* S_hyd, rsd_step_info* info, float* rpp_out,
+                    int64_t rpp_ld) {
   cudaStream_t s = ctx->stream;
   const int64_t N = nn, n = 11 * N, P = 6 * N, Q = 5 * N;
   const int have_fe = Fe != nullptr;
@@ -458,13 +461,18 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   // block-scaled factors for one-launch-per-block refinement solves (the
   // tensor-core GEMMs that form them need leading dimensions divisible by 4)
   rsd_uhat uh_m, uh_r;
-  const bool use_uh = ctx->use_tc && n % 4 == 0 && P % 4 == 0;
+  const bool use_uh = ctx->use_tc && n % 4 == 0 && P % 4 == 0 && !rpp_out;
   if (use_uh) RSD_TRY(rsd_uhat_build(ctx, (int)n, M32, n, W_m, "m32", &uh_m));
   // A^-1 from the trailing factor block, then RPP32 = A^-1 + rfu and its factor
   copy_block_f<<<nblk(P * P), 256, 0, s>>>(P, P, M32 + Q + Q * n, n, A32, P); RSD_LAUNCH_NOTE();
   RSD_TRY(rsd_potri_upper_t<float>(ctx, (int)P, A32, P, "a32", ctx->use_tc == 3 ? 3 : 1));
   RSD_TRY(rsd_mirror_upper_t<float>(ctx, (int)P, A32, P));
   if (p->use_lub) RSD_TRY(rsd_lub_add_pp_f32(ctx, &lub, A32, P));
+  if (rpp_out) {
+    RSD_CUDA(ctx, cudaMemcpy2DAsync(rpp_out, sizeof(float) * rpp_ld, A32, sizeof(float) * P, sizeof(float) * P, P,
+                                    cudaMemcpyDeviceToDevice, s));
+    return RSD_OK;
+  }
   RSD_TRY(rsd_potrf_upper_t<float>(ctx, (int)P, A32, P, &inf, "rpp32", 3));
   if (inf) {
     info->info = inf;

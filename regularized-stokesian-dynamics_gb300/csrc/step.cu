@@ -182,13 +182,19 @@ static void ei5_of(const double E[9], double out[5]) {
 
 int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d_pos, const double* d_radii,
                     const rsd_lattice* lat, const rsd_lubtab* tab, const rsd_step_params* p, const double* ein,
-                    const double* Fe, double* U_par, double* S_hyd, rsd_step_info* info);
+                    const double* Fe, double* U_par, double* S_hyd, rsd_step_info* info, float* rpp_out = nullptr,
+                    int64_t rpp_ld = 0);
+int rsd_lp_pcg_internal(rsd_ctx* ctx, rsd_lp* net, int mode, int nn, const double* d_pos, const double* d_radii,
+                        const rsd_lattice* lat, const double* d_rpp, int64_t ld, int nrhs, const double* d_b,
+                        double* d_x, double tol, int maxit, int* iters, double* resid);
 
-extern "C" int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_step_params* p,
-                                         double* d_conf, const double* d_radii, const double* d_Fe, double* d_U_pos,
-                                         double* d_SijN, double yeta_mu[5], rsd_step_info* info) {
-  if (!ctx || !p || !d_conf || !d_radii || !d_U_pos || !d_SijN || p->nn < 1 || p->nb < 0 || p->nb > p->nn ||
-      !(p->mu_f > 0) || !(p->ews_err > 0) || (p->use_lub && !tab))
+// The step; with rpp_out it stops once RPP = (M^-1)_PP + rfu is formed and
+// copies it there (FP64 for the FP64 form, FP32 for the mixed form).
+static int step_impl(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_step_params* p, double* d_conf,
+                     const double* d_radii, const double* d_Fe, double* d_U_pos, double* d_SijN, double yeta_mu[5],
+                     rsd_step_info* info, void* rpp_out, int64_t rpp_ld, rsd_lattice* lat_out) {
+  if (!ctx || !p || !d_conf || !d_radii || (!rpp_out && (!d_U_pos || !d_SijN)) || p->nn < 1 || p->nb < 0 ||
+      p->nb > p->nn || !(p->mu_f > 0) || !(p->ews_err > 0) || (p->use_lub && !tab))
     return rsd_fail(ctx, RSD_EARG, "rsd_stepper_stokesian_dev: bad arguments");
   if (p->precision != RSD_PREC_FP64 && p->precision != RSD_PREC_MIXED)
     return rsd_fail(ctx, RSD_EARG, "unknown precision %d", p->precision);
@@ -208,6 +214,7 @@ extern "C" int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, co
   loc.NI = lat.NI;
   loc.phi = lat.phi;
   loc.LV = lat.LV;
+  if (lat_out) *lat_out = lat;
   double* M = (double*)rsd_scratch(ctx, "step_M", sizeof(double) * n * n);
   double* V = (double*)rsd_scratch(ctx, "step_vec", sizeof(double) * (4 * P + 4 * Q + 1024));
   if (!M || !V) return RSD_ENOMEM;
@@ -259,27 +266,62 @@ extern "C" int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, co
     int nc = 0;
     if (p->use_lub) RSD_TRY(rsd_lub_assemble(ctx, tab, nn, p->nb, 1, d_conf, d_radii, &lat, p->mu_f, M, n, 1, &nc));
     loc.n_contact = nc;
+    if (rpp_out) {
+      RSD_CUDA(ctx, cudaMemcpy2DAsync(rpp_out, sizeof(double) * rpp_ld, M, sizeof(double) * n, sizeof(double) * P, P,
+                                      cudaMemcpyDeviceToDevice, s));
+      RSD_CUDA(ctx, cudaStreamSynchronize(s));
+      if (info) *info = loc;
+      return RSD_OK;
+    }
     cudaEventRecord(ctx->ev[3], s);
     // RHS [Fe + RPQ EIN, RPQ EIN]; RPP factored in place (RPQ, RQQ untouched)
     const double* RPQ = M + P * n;
     RSD_CUDA(ctx, cudaMemcpyAsync(X, Fe, sizeof(double) * P, cudaMemcpyDeviceToDevice, s));
     rsd_gemm_f64(s, (int)P, 1, (int)Q, 1.0, RPQ, n, 0, ein, Q, 0, 1.0, X, P);
     rsd_gemm_f64(s, (int)P, 1, (int)Q, 1.0, RPQ, n, 0, ein, Q, 0, 0.0, X + P, P);
-    int info_r = 0;
-    RSD_TRY(rsd_potrf_upper_tag(ctx, (int)P, M, n, &info_r, "rpp"));
-    if (info_r) {
-      loc.info = info_r;
-      if (info) *info = loc;
-      return info_r;
+    bool solved = false;
+    if (ctx->rpp_mode != RSD_PC_NONE) {
+      // PCG on RPP with the chosen preconditioner; the factorisation stays
+      // the fallback when it does not reach the tolerance
+      double* B = (double*)rsd_scratch(ctx, "step_rhs", sizeof(double) * 2 * P);
+      if (!B) return RSD_ENOMEM;
+      RSD_CUDA(ctx, cudaMemcpyAsync(B, X, sizeof(double) * 2 * P, cudaMemcpyDeviceToDevice, s));
+      const double tol = ctx->rpp_tol > 0 ? ctx->rpp_tol : 1e-12;
+      int it = 0;
+      double res = 0.0;
+      RSD_TRY(rsd_lp_pcg_internal(ctx, (rsd_lp*)ctx->rpp_net, ctx->rpp_mode, nn, d_conf, d_radii, &lat, M, n, 2, B, X,
+                                  tol, ctx->rpp_maxit > 0 ? ctx->rpp_maxit : 1000, &it, &res));
+      loc.rpp_iterations = it;
+      if (res <= tol) {
+        solved = true;
+      } else {
+        loc.rpp_iterations = -it;  // did not converge: factorisation below
+        RSD_CUDA(ctx, cudaMemcpyAsync(X, B, sizeof(double) * 2 * P, cudaMemcpyDeviceToDevice, s));
+      }
     }
-    RSD_TRY(rsd_potrs_upper_tag(ctx, (int)P, M, n, X, P, 2, "rpp"));
+    if (!solved) {
+      int info_r = 0;
+      RSD_TRY(rsd_potrf_upper_tag(ctx, (int)P, M, n, &info_r, "rpp"));
+      if (info_r) {
+        loc.info = info_r;
+        if (info) *info = loc;
+        return info_r;
+      }
+      RSD_TRY(rsd_potrs_upper_tag(ctx, (int)P, M, n, X, P, 2, "rpp"));
+    }
     // SijN_hyd = RPQ^T RPP^-1 RPQ EIN - RQQ EIN
     rsd_gemm_f64(s, (int)Q, 1, (int)P, 1.0, RPQ, n, 1, X + P, P, 0, 0.0, S, Q);
     rsd_gemm_f64(s, (int)Q, 1, (int)Q, -1.0, M + P + P * n, n, 0, ein, Q, 0, 1.0, S, Q);
     RSD_CUDA(ctx, cudaGetLastError());
   } else {
     cudaEventRecord(ctx->ev[2], s);
-    RSD_TRY(rsd_mixed_solve(ctx, nn, M, n, d_conf, d_radii, &lat, tab, p, ein, d_Fe ? Fe : nullptr, Upar, S, &loc));
+    RSD_TRY(rsd_mixed_solve(ctx, nn, M, n, d_conf, d_radii, &lat, tab, p, ein, d_Fe ? Fe : nullptr, Upar, S, &loc,
+                            (float*)rpp_out, rpp_ld));
+    if (rpp_out) {
+      RSD_CUDA(ctx, cudaStreamSynchronize(s));
+      if (info) *info = loc;
+      return RSD_OK;
+    }
     cudaEventRecord(ctx->ev[3], s);
   }
   cudaEventRecord(ctx->ev[4], s);
@@ -337,6 +379,21 @@ extern "C" int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, co
   if (info) *info = loc;
   if (ctx->h_info[8]) return rsd_fail(ctx, RSD_ENAN, "non-finite velocity (main.f90:223 NaN check)");
   return RSD_OK;
+}
+
+extern "C" int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_step_params* p,
+                                         double* d_conf, const double* d_radii, const double* d_Fe, double* d_U_pos,
+                                         double* d_SijN, double yeta_mu[5], rsd_step_info* info) {
+  return step_impl(ctx, tab, p, d_conf, d_radii, d_Fe, d_U_pos, d_SijN, yeta_mu, info, nullptr, 0, nullptr);
+}
+
+extern "C" int rsd_resistance_pp_dev(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_step_params* p,
+                                     const double* d_conf, const double* d_radii, void* d_rpp, int64_t ld,
+                                     rsd_lattice* lat) {
+  if (!ctx || !p || !d_rpp || ld < 6LL * p->nn) return rsd_fail(ctx, RSD_EARG, "rsd_resistance_pp_dev: bad arguments");
+  rsd_step_info info{};
+  return step_impl(ctx, tab, p, const_cast<double*>(d_conf), d_radii, nullptr, nullptr, nullptr, nullptr, &info, d_rpp,
+                   ld, lat);
 }
 
 extern "C" int rsd_stepper_stokesian(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_step_params* p, double* conf,

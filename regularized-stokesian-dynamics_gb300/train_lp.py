@@ -1,0 +1,117 @@
+"""Training of the learned preconditioner of the RPP solve (run on a GPU).
+
+    python regularized-stokesian-dynamics_gb300/train_lp.py [--systems 2000] [--out lp_params.npy]
+
+Data: the learned-preconditioner workload -- N = 1000 spheres of radius 1 at
+volume fraction 0.5, a quarter of them in near-contact pairs with surface
+gaps log-uniform in [1e-4, 1e-1] (configs.packing, near_contact=True) --
+generated by the method itself: each trajectory starts from a seeded packing
+sheared to its own Lees-Edwards strain (configs.sheared_series) and is
+advanced by the mixed-precision step (rsd_stepper_stokesian_dev, dt 5e-4,
+shear rate 1); every `stride` steps the resistance matrix RPP of the current
+configuration (FP32, from the mixed form's factors: rsd_resistance_pp_dev)
+is one training sample.  Each sample makes one supervised step: the network
+emits the blocks of Z, the loss is their mean squared difference from the
+exact FSAI blocks of that matrix, and Adam updates the weights (kernels in
+csrc/learned.cu).  After training, one held-out system in FP64 gives the PCG
+iteration counts of every preconditioner.  Prints one JSON line and writes
+the FP32 parameters to --out.
+"""
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--systems", type=int, default=2000)
+    ap.add_argument("--trajectories", type=int, default=10)
+    ap.add_argument("--stride", type=int, default=2)
+    ap.add_argument("--N", type=int, default=1000)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--sweeps", type=int, default=100)
+    ap.add_argument("--out", default=os.path.join(HERE, "lp_params.npy"))
+    ap.add_argument("--seed", type=int, default=20264000)
+    args = ap.parse_args()
+    import torch
+
+    import __graft_entry__ as ge
+    rsd = ge.load_package()
+    dev = torch.device("cuda", 0)
+    ctx = rsd.Context(0)
+    tab = rsd.LubTab(rsd.lubdat_dir())
+    mu = rsd.mu_f_dimensionless(1.0)
+    net = rsd.LearnedPreconditioner(0, seed=args.seed)
+    N, dt = args.N, 5e-4
+    per_traj = (args.systems + args.trajectories - 1) // args.trajectories
+    log, done, t0 = [], 0, time.time()
+    U_t = torch.empty(6 * N, dtype=torch.float64, device=dev)
+    S_t = torch.empty(5 * N, dtype=torch.float64, device=dev)
+    k = 0
+    while done < args.systems and k < 3 * args.trajectories:  # more trajectories if one stops early
+        strain = (k % args.trajectories) / args.trajectories
+        series, radii, L = rsd.configs.sheared_series(N, 0.5, 1e-4, args.seed + k, [strain], sweeps=args.sweeps,
+                                                      near_contact=True)
+        conf_t = torch.tensor(series[0], dtype=torch.float64, device=dev)
+        radii_t = torch.tensor(radii, dtype=torch.float64, device=dev)
+        T = strain
+        for s in range(per_traj):
+            if done >= args.systems:
+                break
+            try:
+                rpp, lat = rsd.resistance_pp_dev(ctx, tab, conf_t, radii_t, T, [L, L, L], 1.0, mu, 1e-10,
+                                                 precision=rsd.PREC_MIXED)
+            except rsd.RSDError as e:  # e.g. a factor that is not positive: next trajectory
+                print("trajectory %d stops at strain %.3f: %s" % (k, T, e), flush=True)
+                break
+            frac = done / args.systems
+            lr = args.lr * (1.0 if frac < 0.5 else (0.25 if frac < 0.8 else 0.05))
+            try:
+                loss = net.train_step(ctx, conf_t, radii_t, lat, rpp, lr)
+            except rsd.RSDError as e:  # a local block not positive definite in FP32: skip the sample
+                print("sample skipped at strain %.3f: %s" % (T, e), flush=True)
+                loss = None
+            if loss is None:
+                T += dt
+                continue
+            done += 1
+            if done % 50 == 0 or done == 1:
+                log.append((done, loss))
+                print("sample %d traj %d strain %.3f loss %.4e (%.0f s)" % (done, k, T, loss, time.time() - t0),
+                      flush=True)
+            try:
+                for _ in range(args.stride):
+                    rsd.stepper_stokesian_dev(ctx, tab, conf_t, radii_t, T, dt, [L, L, L], 1.0, mu, 1e-10, U_t, S_t,
+                                              precision=rsd.PREC_MIXED)
+                    T += dt
+            except rsd.RSDError as e:
+                print("trajectory %d stops at strain %.3f: %s" % (k, T, e), flush=True)
+                break
+        k += 1
+    params = net.params()
+    np.save(args.out, params)
+    # held-out evaluation in FP64
+    series, radii, L = rsd.configs.sheared_series(N, 0.5, 1e-4, args.seed + 999, [0.5], sweeps=args.sweeps,
+                                                  near_contact=True)
+    conf_t = torch.tensor(series[0], dtype=torch.float64, device=dev)
+    radii_t = torch.tensor(radii, dtype=torch.float64, device=dev)
+    rpp, lat = rsd.resistance_pp_dev(ctx, tab, conf_t, radii_t, 0.5, [L, L, L], 1.0, mu, 1e-10)
+    b = torch.tensor(np.random.default_rng(1).normal(size=6 * N), device=dev)
+    evals = {}
+    for name, mode in (("none", rsd.PC_NONE), ("jacobi", rsd.PC_JACOBI), ("block_jacobi", rsd.PC_BLOCK_JACOBI),
+                       ("fsai", rsd.PC_FSAI), ("learned", rsd.PC_LEARNED)):
+        x, it, res = rsd.pcg_dev(ctx, net, mode, conf_t, radii_t, lat, rpp, b, tol=1e-12, maxit=20000)
+        evals[name] = {"iterations": it, "residual": res}
+    print(json.dumps({"trained_on": done, "N": N, "loss_log": log, "final_loss": log[-1][1] if log else None,
+                      "seconds": time.time() - t0, "heldout_pcg": evals, "out": args.out}), flush=True)
+
+
+if __name__ == "__main__":
+    main()
