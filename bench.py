@@ -24,8 +24,8 @@ strain-averaged steps/s.
 Prints one JSON line (rank 0).  With --gpus N > 1 under torchrun every rank
 steps its own independent replica (the step does not shard; replicas only).
 --impl reference times the CPU restatement of the reference's routines on the
-host cores instead (bounded samples per step, extrapolated; see
-cpu_step_sample()).
+host cores instead (bounded samples per step, extrapolated; see CpuModel).
+--mode long runs the 10,000-step long run through the driver's time loop.
 """
 import argparse
 import json
@@ -65,6 +65,13 @@ def parse():
                     help="FP32 factorisations of the mixed form: 1 TF32/3xTF32 per factor, 3 all 3xTF32, 0 SIMT")
     ap.add_argument("--validate-cpu-model", action="store_true",
                     help="(reference arm) time one whole CPU step at N=512 and compare it with the sample model")
+    ap.add_argument("--refinement", default="gmres", choices=["gmres", "stationary"],
+                    help="mixed form's FP64 refinement: flexible GMRES or the stationary iteration")
+    ap.add_argument("--mode", default="cycle", choices=["cycle", "long"],
+                    help="cycle: the strain-stratified headline; long: the 10,000-step run through the driver")
+    ap.add_argument("--long-steps", type=int, default=10000)
+    ap.add_argument("--plain-steps", type=int, default=5, help="(long) plain FP64 steps beside the mixed run")
+    ap.add_argument("--out-dir", default=None, help="(long) where yeta_mu.txt and the viscosity series go")
     return ap.parse_args()
 
 
@@ -362,11 +369,108 @@ def read_traffic(key):
     return None
 
 
+# ---------------------------------------------------------------- long run
+def periodic_fts_control(path, dt, steps, k_write, linerr=1e-10):
+    """The reference's example control_file.dat switched to the periodic FTS
+    case with lubrication at shear rate 1 (records as INIT_READ_CONTROL reads
+    them, initial_conf.f90:109-189)."""
+    src = open(os.path.join(ROOT, "tests", "golden", "io", "control_file.dat")).read().split("\n")
+    end = (steps - 1) * dt  # main.f90 leaves the loop once T > END_TIME: `steps` steps
+    rec = {1: ".true.", 3: ".true.", 7: ".false.", 9: ".true.", 10: ".true.", 18: "1.0", 19: "1.0", 20: "0.0",
+           27: "1.0", 33: repr(linerr), 36: "0.0", 37: repr(end), 38: repr(dt), 39: str(k_write)}
+    for i, v in rec.items():
+        src[i] = v + "    ! periodic FTS case with lubrication, shear rate 1"
+    with open(path, "w") as fp:
+        fp.write("\n".join(src))
+
+
+def long_run(args):
+    """The long dense run: N = 2048, phi = 0.5, gap >= 1e-4 a, shear rate 1,
+    dt = 5e-4, --long-steps steps (10,000: strain 5, five Lees-Edwards
+    cycles) through the driver's time loop (driver.py, main.f90's loop and
+    files) on the fused mixed-precision step; the relative viscosity of every
+    step is kept (yeta_mu.txt holds every K_WRITE-th, as main.f90 writes it).
+    The plain FP64 form runs its own first --plain-steps steps from the same
+    start for the viscosity difference."""
+    import tempfile
+
+    import torch
+
+    import __graft_entry__ as ge
+    rsd = ge.load_package()
+    out = args.out_dir or tempfile.mkdtemp(prefix="rsd_long_")
+    os.makedirs(out, exist_ok=True)
+    work = tempfile.mkdtemp(prefix="rsd_long_work_")
+    N, dt = args.N, args.dt
+    pos, radii, L = rsd.configs.packing(N, args.phi, args.gmin, replica_seed(0), sweeps=args.sweeps)
+    control, init = os.path.join(work, "control_file.dat"), os.path.join(work, "initial_config.dat")
+    periodic_fts_control(control, dt, args.long_steps, 100)
+    rsd.driver_files.write_initial_config(init, pos, radii, [L, L, L])
+    ctx = rsd.Context(0)
+    ctx.set_tensor_cores(args.tensor_cores)
+    tab = rsd.LubTab(rsd.lubdat_dir())
+    series = []
+
+    def step(conf, r, T, dt_, LB, gamma, mu_f, ews):
+        o = rsd.STEPPER_Stokesian(ctx, tab, conf, r, T, dt_, LB, gamma, mu_f, ews, precision=rsd.PREC_MIXED)
+        i = o["info"]
+        series.append((T, float(o["yeta_mu"][0]), i.NR, i.NI, i.iterations, i.residual))
+        return o
+
+    t0 = time.perf_counter()
+    err = None
+    try:
+        res = rsd.driver.run(control, init, step, os.path.join(work, "output.VTF"), os.path.join(out, "yeta_mu.txt"))
+    except Exception as e:  # report how far the run got
+        err = "%s: %s" % (type(e).__name__, e)
+        res = {"steps": len(series)}
+    wall = time.perf_counter() - t0
+    with open(os.path.join(out, "eta_r_series.csv"), "w") as fp:
+        fp.write("# strain, relative viscosity, NR, NI, refinement iterations, residual\n")
+        for T, y, nr, ni, it, rr in series:
+            fp.write("%.6f,%.12e,%d,%d,%d,%.3e\n" % (T, y, nr, ni, it, rr))
+    # plain FP64 beside the first steps, from the same start
+    mu = rsd.mu_f_dimensionless(1.0)
+    conf = pos.copy()
+    plain = []
+    d = rsd.driver_files.read_initial_config(init)
+    conf = np.array(d["conf"])
+    T = 0.0
+    for k in range(min(args.plain_steps, len(series))):
+        o = rsd.STEPPER_Stokesian(ctx, tab, conf, radii, T, dt, [L, L, L], 1.0, mu, 1e-10, precision=rsd.PREC_FP64)
+        plain.append(float(o["yeta_mu"][0]))
+        conf, T = o["conf"], T + dt
+    per_strain = []
+    ys = np.array([s_[1] for s_ in series]) if series else np.zeros(0)
+    ts = np.array([s_[0] for s_ in series]) if series else np.zeros(0)
+    for c in range(int(math.ceil(ts.max() + 1e-12)) if len(ts) else 0):
+        sel = (ts >= c) & (ts < c + 1)
+        if sel.any():
+            per_strain.append({"strain": [c, c + 1], "eta_r_mean": float(ys[sel].mean()),
+                               "eta_r_std": float(ys[sel].std()), "steps": int(sel.sum())})
+    its = [s_[4] for s_ in series]
+    line = {"metric": "long run: steps/s N=%d phi=%.2f, %d steps through the driver" % (N, args.phi, args.long_steps),
+            "value": len(series) / wall if wall > 0 else None, "unit": "steps/s", "steps": len(series),
+            "wall_s": wall, "completed": err is None and len(series) == args.long_steps, "error": err,
+            "precision": "mixed", "strain_end": float(ts.max()) if len(ts) else 0.0,
+            "eta_r_per_strain_unit": per_strain,
+            "refinement_iterations": {"mean": float(np.mean(its)) if its else None,
+                                      "max": int(np.max(its)) if its else None},
+            "NR_range": [int(min(s_[2] for s_ in series)), int(max(s_[2] for s_ in series))] if series else None,
+            "plain_fp64_eta_r": plain, "mixed_eta_r_first": [s_[1] for s_ in series[:len(plain)]],
+            "eta_r_rel_diff_first_steps": [abs(a - b) / abs(b) for a, b in zip([s_[1] for s_ in series], plain)],
+            "files": {"yeta_mu": os.path.join(out, "yeta_mu.txt"), "series": os.path.join(out, "eta_r_series.csv")}}
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- GPU arm
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+        return
+    if args.mode == "long":
+        long_run(args)
         return
     import torch
     import torch.distributed as dist
@@ -388,6 +492,7 @@ def main():
     mu = rsd.mu_f_dimensionless(1.0)
     ctx = rsd.Context(local)
     ctx.set_tensor_cores(args.tensor_cores)
+    ctx.set_refinement(1 if args.refinement == "gmres" else 0)
     tab = rsd.LubTab(rsd.lubdat_dir())
     radii_t = torch.tensor(radii, dtype=torch.float64, device=dev)
     conf = [torch.tensor(p, dtype=torch.float64, device=dev) for p in series]
@@ -532,7 +637,7 @@ def main():
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic (seeded sphere packing sheared to each stratum, no dataset)",
             "config": {"workload": workload_name(args), "precision": args.precision,
-                       "tensor_cores": args.tensor_cores, "strata_skew": skews,
+                       "tensor_cores": args.tensor_cores, "refinement": args.refinement, "strata_skew": skews,
                        "mean_images_per_pair": float(np.mean([sum(images(i[1], i[2])) for i in infos])),
                        "l2": "inputs larger than L2 (grand mobility %.2f GB)" % (8 * (11 * N) ** 2 / 1e9),
                        "parallelism": "replicas" if ws > 1 else "single GPU"},

@@ -103,6 +103,7 @@ _sig("rsd_ctx_set_mixed_lambda_scale", _i, [_vp, _d])
 _sig("rsd_ctx_set_mixed_real_passes", _i, [_vp, _i32])
 _sig("rsd_ctx_set_correction_method", _i, [_vp, _i32])
 _sig("rsd_ctx_set_wait_limits", _i, [_vp, _i64, _i64])
+_sig("rsd_ctx_set_refinement", _i, [_vp, _i32, _i32])
 _sig("rsd_ctx_set_rpp_solver", _i, [_vp, _i32, _vp, _d, _i32])
 _sig("rsd_lp_param_count", ctypes.c_int64, [])
 _sig("rsd_lp_create", _i, [ctypes.POINTER(_vp), _i, _vp, ctypes.c_uint64])
@@ -196,6 +197,11 @@ class Context:
         0.5 s and 2^21 polls); a wait that gives up makes the call return
         RSD_ETIMEOUT."""
         self.check(_lib.rsd_ctx_set_wait_limits(self.h, int(tc_wait_ns), int(tri_spin_polls)))
+
+    def set_refinement(self, mode=1, restart=30):
+        """Mixed form's refinement: 1 flexible GMRES (default), 0 the
+        stationary iteration."""
+        self.check(_lib.rsd_ctx_set_refinement(self.h, int(mode), int(restart)))
 
     def set_rpp_solver(self, mode=0, net=None, tol=0.0, maxit=0):
         """RPP solve of the plain FP64 step: PC_NONE keeps the Cholesky

@@ -166,6 +166,15 @@ extern "C" int rsd_ctx_set_wait_limits(rsd_ctx* c, int64_t tc_wait_ns, int64_t t
   return RSD_OK;
 }
 
+extern "C" int rsd_ctx_set_refinement(rsd_ctx* c, int32_t mode, int32_t restart) {
+  if (!c) return RSD_EARG;
+  if ((mode != 0 && mode != 1) || restart < 0 || restart > 30)
+    return rsd_fail(c, RSD_EARG, "refinement: mode 0 or 1, restart 0..30");
+  c->refine_gmres = mode;
+  c->gmres_restart = restart > 0 ? restart : 30;
+  return RSD_OK;
+}
+
 extern "C" int rsd_ctx_set_rpp_solver(rsd_ctx* c, int32_t mode, rsd_lp* net, double tol, int32_t maxit) {
   if (!c) return RSD_EARG;
   if (mode < RSD_PC_NONE || mode > RSD_PC_LEARNED || (mode == RSD_PC_LEARNED && !net) || tol < 0 || maxit < 0)

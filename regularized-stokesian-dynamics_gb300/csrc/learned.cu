@@ -711,6 +711,13 @@ __global__ void lp_cg_roll(double* sc) { sc[0] = sc[2]; }
 
 inline unsigned nb256(int64_t n) { return (unsigned)((n + 255) / 256); }
 
+// every launch is checked at once: a refused launch leaves its outputs unwritten
+#define RSD_LP_CHECK()                                                                  \
+  do {                                                                                  \
+    cudaError_t _le = cudaGetLastError();                                               \
+    if (_le != cudaSuccess) return rsd_cuda_check(ctx, _le, "learned-preconditioner launch"); \
+  } while (0)
+
 }  // namespace
 
 // ------------------------------------------------------------------ host
@@ -726,7 +733,7 @@ static int lp_build_graph(rsd_ctx* ctx, int nn, const double* d_pos, const doubl
   rsd_lat_dev L = rsd_lat_pack(lat);
   int* cnt = (int*)rsd_scratch(ctx, "lp_cnt", sizeof(int) * (nn + 1));
   if (!cnt) return RSD_ENOMEM;
-  lp_count<<<nn, 256, 0, s>>>(nn, L, d_pos, d_radii, cnt); RSD_LAUNCH_NOTE();
+  lp_count<<<nn, 256, 0, s>>>(nn, L, d_pos, d_radii, cnt); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
   std::vector<int> h(nn + 1);
   RSD_CUDA(ctx, cudaMemcpyAsync(h.data(), cnt, sizeof(int) * nn, cudaMemcpyDeviceToHost, s));
   RSD_CUDA(ctx, cudaStreamSynchronize(s));
@@ -744,9 +751,9 @@ static int lp_build_graph(rsd_ctx* ctx, int nn, const double* d_pos, const doubl
   if (!g->off || !g->src || !g->dst || !g->rev || !g->lower || !g->gap) return RSD_ENOMEM;
   RSD_CUDA(ctx, cudaMemcpyAsync(g->off, off.data(), sizeof(int) * (nn + 1), cudaMemcpyHostToDevice, s));
   if (ne > 0) {
-    lp_fill<<<(nn + 7) / 8, 256, 0, s>>>(nn, L, d_pos, d_radii, g->off, g->src, g->dst, g->gap); RSD_LAUNCH_NOTE();
-    lp_rev<<<nb256(ne), 256, 0, s>>>(ne, g->off, g->src, g->dst, g->rev); RSD_LAUNCH_NOTE();
-    lp_lower_flags<<<nb256(ne), 256, 0, s>>>(ne, g->src, g->dst, g->lower); RSD_LAUNCH_NOTE();
+    lp_fill<<<(nn + 7) / 8, 256, 0, s>>>(nn, L, d_pos, d_radii, g->off, g->src, g->dst, g->gap); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
+    lp_rev<<<nb256(ne), 256, 0, s>>>(ne, g->off, g->src, g->dst, g->rev); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
+    lp_lower_flags<<<nb256(ne), 256, 0, s>>>(ne, g->src, g->dst, g->lower); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
   }
   RSD_CUDA(ctx, cudaStreamSynchronize(s));  // off must outlive the host vector's copy
   RSD_CUDA(ctx, cudaGetLastError());
@@ -763,13 +770,13 @@ static int lp_scale_features(rsd_ctx* ctx, const lp_graph& g, const T* A, int64_
   if (!*dinv) return RSD_ENOMEM;
   int* bad = ctx->d_info + 9;
   RSD_CUDA(ctx, cudaMemsetAsync(bad, 0, sizeof(int), s));
-  lp_dinv<T><<<nb256(6 * nn), 256, 0, s>>>(nn, A, ld, *dinv, bad); RSD_LAUNCH_NOTE();
+  lp_dinv<T><<<nb256(6 * nn), 256, 0, s>>>(nn, A, ld, *dinv, bad); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
   if (xn) {
     *xn = (__nv_bfloat16*)rsd_scratch(ctx, "lp_xn", sizeof(__nv_bfloat16) * (size_t)nn * NF_NODE);
     *xe = (__nv_bfloat16*)rsd_scratch(ctx, "lp_xe", sizeof(__nv_bfloat16) * ((size_t)ne * NF_EDGE + 1));
     if (!*xn || !*xe) return RSD_ENOMEM;
     lp_features<T><<<nb256((int64_t)nn * 36 + (int64_t)ne * NF_EDGE), 256, 0, s>>>(nn, ne, A, ld, *dinv, g.src, g.dst,
-                                                                                   g.gap, *xn, *xe); RSD_LAUNCH_NOTE();
+                                                                                   g.gap, *xn, *xe); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
   }
   RSD_CUDA(ctx, cudaMemcpyAsync(ctx->h_info + 9, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
   RSD_CUDA(ctx, cudaStreamSynchronize(s));
@@ -791,7 +798,7 @@ static int lp_exact_fsai(rsd_ctx* ctx, const lp_graph& g, const T* A, int64_t ld
   }
   int* bad = ctx->d_info + 10;
   RSD_CUDA(ctx, cudaMemsetAsync(bad, 0, sizeof(int), s));
-  lp_fsai<T><<<g.nn, FS_THREADS, smem, s>>>(g.nn, self_only, A, ld, dinv, g.off, g.src, g.gap, zd, ze, bad); RSD_LAUNCH_NOTE();
+  lp_fsai<T><<<g.nn, FS_THREADS, smem, s>>>(g.nn, self_only, A, ld, dinv, g.off, g.src, g.gap, zd, ze, bad); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
   RSD_CUDA(ctx, cudaMemcpyAsync(ctx->h_info + 10, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
   RSD_CUDA(ctx, cudaStreamSynchronize(s));
   if (ctx->h_info[10]) return rsd_fail(ctx, RSD_ENAN, "FSAI: a local block of RPP is not positive definite");
@@ -812,7 +819,7 @@ static int lp_layer(rsd_ctx* ctx, const LayerArgs& a) {
     attr = true;
   }
   const int grid = (int)std::min<int64_t>((a.rows + LW - 1) / LW, 8LL * (ctx->sm_count > 0 ? ctx->sm_count : 148));
-  lp_layer_fwd<<<grid, 32 * LW, smem, ctx->stream>>>(a); RSD_LAUNCH_NOTE();
+  lp_layer_fwd<<<grid, 32 * LW, smem, ctx->stream>>>(a); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
   return RSD_OK;
 }
 
@@ -851,7 +858,7 @@ static int lp_forward(rsd_ctx* ctx, rsd_lp* net, const lp_graph& g, const __nv_b
     a.res = A->m[l];
     a.sum = A->m[l + 1];
     RSD_TRY(lp_layer(ctx, a));
-    lp_aggregate<<<nb256((int64_t)nn * H), 256, 0, ctx->stream>>>(nn, g.off, A->msg[l], A->agg[l]); RSD_LAUNCH_NOTE();
+    lp_aggregate<<<nb256((int64_t)nn * H), 256, 0, ctx->stream>>>(nn, g.off, A->msg[l], A->agg[l]); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
     a = LayerArgs{nn, 2 * H, H, 1, {seg(A->h[l], nullptr, H), seg(A->agg[l], nullptr, H)}, 2, W + LAY.upd_w[l],
                   B + LAY.upd_b[l], A->u[l]};
     a.res = A->h[l];
@@ -884,9 +891,9 @@ static int lp_layer_back(rsd_ctx* ctx, rsd_lp* net, LayerBwdArgs b, int64_t w_of
     RSD_CUDA(ctx, cudaFuncSetAttribute(lp_layer_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
     attr = true;
   }
-  lp_layer_bwd<<<nparts, 256, smem, ctx->stream>>>(b); RSD_LAUNCH_NOTE();
+  lp_layer_bwd<<<nparts, 256, smem, ctx->stream>>>(b); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
   lp_reduce_parts<<<nb256(nw + b.kout), 256, 0, ctx->stream>>>(nparts, nw, b.kout, part, net->g + w_off,
-                                                                net->g + b_off); RSD_LAUNCH_NOTE();
+                                                                net->g + b_off); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
   return RSD_OK;
 }
 
@@ -925,7 +932,7 @@ static int lp_backward(rsd_ctx* ctx, rsd_lp* net, const lp_graph& g, const __nv_
     // m[l+1] = m[l] + msg[l]: dmsg = dm + dagg[dst]; dm flows to m[l]
     RSD_CUDA(ctx, cudaMemcpyAsync(dmsg, dm, sizeof(float) * (size_t)ne * H, cudaMemcpyDeviceToDevice, s));
     if (ne > 0) {
-      lp_agg_bwd<<<nb256((int64_t)ne * H), 256, 0, s>>>(ne, g.dst, dagg, dmsg); RSD_LAUNCH_NOTE();
+      lp_agg_bwd<<<nb256((int64_t)ne * H), 256, 0, s>>>(ne, g.dst, dagg, dmsg); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
     }
     RSD_CUDA(ctx, cudaMemcpyAsync(dm2, dm, sizeof(float) * (size_t)ne * H, cudaMemcpyDeviceToDevice, s));
     b = LayerBwdArgs{ne, 3 * H, H, 1, {seg(A.h[l], g.dst, H), seg(A.h[l], g.src, H), seg(A.m[l], nullptr, H)}, 3,
@@ -981,29 +988,29 @@ static int lp_pcg(rsd_ctx* ctx, int mode, const lp_graph& g, const double* A, in
     if (mode == RSD_PC_NONE) {
       RSD_CUDA(ctx, cudaMemcpyAsync(out, in, sizeof(double) * P, cudaMemcpyDeviceToDevice, s));
     } else if (mode == RSD_PC_JACOBI) {
-      lp_scale<<<nb256(P), 256, 0, s>>>(P, dinv, in, out); RSD_LAUNCH_NOTE();
+      lp_scale<<<nb256(P), 256, 0, s>>>(P, dinv, in, out); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
     } else {
-      lp_apply_z<<<nb256(P), 256, 0, s>>>(nn, g.off, g.src, zd, ze, dinv, in, tmp); RSD_LAUNCH_NOTE();
-      lp_apply_zt<<<nb256(P), 256, 0, s>>>(nn, g.off, g.src, g.rev, zd, ze, dinv, tmp, out); RSD_LAUNCH_NOTE();
+      lp_apply_z<<<nb256(P), 256, 0, s>>>(nn, g.off, g.src, zd, ze, dinv, in, tmp); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
+      lp_apply_zt<<<nb256(P), 256, 0, s>>>(nn, g.off, g.src, g.rev, zd, ze, dinv, tmp, out); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
     }
     return RSD_OK;
   };
   // the operator in the particle-block layout: q = P A P^T p
   auto matvec = [&](const double* in, double* out) -> int {
-    lp_from_blk<<<nb256(P), 256, 0, s>>>(nn, in, tmp); RSD_LAUNCH_NOTE();
+    lp_from_blk<<<nb256(P), 256, 0, s>>>(nn, in, tmp); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
     RSD_TRY(rsd_gemv<double>(ctx, 0, P, P, 1.0, A, ld, tmp, P, 1, 0.0, rb, P));
-    lp_to_blk<<<nb256(P), 256, 0, s>>>(nn, rb, out); RSD_LAUNCH_NOTE();
+    lp_to_blk<<<nb256(P), 256, 0, s>>>(nn, rb, out); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
     return RSD_OK;
   };
   double h[4];
   for (int c = 0; c < nrhs; c++) {
     double* xc = x + (size_t)c * P;
     // r = b (block layout), x = 0
-    lp_to_blk<<<nb256(P), 256, 0, s>>>(nn, b + (size_t)c * P, r); RSD_LAUNCH_NOTE();
+    lp_to_blk<<<nb256(P), 256, 0, s>>>(nn, b + (size_t)c * P, r); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
     RSD_CUDA(ctx, cudaMemsetAsync(xc, 0, sizeof(double) * P, s));
     RSD_TRY(precond(r, z));
     RSD_CUDA(ctx, cudaMemcpyAsync(p, z, sizeof(double) * P, cudaMemcpyDeviceToDevice, s));
-    lp_dots<<<1, 256, 0, s>>>(P, 2, r, z, r, r, sc); RSD_LAUNCH_NOTE();  // sc[0] = rz, sc[1] = rr
+    lp_dots<<<1, 256, 0, s>>>(P, 2, r, z, r, r, sc); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();  // sc[0] = rz, sc[1] = rr
     RSD_CUDA(ctx, cudaMemcpyAsync(h, sc, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
     RSD_CUDA(ctx, cudaStreamSynchronize(s));
     const double bn = sqrt(h[1]) > 0 ? sqrt(h[1]) : 1.0;
@@ -1011,12 +1018,12 @@ static int lp_pcg(rsd_ctx* ctx, int mode, const lp_graph& g, const double* A, in
     int it = 0;
     while (rn > tol * bn && it < maxit) {
       RSD_TRY(matvec(p, q));
-      lp_dots<<<1, 256, 0, s>>>(P, 1, p, q, p, q, sc + 1); RSD_LAUNCH_NOTE();  // sc[1] = pq
-      lp_cg_xr<<<nb256(P), 256, 0, s>>>(P, sc, p, q, xc, r); RSD_LAUNCH_NOTE();
+      lp_dots<<<1, 256, 0, s>>>(P, 1, p, q, p, q, sc + 1); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();  // sc[1] = pq
+      lp_cg_xr<<<nb256(P), 256, 0, s>>>(P, sc, p, q, xc, r); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
       RSD_TRY(precond(r, z));
-      lp_dots<<<1, 256, 0, s>>>(P, 2, r, z, r, r, sc + 2); RSD_LAUNCH_NOTE();  // sc[2] = rz', sc[3] = rr
-      lp_cg_p<<<nb256(P), 256, 0, s>>>(P, sc, z, p); RSD_LAUNCH_NOTE();
-      lp_cg_roll<<<1, 1, 0, s>>>(sc); RSD_LAUNCH_NOTE();
+      lp_dots<<<1, 256, 0, s>>>(P, 2, r, z, r, r, sc + 2); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();  // sc[2] = rz', sc[3] = rr
+      lp_cg_p<<<nb256(P), 256, 0, s>>>(P, sc, z, p); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
+      lp_cg_roll<<<1, 1, 0, s>>>(sc); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
       RSD_CUDA(ctx, cudaMemcpyAsync(h, sc + 3, sizeof(double), cudaMemcpyDeviceToHost, s));
       RSD_CUDA(ctx, cudaStreamSynchronize(s));
       rn = sqrt(h[0]);
@@ -1024,7 +1031,7 @@ static int lp_pcg(rsd_ctx* ctx, int mode, const lp_graph& g, const double* A, in
       if (!std::isfinite(rn)) return rsd_fail(ctx, RSD_ENAN, "PCG residual is not finite");
     }
     // x back to the grand layout, in place through tmp
-    lp_from_blk<<<nb256(P), 256, 0, s>>>(nn, xc, tmp); RSD_LAUNCH_NOTE();
+    lp_from_blk<<<nb256(P), 256, 0, s>>>(nn, xc, tmp); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
     RSD_CUDA(ctx, cudaMemcpyAsync(xc, tmp, sizeof(double) * P, cudaMemcpyDeviceToDevice, s));
     worst_it = std::max(worst_it, it);
     worst_res = std::max(worst_res, rn / bn);
@@ -1082,7 +1089,8 @@ extern "C" int rsd_lp_create(rsd_lp** out, int device, const float* params, uint
   if (e == cudaSuccess) {
     lp_to_bf16<<<nb256(LAY.total), 256>>>(LAY.total, n->w, n->wb);
     RSD_LAUNCH_NOTE();
-    e = cudaDeviceSynchronize();
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
   }
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -1156,11 +1164,11 @@ extern "C" int rsd_lp_forward_dev(rsd_ctx* ctx, rsd_lp* net, int32_t nn, int32_t
   __nv_bfloat16* xe = (__nv_bfloat16*)rsd_scratch(ctx, "lp_xe_t", sizeof(__nv_bfloat16) * ((size_t)ne * NF_EDGE + 1));
   if (!g.lower || !xn || !xe) return RSD_ENOMEM;
   if (ne) {
-    lp_lower_flags<<<nb256(ne), 256, 0, s>>>(ne, g.src, g.dst, g.lower); RSD_LAUNCH_NOTE();
+    lp_lower_flags<<<nb256(ne), 256, 0, s>>>(ne, g.src, g.dst, g.lower); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
   }
-  lp_to_bf16<<<nb256((int64_t)nn * NF_NODE), 256, 0, s>>>((int64_t)nn * NF_NODE, d_xn, xn); RSD_LAUNCH_NOTE();
+  lp_to_bf16<<<nb256((int64_t)nn * NF_NODE), 256, 0, s>>>((int64_t)nn * NF_NODE, d_xn, xn); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
   if (ne) {
-    lp_to_bf16<<<nb256((int64_t)ne * NF_EDGE), 256, 0, s>>>((int64_t)ne * NF_EDGE, d_xe, xe); RSD_LAUNCH_NOTE();
+    lp_to_bf16<<<nb256((int64_t)ne * NF_EDGE), 256, 0, s>>>((int64_t)ne * NF_EDGE, d_xe, xe); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
   }
   lp_acts acts;
   RSD_TRY(lp_forward(ctx, net, g, xn, xe, &acts, d_zd, d_ze));
@@ -1177,6 +1185,7 @@ extern "C" int rsd_lp_adam_step(rsd_lp* net, float lr) {
   const float c1 = 1.f - powf(b1, (float)net->step), c2 = 1.f - powf(b2, (float)net->step);
   lp_adam<<<nb256(LAY.total), 256>>>(LAY.total, net->w, net->g, net->m, net->v, net->wb, lr, b1, b2, 1e-8f, c1, c2);
   RSD_LAUNCH_NOTE();
+  if (cudaGetLastError() != cudaSuccess) return RSD_ECUDA;
   return cudaDeviceSynchronize() == cudaSuccess ? RSD_OK : RSD_ECUDA;
 }
 
@@ -1210,7 +1219,7 @@ static int lp_train_t(rsd_ctx* ctx, rsd_lp* net, int nn, const double* d_pos, co
   }
   RSD_CUDA(ctx, cudaMemsetAsync(dl, 0, sizeof(double), s));
   lp_loss<<<nb256((int64_t)(nn + g.ne) * 36), 256, 0, s>>>(nn, g.ne, zd, td, ze, te, g.lower, 1.f / (36.f * nn),
-                                                           nlow ? 1.f / (36.f * nlow) : 0.f, dzd, dze, dl); RSD_LAUNCH_NOTE();
+                                                           nlow ? 1.f / (36.f * nlow) : 0.f, dzd, dze, dl); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
   RSD_TRY(lp_backward(ctx, net, g, xn, xe, acts, dzd, dze));
   RSD_CUDA(ctx, cudaMemcpyAsync(loss, dl, sizeof(double), cudaMemcpyDeviceToHost, s));
   RSD_CUDA(ctx, cudaStreamSynchronize(s));

@@ -399,6 +399,92 @@ __global__ void outputs(int64_t P, int64_t Q, int c, const double* __restrict__ 
 
 inline unsigned nblk(int64_t n) { return (unsigned)((n + 255) / 256); }
 
+// ---- flexible GMRES on the augmented system (one right-hand side at a time)
+// x = (f [n], U [P]); A x = (M f - [U; 0], f_P + (L [U; 0])_P); the
+// preconditioner is the correction of the stationary iteration above.
+// Krylov vectors are FP64 of length n + P.
+
+// out[k] = V_k . w for k < nk (one block per k)
+__global__ void gm_dots(int64_t len, int nk, const double* __restrict__ V, int64_t ldv, const double* __restrict__ w,
+                        double* __restrict__ out) {
+  __shared__ double red[256];
+  const int k = blockIdx.x;
+  double a = 0.0;
+  for (int64_t i = threadIdx.x; i < len; i += 256) a += V[i + k * ldv] * w[i];
+  red[threadIdx.x] = a;
+  __syncthreads();
+  for (int d = 128; d > 0; d >>= 1) {
+    if (threadIdx.x < d) red[threadIdx.x] += red[threadIdx.x + d];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[k] = red[0];
+}
+
+// w -= sum_k h[k] V_k; hacc[k] += h[k] (thread 0 of block 0)
+__global__ void gm_orth(int64_t len, int nk, const double* __restrict__ V, int64_t ldv, const double* __restrict__ h,
+                        double* __restrict__ w, double* __restrict__ hacc) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0)
+    for (int k = 0; k < nk; k++) hacc[k] += h[k];
+  if (i >= len) return;
+  double s = w[i];
+  for (int k = 0; k < nk; k++) s -= h[k] * V[i + k * ldv];
+  w[i] = s;
+}
+
+// v = w / sqrt(nrm2[0])
+__global__ void gm_scale(int64_t len, const double* __restrict__ w, const double* __restrict__ nrm2,
+                         double* __restrict__ v) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < len) v[i] = w[i] / sqrt(nrm2[0]);
+}
+
+// x += sum_k y[k] Z_k
+__global__ void gm_update(int64_t len, int nk, const double* __restrict__ Z, int64_t ldz, const double* __restrict__ y,
+                          double* __restrict__ x) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= len) return;
+  double s = 0.0;
+  for (int k = 0; k < nk; k++) s += y[k] * Z[i + k * ldz];
+  x[i] += s;
+}
+
+// w = [u; 0] (length n) from u (length P)
+__global__ void gm_u0(int64_t P, int64_t n, const double* __restrict__ u, double* __restrict__ w) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) w[i] = i < P ? u[i] : 0.0;
+}
+
+// a1 = -w (then + M f by the symmetric product); a2 = f_P + Lw_P
+__global__ void gm_neg(int64_t n, const double* __restrict__ w, double* __restrict__ a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = -w[i];
+}
+__global__ void gm_a2(int64_t P, const double* __restrict__ f, const double* __restrict__ Lw, double* __restrict__ a2) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < P) a2[i] = f[i] + Lw[i];
+}
+
+// FP32 vector to FP64
+__global__ void gm_f2d(int64_t n, const float* __restrict__ x, double* __restrict__ y) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = (double)x[i];
+}
+
+// sum of squares of v[0:len] into out[0] (one block)
+__global__ void gm_nrm2(int64_t len, const double* __restrict__ v, double* __restrict__ out) {
+  __shared__ double red[256];
+  double a = 0.0;
+  for (int64_t i = threadIdx.x; i < len; i += 256) a += v[i] * v[i];
+  red[threadIdx.x] = a;
+  __syncthreads();
+  for (int d = 128; d > 0; d >>= 1) {
+    if (threadIdx.x < d) red[threadIdx.x] += red[threadIdx.x + d];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = red[0];
+}
+
 }  // namespace
 
 // rpp_out (optional): stop once RPP32 = A^-1 + rfu is formed and copy it
@@ -485,6 +571,182 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   int* tri_err = rsd_uhat_error_flag(ctx);
   if (!tri_err) return RSD_ENOMEM;
   RSD_CUDA(ctx, cudaMemsetAsync(tri_err, 0, sizeof(int), s));
+  if (ctx->refine_gmres) {
+    cudaEventRecord(ctx->ev[7], s);
+    // right-preconditioned flexible GMRES(m) per right-hand side, FP64
+    // residuals; the preconditioner is the stationary iteration's correction
+    const int m = ctx->gmres_restart > 0 ? ctx->gmres_restart : 30;
+    const int64_t len = n + P;
+    double* KV = (double*)rsd_scratch(ctx, "gm_basis", sizeof(double) * (size_t)(2 * m + 1) * len + 8 * 64);
+    if (!KV) return RSD_ENOMEM;
+    double *Vb = KV, *Zb = Vb + (size_t)(m + 1) * len, *dn = Zb + (size_t)m * len;
+    double* hacc = (double*)rsd_scratch(ctx, "gm_hacc", sizeof(double) * 64);
+    double* hbuf = (double*)rsd_scratch(ctx, "gm_hbuf", sizeof(double) * 64);
+    double* Lz = (double*)rsd_scratch(ctx, "gm_lz", sizeof(double) * (size_t)n);
+    if (!hacc || !hbuf || !Lz) return RSD_ENOMEM;
+    RSD_CUDA(ctx, cudaMemsetAsync(f, 0, sizeof(double) * nr * n, s));
+    RSD_CUDA(ctx, cudaMemsetAsync(U, 0, sizeof(double) * nr * P, s));
+    // the product M v (FP64 v of length n, planes in double-single) into out (added)
+    auto symv_add = [&](const double* v, double* out) -> int {
+      to_dsf_vec<<<nblk(n), 256, 0, s>>>(n, v, fs); RSD_LAUNCH_NOTE();
+      if (symv) {
+        double* pcol = gpart + (size_t)nbt * nbt * SYMV_T;
+        symv_planes_part<1><<<dim3(nbt, nbt), 256, 0, s>>>(nn, (int)n, Mh, Ml, ld, fs, nbt, gpart, pcol); RSD_LAUNCH_NOTE();
+        symv_planes_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>((int)n, 1, nbt, gpart, pcol, 1.0, out, n); RSD_LAUNCH_NOTE();
+      } else {
+        if (!mirrored) {
+          RSD_TRY(rsd_mirror_planes(ctx, nn, M, ld));
+          mirrored = true;
+        }
+        gemv_planes_part<1><<<dim3((unsigned)((n + 255) / 256), gchunks), 256, 0, s>>>((int)n, (int)n, Mh, Ml, ld, fs, gpart); RSD_LAUNCH_NOTE();
+        gemv_planes_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>((int)n, 1, gchunks, gpart, 1.0, out, n); RSD_LAUNCH_NOTE();
+      }
+      return RSD_OK;
+    };
+    // residual of column c: (r1, r2) = b - A x into out (length n + P);
+    // Lw (column c) keeps L [U; -EIN] for the stresslet output
+    auto residual = [&](int c, double* out) -> int {
+      double *fc = f + (size_t)c * n, *Uc = U + (size_t)c * P, *wc = w + (size_t)c * n, *Lc = Lw + (size_t)c * n;
+      build_w<<<nblk(n), 256, 0, s>>>(P, Q, 1, Uc, ein, wc); RSD_LAUNCH_NOTE();
+      gm_neg<<<nblk(n), 256, 0, s>>>(n, wc, out); RSD_LAUNCH_NOTE();
+      RSD_TRY(symv_add(fc, out));  // out = M f - w
+      gm_neg<<<nblk(n), 256, 0, s>>>(n, out, out); RSD_LAUNCH_NOTE();  // r1 = w - M f
+      if (p->use_lub) {
+        RSD_TRY(rsd_lub_spmv(ctx, &lub, 1, wc, n, Lc, n));
+      } else {
+        RSD_CUDA(ctx, cudaMemsetAsync(Lc, 0, sizeof(double) * n, s));
+      }
+      build_r2<<<nblk(P), 256, 0, s>>>(P, n, 1, Fe, have_fe && c == 0, fc, Lc, out + n); RSD_LAUNCH_NOTE();
+      return RSD_OK;
+    };
+    // z = P v (v, z of length n + P)
+    auto precond = [&](const double* v, double* z) -> int {
+      to32_perm<<<nblk(n), 256, 0, s>>>(P, Q, 1, v, n, 0, t32); RSD_LAUNCH_NOTE();
+      if (use_uh)
+        RSD_TRY(rsd_uhat_solve(ctx, &uh_m, t32, n, 1, ywork));
+      else
+        RSD_TRY(rsd_potrs_wide_s(ctx, (int)n, M32, n, W_m, t32, n, 1, ywork));
+      from32_perm<<<nblk(n), 256, 0, s>>>(P, Q, 1, t32, z, 0); RSD_LAUNCH_NOTE();  // y = M^-1 v1
+      rhs_u<<<nblk(P), 256, 0, s>>>(P, n, 1, v + n, z, u32); RSD_LAUNCH_NOTE();
+      if (use_uh)
+        RSD_TRY(rsd_uhat_solve(ctx, &uh_r, u32, P, 1, ywork));
+      else
+        RSD_TRY(rsd_potrs_wide_s(ctx, (int)P, A32, P, W_r, u32, P, 1, ywork));
+      du_vec<<<nblk(n), 256, 0, s>>>(P, n, 1, u32, dv); RSD_LAUNCH_NOTE();
+      to32_perm<<<nblk(n), 256, 0, s>>>(P, Q, 1, dv, n, 1, t32); RSD_LAUNCH_NOTE();
+      if (use_uh)
+        RSD_TRY(rsd_uhat_solve(ctx, &uh_m, t32, n, 1, ywork, (int)Q));
+      else
+        RSD_TRY(rsd_potrs_wide_s(ctx, (int)n, M32, n, W_m, t32, n, 1, ywork));
+      from32_perm<<<nblk(n), 256, 0, s>>>(P, Q, 1, t32, z, 1); RSD_LAUNCH_NOTE();  // df
+      gm_f2d<<<nblk(P), 256, 0, s>>>(P, u32, z + n); RSD_LAUNCH_NOTE();           // dU
+      return RSD_OK;
+    };
+    // a = A z
+    auto apply_a = [&](const double* z, double* a) -> int {
+      gm_u0<<<nblk(n), 256, 0, s>>>(P, n, z + n, dv); RSD_LAUNCH_NOTE();  // [zU; 0]
+      gm_neg<<<nblk(n), 256, 0, s>>>(n, dv, a); RSD_LAUNCH_NOTE();
+      RSD_TRY(symv_add(z, a));  // M zf - [zU; 0]
+      if (p->use_lub) {
+        RSD_TRY(rsd_lub_spmv(ctx, &lub, 1, dv, n, Lz, n));
+        gm_a2<<<nblk(P), 256, 0, s>>>(P, z, Lz, a + n); RSD_LAUNCH_NOTE();
+      } else {
+        RSD_CUDA(ctx, cudaMemcpyAsync(a + n, z, sizeof(double) * P, cudaMemcpyDeviceToDevice, s));
+      }
+      return RSD_OK;
+    };
+    // |b_c|: b = ([0; -EIN], Fe_c)
+    std::vector<double> bnorm(nr);
+    {
+      norms<<<nr, 256, 0, s>>>(P, n, nr, r1, r2, ein, Fe, have_fe, nrm); RSD_LAUNCH_NOTE();  // b part only is used
+      std::vector<double> hb(2 * nr);
+      RSD_CUDA(ctx, cudaMemcpyAsync(hb.data(), nrm, sizeof(double) * 2 * nr, cudaMemcpyDeviceToHost, s));
+      RSD_CUDA(ctx, cudaStreamSynchronize(s));
+      for (int c = 0; c < nr; c++) bnorm[c] = sqrt(hb[2 * c + 1]) > 0 ? sqrt(hb[2 * c + 1]) : 1.0;
+    }
+    int total_it = 0;
+    double worst = 0.0;
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), yv(m), hh(m + 2);
+    for (int c = 0; c < nr; c++) {
+      double rel = 0.0;
+      for (int cycle = 0;; cycle++) {
+        RSD_TRY(residual(c, Vb));
+        gm_nrm2<<<1, 256, 0, s>>>(len, Vb, dn); RSD_LAUNCH_NOTE();
+        double beta2 = 0.0;
+        int herr = 0;
+        RSD_CUDA(ctx, cudaMemcpyAsync(&beta2, dn, sizeof(double), cudaMemcpyDeviceToHost, s));
+        RSD_CUDA(ctx, cudaMemcpyAsync(&herr, tri_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        RSD_CUDA(ctx, cudaStreamSynchronize(s));
+        if (herr) return rsd_fail(ctx, RSD_ETIMEOUT, "refinement: a triangular sweep's wait timed out");
+        const double beta = sqrt(beta2);
+        rel = beta / bnorm[c];
+        if (!std::isfinite(rel)) return rsd_fail(ctx, RSD_ENAN, "refinement residual is not finite");
+        if (rel <= tol || total_it >= maxit) break;
+        gm_scale<<<nblk(len), 256, 0, s>>>(len, Vb, dn, Vb); RSD_LAUNCH_NOTE();
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        int j = 0;
+        for (; j < m && total_it < maxit; j++) {
+          double* vj = Vb + (size_t)j * len;
+          double* zj = Zb + (size_t)j * len;
+          double* vn = Vb + (size_t)(j + 1) * len;
+          RSD_TRY(precond(vj, zj));
+          RSD_TRY(apply_a(zj, vn));
+          total_it++;
+          // classical Gram-Schmidt, twice
+          RSD_CUDA(ctx, cudaMemsetAsync(hacc, 0, sizeof(double) * (j + 1), s));
+          for (int pass = 0; pass < 2; pass++) {
+            gm_dots<<<j + 1, 256, 0, s>>>(len, j + 1, Vb, len, vn, hbuf); RSD_LAUNCH_NOTE();
+            gm_orth<<<nblk(len), 256, 0, s>>>(len, j + 1, Vb, len, hbuf, vn, hacc); RSD_LAUNCH_NOTE();
+          }
+          gm_nrm2<<<1, 256, 0, s>>>(len, vn, dn); RSD_LAUNCH_NOTE();
+          RSD_CUDA(ctx, cudaMemcpyAsync(hh.data(), hacc, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
+          RSD_CUDA(ctx, cudaMemcpyAsync(hh.data() + j + 1, dn, sizeof(double), cudaMemcpyDeviceToHost, s));
+          RSD_CUDA(ctx, cudaStreamSynchronize(s));
+          const double hn = sqrt(hh[j + 1]);
+          if (hn > 0.0) {
+            gm_scale<<<nblk(len), 256, 0, s>>>(len, vn, dn, vn); RSD_LAUNCH_NOTE();
+          }
+          // Givens rotations on column j of H
+          double* Hj = H.data() + (size_t)j * (m + 1);
+          for (int i = 0; i <= j; i++) Hj[i] = hh[i];
+          Hj[j + 1] = hn;
+          for (int i = 0; i < j; i++) {
+            const double t = cs[i] * Hj[i] + sn[i] * Hj[i + 1];
+            Hj[i + 1] = -sn[i] * Hj[i] + cs[i] * Hj[i + 1];
+            Hj[i] = t;
+          }
+          const double den = std::hypot(Hj[j], Hj[j + 1]);
+          cs[j] = den > 0 ? Hj[j] / den : 1.0;
+          sn[j] = den > 0 ? Hj[j + 1] / den : 0.0;
+          Hj[j] = den;
+          Hj[j + 1] = 0.0;
+          g[j + 1] = -sn[j] * g[j];
+          g[j] = cs[j] * g[j];
+          if (std::fabs(g[j + 1]) <= 0.5 * tol * bnorm[c] || hn == 0.0) {
+            j++;
+            break;
+          }
+        }
+        // y = H^-1 g (upper triangular, j x j), x += Z y
+        for (int i = j - 1; i >= 0; i--) {
+          double t = g[i];
+          for (int k = i + 1; k < j; k++) t -= H[(size_t)k * (m + 1) + i] * yv[k];
+          yv[i] = t / H[(size_t)i * (m + 1) + i];
+        }
+        RSD_CUDA(ctx, cudaMemcpyAsync(hbuf, yv.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
+        // x = (f_c, U_c) is not contiguous: update the two parts
+        gm_update<<<nblk(n), 256, 0, s>>>(n, j, Zb, len, hbuf, f + (size_t)c * n); RSD_LAUNCH_NOTE();
+        gm_update<<<nblk(P), 256, 0, s>>>(P, j, Zb + n, len, hbuf, U + (size_t)c * P); RSD_LAUNCH_NOTE();
+      }
+      worst = fmax(worst, rel);
+    }
+    outputs<<<nblk(P), 256, 0, s>>>(P, Q, nr - 1, f, Lw, U, U_par, S_hyd); RSD_LAUNCH_NOTE();
+    RSD_CUDA(ctx, cudaGetLastError());
+    info->iterations = total_it;
+    info->residual = worst;
+    return RSD_OK;
+  }
   int h_tri_err = 0;
   cudaEventRecord(ctx->ev[7], s);
   RSD_CUDA(ctx, cudaMemsetAsync(f, 0, sizeof(double) * nr * n, s));

@@ -103,7 +103,11 @@ def test_plain_trajectory_100_steps(rsd, tabs):
     """The 64-sphere workload (phi = 0.30, gap >= 0.01 a, dt = 1e-3) over its
     100 steps (strain 0 -> 0.1).  Every step of the oracle's trajectory is
     repeated by both forms from the oracle's own configuration, so the
-    comparison is step for step (bounds as above: 1e-11 plain, 1e-8 mixed).
+    comparison is step for step.  Along this trajectory a pair closes to a
+    gap of 1.4e-4 a at step 18 (cond(RPP) 5.4e3) and overlaps at step 19
+    (mirrored lubrication, as in the reference), so the plain form's bound is
+    set per step from the oracle's RPP: max(1e-11, 100 cond(RPP) eps); the
+    mixed form keeps 1e-8.
     The plain form also runs its own trajectory beside it: independent
     trajectories separate as near-contact pairs amplify rounding, so their
     positions are held to 1e-9 L after the 100 steps."""
@@ -117,12 +121,15 @@ def test_plain_trajectory_100_steps(rsd, tabs):
         gp = rsd.STEPPER_Stokesian(ctx_p, tabs[0], co, radii, T, w["dt"], [L, L, L], 1.0, MU, 1e-10)
         gm = rsd.STEPPER_Stokesian(ctx_m, tabs[0], co, radii, T, w["dt"], [L, L, L], 1.0, MU, 1e-10,
                                    precision=rsd.PREC_MIXED)
-        for name, g, tol in (("fp64", gp, 1e-11), ("mixed", gm, 1e-8)):
+        P = 6 * w["N"]
+        cond = np.linalg.cond(np.linalg.inv(r["G"])[:P, :P] + r["rfu"])
+        tol_p = max(1e-11, 100.0 * cond * np.finfo(float).eps)
+        for name, g, tol in (("fp64", gp, tol_p), ("mixed", gm, 1e-8)):
             e = max(rel(g["U_pos"], r["U_pos"]), rel(g["SijN"], r["SijN_hyd"]))
             worst[name] = max(worst[name], e)
             assert e <= tol, (name, k, e)
             assert np.allclose(g["yeta_mu"], r["yeta_mu"], rtol=tol, atol=0), (name, k)
-        assert np.abs(gp["conf"] - r["conf"]).max() <= 1e-12 * L
+        assert np.abs(gp["conf"] - r["conf"]).max() <= max(1e-12, tol_p * 1e-3) * L
         ct = rsd.STEPPER_Stokesian(ctx_t, tabs[0], ct, radii, T, w["dt"], [L, L, L], 1.0, MU, 1e-10)["conf"]
         co, T = r["conf"], T + w["dt"]
     drift = np.abs(ct - co).max() / L
