@@ -65,7 +65,7 @@ def parse():
                     help="FP32 factorisations of the mixed form: 1 TF32/3xTF32 per factor, 3 all 3xTF32, 0 SIMT")
     ap.add_argument("--validate-cpu-model", action="store_true",
                     help="(reference arm) time one whole CPU step at N=512 and compare it with the sample model")
-    ap.add_argument("--refinement", default="gmres", choices=["gmres", "stationary"],
+    ap.add_argument("--refinement", default="stationary", choices=["gmres", "stationary"],
                     help="mixed form's FP64 refinement: flexible GMRES or the stationary iteration")
     ap.add_argument("--mode", default="cycle", choices=["cycle", "long"],
                     help="cycle: the strain-stratified headline; long: the 10,000-step run through the driver")

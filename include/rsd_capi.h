@@ -111,12 +111,13 @@ int rsd_ctx_set_mixed_real_passes(rsd_ctx* ctx, int32_t passes);
 int rsd_ctx_set_correction_method(rsd_ctx* ctx, int32_t method);
 
 /* Refinement of the mixed-precision form (no counterpart in the reference,
- * which solves in FP64 directly): mode 1 (the default) = flexible GMRES with
- * FP64 residuals, right-preconditioned by the correction that the FP32
- * factors give, restarted every `restart` iterations (1..30, 0: 30); mode 0 =
- * the stationary iteration x += P (b - A x) with the same correction.  Both
- * stop at the step's relative residual tolerance; GMRES also converges where
- * the FP32 factors contract the error only slowly (many near-contact pairs). */
+ * which solves in FP64 directly): mode 0 (the default) = the stationary
+ * iteration x += P (b - A x), P the correction that the FP32 factors give,
+ * FP64 residuals; it stops at the step's relative residual tolerance, or
+ * within 100 times it once an iteration no longer halves the residual (the
+ * floor of the residual arithmetic on stiff systems).  Mode 1 = flexible
+ * GMRES with the same preconditioner and FP64 residuals, restarted every
+ * `restart` iterations (1..30, 0: 30). */
 int rsd_ctx_set_refinement(rsd_ctx* ctx, int32_t mode, int32_t restart);
 /* Bounds of the device-side waits of the mixed form's FP32 kernels (no
  * counterpart in the reference): every mbarrier wait of the tensor-core

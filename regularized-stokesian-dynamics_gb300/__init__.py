@@ -198,9 +198,9 @@ class Context:
         RSD_ETIMEOUT."""
         self.check(_lib.rsd_ctx_set_wait_limits(self.h, int(tc_wait_ns), int(tri_spin_polls)))
 
-    def set_refinement(self, mode=1, restart=30):
-        """Mixed form's refinement: 1 flexible GMRES (default), 0 the
-        stationary iteration."""
+    def set_refinement(self, mode=0, restart=30):
+        """Mixed form's refinement: 0 the stationary iteration (default), 1
+        flexible GMRES."""
         self.check(_lib.rsd_ctx_set_refinement(self.h, int(mode), int(restart)))
 
     def set_rpp_solver(self, mode=0, net=None, tol=0.0, maxit=0):

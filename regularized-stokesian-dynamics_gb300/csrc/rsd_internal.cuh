@@ -41,7 +41,7 @@ struct rsd_ctx {
   int correction_method = 0;  // fused step: overlap corrections of the grand mobility (0, 1 or 2)
   long long tc_wait_ns = 0;      // bound of the tensor-core kernels' mbarrier waits (0: 0.5 s)
   long long tri_spin_polls = 0;  // bound of the dataflow sweeps' waits in polls (0: 2^21)
-  int refine_gmres = 1;      // mixed form: flexible GMRES (1) or the stationary iteration (0) as refinement
+  int refine_gmres = 0;      // mixed form: flexible GMRES (1) or the stationary iteration (0) as refinement
   int gmres_restart = 30;    // GMRES restart length
   int rpp_mode = 0;          // plain FP64 step: RPP by Cholesky (0) or PCG with this preconditioner
   void* rpp_net = nullptr;   // the network of the learned preconditioner

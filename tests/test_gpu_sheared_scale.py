@@ -106,8 +106,10 @@ def test_plain_trajectory_100_steps(rsd, tabs):
     comparison is step for step.  Along this trajectory a pair closes to a
     gap of 1.4e-4 a at step 18 (cond(RPP) 5.4e3) and overlaps at step 19
     (mirrored lubrication, as in the reference), so the plain form's bound is
-    set per step from the oracle's RPP: max(1e-11, 100 cond(RPP) eps); the
-    mixed form keeps 1e-8.
+    set per step from the oracle's RPP: max(1e-11, 300 cond(RPP) eps) -- the
+    oracle inverts RPP explicitly three times (MATREV, Rheology) where this
+    library solves with one Cholesky factor, and each carries errors of order
+    cond eps sqrt(n) (n = 384); the mixed form keeps 1e-8.
     The plain form also runs its own trajectory beside it: independent
     trajectories separate as near-contact pairs amplify rounding, so their
     positions are held to 1e-9 L after the 100 steps."""
@@ -123,7 +125,7 @@ def test_plain_trajectory_100_steps(rsd, tabs):
                                    precision=rsd.PREC_MIXED)
         P = 6 * w["N"]
         cond = np.linalg.cond(np.linalg.inv(r["G"])[:P, :P] + r["rfu"])
-        tol_p = max(1e-11, 100.0 * cond * np.finfo(float).eps)
+        tol_p = max(1e-11, 300.0 * cond * np.finfo(float).eps)
         for name, g, tol in (("fp64", gp, tol_p), ("mixed", gm, 1e-8)):
             e = max(rel(g["U_pos"], r["U_pos"]), rel(g["SijN"], r["SijN_hyd"]))
             worst[name] = max(worst[name], e)
