@@ -25,7 +25,10 @@ Prints one JSON line (rank 0).  With --gpus N > 1 under torchrun every rank
 steps its own independent replica (the step does not shard; replicas only).
 --impl reference times the CPU restatement of the reference's routines on the
 host cores instead (bounded samples per step, extrapolated; see CpuModel).
---mode long runs the 10,000-step long run through the driver's time loop.
+--mode long runs the 10,000-step long run through the driver's time loop,
+--mode ensemble the ensemble of 256 uneven replicas (replica-steps/s), and
+--mode learned the learned preconditioner's PCG solves on the N = 1000
+near-contact workload.
 """
 import argparse
 import json
@@ -67,8 +70,12 @@ def parse():
                     help="(reference arm) time one whole CPU step at N=512 and compare it with the sample model")
     ap.add_argument("--refinement", default="stationary", choices=["gmres", "stationary"],
                     help="mixed form's FP64 refinement: flexible GMRES or the stationary iteration")
-    ap.add_argument("--mode", default="cycle", choices=["cycle", "long"],
-                    help="cycle: the strain-stratified headline; long: the 10,000-step run through the driver")
+    ap.add_argument("--mode", default="cycle", choices=["cycle", "long", "ensemble", "learned"],
+                    help="cycle: the strain-stratified headline; long: the 10,000-step run through the driver; "
+                         "ensemble: 256 uneven replicas; learned: the learned preconditioner's PCG solves")
+    ap.add_argument("--replicas", type=int, default=256, help="(ensemble) number of replicas")
+    ap.add_argument("--ens-steps", type=int, default=50, help="(ensemble) steps of every replica")
+    ap.add_argument("--workers", type=int, default=16, help="(ensemble) concurrent contexts")
     ap.add_argument("--long-steps", type=int, default=10000)
     ap.add_argument("--plain-steps", type=int, default=5, help="(long) plain FP64 steps beside the mixed run")
     ap.add_argument("--out-dir", default=None, help="(long) where yeta_mu.txt and the viscosity series go")
@@ -463,6 +470,97 @@ def long_run(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- ensemble
+def ensemble_run(args):
+    """The ensemble workload: --replicas replicas, N uniform in [32, 256], phi
+    uniform in [0.10, 0.50], shear rate log-uniform in [0.1, 10], seeded
+    minimum gap 1e-3 a, dt 1e-3, --ens-steps steps each, mixed precision;
+    replica-steps/s over the whole ensemble (replicas on --workers
+    concurrent contexts, largest first, kernel settings per size class from
+    the autotuner)."""
+    import __graft_entry__ as ge
+    rsd = ge.load_package()
+    ens_mod = rsd.ensemble
+    specs = ens_mod.replica_specs(args.replicas, SEED_BASE + 3000)
+    t0 = time.perf_counter()
+    packs = ens_mod.build_packings(specs, 1e-3, sweeps=min(args.sweeps, 30))
+    t_pack = time.perf_counter() - t0
+    ens = ens_mod.Ensemble(rsd, specs, packs, dt=1e-3, workers=args.workers)
+    table = ens.autotune()
+    lib = rsd.library()
+    ens.run(1)  # warm-up: every context grows its buffers
+    n0 = lib.rsd_launch_count()
+    wall = ens.run(args.ens_steps)
+    launches = lib.rsd_launch_count() - n0
+    its = [i[2] for i in ens.info]
+    res = [i[3] for i in ens.info]
+    by_class = {}
+    for k in range(len(ens_mod.SIZE_CLASSES)):
+        members = [r for r, s_ in enumerate(specs) if ens_mod.size_class(s_["N"]) == k]
+        if members:
+            by_class[str(k)] = {"replicas": len(members), "N_range": ens_mod.SIZE_CLASSES[k],
+                                "setting": table.get(str(k))}
+    line = {"metric": "replica-steps/s, %d replicas N in [32,256], phi in [0.10,0.50], shear log-uniform [0.1,10]"
+                      % args.replicas,
+            "value": args.replicas * args.ens_steps / wall, "unit": "replica-steps/s", "higher_is_better": True,
+            "steps_per_replica": args.ens_steps, "wall_s": wall, "workers": ens.workers, "precision": "mixed",
+            "refinement_iterations": {"mean": float(np.mean(its)), "max": int(np.max(its))},
+            "worst_residual": float(np.max(res)), "size_classes": by_class, "packing_s": t_pack,
+            "gpu_launches": launches,
+            "schedule": "replicas on concurrent contexts (one CUDA stream each), largest first; not one launch"}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- learned preconditioner
+def learned_run(args):
+    """The learned-preconditioner workload: N = 1000, phi = 0.5, a quarter of
+    the spheres in near-contact pairs with gaps log-uniform in [1e-4, 1e-1] a
+    (a seed not used in training), strain 0.25; RPP in FP64 (plain path);
+    RPP x = b by PCG in FP64 to 1e-12 with each preconditioner: iterations,
+    FP64 residual and time, beside a library Cholesky solve for scale."""
+    import torch
+
+    import __graft_entry__ as ge
+    rsd = ge.load_package()
+    N = 1000
+    dev = torch.device("cuda", 0)
+    series, radii, L = rsd.configs.sheared_series(N, 0.5, 1e-4, SEED_BASE + 4999, [0.25],
+                                                  sweeps=min(args.sweeps, 100), near_contact=True)
+    ctx = rsd.Context(0)
+    tab = rsd.LubTab(rsd.lubdat_dir())
+    mu = rsd.mu_f_dimensionless(1.0)
+    conf_t = torch.tensor(series[0], dtype=torch.float64, device=dev)
+    radii_t = torch.tensor(radii, dtype=torch.float64, device=dev)
+    rpp, lat = rsd.resistance_pp_dev(ctx, tab, conf_t, radii_t, 0.25, [L, L, L], 1.0, mu, 1e-10)
+    net = rsd.LearnedPreconditioner.trained(0)
+    b = torch.tensor(np.random.default_rng(2).normal(size=6 * N), device=dev)
+    out = {}
+    for name, mode in (("none", rsd.PC_NONE), ("jacobi", rsd.PC_JACOBI), ("block_jacobi", rsd.PC_BLOCK_JACOBI),
+                       ("fsai", rsd.PC_FSAI), ("learned", rsd.PC_LEARNED)):
+        rsd.pcg_dev(ctx, net, mode, conf_t, radii_t, lat, rpp, b, tol=1e-12, maxit=20000)  # warm-up
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        x, it, res = rsd.pcg_dev(ctx, net, mode, conf_t, radii_t, lat, rpp, b, tol=1e-12, maxit=20000)
+        rsd._sync_ctx(ctx)
+        dt_ = time.perf_counter() - t0
+        r = b - rpp @ x
+        out[name] = {"iterations": it, "residual": res, "fp64_residual": float(r.norm() / b.norm()),
+                     "seconds": dt_}
+    A = rpp.contiguous().clone()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    Lc = torch.linalg.cholesky(A)
+    xc = torch.cholesky_solve(b[:, None], Lc)[:, 0]
+    torch.cuda.synchronize(dev)
+    out["cholesky_library"] = {"seconds": time.perf_counter() - t0,
+                               "fp64_residual": float((b - rpp @ xc).norm() / b.norm()),
+                               "note": "torch (cuSOLVER) Cholesky, for scale only"}
+    line = {"metric": "learned preconditioner, N=1000 phi=0.5 near-contact: PCG iterations to 1e-12 on RPP",
+            "value": out["learned"]["iterations"], "unit": "iterations", "higher_is_better": False,
+            "unpreconditioned_iterations": out["none"]["iterations"], "solves": out}
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- GPU arm
 def main():
     args = parse()
@@ -471,6 +569,12 @@ def main():
         return
     if args.mode == "long":
         long_run(args)
+        return
+    if args.mode == "ensemble":
+        ensemble_run(args)
+        return
+    if args.mode == "learned":
+        learned_run(args)
         return
     import torch
     import torch.distributed as dist

@@ -662,6 +662,7 @@ def lubdat_dir():
 from . import configs  # noqa: E402,F401
 from . import driver  # noqa: E402,F401
 from . import driver_files  # noqa: E402,F401
+from . import ensemble  # noqa: E402,F401
 
 
 def driver_step(ctx: Context, tab: LubTab, precision=PREC_MIXED):
