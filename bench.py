@@ -471,6 +471,13 @@ def long_run(args):
 
 
 # ---------------------------------------------------------------- ensemble
+def _pack_replica(job):
+    """One replica's packing (a top-level function, so that spawned worker
+    processes can run it)."""
+    N, phi, gmin, seed, sweeps = job
+    return _configs().packing(N, phi, gmin, seed, sweeps=sweeps)
+
+
 def ensemble_run(args):
     """The ensemble workload: --replicas replicas, N uniform in [32, 256], phi
     uniform in [0.10, 0.50], shear rate log-uniform in [0.1, 10], seeded
@@ -483,7 +490,11 @@ def ensemble_run(args):
     ens_mod = rsd.ensemble
     specs = ens_mod.replica_specs(args.replicas, SEED_BASE + 3000)
     t0 = time.perf_counter()
-    packs = ens_mod.build_packings(specs, 1e-3, sweeps=min(args.sweeps, 30))
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    jobs = [(s_["N"], s_["phi"], 1e-3, s_["seed"], min(args.sweeps, 30)) for s_ in specs]
+    with ProcessPoolExecutor(mp_context=mp.get_context("spawn")) as ex:  # before any CUDA work
+        packs = list(ex.map(_pack_replica, jobs, chunksize=4))
     t_pack = time.perf_counter() - t0
     ens = ens_mod.Ensemble(rsd, specs, packs, dt=1e-3, workers=args.workers)
     table = ens.autotune()

@@ -55,22 +55,6 @@ def replica_specs(nrep, seed, n_range=(32, 256), phi_range=(0.10, 0.50), gamma_r
     return out
 
 
-def _pack(args):
-    from . import configs
-    N, phi, gmin, seed, sweeps = args
-    return configs.packing(N, phi, gmin, seed, sweeps=sweeps)
-
-
-def build_packings(specs, gmin, sweeps, processes=None):
-    """Seeded packings of every replica, in worker processes (spawned, so
-    that no CUDA state is inherited)."""
-    import multiprocessing as mp
-    from concurrent.futures import ProcessPoolExecutor
-    jobs = [(s["N"], s["phi"], gmin, s["seed"], sweeps) for s in specs]
-    with ProcessPoolExecutor(max_workers=processes, mp_context=mp.get_context("spawn")) as ex:
-        return list(ex.map(_pack, jobs, chunksize=4))
-
-
 def lpt_assign(costs, workers):
     """Largest-first assignment to the least-loaded worker."""
     load = [0.0] * workers
