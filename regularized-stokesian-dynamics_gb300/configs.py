@@ -8,7 +8,12 @@ box of edge L = (N 4/3 pi / phi)^(1/3).
   phi >  0.35  start from a lattice (simple cubic when its spacing clears
                2a + g_min, else face-centred cubic), drop surplus sites at
                random, then Metropolis hard-sphere sweeps with hard core
-               2a + g_min and a step tuned towards 40 % acceptance.
+               2a + g_min and a step tuned towards 40 % acceptance.  Where
+               no cubic lattice of the box holds N sites that far apart (a
+               few small N just above a lattice's site count), the start is
+               instead random sequential addition at phi = 0.3 in a larger
+               box, compressed to the target box in small affine steps with
+               the overlaps of each step pushed apart.
 Near-contact pairs (the learned-preconditioner workload): after the sweeps,
 N/4 disjoint nearest-neighbour pairs are brought to a surface gap drawn
 log-uniform in [1e-4, 1e-1] a, accepting a move only if every other gap
@@ -91,6 +96,33 @@ def _lattice_start(N, L, hard, rng):
     return sites[np.sort(keep)].copy()
 
 
+def _compressed_start(N, L, hard, rng, phi0=0.3, steps=200):
+    """Random sequential addition in the box of volume fraction phi0, then
+    affine compression to edge L in `steps` steps, each followed by pushing
+    overlapping pairs (minimum image) apart along their centre lines."""
+    L0 = max(box_edge(N, phi0, hard / 2.0), L)
+    pos = _rsa(N, L0, hard, rng)
+    push = hard + 0.01
+    for k in range(1, steps + 1):
+        Lk = L0 + (L - L0) * k / steps
+        pos = pos * (Lk / (L0 + (L - L0) * (k - 1) / steps))
+        for _ in range(5000):
+            d = pos[None, :, :] - pos[:, None, :]
+            d = _min_image(d, Lk)
+            r = np.sqrt(np.einsum("ijk,ijk->ij", d, d))
+            np.fill_diagonal(r, np.inf)
+            i, j = np.nonzero(np.triu(r < hard, 1))
+            if len(i) == 0:
+                break
+            u = d[i, j] / r[i, j, None] * (0.5 * (push - r[i, j]))[:, None]
+            np.add.at(pos, i, -u)
+            np.add.at(pos, j, u)
+            pos %= Lk
+        else:
+            raise RuntimeError("compression did not clear the overlaps")
+    return pos % L
+
+
 def _mc_sweeps(pos, L, hard, rng, sweeps):
     N = len(pos)
     step = 0.1 * hard
@@ -145,7 +177,10 @@ def packing(N, phi, g_min, seed, sweeps=200, near_contact=False, a=1.0):
     if phi <= 0.35:
         pos = _rsa(N, L, hard, rng)
     else:
-        pos = _lattice_start(N, L, hard, rng)
+        try:
+            pos = _lattice_start(N, L, hard, rng)
+        except RuntimeError:
+            pos = _compressed_start(N, L, hard, rng)
         pos = _mc_sweeps(pos, L, hard, rng, sweeps)
     if near_contact:
         pos = _near_contact_pairs(pos, L, rng, a)
