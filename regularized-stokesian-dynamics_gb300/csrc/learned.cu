@@ -226,55 +226,36 @@ __global__ void lp_features(int nn, int ne, const T* __restrict__ A, int64_t ld,
 // ------------------------------------------------------------ exact FSAI
 // One CTA per particle a: J = (up to LP_KMAX nearest lower neighbours, a),
 // the scaled local matrix B = A^[J, J] in shared memory (FP64), its
-// Cholesky factor, Y = B^-1 E_a (6 right-hand sides), S = (Y_aa)^-1/2
-// (symmetric, by Jacobi rotations), and the row block Z_a = S Y^T, written
+// Cholesky factor, Y = B^-1 E_a (6 right-hand sides), S = L^-1 for the
+// Cholesky factor L of Y_aa (so that S Y_aa S^T = I), and the row block
+// Z_a = S Y^T, written
 // as the diagonal block zd[a] and the blocks ze[e] of the kept lower edges
 // (other lower edges of a get zero blocks).
 constexpr int FS_THREADS = 128;
 
-__device__ void sym6_inv_sqrt(double* Ain, double* S) {
-  // eigen-decomposition of a symmetric 6 x 6 matrix by cyclic Jacobi
-  double a[6][6], v[6][6];
+// S = L^-1 for Y = L L^T (Cholesky of a symmetric positive definite 6 x 6
+// matrix, row-major in and out).  Any factor C with C Y C^T = I gives the same
+// G = Z^T Z; the Cholesky one is the cheapest and needs no iteration.
+__device__ void sym6_chol_inv(const double* Y, double* S) {
+  double L[6][6];
   for (int i = 0; i < 6; i++)
-    for (int j = 0; j < 6; j++) {
-      a[i][j] = 0.5 * (Ain[i * 6 + j] + Ain[j * 6 + i]);
-      v[i][j] = i == j;
+    for (int j = 0; j < 6; j++) L[i][j] = 0.0;
+  for (int j = 0; j < 6; j++) {
+    double d = 0.5 * (Y[j * 6 + j] + Y[j * 6 + j]);
+    for (int k = 0; k < j; k++) d -= L[j][k] * L[j][k];
+    L[j][j] = sqrt(fmax(d, 1e-300));
+    for (int i = j + 1; i < 6; i++) {
+      double x = 0.5 * (Y[i * 6 + j] + Y[j * 6 + i]);
+      for (int k = 0; k < j; k++) x -= L[i][k] * L[j][k];
+      L[i][j] = x / L[j][j];
     }
-  for (int sweep = 0; sweep < 30; sweep++) {
-    double off = 0.0;
-    for (int p = 0; p < 6; p++)
-      for (int q = p + 1; q < 6; q++) off += a[p][q] * a[p][q];
-    if (off < 1e-30) break;
-    for (int p = 0; p < 5; p++)
-      for (int q = p + 1; q < 6; q++) {
-        if (a[p][q] == 0.0) continue;
-        const double th = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
-        const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-        for (int k = 0; k < 6; k++) {
-          const double x = a[k][p], y = a[k][q];
-          a[k][p] = c * x - s * y;
-          a[k][q] = s * x + c * y;
-        }
-        for (int k = 0; k < 6; k++) {
-          const double x = a[p][k], y = a[q][k];
-          a[p][k] = c * x - s * y;
-          a[q][k] = s * x + c * y;
-        }
-        for (int k = 0; k < 6; k++) {
-          const double x = v[k][p], y = v[k][q];
-          v[k][p] = c * x - s * y;
-          v[k][q] = s * x + c * y;
-        }
-      }
   }
-  double w[6];
-  for (int i = 0; i < 6; i++) w[i] = 1.0 / sqrt(fmax(a[i][i], 1e-300));
-  for (int i = 0; i < 6; i++)
-    for (int j = 0; j < 6; j++) {
-      double s = 0.0;
-      for (int k = 0; k < 6; k++) s += v[i][k] * w[k] * v[j][k];
-      S[i * 6 + j] = s;
+  // S = L^-1 (lower triangular), column by column
+  for (int c = 0; c < 6; c++)
+    for (int i = 0; i < 6; i++) {
+      double x = i == c ? 1.0 : 0.0;
+      for (int k = c; k < i; k++) x -= L[i][k] * S[k * 6 + c];
+      S[i * 6 + c] = i < c ? 0.0 : x / L[i][i];
     }
 }
 
@@ -359,7 +340,7 @@ __global__ void __launch_bounds__(FS_THREADS) lp_fsai(int nn, int lower_only_sel
     double Yaa[36];
     for (int r = 0; r < 6; r++)
       for (int c = 0; c < 6; c++) Yaa[r * 6 + c] = Y[c * m + (m - 6 + r)];
-    sym6_inv_sqrt(Yaa, S_s);
+    sym6_chol_inv(Yaa, S_s);
   }
   __syncthreads();
   // Z_a = S Y^T: block of column group g is S (Y[g rows])^T

@@ -145,7 +145,7 @@ def system(rsd, ctx, tab, N, phi, gmin, seed, T=0.0, near_contact=False):
 def numpy_fsai(R, N, off, src, gap, kmax=16):
     """Block FSAI restated: particle-block layout, Jacobi scaling, per
     particle the nearest (by gap) kmax lower neighbours and itself; Z_a =
-    (Y_aa)^-1/2 Y^T with Y = B^-1 E_a."""
+    L^-1 Y^T with Y = B^-1 E_a and Y_aa = L L^T (Cholesky)."""
     p = np.array([[3 * a, 3 * a + 1, 3 * a + 2, 3 * N + 3 * a, 3 * N + 3 * a + 1, 3 * N + 3 * a + 2]
                   for a in range(N)]).ravel()
     A = R[np.ix_(p, p)]
@@ -161,8 +161,7 @@ def numpy_fsai(R, N, off, src, gap, kmax=16):
         E = np.zeros((len(J), 6))
         E[-6:] = np.eye(6)
         Y = np.linalg.solve(A[np.ix_(J, J)], E)
-        w, V = np.linalg.eigh(0.5 * (Y[-6:] + Y[-6:].T))
-        S = V @ np.diag(w ** -0.5) @ V.T
+        S = np.linalg.inv(np.linalg.cholesky(0.5 * (Y[-6:] + Y[-6:].T)))
         Z = S @ Y.T
         zd[a] = Z[:, -6:]
         for q, e in enumerate(es):
