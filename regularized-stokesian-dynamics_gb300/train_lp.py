@@ -10,7 +10,8 @@ sheared to its own Lees-Edwards strain (configs.sheared_series) and is
 advanced by the mixed-precision step (rsd_stepper_stokesian_dev, dt 5e-4,
 shear rate 1); every `stride` steps the resistance matrix RPP of the current
 configuration (FP32, from the mixed form's factors: rsd_resistance_pp_dev)
-is one training sample.  Each sample makes one supervised step: the network
+is one training sample.  Each sample makes one supervised step (Adam, the
+learning rate warmed up linearly over the first samples): the network
 emits the blocks of Z, the loss is their mean squared difference from the
 exact FSAI blocks of that matrix, and Adam updates the weights (kernels in
 csrc/learned.cu).  After training, one held-out system in FP64 gives the PCG
@@ -35,7 +36,8 @@ def main():
     ap.add_argument("--trajectories", type=int, default=10)
     ap.add_argument("--stride", type=int, default=2)
     ap.add_argument("--N", type=int, default=1000)
-    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--warmup", type=int, default=50, help="samples of linear learning-rate warm-up")
     ap.add_argument("--sweeps", type=int, default=100)
     ap.add_argument("--out", default=os.path.join(HERE, "lp_params.npy"))
     ap.add_argument("--seed", type=int, default=20264000)
@@ -72,7 +74,9 @@ def main():
                 print("trajectory %d stops at strain %.3f: %s" % (k, T, e), flush=True)
                 break
             frac = done / args.systems
-            lr = args.lr * (1.0 if frac < 0.5 else (0.25 if frac < 0.8 else 0.05))
+            # linear warm-up (the heads start at zero, Z = I: full-size first
+            # Adam steps overshoot), then steps down at 50 % and 80 %
+            lr = args.lr * min(1.0, (done + 1) / args.warmup) * (1.0 if frac < 0.5 else (0.25 if frac < 0.8 else 0.05))
             try:
                 loss = net.train_step(ctx, conf_t, radii_t, lat, rpp, lr)
             except rsd.RSDError as e:  # a local block not positive definite in FP32: skip the sample
