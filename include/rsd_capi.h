@@ -317,9 +317,12 @@ int rsd_stepper_stokesian_dev(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_ste
  * block lower triangular with 6 x 6 blocks on each particle and on each pair
  * of particles closer than 3 a_avg, b < a), either exact (the factorised
  * sparse approximate inverse, from one local dense solve per particle) or
- * emitted by a 3-layer message-passing network (hidden width 64, BF16
- * weights and activations, FP32 accumulation) over those pairs, whose inputs
- * are the Jacobi-scaled blocks of RPP and the pair gaps. */
+ * learned: a 3-layer message-passing network (hidden width 64, BF16 weights
+ * and activations, FP32 accumulation) over those pairs, whose inputs are the
+ * Jacobi-scaled blocks of RPP and the pair gaps, emits the direction
+ * W_ab = Z_aa^-1 Z_ab of every pair block, and each row block of Z is
+ * normalised from the local matrix so that (Z A Z^T)_aa = I (G is SPD
+ * whatever the network emits). */
 #define RSD_PC_NONE 0
 #define RSD_PC_JACOBI 1
 #define RSD_PC_BLOCK_JACOBI 2
@@ -352,8 +355,9 @@ int rsd_lp_forward_dev(rsd_ctx* ctx, rsd_lp* net, int32_t nn, int32_t ne, const 
 int rsd_lp_adam_step(rsd_lp* net, float lr);
 /* One training step on one resistance matrix: d_rpp (6nn x 6nn, grand
  * layout, ld, FP32 if fp32 != 0 else FP64, full symmetric storage) of the
- * configuration d_pos/d_radii on lattice lat; the targets are its exact FSAI
- * blocks; loss returns the mean squared block error before the step. */
+ * configuration d_pos/d_radii on lattice lat; the targets are the
+ * directions W of its exact FSAI; loss returns their mean squared error
+ * before the step. */
 int rsd_lp_train_step(rsd_ctx* ctx, rsd_lp* net, int32_t nn, const double* d_pos, const double* d_radii,
                       const rsd_lattice* lat, int32_t fp32, const void* d_rpp, int64_t ld, float lr, double* loss);
 /* The blocks of Z for mode RSD_PC_BLOCK_JACOBI, RSD_PC_FSAI or

@@ -15,9 +15,12 @@
 //     lower neighbours of a) or learned: a 3-layer message-passing network,
 //     hidden width 64, BF16 weights and activations with FP32 accumulation,
 //     whose inputs are the Jacobi-scaled blocks of RPP on the graph and the
-//     pair gaps, and whose outputs are the blocks of Z;
+//     pair gaps, emits for every lower edge (a <- b) the direction
+//     W_ab = Z_aa^-1 Z_ab; the row block is then Z_a = C [W_a.., I] with C
+//     fixed by (Z A Z^T)_aa = I from the local matrix (lp_normalize), which
+//     keeps G SPD and its diagonal blocks exact whatever the network emits;
 //   - the network's forward pass, its backward pass against a supervised
-//     loss (the exact FSAI blocks of the training matrices), and an Adam
+//     loss (the exact FSAI directions of the training matrices), and an Adam
 //     step, all as kernels here;
 //   - preconditioned conjugate gradients in FP64 on RPP (dense symmetric
 //     products), with the preconditioner none, Jacobi, block-Jacobi (FSAI
@@ -264,12 +267,12 @@ __global__ void __launch_bounds__(FS_THREADS) lp_fsai(int nn, int lower_only_sel
                                                       const double* __restrict__ dinv, const int* __restrict__ off,
                                                       const int* __restrict__ src, const float* __restrict__ gap,
                                                       float* __restrict__ zd, float* __restrict__ ze,
-                                                      int* __restrict__ bad) {
+                                                      float* __restrict__ wt, int* __restrict__ bad) {
   extern __shared__ double fs_smem[];
   __shared__ int nb_s[LP_KMAX + 1];
   __shared__ int eidx_s[LP_KMAX];
   __shared__ int k_s;
-  __shared__ double S_s[36];
+  __shared__ double S_s[36], P_s[36];
   const int a = blockIdx.x, t = threadIdx.x;
   const int e0 = off[a], e1 = off[a + 1];
   if (t == 0) {
@@ -341,8 +344,31 @@ __global__ void __launch_bounds__(FS_THREADS) lp_fsai(int nn, int lower_only_sel
     for (int r = 0; r < 6; r++)
       for (int c = 0; c < 6; c++) Yaa[r * 6 + c] = Y[c * m + (m - 6 + r)];
     sym6_chol_inv(Yaa, S_s);
+    for (int r = 0; r < 6; r++)  // P = S^T S = Y_aa^-1
+      for (int c = 0; c < 6; c++) {
+        double x = 0.0;
+        for (int q = 0; q < 6; q++) x += S_s[q * 6 + r] * S_s[q * 6 + c];
+        P_s[r * 6 + c] = x;
+      }
   }
   __syncthreads();
+  // the directions W_ab = Z_aa^-1 Z_ab = Y_aa^-1 Y_b^T of the kept edges
+  // (NaN for lower edges not kept): the learned network's targets
+  if (wt) {
+    for (int q = t; q < 36 * k; q += FS_THREADS) {
+      const int grp = q / 36, r = (q % 36) / 6, c = q % 6;
+      double x = 0.0;
+      for (int y = 0; y < 6; y++) x += P_s[r * 6 + y] * Y[y * m + 6 * grp + c];
+      wt[(size_t)eidx_s[grp] * 36 + r * 6 + c] = (float)x;
+    }
+    for (int e = e0 + t; e < e1; e += FS_THREADS) {
+      if (src[e] >= a) continue;
+      bool kept = false;
+      for (int q = 0; q < k; q++) kept |= eidx_s[q] == e;
+      if (!kept)
+        for (int x = 0; x < 36; x++) wt[(size_t)e * 36 + x] = __int_as_float(0x7fc00000);
+    }
+  }
   // Z_a = S Y^T: block of column group g is S (Y[g rows])^T
   for (int q = t; q < 36 * (k + 1); q += FS_THREADS) {
     const int grp = q / 36, r = (q % 36) / 6, c = q % 6;
@@ -354,6 +380,92 @@ __global__ void __launch_bounds__(FS_THREADS) lp_fsai(int nn, int lower_only_sel
       ze[(size_t)eidx_s[grp] * 36 + r * 6 + c] = (float)s;
   }
   // the lower edges not kept get zero blocks
+  for (int e = e0 + t; e < e1; e += FS_THREADS) {
+    if (src[e] >= a) continue;
+    bool kept = false;
+    for (int q = 0; q < k; q++) kept |= eidx_s[q] == e;
+    if (!kept)
+      for (int x = 0; x < 36; x++) ze[(size_t)e * 36 + x] = 0.f;
+  }
+}
+
+// From directions W_ab (edge blocks of w, the network's output for the kept
+// lower edges) to the factor Z: the row block Z_a = C [W_a.., I] with C the
+// inverse Cholesky factor of M_a = [W_a.., I] A^_JJ [W_a.., I]^T (6 x 6, SPD
+// for any W since the last block is I), so that (Z A^ Z^T)_aa = I and
+// G = Z^T Z is SPD whatever the network emits.  One CTA per particle, the
+// same neighbour selection as lp_fsai.
+template <typename T>
+__global__ void __launch_bounds__(FS_THREADS) lp_normalize(int nn, const T* __restrict__ A, int64_t ld,
+                                                           const double* __restrict__ dinv,
+                                                           const int* __restrict__ off, const int* __restrict__ src,
+                                                           const float* __restrict__ gap,
+                                                           const float* __restrict__ w, float* __restrict__ zd,
+                                                           float* __restrict__ ze) {
+  extern __shared__ double fs_smem[];
+  __shared__ int nb_s[LP_KMAX + 1];
+  __shared__ int eidx_s[LP_KMAX];
+  __shared__ int k_s;
+  __shared__ double M_s[36], S_s[36];
+  const int a = blockIdx.x, t = threadIdx.x;
+  const int e0 = off[a], e1 = off[a + 1];
+  if (t == 0) {
+    int k = 0;
+    for (int e = e0; e < e1; e++) {
+      if (src[e] >= a) continue;
+      if (k < LP_KMAX) {
+        eidx_s[k++] = e;
+      } else {
+        int worst = 0;
+        for (int q = 1; q < k; q++)
+          if (gap[eidx_s[q]] > gap[eidx_s[worst]]) worst = q;
+        if (gap[e] < gap[eidx_s[worst]]) eidx_s[worst] = e;
+      }
+    }
+    for (int q = 0; q < k; q++) nb_s[q] = src[eidx_s[q]];
+    nb_s[k] = a;
+    k_s = k;
+  }
+  __syncthreads();
+  const int k = k_s, m = 6 * (k + 1);
+  double* B = fs_smem;      // m x m, column-major
+  double* Wf = B + m * m;   // 6 x m, row-major: [W_a.., I]
+  double* Tm = Wf + 6 * m;  // m x 6: B Wf^T
+  for (int q = t; q < m * m; q += FS_THREADS) {
+    const int r = q % m, c = q / m;
+    const int i = 6 * nb_s[r / 6] + r % 6, j = 6 * nb_s[c / 6] + c % 6;
+    B[q] = rpp_at(A, ld, nn, i, j) * dinv[i] * dinv[j];
+  }
+  for (int q = t; q < 6 * m; q += FS_THREADS) {
+    const int r = q / m, j = q % m, grp = j / 6, c = j % 6;
+    Wf[q] = grp == k ? (r == c ? 1.0 : 0.0) : (double)w[(size_t)eidx_s[grp] * 36 + r * 6 + c];
+  }
+  __syncthreads();
+  for (int q = t; q < 6 * m; q += FS_THREADS) {
+    const int i = q / 6, r = q % 6;
+    double x = 0.0;
+    for (int j = 0; j < m; j++) x += B[i + (size_t)j * m] * Wf[r * m + j];
+    Tm[i * 6 + r] = x;
+  }
+  __syncthreads();
+  if (t < 36) {
+    const int r = t / 6, c = t % 6;
+    double x = 0.0;
+    for (int i = 0; i < m; i++) x += Wf[r * m + i] * Tm[i * 6 + c];
+    M_s[t] = x;
+  }
+  __syncthreads();
+  if (t == 0) sym6_chol_inv(M_s, S_s);
+  __syncthreads();
+  for (int q = t; q < 36 * (k + 1); q += FS_THREADS) {
+    const int grp = q / 36, r = (q % 36) / 6, c = q % 6;
+    double x = 0.0;
+    for (int y = 0; y < 6; y++) x += S_s[r * 6 + y] * Wf[y * m + 6 * grp + c];
+    if (grp == k)
+      zd[(size_t)a * 36 + r * 6 + c] = (float)x;
+    else
+      ze[(size_t)eidx_s[grp] * 36 + r * 6 + c] = (float)x;
+  }
   for (int e = e0 + t; e < e1; e += FS_THREADS) {
     if (src[e] >= a) continue;
     bool kept = false;
@@ -542,31 +654,40 @@ __global__ void lp_agg_bwd(int ne, const int* __restrict__ dst, const float* __r
   dmsg[t] += dagg[(size_t)dst[t / H] * H + t % H];
 }
 
-// supervised loss on the Z blocks: L = |zd - td|^2 / (36 N) + |ze - te|^2 /
-// (36 E_lower) over the lower edges; dzd, dze its gradient
-__global__ void lp_loss(int nn, int ne, const float* __restrict__ zd, const float* __restrict__ td,
-                        const float* __restrict__ ze, const float* __restrict__ te, const int* __restrict__ lower,
-                        float inv_nd, float inv_ne, float* __restrict__ dzd, float* __restrict__ dze,
+// supervised loss on the directions W of the lower edges kept by the FSAI
+// pattern (targets NaN elsewhere; targets beyond 20 in magnitude, from
+// nearly singular FP32 local blocks, are left out): L = mean squared error
+// over the kept entries; dze its gradient (zero elsewhere)
+__global__ void lp_loss(int ne, const float* __restrict__ ze, const float* __restrict__ te,
+                        const int* __restrict__ lower, float inv_cnt, float* __restrict__ dze,
                         double* __restrict__ loss) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
   double l = 0.0;
-  if (t < nn * 36) {
-    const float d = zd[t] - td[t];
-    dzd[t] = 2.f * d * inv_nd;
-    l = (double)d * d * inv_nd;
-  }
-  const int u = t - nn * 36;
-  if (u >= 0 && u < ne * 36) {
-    if (lower[u / 36]) {
-      const float d = ze[u] - te[u];
-      dze[u] = 2.f * d * inv_ne;
-      l = (double)d * d * inv_ne;
+  if (u < ne * 36) {
+    const float tv = te[u];
+    if (lower[u / 36] && isfinite(tv) && fabsf(tv) <= 20.f) {
+      const float d = ze[u] - tv;
+      dze[u] = 2.f * d * inv_cnt;
+      l = (double)d * d * inv_cnt;
     } else {
       dze[u] = 0.f;
     }
   }
   for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
   if ((threadIdx.x & 31) == 0 && l != 0.0) atomicAdd(loss, l);
+}
+
+// entries of the targets that enter the loss
+__global__ void lp_count_targets(int ne, const float* __restrict__ te, const int* __restrict__ lower,
+                                 int* __restrict__ cnt) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  int c = 0;
+  if (u < ne * 36) {
+    const float tv = te[u];
+    c = lower[u / 36] && isfinite(tv) && fabsf(tv) <= 20.f;
+  }
+  c = __reduce_add_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(cnt, c);
 }
 
 __global__ void lp_lower_flags(int ne, const int* __restrict__ src, const int* __restrict__ dst, int* __restrict__ f) {
@@ -765,21 +886,24 @@ static int lp_scale_features(rsd_ctx* ctx, const lp_graph& g, const T* A, int64_
   return RSD_OK;
 }
 
+// shared memory of lp_fsai and lp_normalize: the local matrix (m x m) and
+// two m x 6 panels, m at most 6 (LP_KMAX + 1)
+constexpr size_t LP_LOCAL_SMEM = sizeof(double) * ((size_t)(6 * (LP_KMAX + 1)) * (6 * (LP_KMAX + 1)) +
+                                                   2 * (size_t)(6 * (LP_KMAX + 1)) * 6);
+
 template <typename T>
 static int lp_exact_fsai(rsd_ctx* ctx, const lp_graph& g, const T* A, int64_t ld, const double* dinv, int self_only,
-                         float* zd, float* ze) {
+                         float* zd, float* ze, float* wt = nullptr) {
   cudaStream_t s = ctx->stream;
-  const int mmax = 6 * (LP_KMAX + 1);
-  const size_t smem = sizeof(double) * ((size_t)mmax * mmax + (size_t)mmax * 6);
   static bool attr[2] = {false, false};
   const int which = sizeof(T) == 8;
   if (!attr[which]) {
-    RSD_CUDA(ctx, cudaFuncSetAttribute(lp_fsai<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    RSD_CUDA(ctx, cudaFuncSetAttribute(lp_fsai<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LP_LOCAL_SMEM));
     attr[which] = true;
   }
   int* bad = ctx->d_info + 10;
   RSD_CUDA(ctx, cudaMemsetAsync(bad, 0, sizeof(int), s));
-  lp_fsai<T><<<g.nn, FS_THREADS, smem, s>>>(g.nn, self_only, A, ld, dinv, g.off, g.src, g.gap, zd, ze, bad); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
+  lp_fsai<T><<<g.nn, FS_THREADS, LP_LOCAL_SMEM, s>>>(g.nn, self_only, A, ld, dinv, g.off, g.src, g.gap, zd, ze, wt, bad); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
   RSD_CUDA(ctx, cudaMemcpyAsync(ctx->h_info + 10, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
   RSD_CUDA(ctx, cudaStreamSynchronize(s));
   if (ctx->h_info[10]) return rsd_fail(ctx, RSD_ENAN, "FSAI: a local block of RPP is not positive definite");
@@ -940,11 +1064,26 @@ static int lp_make_z(rsd_ctx* ctx, rsd_lp* net, int mode, const lp_graph& g, con
   *ze = (float*)rsd_scratch(ctx, "lp_ze", sizeof(float) * ((size_t)g.ne * 36 + 1));
   if (!*zd || !*ze) return RSD_ENOMEM;
   if (mode == RSD_PC_LEARNED) {
+    // the network emits the directions W of the lower edges; lp_normalize
+    // turns them into the factor Z (SPD G whatever W is)
     if (!net) return rsd_fail(ctx, RSD_EARG, "learned preconditioner: no network");
     __nv_bfloat16 *xn, *xe;
     RSD_TRY(lp_scale_features<T>(ctx, g, A, ld, dinv, &xn, &xe));
+    float* hd = (float*)rsd_scratch(ctx, "lp_head_d", sizeof(float) * (size_t)g.nn * 36);
+    float* wp = (float*)rsd_scratch(ctx, "lp_wpred", sizeof(float) * ((size_t)g.ne * 36 + 1));
+    if (!hd || !wp) return RSD_ENOMEM;
     lp_acts acts;
-    return lp_forward(ctx, net, g, xn, xe, &acts, *zd, *ze);
+    RSD_TRY(lp_forward(ctx, net, g, xn, xe, &acts, hd, wp));
+    static bool attr[2] = {false, false};
+    const int which = sizeof(T) == 8;
+    if (!attr[which]) {
+      RSD_CUDA(ctx, cudaFuncSetAttribute(lp_normalize<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)LP_LOCAL_SMEM));
+      attr[which] = true;
+    }
+    lp_normalize<T><<<g.nn, FS_THREADS, LP_LOCAL_SMEM, ctx->stream>>>(g.nn, A, ld, *dinv, g.off, g.src, g.gap, wp,
+                                                                      *zd, *ze); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
+    return RSD_OK;
   }
   RSD_TRY(lp_scale_features<T>(ctx, g, A, ld, dinv, nullptr, nullptr));
   if (mode == RSD_PC_FSAI || mode == RSD_PC_BLOCK_JACOBI)
@@ -1179,28 +1318,33 @@ static int lp_train_t(rsd_ctx* ctx, rsd_lp* net, int nn, const double* d_pos, co
   double* dinv;
   __nv_bfloat16 *xn, *xe;
   RSD_TRY(lp_scale_features<T>(ctx, g, A, ld, &dinv, &xn, &xe));
-  // targets: the exact FSAI blocks of this matrix
+  // targets: the directions W of this matrix's exact FSAI (its Z blocks go
+  // to td / tz, unused here)
   float* td = (float*)rsd_scratch(ctx, "lp_td", sizeof(float) * (size_t)nn * 36);
+  float* tz = (float*)rsd_scratch(ctx, "lp_tz", sizeof(float) * ((size_t)g.ne * 36 + 1));
   float* te = (float*)rsd_scratch(ctx, "lp_te", sizeof(float) * ((size_t)g.ne * 36 + 1));
+  int* cnt = (int*)rsd_scratch(ctx, "lp_tcount", sizeof(int));
   float* zd = (float*)rsd_scratch(ctx, "lp_zd", sizeof(float) * (size_t)nn * 36);
   float* ze = (float*)rsd_scratch(ctx, "lp_ze", sizeof(float) * ((size_t)g.ne * 36 + 1));
   float* dzd = (float*)rsd_scratch(ctx, "lp_dzd", sizeof(float) * (size_t)nn * 36);
   float* dze = (float*)rsd_scratch(ctx, "lp_dze", sizeof(float) * ((size_t)g.ne * 36 + 1));
   double* dl = (double*)rsd_scratch(ctx, "lp_loss", sizeof(double));
-  if (!td || !te || !zd || !ze || !dzd || !dze || !dl) return RSD_ENOMEM;
-  RSD_TRY(lp_exact_fsai<T>(ctx, g, A, ld, dinv, 0, td, te));
+  if (!td || !tz || !te || !cnt || !zd || !ze || !dzd || !dze || !dl) return RSD_ENOMEM;
+  if (g.ne == 0) {
+    *loss = 0.0;
+    return RSD_OK;
+  }
+  RSD_TRY(lp_exact_fsai<T>(ctx, g, A, ld, dinv, 0, td, tz, te));
   lp_acts acts;
   RSD_TRY(lp_forward(ctx, net, g, xn, xe, &acts, zd, ze));
-  int nlow = 0;
-  {
-    std::vector<int> h(nn + 1);
-    RSD_CUDA(ctx, cudaMemcpyAsync(h.data(), g.off, sizeof(int) * (nn + 1), cudaMemcpyDeviceToHost, s));
-    RSD_CUDA(ctx, cudaStreamSynchronize(s));
-    nlow = g.ne / 2;  // every pair appears once as a lower edge
-  }
+  int hcnt = 0;
+  RSD_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int), s));
+  lp_count_targets<<<nb256((int64_t)g.ne * 36), 256, 0, s>>>(g.ne, te, g.lower, cnt); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
+  RSD_CUDA(ctx, cudaMemcpyAsync(&hcnt, cnt, sizeof(int), cudaMemcpyDeviceToHost, s));
+  RSD_CUDA(ctx, cudaStreamSynchronize(s));
   RSD_CUDA(ctx, cudaMemsetAsync(dl, 0, sizeof(double), s));
-  lp_loss<<<nb256((int64_t)(nn + g.ne) * 36), 256, 0, s>>>(nn, g.ne, zd, td, ze, te, g.lower, 1.f / (36.f * nn),
-                                                           nlow ? 1.f / (36.f * nlow) : 0.f, dzd, dze, dl); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
+  RSD_CUDA(ctx, cudaMemsetAsync(dzd, 0, sizeof(float) * (size_t)nn * 36, s));  // the node head is not trained
+  lp_loss<<<nb256((int64_t)g.ne * 36), 256, 0, s>>>(g.ne, ze, te, g.lower, hcnt ? 1.f / hcnt : 0.f, dze, dl); RSD_LAUNCH_NOTE(); RSD_LP_CHECK();
   RSD_TRY(lp_backward(ctx, net, g, xn, xe, acts, dzd, dze));
   RSD_CUDA(ctx, cudaMemcpyAsync(loss, dl, sizeof(double), cudaMemcpyDeviceToHost, s));
   RSD_CUDA(ctx, cudaStreamSynchronize(s));

@@ -12,9 +12,9 @@ shear rate 1); every `stride` steps the resistance matrix RPP of the current
 configuration (FP32, from the mixed form's factors: rsd_resistance_pp_dev)
 is one training sample.  Each sample makes one supervised step (Adam, the
 learning rate warmed up linearly over the first samples): the network
-emits the blocks of Z, the loss is their mean squared difference from the
-exact FSAI blocks of that matrix, and Adam updates the weights (kernels in
-csrc/learned.cu).  After training, one held-out system in FP64 gives the PCG
+emits the directions W_ab = Z_aa^-1 Z_ab of the pair blocks, the loss is
+their mean squared difference from those of that matrix's exact FSAI, and
+Adam updates the weights (kernels in csrc/learned.cu).  After training, one held-out system in FP64 gives the PCG
 iteration counts of every preconditioner.  Prints one JSON line and writes
 the FP32 parameters to --out.
 """

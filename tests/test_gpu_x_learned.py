@@ -186,6 +186,36 @@ def test_exact_fsai_against_numpy(rsd, ctx):
     assert len(src) % 2 == 0
 
 
+def test_learned_blocks_are_normalised(rsd, ctx):
+    """Whatever the network emits (here an untrained one), each row block of
+    the learned Z satisfies (Z A^ Z^T)_aa = I on the Jacobi-scaled RPP, so
+    that G = Z^T Z is SPD (FP32 storage of the blocks: 1e-4)."""
+    tab = rsd.LubTab(rsd.lubdat_dir())
+    pos, radii, L, pos_t, radii_t, rpp, lat = system(rsd, ctx, tab, 64, 0.45, 1e-3, 20262204, T=0.3)
+    net = rsd.LearnedPreconditioner(0, seed=9)
+    p0 = net.params()
+    p0 += 0.05 * np.random.default_rng(9).normal(size=p0.size).astype(np.float32)  # non-zero heads
+    net = rsd.LearnedPreconditioner(0, params=p0)
+    zd, ze, off, src = rsd.lp_blocks_dev(ctx, net, rsd.PC_LEARNED, pos_t, radii_t, lat, rpp)
+    N = 64
+    R = rpp.cpu().numpy()
+    p = np.array([[3 * a, 3 * a + 1, 3 * a + 2, 3 * N + 3 * a, 3 * N + 3 * a + 1, 3 * N + 3 * a + 2]
+                  for a in range(N)]).ravel()
+    A = R[np.ix_(p, p)]
+    d = 1.0 / np.sqrt(np.diag(A))
+    A = A * d[:, None] * d[None, :]
+    Z = np.zeros((6 * N, 6 * N))
+    for a in range(N):
+        Z[6 * a:6 * a + 6, 6 * a:6 * a + 6] = zd[a]
+        for e in range(off[a], off[a + 1]):
+            if src[e] < a:
+                Z[6 * a:6 * a + 6, 6 * src[e]:6 * src[e] + 6] = ze[e]
+    C = Z @ A @ Z.T
+    for a in range(N):
+        assert np.abs(C[6 * a:6 * a + 6, 6 * a:6 * a + 6] - np.eye(6)).max() <= 1e-4
+    assert np.linalg.eigvalsh(0.5 * (C + C.T)).min() > 0
+
+
 def test_pcg_every_preconditioner(rsd, ctx):
     import torch
     tab = rsd.LubTab(rsd.lubdat_dir())
