@@ -269,6 +269,6 @@ def test_training_step_reduces_the_loss(rsd, ctx):
     # Z starts at I (zero heads), already close to the targets after the
     # Jacobi scaling: a learning rate warmed up over 20 steps keeps the first
     # Adam steps from overshooting
-    losses = [net.train_step(ctx, pos_t, radii_t, lat, rpp32, 1e-3 * min(1.0, (k + 1) / 20.0)) for k in range(80)]
+    losses = [net.train_step(ctx, pos_t, radii_t, lat, rpp32, 1e-3 * min(1.0, (k + 1) / 20.0)) for k in range(200)]
     assert np.isfinite(losses).all()
-    assert losses[-1] < 0.85 * losses[0], losses[::10]
+    assert np.mean(losses[-10:]) < 0.8 * losses[0], losses[::20]
