@@ -351,13 +351,23 @@ int rsd_lp_graph_dev(rsd_ctx* ctx, int32_t nn, const double* d_pos, const double
 int rsd_lp_forward_dev(rsd_ctx* ctx, rsd_lp* net, int32_t nn, int32_t ne, const int32_t* d_off, const int32_t* d_src,
                        const int32_t* d_dst, const float* d_xn, const float* d_xe, const float* d_dzd,
                        const float* d_dze, float* d_zd, float* d_ze);
-/* One Adam step (beta 0.9, 0.999, eps 1e-8) on the stored gradient. */
+/* One Adam step (beta 0.9, 0.999, eps 1e-8) on the stored gradient, scaled
+ * to norm clip_norm when it is larger (rsd_lp_set_training); a gradient
+ * whose norm is not finite makes no update. */
 int rsd_lp_adam_step(rsd_lp* net, float lr);
+/* Training guards: clip_norm > 0 clips the gradient to that global norm;
+ * max_loss > 0 makes a train step whose loss is larger (or not finite) make
+ * no update.  0 switches either off (the default). */
+int rsd_lp_set_training(rsd_lp* net, float clip_norm, double max_loss);
+/* The norm of the last gradient, the train steps that made no update and the
+ * Adam steps taken; any pointer may be NULL. */
+int rsd_lp_training_stats(rsd_lp* net, double* last_grad_norm, int64_t* skipped, int64_t* steps);
 /* One training step on one resistance matrix: d_rpp (6nn x 6nn, grand
  * layout, ld, FP32 if fp32 != 0 else FP64, full symmetric storage) of the
  * configuration d_pos/d_radii on lattice lat; the targets are the
  * directions W of its exact FSAI; loss returns their mean squared error
- * before the step. */
+ * before the step (a loss above the max_loss of rsd_lp_set_training, or not
+ * finite, makes no update). */
 int rsd_lp_train_step(rsd_ctx* ctx, rsd_lp* net, int32_t nn, const double* d_pos, const double* d_radii,
                       const rsd_lattice* lat, int32_t fp32, const void* d_rpp, int64_t ld, float lr, double* loss);
 /* The blocks of Z for mode RSD_PC_BLOCK_JACOBI, RSD_PC_FSAI or

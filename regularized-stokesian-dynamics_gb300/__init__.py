@@ -112,6 +112,8 @@ _sig("rsd_lp_get_params", _i, [_vp, _vp, _vp])
 _sig("rsd_lp_graph_dev", _i, [_vp, _i32, _vp, _vp, _LP, ctypes.POINTER(_i32), _vp, _vp, _vp])
 _sig("rsd_lp_forward_dev", _i, [_vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp])
 _sig("rsd_lp_adam_step", _i, [_vp, ctypes.c_float])
+_sig("rsd_lp_set_training", _i, [_vp, ctypes.c_float, ctypes.c_double])
+_sig("rsd_lp_training_stats", _i, [_vp, _dp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)])
 _sig("rsd_lp_train_step", _i, [_vp, _vp, _i32, _vp, _vp, _LP, _i32, _vp, _i64, ctypes.c_float, _dp])
 _sig("rsd_lp_blocks_dev", _i, [_vp, _vp, _i32, _i32, _vp, _vp, _LP, _i32, _vp, _i64, _vp, _vp,
                                ctypes.POINTER(_i32)])
@@ -558,6 +560,21 @@ class LearnedPreconditioner:
         rc = _lib.rsd_lp_adam_step(self.h, ctypes.c_float(lr))
         if rc:
             raise RSDError(rc, "rsd_lp_adam_step")
+
+    def set_training(self, clip_norm=0.0, max_loss=0.0):
+        """Guards of train_step: clip the gradient to global norm clip_norm;
+        make no update on a step whose loss exceeds max_loss (0: off)."""
+        rc = _lib.rsd_lp_set_training(self.h, ctypes.c_float(clip_norm), ctypes.c_double(max_loss))
+        if rc:
+            raise RSDError(rc, "rsd_lp_set_training")
+
+    def training_stats(self):
+        """(norm of the last gradient, steps that made no update, Adam steps)."""
+        g, sk, st = ctypes.c_double(0.0), ctypes.c_int64(0), ctypes.c_int64(0)
+        rc = _lib.rsd_lp_training_stats(self.h, ctypes.byref(g), ctypes.byref(sk), ctypes.byref(st))
+        if rc:
+            raise RSDError(rc, "rsd_lp_training_stats")
+        return g.value, sk.value, st.value
 
     def train_step(self, ctx, pos_t, radii_t, lattice, rpp_t, lr):
         """One supervised step on one resistance matrix (torch CUDA tensor,

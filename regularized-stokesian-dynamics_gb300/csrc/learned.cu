@@ -87,6 +87,11 @@ struct rsd_lp {
   float* g = nullptr;            // gradient
   float* m = nullptr;            // Adam moments
   float* v = nullptr;
+  double* gn2 = nullptr;         // squared norm of the last gradient (device)
+  float clip = 0.f;              // global gradient-norm clip (0: off)
+  double max_loss = 0.0;         // a train step with a larger loss makes no update (0: off)
+  double last_gnorm = 0.0;       // norm of the last gradient
+  int64_t skipped = 0;           // train steps that made no update
   int64_t step = 0;
 };
 
@@ -695,13 +700,28 @@ __global__ void lp_lower_flags(int ne, const int* __restrict__ src, const int* _
   if (e < ne) f[e] = src[e] < dst[e];
 }
 
-// Adam (Kingma and Ba, 2015), FP32 master weights; BF16 copies refreshed
+// squared Euclidean norm of the gradient, accumulated in FP64
+__global__ void lp_gnorm2(int64_t n, const float* __restrict__ g, double* __restrict__ out) {
+  double l = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    l += (double)g[i] * g[i];
+  for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+  if ((threadIdx.x & 31) == 0 && l != 0.0) atomicAdd(out, l);
+}
+
+// Adam (Kingma and Ba, 2015), FP32 master weights; BF16 copies refreshed.
+// The gradient is scaled by min(1, clip / |g|) when clip > 0 (global norm
+// clipping, Pascanu et al., 2013); a gradient whose norm is not finite makes
+// no update.
 __global__ void lp_adam(int64_t n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
                         float* __restrict__ v, __nv_bfloat16* __restrict__ wb, float lr, float b1, float b2, float eps,
-                        float c1, float c2) {
+                        float c1, float c2, const double* __restrict__ gn2, float clip) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float gi = g[i];
+  const double gn = sqrt(*gn2);
+  if (!isfinite(gn)) return;
+  const float sc = (clip > 0.f && gn > clip) ? (float)(clip / gn) : 1.f;
+  const float gi = g[i] * sc;
   const float mi = b1 * m[i] + (1.f - b1) * gi, vi = b2 * v[i] + (1.f - b2) * gi * gi;
   m[i] = mi;
   v[i] = vi;
@@ -1177,6 +1197,7 @@ extern "C" int rsd_lp_create(rsd_lp** out, int device, const float* params, uint
   if (e == cudaSuccess) e = cudaMalloc(&n->m, bytes);
   if (e == cudaSuccess) e = cudaMalloc(&n->v, bytes);
   if (e == cudaSuccess) e = cudaMalloc(&n->wb, sizeof(__nv_bfloat16) * LAY.total);
+  if (e == cudaSuccess) e = cudaMalloc(&n->gn2, sizeof(double));
   std::vector<float> h(LAY.total, 0.f);
   if (params) {
     memcpy(h.data(), params, bytes);
@@ -1219,6 +1240,7 @@ extern "C" int rsd_lp_create(rsd_lp** out, int device, const float* params, uint
     cudaFree(n->m);
     cudaFree(n->v);
     cudaFree(n->wb);
+    cudaFree(n->gn2);
     delete n;
     return RSD_ECUDA;
   }
@@ -1234,7 +1256,23 @@ extern "C" int rsd_lp_destroy(rsd_lp* n) {
   cudaFree(n->m);
   cudaFree(n->v);
   cudaFree(n->wb);
+  cudaFree(n->gn2);
   delete n;
+  return RSD_OK;
+}
+
+extern "C" int rsd_lp_set_training(rsd_lp* n, float clip_norm, double max_loss) {
+  if (!n || !(clip_norm >= 0.f) || !(max_loss >= 0.0)) return RSD_EARG;
+  n->clip = clip_norm;
+  n->max_loss = max_loss;
+  return RSD_OK;
+}
+
+extern "C" int rsd_lp_training_stats(rsd_lp* n, double* last_grad_norm, int64_t* skipped, int64_t* steps) {
+  if (!n) return RSD_EARG;
+  if (last_grad_norm) *last_grad_norm = n->last_gnorm;
+  if (skipped) *skipped = n->skipped;
+  if (steps) *steps = n->step;
   return RSD_OK;
 }
 
@@ -1300,10 +1338,23 @@ extern "C" int rsd_lp_forward_dev(rsd_ctx* ctx, rsd_lp* net, int32_t nn, int32_t
 extern "C" int rsd_lp_adam_step(rsd_lp* net, float lr) {
   if (!net || !(lr > 0)) return RSD_EARG;
   if (cudaSetDevice(net->device) != cudaSuccess) return RSD_ECUDA;
+  if (cudaMemset(net->gn2, 0, sizeof(double)) != cudaSuccess) return RSD_ECUDA;
+  lp_gnorm2<<<4 * 152, 256>>>(LAY.total, net->g, net->gn2);
+  RSD_LAUNCH_NOTE();
+  double gn2 = 0.0;
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemcpy(&gn2, net->gn2, sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return RSD_ECUDA;
+  net->last_gnorm = sqrt(gn2);
+  if (!std::isfinite(net->last_gnorm)) {
+    net->skipped++;
+    return RSD_OK;
+  }
   net->step++;
   const float b1 = 0.9f, b2 = 0.999f;
   const float c1 = 1.f - powf(b1, (float)net->step), c2 = 1.f - powf(b2, (float)net->step);
-  lp_adam<<<nb256(LAY.total), 256>>>(LAY.total, net->w, net->g, net->m, net->v, net->wb, lr, b1, b2, 1e-8f, c1, c2);
+  lp_adam<<<nb256(LAY.total), 256>>>(LAY.total, net->w, net->g, net->m, net->v, net->wb, lr, b1, b2, 1e-8f, c1, c2,
+                                     net->gn2, net->clip);
   RSD_LAUNCH_NOTE();
   if (cudaGetLastError() != cudaSuccess) return RSD_ECUDA;
   return cudaDeviceSynchronize() == cudaSuccess ? RSD_OK : RSD_ECUDA;
@@ -1348,6 +1399,10 @@ static int lp_train_t(rsd_ctx* ctx, rsd_lp* net, int nn, const double* d_pos, co
   RSD_TRY(lp_backward(ctx, net, g, xn, xe, acts, dzd, dze));
   RSD_CUDA(ctx, cudaMemcpyAsync(loss, dl, sizeof(double), cudaMemcpyDeviceToHost, s));
   RSD_CUDA(ctx, cudaStreamSynchronize(s));
+  if (!std::isfinite(*loss) || (net->max_loss > 0.0 && *loss > net->max_loss)) {  // an outlier: no update
+    net->skipped++;
+    return RSD_OK;
+  }
   return rsd_lp_adam_step(net, lr);
 }
 

@@ -213,7 +213,10 @@ def test_learned_blocks_are_normalised(rsd, ctx):
     C = Z @ A @ Z.T
     for a in range(N):
         assert np.abs(C[6 * a:6 * a + 6, 6 * a:6 * a + 6] - np.eye(6)).max() <= 1e-4
-    assert np.linalg.eigvalsh(0.5 * (C + C.T)).min() > 0
+    ev = np.linalg.eigvalsh(0.5 * (C + C.T))
+    # Z A Z^T is positive definite in exact arithmetic; in FP64 its smallest
+    # eigenvalue may round to a few ulps of the largest below zero
+    assert ev.min() > -1e-12 * ev.max()
 
 
 def test_pcg_every_preconditioner(rsd, ctx):
@@ -272,3 +275,36 @@ def test_training_step_reduces_the_loss(rsd, ctx):
     losses = [net.train_step(ctx, pos_t, radii_t, lat, rpp32, 1e-3 * min(1.0, (k + 1) / 20.0)) for k in range(200)]
     assert np.isfinite(losses).all()
     assert np.mean(losses[-10:]) < 0.8 * losses[0], losses[::20]
+
+
+def test_training_guards(rsd, ctx):
+    """A step whose loss is above the loss guard makes no update; the
+    gradient clip bounds the first Adam step whatever the gradient's size."""
+    import torch
+    tab = rsd.LubTab(rsd.lubdat_dir())
+    pos, radii, L = rsd.configs.packing(64, 0.45, 1e-3, 20262204, sweeps=30)
+    pos_t = torch.tensor(pos, dtype=torch.float64, device="cuda")
+    radii_t = torch.tensor(radii, dtype=torch.float64, device="cuda")
+    rpp32, lat = rsd.resistance_pp_dev(ctx, tab, pos_t, radii_t, 0.0, [L, L, L], 1.0, MU, 1e-10,
+                                       precision=rsd.PREC_MIXED)
+    net = rsd.LearnedPreconditioner(0, seed=6)
+    w0 = net.params()
+    net.set_training(0.0, 1e-30)  # every loss is above the guard
+    l0 = net.train_step(ctx, pos_t, radii_t, lat, rpp32, 1e-3)
+    assert l0 > 1e-30
+    assert np.array_equal(net.params(), w0)
+    g0, skipped, steps = net.training_stats()
+    assert (skipped, steps) == (1, 0) and g0 == 0.0
+    gn = np.linalg.norm(net.grad().astype(np.float64))  # the skipped step's gradient is kept
+    assert gn > 1e-4
+    net.set_training(0.1 * gn, 0.0)  # a clip at a tenth of the norm
+    l1 = net.train_step(ctx, pos_t, radii_t, lat, rpp32, 1e-3)
+    assert abs(l1 - l0) <= 1e-6 * l0  # same weights, same sample (up to the order of atomic sums)
+    g1, skipped, steps = net.training_stats()
+    assert (skipped, steps) == (1, 1)
+    assert abs(g1 - gn) <= 1e-4 * gn  # the norm before the clip
+    w1 = net.params()
+    # Adam's first step moves each weight by lr * sign(g) whatever the scale
+    # of g (to within eps / |g|), so the clip leaves its size unchanged
+    d = np.abs(w1 - w0)
+    assert d.max() <= 1e-3 * 1.001 and d.max() >= 0.5e-3
