@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--no-peaks", action="store_true")
     ap.add_argument("--tensor-cores", type=int, default=1, choices=[0, 1, 3],
                     help="FP32 factorisations of the mixed form: 1 TF32/3xTF32 per factor, 3 all 3xTF32, 0 SIMT")
+    ap.add_argument("--factor-schedule", type=int, default=1, choices=[0, 1],
+                    help="mixed form's FP32 Cholesky: 1 look-ahead on the diagonal chain, 0 in-order panels")
     ap.add_argument("--validate-cpu-model", action="store_true",
                     help="(reference arm) time one whole CPU step at N=512 and compare it with the sample model")
     ap.add_argument("--refinement", default="stationary", choices=["gmres", "stationary"],
@@ -607,6 +609,7 @@ def main():
     mu = rsd.mu_f_dimensionless(1.0)
     ctx = rsd.Context(local)
     ctx.set_tensor_cores(args.tensor_cores)
+    ctx.set_factor_schedule(args.factor_schedule)
     ctx.set_refinement(1 if args.refinement == "gmres" else 0)
     tab = rsd.LubTab(rsd.lubdat_dir())
     radii_t = torch.tensor(radii, dtype=torch.float64, device=dev)
@@ -752,7 +755,8 @@ def main():
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic (seeded sphere packing sheared to each stratum, no dataset)",
             "config": {"workload": workload_name(args), "precision": args.precision,
-                       "tensor_cores": args.tensor_cores, "refinement": args.refinement, "strata_skew": skews,
+                       "tensor_cores": args.tensor_cores, "factor_schedule": args.factor_schedule,
+                       "refinement": args.refinement, "strata_skew": skews,
                        "mean_images_per_pair": float(np.mean([sum(images(i[1], i[2])) for i in infos])),
                        "l2": "inputs larger than L2 (grand mobility %.2f GB)" % (8 * (11 * N) ** 2 / 1e9),
                        "parallelism": "replicas" if ws > 1 else "single GPU"},

@@ -129,6 +129,13 @@ int rsd_ctx_set_refinement(rsd_ctx* ctx, int32_t mode, int32_t restart);
  * raises an error word; the call returns RSD_ETIMEOUT and the context stays
  * usable.  Values far below the defaults only serve to exercise that path. */
 int rsd_ctx_set_wait_limits(rsd_ctx* ctx, int64_t tc_wait_ns, int64_t tri_spin_polls);
+/* Schedule of the mixed form's FP32 Cholesky factorisations on tensor
+ * cores: 1 (default) keeps only the next diagonal tile on the chain of
+ * diagonal blocks and runs the wide row-panel work on a second stream beside
+ * the next block's factor; 0 runs each 128-wide step's panel work in order
+ * before the next factor.  Both give the same factor up to the order of
+ * FP32 sums. */
+int rsd_ctx_set_factor_schedule(rsd_ctx* ctx, int32_t schedule);
 
 /* ---------------------------------------------------------------- lattice */
 /* SET_LATTICE_SKEW (src/csd_post.f90:105-136) with MAT_INV3

@@ -103,6 +103,7 @@ _sig("rsd_ctx_set_mixed_lambda_scale", _i, [_vp, _d])
 _sig("rsd_ctx_set_mixed_real_passes", _i, [_vp, _i32])
 _sig("rsd_ctx_set_correction_method", _i, [_vp, _i32])
 _sig("rsd_ctx_set_wait_limits", _i, [_vp, _i64, _i64])
+_sig("rsd_ctx_set_factor_schedule", _i, [_vp, _i32])
 _sig("rsd_ctx_set_refinement", _i, [_vp, _i32, _i32])
 _sig("rsd_ctx_set_rpp_solver", _i, [_vp, _i32, _vp, _d, _i32])
 _sig("rsd_lp_param_count", ctypes.c_int64, [])
@@ -199,6 +200,11 @@ class Context:
         0.5 s and 2^21 polls); a wait that gives up makes the call return
         RSD_ETIMEOUT."""
         self.check(_lib.rsd_ctx_set_wait_limits(self.h, int(tc_wait_ns), int(tri_spin_polls)))
+
+    def set_factor_schedule(self, schedule=1):
+        """Mixed form's FP32 Cholesky schedule: 1 look-ahead on the chain of
+        diagonal blocks (default), 0 in-order panel steps."""
+        self.check(_lib.rsd_ctx_set_factor_schedule(self.h, int(schedule)))
 
     def set_refinement(self, mode=0, restart=30):
         """Mixed form's refinement: 0 the stationary iteration (default), 1

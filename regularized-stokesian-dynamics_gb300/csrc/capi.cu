@@ -97,8 +97,10 @@ int rsd_side_stream(rsd_ctx* c) {
   int lo = 0, hi = 0;
   RSD_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
   RSD_CUDA(c, cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, hi));
+  RSD_CUDA(c, cudaStreamCreateWithPriority(&c->side2, cudaStreamNonBlocking, hi));
   RSD_CUDA(c, cudaEventCreateWithFlags(&c->ev_panel, cudaEventDisableTiming));
   RSD_CUDA(c, cudaEventCreateWithFlags(&c->ev_next, cudaEventDisableTiming));
+  for (int i = 0; i < 4; i++) RSD_CUDA(c, cudaEventCreateWithFlags(&c->ev_la[i], cudaEventDisableTiming));
   return RSD_OK;
 }
 
@@ -110,6 +112,12 @@ extern "C" int rsd_ctx_destroy(rsd_ctx* c) {
     cudaStreamSynchronize(c->side);
     cudaStreamDestroy(c->side);
   }
+  if (c->side2) {
+    cudaStreamSynchronize(c->side2);
+    cudaStreamDestroy(c->side2);
+  }
+  for (int i = 0; i < 4; i++)
+    if (c->ev_la[i]) cudaEventDestroy(c->ev_la[i]);
   if (c->ev_panel) cudaEventDestroy(c->ev_panel);
   if (c->ev_next) cudaEventDestroy(c->ev_next);
   for (auto& kv : c->bufs)
@@ -163,6 +171,13 @@ extern "C" int rsd_ctx_set_wait_limits(rsd_ctx* c, int64_t tc_wait_ns, int64_t t
   if (tc_wait_ns < 0 || tri_spin_polls < 0) return rsd_fail(c, RSD_EARG, "wait limits must be >= 0");
   c->tc_wait_ns = tc_wait_ns;
   c->tri_spin_polls = tri_spin_polls;
+  return RSD_OK;
+}
+
+extern "C" int rsd_ctx_set_factor_schedule(rsd_ctx* c, int32_t schedule) {
+  if (!c) return RSD_EARG;
+  if (schedule != 0 && schedule != 1) return rsd_fail(c, RSD_EARG, "factor schedule: 0 or 1");
+  c->factor_schedule = schedule;
   return RSD_OK;
 }
 

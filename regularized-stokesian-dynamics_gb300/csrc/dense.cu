@@ -1095,11 +1095,24 @@ int trailing_update(rsd_ctx* ctx, int tc, const T* P, int64_t ldp, int kb, int m
 // are factored in NB = 128 steps (diagonal block, row panel by
 // substitution, and an update of the outer panel's remaining rows only),
 // then the trailing matrix takes one K = 512 update per outer panel, so it
-// is read and written a quarter as often as with 128-wide steps.  One outer
-// step of look-ahead: the next outer panel is factored on the side stream
-// once the first 512 rows of the trailing update have landed.
+// is read and written a quarter as often as with 128-wide steps.
+//
+// Schedule 0: the inner steps run in order on the side stream; the next
+// outer panel starts once the first 512 rows of the trailing update have
+// landed (one outer step of look-ahead).
+//
+// Schedule 1 (default): the chain of diagonal blocks carries only what the
+// next diagonal block needs.  On stream a (side): the factor and inverse of
+// block k, then block k+1's column tile of row panel k and the update of the
+// diagonal tile (k+1, k+1); block k+1's factor can start at once.  On stream
+// b (side2), beside that factor: the rest of row panel k and of the
+// in-panel update.  Between outer panels likewise: a updates the next
+// diagonal tile with the K = 512 product, the main stream the rest of the
+// next outer panel's rows and then the remainder of the trailing matrix.
+// Events: A (a's near work done), B (the work the next near step reads),
+// M (the previous remainder, which the next diagonal tile reads).
 constexpr int NBO = 512;
-int potrf_two_level_f32(rsd_ctx* ctx, int n, float* d_A, int64_t lda, int tc, float* W) {
+static int potrf_two_level_sched0(rsd_ctx* ctx, int n, float* d_A, int64_t lda, int tc, float* W) {
   cudaStream_t s = ctx->stream, s2 = ctx->side;
   RSD_CUDA(ctx, cudaEventRecord(ctx->ev_next, s));
   for (int J0 = 0; J0 < n; J0 += NBO) {
@@ -1137,6 +1150,89 @@ int potrf_two_level_f32(rsd_ctx* ctx, int n, float* d_A, int64_t lda, int tc, fl
     }
   }
   return RSD_OK;
+}
+
+static int potrf_two_level_sched1(rsd_ctx* ctx, int n, float* d_A, int64_t lda, int tc, float* W) {
+  cudaStream_t s = ctx->stream, sa = ctx->side, sb = ctx->side2;
+  cudaEvent_t evA = ctx->ev_la[0], evB = ctx->ev_la[1], evM = ctx->ev_la[2], evS = ctx->ev_la[3];
+  int* err = ctx->d_info + 1;
+  // the matrix is ready on the main stream; B and M start out satisfied
+  RSD_CUDA(ctx, cudaEventRecord(evS, s));
+  RSD_CUDA(ctx, cudaStreamWaitEvent(sa, evS, 0));
+  RSD_CUDA(ctx, cudaStreamWaitEvent(sb, evS, 0));
+  RSD_CUDA(ctx, cudaEventRecord(evB, s));
+  RSD_CUDA(ctx, cudaEventRecord(evM, s));
+  for (int J0 = 0; J0 < n; J0 += NBO) {
+    const int JB = n - J0 < NBO ? n - J0 : NBO;
+    for (int j0 = J0; j0 < J0 + JB; j0 += NB) {
+      const int jb = J0 + JB - j0 < NB ? J0 + JB - j0 : NB;
+      float* Ajj = d_A + j0 + (int64_t)j0 * lda;
+      const int rest = n - j0 - jb;
+      float* Apan = d_A + j0 + (int64_t)(j0 + jb) * lda;
+      float* Wb = W + (size_t)(j0 / NB) * NB * NB;
+      potf2_inv_f32<<<1, 256, SMEM_POTF2_INV, sa>>>(Ajj, lda, jb, ctx->d_info, j0, Wb); RSD_LAUNCH_NOTE();
+      if (rest <= 0) continue;
+      RSD_CUDA(ctx, cudaStreamWaitEvent(sa, evB, 0));
+      const int m_in = J0 + JB - (j0 + jb);  // rows of this outer panel below block k
+      if (m_in <= 0) {
+        // last block of the outer panel: its whole row panel on the chain
+        RSD_TRY(rsd_tc_gemm(ctx, tc, jb, rest, jb, 1.0f, Wb, NB, Apan, lda, Apan, lda, 0, 0, 0, err, sa));
+        continue;
+      }
+      const int jn = m_in < NB ? m_in : NB;  // width of block k+1
+      // near: row panel k on block k+1's columns, then the diagonal tile (k+1, k+1)
+      RSD_TRY(rsd_tc_gemm(ctx, tc, jb, jn, jb, 1.0f, Wb, NB, Apan, lda, Apan, lda, 0, 0, 0, err, sa));
+      RSD_TRY(rsd_tc_gemm(ctx, tc, jn, jn, jb, -1.0f, Apan, lda, Apan, lda, Apan + jb, lda, 1, 1, 0, err, sa));
+      RSD_CUDA(ctx, cudaEventRecord(evA, sa));
+      // far, beside block k+1's factor
+      RSD_CUDA(ctx, cudaStreamWaitEvent(sb, evA, 0));
+      if (rest > jn) {
+        float* Afar = Apan + (int64_t)jn * lda;
+        RSD_TRY(rsd_tc_gemm(ctx, tc, jb, rest - jn, jb, 1.0f, Wb, NB, Afar, lda, Afar, lda, 0, 0, 0, err, sb));
+        RSD_TRY(rsd_tc_gemm(ctx, tc, jn, rest - jn, jb, -1.0f, Apan, lda, Afar, lda, Afar + jb, lda, 1, 0, 0, err, sb));
+        if (m_in > jn)
+          RSD_TRY(rsd_tc_gemm(ctx, tc, m_in - jn, rest - jn, jb, -1.0f, Afar, lda, Afar, lda, Afar + jb + jn, lda, 1,
+                              1, 0, err, sb));
+      }
+      RSD_CUDA(ctx, cudaEventRecord(evB, sb));
+    }
+    const int restO = n - J0 - JB;
+    if (restO <= 0) continue;
+    const float* PO = d_A + J0 + (int64_t)(J0 + JB) * lda;
+    float* C = d_A + (J0 + JB) + (int64_t)(J0 + JB) * lda;
+    const int jn = restO < NB ? restO : NB;
+    const int m1 = restO < NBO ? restO : NBO;
+    // near: the next diagonal tile, after the previous remainder reached it
+    RSD_CUDA(ctx, cudaStreamWaitEvent(sa, evM, 0));
+    RSD_TRY(rsd_tc_gemm(ctx, tc, jn, jn, JB, -1.0f, PO, lda, PO, lda, C, lda, 1, 1, 0, err, sa));
+    RSD_CUDA(ctx, cudaEventRecord(evA, sa));
+    // the rest of the next outer panel's rows, then the remainder
+    RSD_CUDA(ctx, cudaStreamWaitEvent(s, evA, 0));
+    if (restO > jn) {
+      const float* POf = PO + (int64_t)jn * lda;
+      float* Cf = C + (int64_t)jn * lda;
+      RSD_TRY(rsd_tc_gemm(ctx, tc, jn, restO - jn, JB, -1.0f, PO, lda, POf, lda, Cf, lda, 1, 0, 0, err, s));
+      if (m1 > jn)
+        RSD_TRY(rsd_tc_gemm(ctx, tc, m1 - jn, restO - jn, JB, -1.0f, POf, lda, POf, lda, Cf + jn, lda, 1, 1, 0, err,
+                            s));
+    }
+    RSD_CUDA(ctx, cudaEventRecord(evB, s));
+    if (restO > NBO)
+      RSD_TRY(rsd_tc_gemm(ctx, tc, restO - NBO, restO - NBO, JB, -1.0f, PO + (int64_t)NBO * lda, lda,
+                          PO + (int64_t)NBO * lda, lda, C + NBO + (int64_t)NBO * lda, lda, 1, 1, 0, err, s));
+    RSD_CUDA(ctx, cudaEventRecord(evM, s));
+  }
+  // join both side streams into the main stream
+  RSD_CUDA(ctx, cudaEventRecord(evA, sa));
+  RSD_CUDA(ctx, cudaStreamWaitEvent(s, evA, 0));
+  RSD_CUDA(ctx, cudaEventRecord(evB, sb));
+  RSD_CUDA(ctx, cudaStreamWaitEvent(s, evB, 0));
+  return RSD_OK;
+}
+
+int potrf_two_level_f32(rsd_ctx* ctx, int n, float* d_A, int64_t lda, int tc, float* W) {
+  return ctx->factor_schedule == 0 ? potrf_two_level_sched0(ctx, n, d_A, lda, tc, W)
+                                   : potrf_two_level_sched1(ctx, n, d_A, lda, tc, W);
 }
 
 // Blocked right-looking upper Cholesky with one step of look-ahead: the

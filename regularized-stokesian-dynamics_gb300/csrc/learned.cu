@@ -200,6 +200,12 @@ __global__ void lp_dinv(int nn, const T* __restrict__ A, int64_t ld, double* __r
 
 // network inputs: node a -> the scaled self block (36); edge e = (a <- b) ->
 // the scaled block (a, b) (36), gap, log(gap + 1e-4) / 4, [b < a], 0
+// Entries of a Jacobi-scaled symmetric positive definite matrix lie in
+// [-1, 1]; an FP32 resistance matrix that has lost definiteness (overlapping
+// spheres) can leave that range, and is clamped back so that the network's
+// inputs stay bounded.
+__device__ __forceinline__ float clamp1(float v) { return fminf(fmaxf(v, -1.f), 1.f); }
+
 template <typename T>
 __global__ void lp_features(int nn, int ne, const T* __restrict__ A, int64_t ld, const double* __restrict__ dinv,
                             const int* __restrict__ src, const int* __restrict__ dst, const float* __restrict__ gap,
@@ -208,7 +214,7 @@ __global__ void lp_features(int nn, int ne, const T* __restrict__ A, int64_t ld,
   if (t < nn * 36) {
     const int a = t / 36, q = t % 36, r = q / 6, c = q % 6;
     const int i = 6 * a + r, j = 6 * a + c;
-    xn[t] = __float2bfloat16((float)(rpp_at(A, ld, nn, i, j) * dinv[i] * dinv[j]));
+    xn[t] = __float2bfloat16(clamp1((float)(rpp_at(A, ld, nn, i, j) * dinv[i] * dinv[j])));
   }
   const int u = t - nn * 36;
   if (u >= 0 && u < ne * NF_EDGE) {
@@ -217,7 +223,7 @@ __global__ void lp_features(int nn, int ne, const T* __restrict__ A, int64_t ld,
     float v;
     if (q < 36) {
       const int i = 6 * a + q / 6, j = 6 * b + q % 6;
-      v = (float)(rpp_at(A, ld, nn, i, j) * dinv[i] * dinv[j]);
+      v = clamp1((float)(rpp_at(A, ld, nn, i, j) * dinv[i] * dinv[j]));
     } else if (q == 36) {
       v = gap[e];
     } else if (q == 37) {

@@ -41,14 +41,17 @@ struct rsd_ctx {
   int correction_method = 0;  // fused step: overlap corrections of the grand mobility (0, 1 or 2)
   long long tc_wait_ns = 0;      // bound of the tensor-core kernels' mbarrier waits (0: 0.5 s)
   long long tri_spin_polls = 0;  // bound of the dataflow sweeps' waits in polls (0: 2^21)
+  int factor_schedule = 1;   // two-level FP32 Cholesky: 1 look-ahead on the diagonal chain, 0 in-order panels
   int refine_gmres = 0;      // mixed form: flexible GMRES (1) or the stationary iteration (0) as refinement
   int gmres_restart = 30;    // GMRES restart length
   int rpp_mode = 0;          // plain FP64 step: RPP by Cholesky (0) or PCG with this preconditioner
   void* rpp_net = nullptr;   // the network of the learned preconditioner
   double rpp_tol = 0.0;      // PCG relative residual (0: 1e-12)
   int rpp_maxit = 0;         // PCG iteration cap (0: 1000)
-  cudaStream_t side = nullptr;  // higher-priority stream for look-ahead panels
+  cudaStream_t side = nullptr;   // higher-priority stream for look-ahead panels
+  cudaStream_t side2 = nullptr;  // second high-priority stream: the wide panel work beside the diagonal chain
   cudaEvent_t ev_panel = nullptr, ev_next = nullptr;
+  cudaEvent_t ev_la[4] = {};     // look-ahead events of the two-level Cholesky
   int* d_info = nullptr;  // device-side status words
   int* h_info = nullptr;  // pinned mirror
 };
@@ -80,7 +83,7 @@ int rsd_cuda_check(rsd_ctx* ctx, cudaError_t e, const char* what);
 // allocation failure.
 void* rsd_scratch(rsd_ctx* ctx, const char* name, size_t bytes);
 int rsd_set_device(rsd_ctx* ctx);
-// creates ctx->side, ev_panel and ev_next on first use
+// creates ctx->side, side2, ev_panel, ev_next and ev_la on first use
 int rsd_side_stream(rsd_ctx* ctx);
 
 // ------------------------------------------------------------ lattice

@@ -105,6 +105,29 @@ def test_potri_f32(rsd, ctx, n, prec):
     assert res <= INV_TOL[prec], res
 
 
+@pytest.mark.parametrize("n", [640, 1001, 1100, 1664, 2560])
+@pytest.mark.parametrize("prec", [1, 3])
+def test_potrf_f32_schedules_agree(rsd, ctx, n, prec):
+    """The look-ahead schedule of the two-level factorisation (the default)
+    and the in-order one give the same factor: every output tile is the same
+    product over the same K range, only split into other launches."""
+    A = spd(n, 20261206 + n)
+    out = {}
+    for sched in (0, 1):
+        dA = colmajor(A)
+        ctx.set_factor_schedule(sched)
+        try:
+            assert rsd.potrf_f32_dev(ctx, dA, prec) == 0
+        finally:
+            ctx.set_factor_schedule(1)
+        out[sched] = np.triu(dA.cpu().numpy().astype(np.float64))
+        res = np.linalg.norm(out[sched].T @ out[sched] - A) / np.linalg.norm(A)
+        assert res <= FACTOR_TOL[prec], (sched, res)
+    d = np.abs(out[0] - out[1]).max() / np.abs(out[0]).max()
+    print("schedules 0 and 1: max difference %.3e (identical: %s)" % (d, d == 0.0))
+    assert d <= 1e-5
+
+
 def test_tensor_cores_off_matches_simt(rsd, ctx):
     """With the context switch off, prec 1 takes the SIMT path."""
     A = spd(640, 11)
