@@ -1,6 +1,7 @@
 // Internal declarations shared by the CUDA translation units.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <cstdio>
@@ -83,6 +84,15 @@ int rsd_cuda_check(rsd_ctx* ctx, cudaError_t e, const char* what);
 // allocation failure.
 void* rsd_scratch(rsd_ctx* ctx, const char* name, size_t bytes);
 int rsd_set_device(rsd_ctx* ctx);
+// Scoped NVTX range around a phase of the step (a no-op unless a profiler
+// is attached), so that a profiler can select one phase's launches.
+struct rsd_range {
+  explicit rsd_range(const char* name) { nvtxRangePushA(name); }
+  ~rsd_range() { nvtxRangePop(); }
+  rsd_range(const rsd_range&) = delete;
+  rsd_range& operator=(const rsd_range&) = delete;
+};
+
 // creates ctx->side, side2, ev_panel, ev_next and ev_la on first use
 int rsd_side_stream(rsd_ctx* ctx);
 

@@ -235,13 +235,16 @@ static int step_impl(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_step_params*
   else
     RSD_CUDA(ctx, cudaMemsetAsync(Fe, 0, sizeof(double) * P, s));
   cudaEventRecord(ctx->ev[0], s);
-  // grand mobility
-  RSD_TRY(rsd_ewald_assemble(ctx, nn, d_conf, d_radii, &lat, p->mu_f, p->precision, M, n));
-  if (ctx->correction_method) {  // overlap corrections (per_GRPY_YZD.f90:98-116)
-    int nov = 0;
-    RSD_TRY(rsd_count_overlaps(ctx, nn, d_conf, d_radii, &lat, &nov));
-    RSD_TRY(rsd_overlap_correct(ctx, ctx->correction_method, p->precision, nn, d_conf, d_radii, &lat, p->mu_f, nov,
-                                M, n));
+  {
+    // grand mobility
+    rsd_range r("rsd_assembly");
+    RSD_TRY(rsd_ewald_assemble(ctx, nn, d_conf, d_radii, &lat, p->mu_f, p->precision, M, n));
+    if (ctx->correction_method) {  // overlap corrections (per_GRPY_YZD.f90:98-116)
+      int nov = 0;
+      RSD_TRY(rsd_count_overlaps(ctx, nn, d_conf, d_radii, &lat, &nov));
+      RSD_TRY(rsd_overlap_correct(ctx, ctx->correction_method, p->precision, nn, d_conf, d_radii, &lat, p->mu_f, nov,
+                                  M, n));
+    }
   }
   cudaEventRecord(ctx->ev[1], s);
   // averageU on APP before it is overwritten
@@ -315,8 +318,11 @@ static int step_impl(rsd_ctx* ctx, const rsd_lubtab* tab, const rsd_step_params*
     RSD_CUDA(ctx, cudaGetLastError());
   } else {
     cudaEventRecord(ctx->ev[2], s);
-    RSD_TRY(rsd_mixed_solve(ctx, nn, M, n, d_conf, d_radii, &lat, tab, p, ein, d_Fe ? Fe : nullptr, Upar, S, &loc,
-                            (float*)rpp_out, rpp_ld));
+    {
+      rsd_range r("rsd_solve");
+      RSD_TRY(rsd_mixed_solve(ctx, nn, M, n, d_conf, d_radii, &lat, tab, p, ein, d_Fe ? Fe : nullptr, Upar, S, &loc,
+                              (float*)rpp_out, rpp_ld));
+    }
     if (rpp_out) {
       RSD_CUDA(ctx, cudaStreamSynchronize(s));
       if (info) *info = loc;
