@@ -419,11 +419,17 @@ def long_run(args):
     ctx.set_tensor_cores(args.tensor_cores)
     tab = rsd.LubTab(rsd.lubdat_dir())
     series = []
+    fp64_steps = []
+    mixed = rsd.driver_step(ctx, tab, rsd.PREC_MIXED, fp64_fallback=True,
+                            on_fallback=lambda T, why: fp64_steps.append((T, why)))
 
     def step(conf, r, T, dt_, LB, gamma, mu_f, ews):
-        o = rsd.STEPPER_Stokesian(ctx, tab, conf, r, T, dt_, LB, gamma, mu_f, ews, precision=rsd.PREC_MIXED)
+        n64 = len(fp64_steps)
+        o = mixed(conf, r, T, dt_, LB, gamma, mu_f, ews)
         i = o["info"]
-        series.append((T, float(o["yeta_mu"][0]), i.NR, i.NI, i.iterations, i.residual))
+        # 0: mixed; 1: mixed, finished by flexible GMRES; 2: taken in FP64
+        how = 2 if len(fp64_steps) > n64 else int(i.fallback)
+        series.append((T, float(o["yeta_mu"][0]), i.NR, i.NI, i.iterations, i.residual, how))
         return o
 
     t0 = time.perf_counter()
@@ -435,9 +441,10 @@ def long_run(args):
         res = {"steps": len(series)}
     wall = time.perf_counter() - t0
     with open(os.path.join(out, "eta_r_series.csv"), "w") as fp:
-        fp.write("# strain, relative viscosity, NR, NI, refinement iterations, residual\n")
-        for T, y, nr, ni, it, rr in series:
-            fp.write("%.6f,%.12e,%d,%d,%d,%.3e\n" % (T, y, nr, ni, it, rr))
+        fp.write("# strain, relative viscosity, NR, NI, refinement iterations, residual, "
+                 "solve (0 mixed, 1 mixed finished by flexible GMRES, 2 FP64)\n")
+        for T, y, nr, ni, it, rr, how in series:
+            fp.write("%.6f,%.12e,%d,%d,%d,%.3e,%d\n" % (T, y, nr, ni, it, rr, how))
     # plain FP64 beside the first steps, from the same start
     mu = rsd.mu_f_dimensionless(1.0)
     conf = pos.copy()
@@ -465,6 +472,8 @@ def long_run(args):
             "eta_r_per_strain_unit": per_strain,
             "refinement_iterations": {"mean": float(np.mean(its)) if its else None,
                                       "max": int(np.max(its)) if its else None},
+            "gmres_finished_steps": int(sum(1 for s_ in series if s_[6] == 1)),
+            "fp64_steps": len(fp64_steps), "fp64_steps_first": [[float(t), w] for t, w in fp64_steps[:10]],
             "NR_range": [int(min(s_[2] for s_ in series)), int(max(s_[2] for s_ in series))] if series else None,
             "plain_fp64_eta_r": plain, "mixed_eta_r_first": [s_[1] for s_ in series[:len(plain)]],
             "eta_r_rel_diff_first_steps": [abs(a - b) / abs(b) for a, b in zip([s_[1] for s_ in series], plain)],

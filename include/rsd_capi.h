@@ -36,6 +36,8 @@ extern "C" {
 #define RSD_EIO (-6)      /* lubrication table files unreadable */
 #define RSD_EUNSUP (-7)   /* option of the reference not built here */
 #define RSD_ELIMIT (-8)   /* request beyond the static scratch of the allocation-free entry point */
+#define RSD_ENOCONV (-9)  /* mixed form: the FP64 refinement (stationary, then flexible GMRES) did not reach
+                             100 x its tolerance; the outputs hold the last iterate */
 
 typedef struct rsd_ctx rsd_ctx;
 typedef struct rsd_lubtab rsd_lubtab;
@@ -298,6 +300,8 @@ typedef struct rsd_step_info {
   double LV;          /* cell volume */
   int32_t rpp_iterations; /* FP64 form with a PCG RPP solver: its iterations
                              (negative: not converged, factorised instead) */
+  int32_t fallback;   /* mixed: 1 when the stationary refinement diverged or
+                         stalled and flexible GMRES finished the solve */
 } rsd_step_info;
 
 /* One STEPPER_Stokesian step (src/stepper.f90:33-156) on the periodic FTS

@@ -21,6 +21,7 @@ LIBPATH = os.path.join(HERE, "librsd_gb300.so")
 
 RSD_OK, RSD_EARG, RSD_ECUDA, RSD_ENAN, RSD_ETIMEOUT, RSD_ENOMEM, RSD_EIO, RSD_EUNSUP = 0, -1, -2, -3, -4, -5, -6, -7
 RSD_ELIMIT = -8
+RSD_ENOCONV = -9
 PREC_FP64, PREC_MIXED = 0, 1
 PC_NONE, PC_JACOBI, PC_BLOCK_JACOBI, PC_FSAI, PC_LEARNED = 0, 1, 2, 3, 4
 PAI = 3.141592653589793238462643383279502884
@@ -52,7 +53,8 @@ class StepParams(ctypes.Structure):
 class StepInfo(ctypes.Structure):
     _fields_ = [("info", ctypes.c_int32), ("n_contact", ctypes.c_int32), ("NR", ctypes.c_int32),
                 ("NI", ctypes.c_int32), ("iterations", ctypes.c_int32), ("residual", ctypes.c_double),
-                ("phi", ctypes.c_double), ("LV", ctypes.c_double), ("rpp_iterations", ctypes.c_int32)]
+                ("phi", ctypes.c_double), ("LV", ctypes.c_double), ("rpp_iterations", ctypes.c_int32),
+                ("fallback", ctypes.c_int32)]
 
 
 def _sig(name, res, args):
@@ -688,8 +690,25 @@ from . import driver_files  # noqa: E402,F401
 from . import ensemble  # noqa: E402,F401
 
 
-def driver_step(ctx: Context, tab: LubTab, precision=PREC_MIXED):
-    """The fused step as the step callable of driver.run."""
+def driver_step(ctx: Context, tab: LubTab, precision=PREC_MIXED, fp64_fallback=False, on_fallback=None, **kw):
+    """The fused step as the step callable of driver.run.  fp64_fallback:
+    a mixed step whose refinement does not converge (RSD_ENOCONV) or whose
+    FP32 factor is not positive definite (a positive INFO) is taken again in
+    the plain FP64 form; on_fallback(T, reason) is told of each such step.
+    kw: further STEPPER_Stokesian arguments (tol, max_iter, nb, use_lub)."""
     def step(conf, radii, T, dt, LB, gamma, mu_f, ews_err):
-        return STEPPER_Stokesian(ctx, tab, conf, radii, T, dt, LB, gamma, mu_f, ews_err, precision=precision)
+        try:
+            out = STEPPER_Stokesian(ctx, tab, conf, radii, T, dt, LB, gamma, mu_f, ews_err, precision=precision,
+                                    **kw)
+            if out["rc"] == 0 or not fp64_fallback or precision == PREC_FP64:
+                return out
+            reason = "INFO %d" % out["rc"]
+        except RSDError as e:
+            if not (fp64_fallback and precision != PREC_FP64 and e.code == RSD_ENOCONV):
+                raise
+            reason = str(e)
+        if on_fallback is not None:
+            on_fallback(T, reason)
+        kw64 = {k: v for k, v in kw.items() if k in ("nb", "use_lub")}
+        return STEPPER_Stokesian(ctx, tab, conf, radii, T, dt, LB, gamma, mu_f, ews_err, precision=PREC_FP64, **kw64)
     return step

@@ -19,6 +19,7 @@
 // Iterates until ||r|| <= tol ||b|| per right-hand side.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -571,10 +572,11 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   int* tri_err = rsd_uhat_error_flag(ctx);
   if (!tri_err) return RSD_ENOMEM;
   RSD_CUDA(ctx, cudaMemsetAsync(tri_err, 0, sizeof(int), s));
-  if (ctx->refine_gmres) {
-    cudaEventRecord(ctx->ev[7], s);
-    // right-preconditioned flexible GMRES(m) per right-hand side, FP64
-    // residuals; the preconditioner is the stationary iteration's correction
+  // Right-preconditioned flexible GMRES(m) per right-hand side, FP64
+  // residuals; the preconditioner is the stationary iteration's correction.
+  // Starts from zero; gm_maxit bounds the iterations over all right-hand
+  // sides; returns the iterations and the worst relative residual.
+  auto run_gmres = [&](int gm_maxit, int* its_out, double* res_out) -> int {
     const int m = ctx->gmres_restart > 0 ? ctx->gmres_restart : 30;
     const int64_t len = n + P;
     double* KV = (double*)rsd_scratch(ctx, "gm_basis", sizeof(double) * (size_t)(2 * m + 1) * len + 8 * 64);
@@ -681,12 +683,12 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
         const double beta = sqrt(beta2);
         rel = beta / bnorm[c];
         if (!std::isfinite(rel)) return rsd_fail(ctx, RSD_ENAN, "refinement residual is not finite");
-        if (rel <= tol || total_it >= maxit) break;
+        if (rel <= tol || total_it >= gm_maxit) break;
         gm_scale<<<nblk(len), 256, 0, s>>>(len, Vb, dn, Vb); RSD_LAUNCH_NOTE();
         std::fill(g.begin(), g.end(), 0.0);
         g[0] = beta;
         int j = 0;
-        for (; j < m && total_it < maxit; j++) {
+        for (; j < m && total_it < gm_maxit; j++) {
           double* vj = Vb + (size_t)j * len;
           double* zj = Zb + (size_t)j * len;
           double* vn = Vb + (size_t)(j + 1) * len;
@@ -741,17 +743,29 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
       }
       worst = fmax(worst, rel);
     }
+    *its_out = total_it;
+    *res_out = worst;
+    return RSD_OK;
+  };
+  // A solve is accepted within the stagnation band of the tolerance.
+  const double accept = 100.0 * tol;
+  cudaEventRecord(ctx->ev[7], s);
+  if (ctx->refine_gmres) {
+    int its = 0;
+    double res = 0.0;
+    RSD_TRY(run_gmres(maxit, &its, &res));
     outputs<<<nblk(P), 256, 0, s>>>(P, Q, nr - 1, f, Lw, U, U_par, S_hyd); RSD_LAUNCH_NOTE();
     RSD_CUDA(ctx, cudaGetLastError());
-    info->iterations = total_it;
-    info->residual = worst;
+    info->iterations = its;
+    info->residual = res;
+    if (!(res <= accept))
+      return rsd_fail(ctx, RSD_ENOCONV, "refinement did not converge: residual %.3e after %d iterations", res, its);
     return RSD_OK;
   }
   int h_tri_err = 0;
-  cudaEventRecord(ctx->ev[7], s);
   RSD_CUDA(ctx, cudaMemsetAsync(f, 0, sizeof(double) * nr * n, s));
   RSD_CUDA(ctx, cudaMemsetAsync(U, 0, sizeof(double) * nr * P, s));
-  double worst = 0.0;
+  double worst = 0.0, best_res = INFINITY;
   int it = 0;
   std::vector<double> hn(2 * nr), hist;
   for (;; it++) {
@@ -792,10 +806,14 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
     worst = 0.0;
     for (int c = 0; c < nr; c++) {
       const double rr = sqrt(hn[2 * c]) / (sqrt(hn[2 * c + 1]) > 0 ? sqrt(hn[2 * c + 1]) : 1.0);
-      if (!std::isfinite(rr)) return rsd_fail(ctx, RSD_ENAN, "refinement residual is not finite");
-      worst = fmax(worst, rr);
+      worst = std::isfinite(rr) ? fmax(worst, rr) : INFINITY;
     }
     if (worst <= tol || it >= maxit) break;
+    // Divergence: FP32 factors too far from the FP64 system (a pair so close
+    // that cond(RPP) times the factors' precision exceeds one) make the
+    // stationary iteration grow; the flexible GMRES below takes over.
+    if (!std::isfinite(worst) || (it >= 2 && worst > 1e3 * best_res)) break;
+    best_res = fmin(best_res, worst);
     // Stagnation: the FP64 residual of a stiff system (many near-contact
     // pairs: forces ~1/gap times the velocities) has a floor of about the
     // residual arithmetic's rounding times |M||f| / |b|, which can sit just
@@ -827,9 +845,22 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
     from32_perm<<<nblk(n * nr), 256, 0, s>>>(P, Q, nr, t32, y, 1); RSD_LAUNCH_NOTE();
     update_fu<<<nblk(n * nr), 256, 0, s>>>(P, n, nr, y, u32, f, U); RSD_LAUNCH_NOTE();
   }
+  if (!(worst <= accept)) {
+    // diverged or stalled above the band: flexible GMRES from zero over the
+    // same corrections, which converges where a few modes of the FP32
+    // factors are poor
+    int its = 0;
+    double res = 0.0;
+    RSD_TRY(run_gmres(std::max(3 * maxit, 100), &its, &res));
+    it += its;
+    worst = res;
+    info->fallback = 1;
+  }
   outputs<<<nblk(P), 256, 0, s>>>(P, Q, nr - 1, f, Lw, U, U_par, S_hyd); RSD_LAUNCH_NOTE();
   RSD_CUDA(ctx, cudaGetLastError());
   info->iterations = it;
   info->residual = worst;
+  if (!(worst <= accept))
+    return rsd_fail(ctx, RSD_ENOCONV, "refinement did not converge: residual %.3e after %d iterations", worst, it);
   return RSD_OK;
 }

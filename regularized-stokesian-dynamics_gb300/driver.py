@@ -75,6 +75,9 @@ def run(control_path, init_path, step, vtf_path, yeta_path, max_steps=None, hot_
             if k % c["K_WRITE"] == 0:
                 files.write_vtf_frame(vtf, T / lam_time, conf, radii, U_pos)
             out = step(conf, radii, T, dt, LB, gamma, mu, c["LINERR"])
+            if out.get("rc", 0) > 0:  # CHOLESKY's INFO > 0 stops the reference (stepper.f90:375-393)
+                raise RuntimeError("step %d (T = %g): the grand resistance is not positive definite (INFO %d)"
+                                   % (k, T / lam_time, out["rc"]))
             conf, U_pos = np.asarray(out["conf"], dtype=np.float64).reshape(N, 3), np.asarray(out["U_pos"])
             if k % c["K_WRITE"] == 0:
                 yeta.write(files.yeta_record(T / lam_time, out["yeta_mu"], LB[0], frequency, gamma, 0.0) + "\n")

@@ -161,3 +161,30 @@ def test_each_unsupported_setting_is_named(drv, tmp_path, key, value):
     with pytest.raises(ValueError) as e:
         driver.check_supported(c, d)
     assert key in str(e.value)
+
+
+def test_a_failed_factorisation_stops_the_loop(drv, tmp_path):
+    """A step that reports a positive INFO (the grand resistance not positive
+    definite) stops the loop, as CHOLESKY's INFO stops the reference; the
+    steps before it are on file."""
+    driver, files = drv
+    control = control_for_periodic_fts(tmp_path)
+    pos, radii, L = configs().packing(8, 0.2, 0.05, seed=20261101)
+    init = str(tmp_path / "initial_config.dat")
+    files.write_initial_config(init, pos, radii, [L, L, L])
+    tab = o.LubTab(LUBDAT)
+    calls = []
+
+    def step(conf, r, T, dt, LB, gamma, mu_f, ews):
+        out = o.stepper_stokesian(conf, r, LB, T, dt, gamma, mu_f, ews, tab)
+        calls.append(T)
+        out = dict(out, U_pos=out["U_pos"], yeta_mu=out["yeta_mu"])
+        if len(calls) == 3:  # the third step's factorisation fails
+            out["rc"] = 37
+        return out
+
+    vtf, yeta = str(tmp_path / "output.VTF"), str(tmp_path / "yeta_mu.txt")
+    with pytest.raises(RuntimeError, match="INFO 37"):
+        driver.run(control, init, step, vtf, yeta)
+    assert len(calls) == 3
+    assert len([line for line in open(yeta) if line.strip()]) == 2
