@@ -80,6 +80,9 @@ def parse():
     ap.add_argument("--workers", type=int, default=16, help="(ensemble) concurrent contexts")
     ap.add_argument("--long-steps", type=int, default=10000)
     ap.add_argument("--plain-steps", type=int, default=5, help="(long) plain FP64 steps beside the mixed run")
+    ap.add_argument("--contact", type=float, default=100.0,
+                    help="(long) host contact repulsion F0 in units of 6 pi mu a^2 gammadot (0: none)")
+    ap.add_argument("--contact-range", type=float, default=0.01, help="(long) its decay length, in radii")
     ap.add_argument("--out-dir", default=None, help="(long) where yeta_mu.txt and the viscosity series go")
     return ap.parse_args()
 
@@ -423,28 +426,32 @@ def long_run(args):
     mixed = rsd.driver_step(ctx, tab, rsd.PREC_MIXED, fp64_fallback=True,
                             on_fallback=lambda T, why: fp64_steps.append((T, why)))
 
-    def step(conf, r, T, dt_, LB, gamma, mu_f, ews):
+    soft = rsd.contact.SoftContact(N, L, f0=args.contact, delta=args.contact_range) if args.contact > 0 else None
+
+    def step(conf, r, T, dt_, LB, gamma, mu_f, ews, Fe=None):
         n64 = len(fp64_steps)
-        o = mixed(conf, r, T, dt_, LB, gamma, mu_f, ews)
+        o = mixed(conf, r, T, dt_, LB, gamma, mu_f, ews, Fe=Fe)
         i = o["info"]
         # 0: mixed; 1: mixed, finished by flexible GMRES; 2: taken in FP64
         how = 2 if len(fp64_steps) > n64 else int(i.fallback)
-        series.append((T, float(o["yeta_mu"][0]), i.NR, i.NI, i.iterations, i.residual, how))
+        gap = soft.min_gap if soft is not None else float("nan")
+        series.append((T, float(o["yeta_mu"][0]), i.NR, i.NI, i.iterations, i.residual, how, gap))
         return o
 
     t0 = time.perf_counter()
     err = None
     try:
-        res = rsd.driver.run(control, init, step, os.path.join(work, "output.VTF"), os.path.join(out, "yeta_mu.txt"))
+        res = rsd.driver.run(control, init, step, os.path.join(work, "output.VTF"), os.path.join(out, "yeta_mu.txt"),
+                             forces=soft.forces if soft is not None else None)
     except Exception as e:  # report how far the run got
         err = "%s: %s" % (type(e).__name__, e)
         res = {"steps": len(series)}
     wall = time.perf_counter() - t0
     with open(os.path.join(out, "eta_r_series.csv"), "w") as fp:
         fp.write("# strain, relative viscosity, NR, NI, refinement iterations, residual, "
-                 "solve (0 mixed, 1 mixed finished by flexible GMRES, 2 FP64)\n")
-        for T, y, nr, ni, it, rr, how in series:
-            fp.write("%.6f,%.12e,%d,%d,%d,%.3e,%d\n" % (T, y, nr, ni, it, rr, how))
+                 "solve (0 mixed, 1 mixed finished by flexible GMRES, 2 FP64), smallest surface gap\n")
+        for T, y, nr, ni, it, rr, how, gap in series:
+            fp.write("%.6f,%.12e,%d,%d,%d,%.3e,%d,%.4e\n" % (T, y, nr, ni, it, rr, how, gap))
     # plain FP64 beside the first steps, from the same start
     mu = rsd.mu_f_dimensionless(1.0)
     conf = pos.copy()
@@ -452,8 +459,11 @@ def long_run(args):
     d = rsd.driver_files.read_initial_config(init)
     conf = np.array(d["conf"])
     T = 0.0
+    soft64 = rsd.contact.SoftContact(N, L, f0=args.contact, delta=args.contact_range) if args.contact > 0 else None
     for k in range(min(args.plain_steps, len(series))):
-        o = rsd.STEPPER_Stokesian(ctx, tab, conf, radii, T, dt, [L, L, L], 1.0, mu, 1e-10, precision=rsd.PREC_FP64)
+        Fe = soft64.forces(conf, T) if soft64 is not None else None
+        o = rsd.STEPPER_Stokesian(ctx, tab, conf, radii, T, dt, [L, L, L], 1.0, mu, 1e-10, Fe=Fe,
+                                  precision=rsd.PREC_FP64)
         plain.append(float(o["yeta_mu"][0]))
         conf, T = o["conf"], T + dt
     per_strain = []
@@ -473,6 +483,9 @@ def long_run(args):
             "refinement_iterations": {"mean": float(np.mean(its)) if its else None,
                                       "max": int(np.max(its)) if its else None},
             "gmres_finished_steps": int(sum(1 for s_ in series if s_[6] == 1)),
+            "contact": ({"F0_over_6pi_mu_a2_gammadot": args.contact, "range_over_a": args.contact_range,
+                         "smallest_gap": float(np.nanmin([s_[7] for s_ in series])) if series else None}
+                        if soft is not None else None),
             "fp64_steps": len(fp64_steps), "fp64_steps_first": [[float(t), w] for t, w in fp64_steps[:10]],
             "NR_range": [int(min(s_[2] for s_ in series)), int(max(s_[2] for s_ in series))] if series else None,
             "plain_fp64_eta_r": plain, "mixed_eta_r_first": [s_[1] for s_ in series[:len(plain)]],

@@ -688,6 +688,7 @@ from . import configs  # noqa: E402,F401
 from . import driver  # noqa: E402,F401
 from . import driver_files  # noqa: E402,F401
 from . import ensemble  # noqa: E402,F401
+from . import contact  # noqa: E402,F401
 
 
 def driver_step(ctx: Context, tab: LubTab, precision=PREC_MIXED, fp64_fallback=False, on_fallback=None, **kw):
@@ -696,10 +697,10 @@ def driver_step(ctx: Context, tab: LubTab, precision=PREC_MIXED, fp64_fallback=F
     FP32 factor is not positive definite (a positive INFO) is taken again in
     the plain FP64 form; on_fallback(T, reason) is told of each such step.
     kw: further STEPPER_Stokesian arguments (tol, max_iter, nb, use_lub)."""
-    def step(conf, radii, T, dt, LB, gamma, mu_f, ews_err):
+    def step(conf, radii, T, dt, LB, gamma, mu_f, ews_err, Fe=None):
         try:
-            out = STEPPER_Stokesian(ctx, tab, conf, radii, T, dt, LB, gamma, mu_f, ews_err, precision=precision,
-                                    **kw)
+            out = STEPPER_Stokesian(ctx, tab, conf, radii, T, dt, LB, gamma, mu_f, ews_err, Fe=Fe,
+                                    precision=precision, **kw)
             if out["rc"] == 0 or not fp64_fallback or precision == PREC_FP64:
                 return out
             reason = "INFO %d" % out["rc"]
@@ -710,5 +711,6 @@ def driver_step(ctx: Context, tab: LubTab, precision=PREC_MIXED, fp64_fallback=F
         if on_fallback is not None:
             on_fallback(T, reason)
         kw64 = {k: v for k, v in kw.items() if k in ("nb", "use_lub")}
-        return STEPPER_Stokesian(ctx, tab, conf, radii, T, dt, LB, gamma, mu_f, ews_err, precision=PREC_FP64, **kw64)
+        return STEPPER_Stokesian(ctx, tab, conf, radii, T, dt, LB, gamma, mu_f, ews_err, Fe=Fe, precision=PREC_FP64,
+                                 **kw64)
     return step

@@ -44,11 +44,15 @@ def check_supported(control, init):
         raise ValueError("not covered by this driver: " + ", ".join(bad))
 
 
-def run(control_path, init_path, step, vtf_path, yeta_path, max_steps=None, hot_start_time_scaled=False):
+def run(control_path, init_path, step, vtf_path, yeta_path, max_steps=None, hot_start_time_scaled=False,
+        forces=None):
     """Runs the loop; returns the last configuration, U_pos, T (in the
     file's time unit) and the number of steps.  hot_start_time_scaled: take
     initial_config.dat's time as written in the file's unit (T / lambda_time)
-    and scale it back; the default reads it unscaled, as the reference does."""
+    and scale it back; the default reads it unscaled, as the reference does.
+    forces: optional host callable forces(conf, T) -> Fe (6N) of external
+    forces for each step (the place of main.f90's DEM contact forces), passed
+    to step as the keyword Fe."""
     c = files.read_control(control_path)
     d = files.read_initial_config(init_path)
     check_supported(c, d)
@@ -74,7 +78,10 @@ def run(control_path, init_path, step, vtf_path, yeta_path, max_steps=None, hot_
         while True:
             if k % c["K_WRITE"] == 0:
                 files.write_vtf_frame(vtf, T / lam_time, conf, radii, U_pos)
-            out = step(conf, radii, T, dt, LB, gamma, mu, c["LINERR"])
+            if forces is None:
+                out = step(conf, radii, T, dt, LB, gamma, mu, c["LINERR"])
+            else:
+                out = step(conf, radii, T, dt, LB, gamma, mu, c["LINERR"], Fe=forces(conf, T))
             if out.get("rc", 0) > 0:  # CHOLESKY's INFO > 0 stops the reference (stepper.f90:375-393)
                 raise RuntimeError("step %d (T = %g): the grand resistance is not positive definite (INFO %d)"
                                    % (k, T / lam_time, out["rc"]))

@@ -188,3 +188,27 @@ def test_a_failed_factorisation_stops_the_loop(drv, tmp_path):
         driver.run(control, init, step, vtf, yeta)
     assert len(calls) == 3
     assert len([line for line in open(yeta) if line.strip()]) == 2
+
+
+def test_external_forces_reach_the_step(drv, tmp_path):
+    """forces(conf, T) is called before every step and its Fe reaches the
+    step (the place of main.f90's DEM contact forces)."""
+    driver, files = drv
+    control = control_for_periodic_fts(tmp_path)
+    pos, radii, L = configs().packing(8, 0.2, 0.05, seed=20261102)
+    init = str(tmp_path / "initial_config.dat")
+    files.write_initial_config(init, pos, radii, [L, L, L])
+    tab = o.LubTab(LUBDAT)
+    seen = []
+
+    def forces(conf, T):
+        Fe = np.zeros(6 * 8)
+        Fe[0] = 1.0 + T
+        return Fe
+
+    def step(conf, r, T, dt, LB, gamma, mu_f, ews, Fe=None):
+        seen.append((T, Fe[0]))
+        return o.stepper_stokesian(conf, r, LB, T, dt, gamma, mu_f, ews, tab, Fe=Fe)
+
+    driver.run(control, init, step, str(tmp_path / "o.VTF"), str(tmp_path / "y.txt"), forces=forces)
+    assert [f for _, f in seen] == pytest.approx([1.0 + t for t, _ in seen]) and len(seen) == 4
