@@ -50,7 +50,7 @@ SEED_BASE = 20260000
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--no-peaks", action="store_true")
     ap.add_argument("--tensor-cores", type=int, default=1, choices=[0, 1, 3],
                     help="FP32 factorisations of the mixed form: 1 TF32/3xTF32 per factor, 3 all 3xTF32, 0 SIMT")
+    ap.add_argument("--real-passes", type=int, default=0, choices=[0, 1, 2, 3, 4],
+                    help="mixed real-space sum: passes over the near images (0: the library's default)")
     ap.add_argument("--factor-schedule", type=int, default=1, choices=[0, 1],
                     help="mixed form's FP32 Cholesky: 1 look-ahead on the diagonal chain, 0 in-order panels")
     ap.add_argument("--validate-cpu-model", action="store_true",
@@ -80,6 +82,7 @@ def parse():
     ap.add_argument("--workers", type=int, default=16, help="(ensemble) concurrent contexts")
     ap.add_argument("--long-steps", type=int, default=10000)
     ap.add_argument("--plain-steps", type=int, default=5, help="(long) plain FP64 steps beside the mixed run")
+    ap.add_argument("--long-seconds", type=float, default=0.0, help="(long) wall-time budget; 0: none")
     ap.add_argument("--contact", type=float, default=100.0,
                     help="(long) host contact repulsion F0 in units of 6 pi mu a^2 gammadot (0: none)")
     ap.add_argument("--contact-range", type=float, default=0.01, help="(long) its decay length, in radii")
@@ -428,7 +431,12 @@ def long_run(args):
 
     soft = rsd.contact.SoftContact(N, L, f0=args.contact, delta=args.contact_range) if args.contact > 0 else None
 
+    class _Stop(Exception):
+        pass
+
     def step(conf, r, T, dt_, LB, gamma, mu_f, ews, Fe=None):
+        if args.long_seconds > 0 and time.perf_counter() - t0 > args.long_seconds:
+            raise _Stop("wall-time budget of %.0f s reached" % args.long_seconds)
         n64 = len(fp64_steps)
         o = mixed(conf, r, T, dt_, LB, gamma, mu_f, ews, Fe=Fe)
         i = o["info"]
@@ -438,14 +446,22 @@ def long_run(args):
         series.append((T, float(o["yeta_mu"][0]), i.NR, i.NI, i.iterations, i.residual, how, gap))
         return o
 
+    import signal
+
+    def _on_term(signum, frame):  # a time limit ends the run: report how far it got
+        raise _Stop("stopped by signal %d" % signum)
+
+    old_term = signal.signal(signal.SIGTERM, _on_term)
     t0 = time.perf_counter()
     err = None
     try:
         res = rsd.driver.run(control, init, step, os.path.join(work, "output.VTF"), os.path.join(out, "yeta_mu.txt"),
-                             forces=soft.forces if soft is not None else None)
-    except Exception as e:  # report how far the run got
+                             forces=soft.forces if soft is not None else None,
+                             max_steps=args.long_steps)
+    except (Exception, _Stop) as e:  # report how far the run got
         err = "%s: %s" % (type(e).__name__, e)
         res = {"steps": len(series)}
+    signal.signal(signal.SIGTERM, old_term)
     wall = time.perf_counter() - t0
     with open(os.path.join(out, "eta_r_series.csv"), "w") as fp:
         fp.write("# strain, relative viscosity, NR, NI, refinement iterations, residual, "
@@ -632,6 +648,8 @@ def main():
     ctx = rsd.Context(local)
     ctx.set_tensor_cores(args.tensor_cores)
     ctx.set_factor_schedule(args.factor_schedule)
+    if args.real_passes:
+        ctx.set_mixed_real_passes(args.real_passes)
     ctx.set_refinement(1 if args.refinement == "gmres" else 0)
     tab = rsd.LubTab(rsd.lubdat_dir())
     radii_t = torch.tensor(radii, dtype=torch.float64, device=dev)

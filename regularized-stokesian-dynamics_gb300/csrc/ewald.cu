@@ -270,46 +270,59 @@ __device__ inline void store_pair_t(const S& sk, int N, int a, int b, const V* v
 // each pair block are written (121 of 242: the pair's rows of the grand
 // matrix, all coalesced along a); the consumers read the other half at the
 // mirrored position, or mirror_planes fills it by symmetry.  Values as in
-// store_pair_t, in four groups of 15 that can be stored separately:
-// group 0 the TT, RR and TR values v[0..14], group 1 QQ v[15..29], group 2
-// G v[30..44], group 3 H v[45..59]; w points at the group's 15 values.
-template <int G>
-__device__ inline void store_pair_group_a(const PlaneSink& sk, int N, int a, int b, const dsf* w, int add) {
+// store_pair_t.
+__device__ inline void store_pair_rows_a(const PlaneSink& sk, int N, int a, int b, const dsf* v, int add) {
   auto at = [&](int r, int c) { return (int64_t)r + (int64_t)c * sk.ld; };
-  if constexpr (G == 0) {
-    constexpr int sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
-    {  // TT and RR
-      int64_t p[18];
-      dsf x[18];
+  constexpr int sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+  {  // TT and RR
+    int64_t p[18];
+    dsf x[18];
 #pragma unroll
-      for (int i = 0; i < 3; i++)
+    for (int i = 0; i < 3; i++)
 #pragma unroll
-        for (int j = 0; j < 3; j++) {
-          p[3 * i + j] = at(3 * a + i, 3 * b + j);
-          x[3 * i + j] = w[sym[i][j]];
-          p[9 + 3 * i + j] = at(3 * N + 3 * a + i, 3 * N + 3 * b + j);
-          x[9 + 3 * i + j] = w[6 + sym[i][j]];
-        }
-      sk.template put<18>(p, x, add);
-    }
-    {  // TR: a's translation rows against b's rotation, a's rotation rows against b's translation
-      int64_t p[18];
-      dsf x[18];
+      for (int j = 0; j < 3; j++) {
+        p[3 * i + j] = at(3 * a + i, 3 * b + j);
+        x[3 * i + j] = v[sym[i][j]];
+        p[9 + 3 * i + j] = at(3 * N + 3 * a + i, 3 * N + 3 * b + j);
+        x[9 + 3 * i + j] = v[6 + sym[i][j]];
+      }
+    sk.template put<18>(p, x, add);
+  }
+  {  // TR: a's translation rows against b's rotation, a's rotation rows against b's translation
+    int64_t p[18];
+    dsf x[18];
 #pragma unroll
-      for (int i = 0; i < 3; i++)
+    for (int i = 0; i < 3; i++)
 #pragma unroll
-        for (int j = 0; j < 3; j++) {
-          dsf tr = dsf(0);
-          if (i < j) tr = w[12 + (i == 0 ? j - 1 : 2)];
-          if (i > j) tr = -w[12 + (j == 0 ? i - 1 : 2)];
-          p[3 * i + j] = at(3 * a + i, 3 * N + 3 * b + j);
-          x[3 * i + j] = tr;
-          p[9 + 3 * i + j] = at(3 * N + 3 * a + j, 3 * b + i);
-          x[9 + 3 * i + j] = -tr;
-        }
-      sk.template put<18>(p, x, add);
-    }
-  } else if constexpr (G == 1) {  // QQ
+      for (int j = 0; j < 3; j++) {
+        dsf tr = dsf(0);
+        if (i < j) tr = v[12 + (i == 0 ? j - 1 : 2)];
+        if (i > j) tr = -v[12 + (j == 0 ? i - 1 : 2)];
+        p[3 * i + j] = at(3 * a + i, 3 * N + 3 * b + j);
+        x[3 * i + j] = tr;
+        p[9 + 3 * i + j] = at(3 * N + 3 * a + j, 3 * b + i);
+        x[9 + 3 * i + j] = -tr;
+      }
+    sk.template put<18>(p, x, add);
+  }
+#pragma unroll
+  for (int grp = 0; grp < 4; grp++) {  // G and H: a's velocity rows, then a's stresslet rows
+    const int h = grp & 1, srow = grp >> 1;
+    const int ro = h ? 3 * N : 0;
+    int64_t p[15];
+    dsf x[15];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int m = 0; m < 5; m++) {
+        dsf g = v[(h ? 45 : 30) + 5 * i + m];
+        if (srow && !h) g = -g;
+        p[5 * i + m] = srow ? at(6 * N + 5 * a + m, ro + 3 * b + i) : at(ro + 3 * a + i, 6 * N + 5 * b + m);
+        x[5 * i + m] = g;
+      }
+    sk.template put<15>(p, x, add);
+  }
+  {  // QQ
     int64_t p[25];
     dsf x[25];
 #pragma unroll
@@ -318,35 +331,10 @@ __device__ inline void store_pair_group_a(const PlaneSink& sk, int N, int a, int
       for (int y = 0; y < 5; y++) {
         const int lo = xi < y ? xi : y, hi = xi < y ? y : xi;
         p[5 * xi + y] = at(6 * N + 5 * a + xi, 6 * N + 5 * b + y);
-        x[5 * xi + y] = w[lo * 5 - lo * (lo - 1) / 2 + (hi - lo)];
+        x[5 * xi + y] = v[15 + lo * 5 - lo * (lo - 1) / 2 + (hi - lo)];
       }
     sk.template put<25>(p, x, add);
-  } else {  // G (group 2) or H (group 3): a's velocity rows, then a's stresslet rows
-    constexpr int h = G == 3 ? 1 : 0;
-    const int ro = h ? 3 * N : 0;
-#pragma unroll
-    for (int srow = 0; srow < 2; srow++) {
-      int64_t p[15];
-      dsf x[15];
-#pragma unroll
-      for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int m = 0; m < 5; m++) {
-          dsf g = w[5 * i + m];
-          if (srow && !h) g = -g;
-          p[5 * i + m] = srow ? at(6 * N + 5 * a + m, ro + 3 * b + i) : at(ro + 3 * a + i, 6 * N + 5 * b + m);
-          x[5 * i + m] = g;
-        }
-      sk.template put<15>(p, x, add);
-    }
   }
-}
-
-__device__ inline void store_pair_rows_a(const PlaneSink& sk, int N, int a, int b, const dsf* v, int add) {
-  store_pair_group_a<0>(sk, N, a, b, v, add);
-  store_pair_group_a<2>(sk, N, a, b, v + 30, add);
-  store_pair_group_a<3>(sk, N, a, b, v + 45, add);
-  store_pair_group_a<1>(sk, N, a, b, v + 15, add);
 }
 
 // particle of grand-matrix index x
@@ -581,9 +569,7 @@ __global__ void __launch_bounds__(128) ewald_pair_k_ds(int nn, rsd_lat_dev L, in
 // its FP32 rounding is no longer amplified by the epilogue's cancellation
 // between moments.
 __host__ __device__ constexpr bool kblock_is_sin(int q) { return (q >= 12 && q < 15) || (q >= 30 && q < 45); }
-constexpr int KBW = 64;  // weights per vector: four groups of 15 (the store groups), each padded to 16
-__host__ __device__ constexpr int kblock_slot(int q) { return 16 * (q / 15) + q % 15; }
-constexpr int KB_Y = 2;  // pair tile of ewald_pair_kblock: 32 x KB_Y
+constexpr int KBW = 64;  // weights per vector (60 used, padded for 16-byte rows)
 
 template <typename T>
 __device__ __forceinline__ void put_weight(T* p, double v) { *p = (T)v; }
@@ -612,9 +598,9 @@ __global__ void ewald_kblock_list(rsd_lat_dev L, int count, const int* __restric
   T* e = W + (size_t)q * KBW;
   for (int i = 0; i < 60; i++) {
     const bool a3 = (i >= 6 && i < 12) || (i >= 15 && i < 30) || i >= 45;
-    put_weight<T>(e + kblock_slot(i), (kblock_is_sin(i) ? w[i] : v[i]) * (a3 ? na3 : na));
+    put_weight<T>(e + i, (kblock_is_sin(i) ? w[i] : v[i]) * (a3 ? na3 : na));
   }
-  for (int g = 0; g < 4; g++) put_weight<T>(e + 16 * g + 15, 0.0);
+  for (int i = 60; i < KBW; i++) put_weight<T>(e + i, 0.0);
 }
 
 __device__ __forceinline__ void acc_norm(dsacc& a) { dsacc_norm(a); }
@@ -643,114 +629,78 @@ __device__ __forceinline__ float trig_s(float2 v) { return v.y; }
 __device__ __forceinline__ dsf trig_c(float4 v) { return dsf(v.x, v.y); }
 __device__ __forceinline__ dsf trig_s(float4 v) { return dsf(v.z, v.w); }
 
-// One chunk of kc staged vectors added into the 15 outputs of group G
-// (q = 15 G .. 15 G + 14, weights at slot 16 G of each vector) for the pair
-// (a, b) of the calling thread, then folded (acc_norm).  Groups 1 and 3 use
-// only cos(k.R), group 2 only sin(k.R).
-template <int G, typename T, typename TT, typename A>
-__device__ __forceinline__ void kblock_group(int kc, const T* __restrict__ sw, const TT* __restrict__ sca,
-                                             const TT* __restrict__ scb, A (&acc)[15]) {
-  for (int hh = 0; hh < kc; hh++) {
-    const TT ua = sca[hh * 32 + threadIdx.x], ub = scb[hh * KB_Y + threadIdx.y];
-    const T ca = trig_c(ua), sa = trig_s(ua), cb = trig_c(ub), sb = trig_s(ub);
-    const T c = ca * cb + sa * sb;   // cos(k.(x_a - x_b))
-    const T sn = sa * cb - ca * sb;  // sin(k.(x_a - x_b))
-    const T* e = sw + hh * KBW + 16 * G;
-#pragma unroll
-    for (int q = 0; q < 15; q++) acc[q] = fma(e[q], kblock_is_sin(15 * G + q) ? sn : c, acc[q]);
-  }
-#pragma unroll
-  for (int q = 0; q < 15; q++) acc_norm(acc[q]);  // at most 16 vectors between renormalisations
-}
-
-// Stages the weights of kc vectors from h0 and the trig values of the CTA's
-// 32 + KB_Y particles in shared memory (every thread of the CTA takes part).
-template <typename T, typename TT>
-__device__ __forceinline__ void kblock_stage(int nn, int h0, int kc, const T* __restrict__ W,
-                                             const TT* __restrict__ cs, T* sw, TT* sca, TT* scb) {
-  const int tid = (threadIdx.z * blockDim.y + threadIdx.y) * blockDim.x + threadIdx.x;
-  const int nthr = blockDim.x * blockDim.y * blockDim.z;
-  const int a0 = blockIdx.x * blockDim.x, b0 = blockIdx.y * blockDim.y;
-  for (int e = tid; e < kc * KBW; e += nthr) sw[e] = W[(size_t)h0 * KBW + e];
-  for (int e = tid; e < kc * (32 + KB_Y); e += nthr) {
-    const int hh = e / (32 + KB_Y), q = e % (32 + KB_Y), part = q < 32 ? a0 + q : b0 + q - 32;
-    if (part < nn) {
-      const TT v = cs[(size_t)(h0 + hh) * nn + part];
-      if (q < 32)
-        sca[hh * 32 + q] = v;
-      else
-        scb[hh * KB_Y + q - 32] = v;
-    }
-  }
-}
-
+// Accumulates sum_k W_q(k) {cos, sin}(k.(x_a - x_b)) over Kh vectors into
+// acc, for the pair (a, b) of the calling thread (block 32 x 4).  The
+// weights of 16 vectors and the trig values of the CTA's 32 + 4 particles
+// are staged in shared memory (sw: 16 x KBW, sca: 16 x 32, scb: 16 x 4).
 template <typename T, typename TT, typename A>
-__device__ __forceinline__ void kblock_dispatch(int g, int kc, const T* sw, const TT* sca, const TT* scb,
-                                                A (&acc)[15]) {
-  switch (g) {
-    case 0: kblock_group<0>(kc, sw, sca, scb, acc); break;
-    case 1: kblock_group<1>(kc, sw, sca, scb, acc); break;
-    case 2: kblock_group<2>(kc, sw, sca, scb, acc); break;
-    default: kblock_group<3>(kc, sw, sca, scb, acc); break;
+__device__ __forceinline__ void kblock_accumulate(int nn, int Kh, const T* __restrict__ W, const TT* __restrict__ cs,
+                                                  T* sw, TT* sca, TT* scb, bool valid, A (&acc)[60]) {
+  constexpr int KC = 16;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  const int a0 = blockIdx.x * blockDim.x, b0 = blockIdx.y * blockDim.y;
+  for (int h0 = 0; h0 < Kh; h0 += KC) {
+    const int kc = min(KC, Kh - h0);
+    __syncthreads();
+    for (int e = tid; e < kc * KBW; e += nthr) sw[e] = W[(size_t)h0 * KBW + e];
+    for (int e = tid; e < kc * 36; e += nthr) {
+      const int hh = e / 36, q = e % 36, part = q < 32 ? a0 + q : b0 + q - 32;
+      if (part < nn) {
+        const TT v = cs[(size_t)(h0 + hh) * nn + part];
+        if (q < 32)
+          sca[hh * 32 + q] = v;
+        else
+          scb[hh * 4 + q - 32] = v;
+      }
+    }
+    __syncthreads();
+    if (!valid) continue;
+    for (int hh = 0; hh < kc; hh++) {
+      const TT ua = sca[hh * 32 + threadIdx.x], ub = scb[hh * 4 + threadIdx.y];
+      const T ca = trig_c(ua), sa = trig_s(ua), cb = trig_c(ub), sb = trig_s(ub);
+      const T c = ca * cb + sa * sb;   // cos(k.(x_a - x_b))
+      const T sn = sa * cb - ca * sb;  // sin(k.(x_a - x_b))
+      const T* e = sw + hh * KBW;
+#pragma unroll
+      for (int q = 0; q < 60; q++) acc[q] = fma(e[q], kblock_is_sin(q) ? sn : c, acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 60; q++) acc_norm(acc[q]);  // at most 16 steps between renormalisations
   }
 }
 
 // Reciprocal-space pair blocks with per-vector block weights (equal radii):
 // the K32 FP32 vectors first, then the K64 double-single ones on top of the
-// FP32 sums; the blocks are written (add = 0) or added (add = 1) once.  CTA
-// 32 x KB_Y x 4: a 32 x KB_Y tile of pairs, and threadIdx.z the group of 15
-// outputs that the thread sums and stores (the group is uniform per warp),
-// so that a thread holds 15 accumulators instead of 60.
-__global__ void __launch_bounds__(32 * KB_Y * 4, 2) ewald_pair_kblock(int nn, int K32, const float* __restrict__ W32,
-                                                                     const float2* __restrict__ c32, int K64,
-                                                                     const dsf* __restrict__ W64,
-                                                                     const float4* __restrict__ c64, PlaneSink sk,
-                                                                     int add) {
+// FP32 sums; the blocks are written (add = 0) or added (add = 1) once.
+__global__ void __launch_bounds__(128) ewald_pair_kblock(int nn, int K32, const float* __restrict__ W32,
+                                                         const float2* __restrict__ c32, int K64,
+                                                         const dsf* __restrict__ W64, const float4* __restrict__ c64,
+                                                         PlaneSink sk, int add) {
   constexpr int KC = 16;
   __shared__ __align__(16) dsf sw[KC * KBW];  // the FP32 phase uses the first half as floats
-  __shared__ __align__(16) float4 sca[KC * 32], scb[KC * KB_Y];
+  __shared__ __align__(16) float4 sca[KC * 32], scb[KC * 4];
   if ((int)(blockIdx.x * blockDim.x) >= (int)(blockIdx.y * blockDim.y + blockDim.y - 1)) return;
   int a, b;
   const bool valid = pair_of(nn, &a, &b);
-  const int g = threadIdx.z;
-  dsacc acc[15];
+  dsacc acc[60];
   {
-    fchunk f[15];
+    fchunk f[60];
 #pragma unroll
-    for (int q = 0; q < 15; q++) f[q] = fchunk{0.f, 0.f, 0.f};
-    for (int h0 = 0; h0 < K32; h0 += KC) {
-      const int kc = min(KC, K32 - h0);
-      __syncthreads();
-      kblock_stage<float, float2>(nn, h0, kc, W32, c32, reinterpret_cast<float*>(sw), reinterpret_cast<float2*>(sca),
-                                  reinterpret_cast<float2*>(scb));
-      __syncthreads();
-      if (valid)
-        kblock_dispatch<float, float2>(g, kc, reinterpret_cast<const float*>(sw), reinterpret_cast<const float2*>(sca),
-                                       reinterpret_cast<const float2*>(scb), f);
-    }
+    for (int q = 0; q < 60; q++) f[q] = fchunk{0.f, 0.f, 0.f};
+    kblock_accumulate<float, float2>(nn, K32, W32, c32, reinterpret_cast<float*>(sw),
+                                     reinterpret_cast<float2*>(sca), reinterpret_cast<float2*>(scb), valid, f);
 #pragma unroll
-    for (int q = 0; q < 15; q++) acc[q] = dsacc(f[q].hi, f[q].lo);
+    for (int q = 0; q < 60; q++) acc[q] = dsacc(f[q].hi, f[q].lo);
   }
-  for (int h0 = 0; h0 < K64; h0 += KC) {
-    const int kc = min(KC, K64 - h0);
-    __syncthreads();
-    kblock_stage<dsf, float4>(nn, h0, kc, W64, c64, sw, sca, scb);
-    __syncthreads();
-    if (valid) kblock_dispatch<dsf, float4>(g, kc, sw, sca, scb, acc);
-  }
+  kblock_accumulate<dsf, float4>(nn, K64, W64, c64, sw, sca, scb, valid, acc);
   if (!valid) return;
-  dsf o[15];
+  dsf o[60];
 #pragma unroll
-  for (int q = 0; q < 15; q++) {
+  for (int q = 0; q < 60; q++) {
     dsacc_norm(acc[q]);
     o[q] = dsf(acc[q].hi, acc[q].lo);
   }
-  switch (g) {
-    case 0: store_pair_group_a<0>(sk, nn, a, b, o, add); break;
-    case 1: store_pair_group_a<1>(sk, nn, a, b, o, add); break;
-    case 2: store_pair_group_a<2>(sk, nn, a, b, o, add); break;
-    default: store_pair_group_a<3>(sk, nn, a, b, o, add); break;
-  }
+  store_pair_rows_a(sk, nn, a, b, o, add);
 }
 
 // Near/far split of the real-space images for the mixed form.  Image nz of
@@ -1503,8 +1453,7 @@ int rsd_ewald_assemble(rsd_ctx* ctx, int nn, const double* d_pos, const double* 
         if (K32) {
           ewald_kblock_list<float><<<(K32 + 127) / 128, 128, 0, s>>>(L, K32, dh + K64, hr[0], inv_pimu, w32); RSD_LAUNCH_NOTE();
         }
-        const dim3 kblk(32, KB_Y, 4), kgrd((nn + 31) / 32, (nn + KB_Y - 1) / KB_Y);
-        ewald_pair_kblock<<<kgrd, kblk, 0, s>>>(nn, K32, w32, c32, K64, w64, c64, psk, 0); RSD_LAUNCH_NOTE();
+        ewald_pair_kblock<<<grd, blk, 0, s>>>(nn, K32, w32, c32, K64, w64, c64, psk, 0); RSD_LAUNCH_NOTE();
       } else {
         if (K64) {
           ewald_ktable_list<double><<<(K64 + 127) / 128, 128, 0, s>>>(L, K64, dh, t64); RSD_LAUNCH_NOTE();
