@@ -148,13 +148,17 @@ __global__ void gemv_planes_part(int m, int k, const float* __restrict__ Mh, con
 // (-> pcol[C][R]), in double-single; tiles with no stored entry write zero
 // partials.  About half of M is read.  Needs n % 4 == 0.
 constexpr int SYMV_T = 128;
+constexpr int symv_smem(int nr) { return (int)(sizeof(dsf) * 8 * nr * SYMV_T + sizeof(float2) * nr * SYMV_T * 33); }
 template <int NR>
 __global__ void __launch_bounds__(256) symv_planes_part(int N, int n, const float* __restrict__ Mh,
                                                         const float* __restrict__ Ml, int64_t ld,
                                                         const float2* __restrict__ xs, int nbt,
                                                         double* __restrict__ prow, double* __restrict__ pcol) {
-  __shared__ dsf red[8][NR][SYMV_T];
-  __shared__ float2 colp[NR][SYMV_T][33];  // per-lane column partials, reduced after the tile
+  // dynamic shared memory (symv_smem(NR) bytes): the row partials of the 8
+  // warps, then the per-lane column partials, reduced after the tile
+  extern __shared__ __align__(16) unsigned char symv_raw[];
+  auto red = reinterpret_cast<dsf(*)[NR][SYMV_T]>(symv_raw);
+  auto colp = reinterpret_cast<float2(*)[SYMV_T][33]>(symv_raw + sizeof(dsf) * 8 * NR * SYMV_T);
   __shared__ int skip;
   const int R = blockIdx.x, C = blockIdx.y, r0 = R * SYMV_T, c0 = C * SYMV_T;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -507,8 +511,10 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
   const bool symv = n % 4 == 0 && ld % 4 == 0;
   bool mirrored = false;
   const int nbt = (int)((n + SYMV_T - 1) / SYMV_T);
+  if (symv)
+    RSD_CUDA(ctx, cudaFuncSetAttribute(symv_planes_part<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, symv_smem(2)));
   float2* fs = (float2*)rsd_scratch(ctx, "mixed_fs", sizeof(float2) * (size_t)nr * n);
-  double* gpart = symv ? (double*)rsd_scratch(ctx, "mixed_symv_part", sizeof(double) * 2 * (size_t)nbt * nbt * SYMV_T)
+  double* gpart = symv ? (double*)rsd_scratch(ctx, "mixed_symv_part", sizeof(double) * 2 * 2 * (size_t)nbt * nbt * SYMV_T)
                        : (double*)rsd_scratch(ctx, "mixed_gemv_part", sizeof(double) * (size_t)gchunks * nr * n);
   if (!fs || !gpart) return RSD_ENOMEM;
   float* M32 = (float*)rsd_scratch(ctx, "mixed_M32", sizeof(float) * n * n);
@@ -593,7 +599,7 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
       to_dsf_vec<<<nblk(n), 256, 0, s>>>(n, v, fs); RSD_LAUNCH_NOTE();
       if (symv) {
         double* pcol = gpart + (size_t)nbt * nbt * SYMV_T;
-        symv_planes_part<1><<<dim3(nbt, nbt), 256, 0, s>>>(nn, (int)n, Mh, Ml, ld, fs, nbt, gpart, pcol); RSD_LAUNCH_NOTE();
+        symv_planes_part<1><<<dim3(nbt, nbt), 256, symv_smem(1), s>>>(nn, (int)n, Mh, Ml, ld, fs, nbt, gpart, pcol); RSD_LAUNCH_NOTE();
         symv_planes_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>((int)n, 1, nbt, gpart, pcol, 1.0, out, n); RSD_LAUNCH_NOTE();
       } else {
         if (!mirrored) {
@@ -773,12 +779,14 @@ int rsd_mixed_solve(rsd_ctx* ctx, int nn, double* M, int64_t ld, const double* d
     RSD_CUDA(ctx, cudaMemcpyAsync(r1, w, sizeof(double) * nr * n, cudaMemcpyDeviceToDevice, s));
     // r1 -= M f, double-single products of the two planes
     to_dsf_vec<<<nblk(n * nr), 256, 0, s>>>(n * nr, f, fs); RSD_LAUNCH_NOTE();
-    if (symv) {  // one right-hand side per pass (the shared-memory budget of a tile)
-      double* pcol = gpart + (size_t)nbt * nbt * SYMV_T;
-      for (int c = 0; c < nr; c++) {
-        symv_planes_part<1><<<dim3(nbt, nbt), 256, 0, s>>>(nn, (int)n, Mh, Ml, ld, fs + (size_t)c * n, nbt, gpart, pcol); RSD_LAUNCH_NOTE();
-        symv_planes_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>((int)n, 1, nbt, gpart, pcol, -1.0, r1 + (size_t)c * n, n); RSD_LAUNCH_NOTE();
+    if (symv) {  // both right-hand sides in one pass over the stored half of M
+      double* pcol = gpart + (size_t)nbt * nbt * SYMV_T * nr;
+      if (nr == 2) {
+        symv_planes_part<2><<<dim3(nbt, nbt), 256, symv_smem(2), s>>>(nn, (int)n, Mh, Ml, ld, fs, nbt, gpart, pcol); RSD_LAUNCH_NOTE();
+      } else {
+        symv_planes_part<1><<<dim3(nbt, nbt), 256, symv_smem(1), s>>>(nn, (int)n, Mh, Ml, ld, fs, nbt, gpart, pcol); RSD_LAUNCH_NOTE();
       }
+      symv_planes_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>((int)n, nr, nbt, gpart, pcol, -1.0, r1, n); RSD_LAUNCH_NOTE();
     } else {
       // full product: the mirrored entries are filled in first
       if (!mirrored) {
