@@ -83,7 +83,7 @@ def parse():
     ap.add_argument("--long-steps", type=int, default=10000)
     ap.add_argument("--plain-steps", type=int, default=5, help="(long) plain FP64 steps beside the mixed run")
     ap.add_argument("--long-seconds", type=float, default=0.0, help="(long) wall-time budget; 0: none")
-    ap.add_argument("--contact", type=float, default=100.0,
+    ap.add_argument("--contact", type=float, default=1000.0,
                     help="(long) host contact repulsion F0 in units of 6 pi mu a^2 gammadot (0: none)")
     ap.add_argument("--contact-range", type=float, default=0.01, help="(long) its decay length, in radii")
     ap.add_argument("--out-dir", default=None, help="(long) where yeta_mu.txt and the viscosity series go")
