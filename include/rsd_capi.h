@@ -117,9 +117,13 @@ int rsd_ctx_set_correction_method(rsd_ctx* ctx, int32_t method);
  * iteration x += P (b - A x), P the correction that the FP32 factors give,
  * FP64 residuals; it stops at the step's relative residual tolerance, or
  * within 100 times it once an iteration no longer halves the residual (the
- * floor of the residual arithmetic on stiff systems).  Mode 1 = flexible
- * GMRES with the same preconditioner and FP64 residuals, restarted every
- * `restart` iterations (1..30, 0: 30). */
+ * floor of the residual arithmetic on stiff systems).  When it diverges
+ * (its residual grows 1000 times above its best) or ends above 100 times the
+ * tolerance, flexible GMRES finishes the solve from zero
+ * (rsd_step_info.fallback = 1).  Mode 1 = flexible GMRES alone, with the
+ * same preconditioner and FP64 residuals, restarted every `restart`
+ * iterations (1..30, 0: 30).  A solve that ends above 100 times the
+ * tolerance returns RSD_ENOCONV. */
 int rsd_ctx_set_refinement(rsd_ctx* ctx, int32_t mode, int32_t restart);
 /* Bounds of the device-side waits of the mixed form's FP32 kernels (no
  * counterpart in the reference): every mbarrier wait of the tensor-core
