@@ -13,8 +13,9 @@ first to the least-loaded worker (LPT), with a replica's cost taken as
 Tuning.  autotune() times one step of a representative replica of every
 size class (N in [32, 64), [64, 128), [128, 192), [192, 256]) under each
 candidate setting of the kernels -- the FP32 factorisations on tcgen05 or on
-the FP32 SIMT pipe (rsd_ctx_set_tensor_cores), and the number of passes over
-the near real-space images (rsd_ctx_set_mixed_real_passes) -- and keeps the
+the FP32 SIMT pipe (rsd_ctx_set_tensor_cores), with the look-ahead or the
+in-order schedule (rsd_ctx_set_factor_schedule), and the number of passes
+over the near real-space images (rsd_ctx_set_mixed_real_passes) -- and keeps the
 fastest per class in a table (JSON), which the workers apply per replica.
 
 The replicas are device-resident (positions, radii, velocities and
@@ -30,8 +31,13 @@ import time
 import numpy as np
 
 SIZE_CLASSES = [(32, 64), (64, 128), (128, 192), (192, 257)]
-CANDIDATES = [dict(tensor_cores=1, real_passes=1), dict(tensor_cores=0, real_passes=1),
-              dict(tensor_cores=1, real_passes=2), dict(tensor_cores=0, real_passes=2)]
+# the factor schedule matters only on the tensor-core path (its two-level
+# Cholesky); a small replica is launch-bound, where the in-order schedule's
+# fewer launches can win
+CANDIDATES = [dict(tensor_cores=1, real_passes=1, factor_schedule=1), dict(tensor_cores=1, real_passes=1, factor_schedule=0),
+              dict(tensor_cores=0, real_passes=1, factor_schedule=1),
+              dict(tensor_cores=1, real_passes=2, factor_schedule=1), dict(tensor_cores=1, real_passes=2, factor_schedule=0),
+              dict(tensor_cores=0, real_passes=2, factor_schedule=1)]
 
 
 def size_class(N):
@@ -98,6 +104,7 @@ class Ensemble:
         if s:
             ctx.set_tensor_cores(s["tensor_cores"])
             ctx.set_mixed_real_passes(s["real_passes"])
+            ctx.set_factor_schedule(s.get("factor_schedule", 1))
 
     def _step_replica(self, w, r):
         rsd, s = self.rsd, self.specs[r]
@@ -153,10 +160,12 @@ class Ensemble:
             for cand in CANDIDATES:
                 ctx.set_tensor_cores(cand["tensor_cores"])
                 ctx.set_mixed_real_passes(cand["real_passes"])
+                ctx.set_factor_schedule(cand["factor_schedule"])
                 times = []
                 for it in range(reps + 1):
                     c = conf0.clone()
-                    torch.cuda.synchronize(self.dev)
+                    if self.dev.type == "cuda":
+                        torch.cuda.synchronize(self.dev)
                     t0 = time.perf_counter()
                     self.rsd.stepper_stokesian_dev(ctx, tab, c, self.radii[r], self.T[r], self.dt, [L, L, L],
                                                    s["gamma"], self.mu, self.ews, self.U[r], self.S[r],
@@ -170,6 +179,7 @@ class Ensemble:
             table[str(k)] = dict(best[0], ms=best[1], N=s["N"])
         ctx.set_tensor_cores(1)
         ctx.set_mixed_real_passes(1)
+        ctx.set_factor_schedule(1)
         self.table = table
         if path:
             with open(path, "w") as fp:
